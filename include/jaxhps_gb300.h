@@ -1,0 +1,219 @@
+/*
+ * jaxhps_gb300 — C ABI of the GB300-native HPS build/solve path.
+ *
+ * The reference (meliao/jaxhps) is pure JAX and binds no native code; its
+ * hot path is three families of stage functions that this library replaces
+ * one for one:
+ *
+ *   local_solve_stage_uniform_{2D,3D}_DtN  src/jaxhps/local_solve/_uniform_2D_DtN.py:9-102
+ *                                          (get_DtN :228-273), _uniform_3D_DtN.py:13-106
+ *   local_solve_stage_uniform_2D_ItI       src/jaxhps/local_solve/_uniform_2D_ItI.py:10-117
+ *                                          (get_ItI :120-186)
+ *   merge_stage_uniform_{2D,3D}_DtN        src/jaxhps/merge/_uniform_2D_DtN.py:13-203
+ *                                          (one level = vmapped_uniform_quad_merge_DtN :358-381)
+ *   merge_stage_uniform_2D_ItI             src/jaxhps/merge/_uniform_2D_ItI.py:19-179
+ *   down_pass_uniform_{2D,3D}_DtN / _ItI   src/jaxhps/down_pass/_uniform_2D_DtN.py:7-122
+ *                                          (one level = _propagate_down_2D_DtN :125-189)
+ *
+ * Python host code (jaxhps_gb300/_native.py) binds these symbols with ctypes.
+ *
+ * Conventions
+ *  - Every pointer argument is a device pointer unless stated otherwise.
+ *    Arrays are dense row-major; batch strides are in elements.
+ *  - The library never allocates device memory: callers pass a workspace
+ *    sized by the matching *_workspace_size() call.
+ *  - `stream` is a cudaStream_t passed as void*; work is enqueued, the call
+ *    returns without synchronising.
+ *  - Return value: HPS_OK (0) or an error code; hps_last_error() gives the
+ *    message of the most recent failure in the calling thread.
+ */
+#ifndef JAXHPS_GB300_H
+#define JAXHPS_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define HPS_API __attribute__((visibility("default")))
+#else
+#define HPS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* element types */
+enum { HPS_F64 = 0, HPS_F32 = 1, HPS_C128 = 2, HPS_C64 = 3 };
+
+/* status codes */
+enum {
+  HPS_OK = 0,
+  HPS_ERR_ARG = 1,        /* invalid argument (shape, null pointer, dtype) */
+  HPS_ERR_SINGULAR = 2,   /* reserved: a zero pivot (reported through info arrays) */
+  HPS_ERR_WORKSPACE = 4,  /* workspace too small */
+  HPS_ERR_CUDA = 5        /* a CUDA launch or runtime call failed */
+};
+
+/* Library version string (static storage). */
+HPS_API const char* hps_version(void);
+
+/* Copies the last error message of this thread into buf (NUL-terminated).
+ * Returns the full message length. */
+HPS_API int hps_last_error(char* buf, size_t len);
+
+/* ---------------------------------------------------------------------------
+ * Batched primitives
+ * ------------------------------------------------------------------------- */
+
+/* D[b] = alpha * A[b] @ B[b] + beta * C[b]  (row-major, m x k times k x n).
+ * alpha/beta are host pointers to {re, im}.  C may be NULL (beta ignored)
+ * and may alias D.  A batch stride of 0 broadcasts that operand.
+ * Replaces the `@` / einsum products of get_DtN (_uniform_2D_DtN.py:264-271),
+ * _assemble_merge_outputs (merge/_schur_complement.py:222-235) and the down
+ * pass (down_pass/_uniform_2D_DtN.py:114-120, :149). */
+HPS_API int hps_gemm_batched(int dtype, int m, int n, int k, const double* alpha, const void* A, long long lda,
+                     long long strideA, const void* B, long long ldb, long long strideB, const double* beta,
+                     const void* C, long long ldc, long long strideC, void* D, long long ldd, long long strideD,
+                     int batch, void* stream);
+
+/* Workspace bytes for hps_inverse_batched (0 for small n). */
+HPS_API size_t hps_inverse_workspace_size(int dtype, int n, int batch);
+
+/* X[b] = inv(A[b]) by Gauss-Jordan elimination with partial pivoting.
+ * X may alias A.  info[b] (device, may be NULL) = 0 or k+1 for a zero pivot
+ * at step k.  Replaces jnp.linalg.inv at local_solve/_uniform_2D_DtN.py:257
+ * and merge/_schur_complement.py:107,146. */
+HPS_API int hps_inverse_batched(int dtype, int n, const void* A, long long lda, long long strideA, void* X,
+                        long long ldx, long long strideX, int batch, int* info, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
+/* Element-type conversion of n contiguous elements (f64<->f32, c128<->c64). */
+HPS_API int hps_convert(int dtype_src, int dtype_dst, long long n, const void* src, void* dst, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Leaf stage (DtN).  Replaces local_solve_stage_uniform_2D_DtN /
+ * local_solve_stage_uniform_3D_DtN (get_DtN, _uniform_2D_DtN.py:228-273):
+ *   A   = sum_o diag(coeffs[o]) ops[o]            (assemble_diff_operator :182-218)
+ *   Y   = [P ; -inv(A_ii) A_ie P],  T = Q Y,
+ *   v   = [0 ; inv(A_ii) f_int],     h = Q v.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int dtype;          /* HPS_F64 or HPS_F32 (HPS_C128/HPS_C64 for complex coefficients) */
+  int coef_complex;   /* 0: coeffs are float64, 1: complex128 */
+  int n_leaves;
+  int n_pts;          /* p^d Chebyshev points per leaf */
+  int n_cb;           /* Chebyshev boundary points (exterior-first prefix) */
+  int n_gauss;        /* Gauss boundary points (4q in 2D, 6q^2 in 3D) */
+  int nsrc;           /* number of right-hand sides (0: no source) */
+  int n_ops;          /* number of active coefficient/operator pairs */
+  const double* ops;  /* (n_ops, n_pts, n_pts) float64 */
+  const void* coeffs; /* (n_ops, n_leaves, n_pts) float64 or complex128 */
+  const void* source; /* (n_leaves, n_pts, nsrc) in dtype, or NULL */
+  const void* P;      /* (n_cb, n_gauss) in dtype */
+  const void* Q;      /* (n_gauss, n_pts) in dtype */
+  void* Y;            /* out (n_leaves, n_pts, n_gauss) */
+  void* T;            /* out (n_leaves, n_gauss, n_gauss) */
+  void* v;            /* out (n_leaves, n_pts, nsrc) or NULL */
+  void* h;            /* out (n_leaves, n_gauss, nsrc) or NULL */
+  void* Aii_inv;      /* out (n_leaves, n_i, n_i), n_i = n_pts - n_cb */
+  int* info;          /* out (n_leaves) pivot status, or NULL */
+  void* workspace;
+  size_t workspace_bytes;
+} hps_leaf_dtn_args;
+
+HPS_API size_t hps_local_solve_dtn_workspace_size(const hps_leaf_dtn_args* a);
+HPS_API int hps_local_solve_dtn(const hps_leaf_dtn_args* a, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Leaf stage (ItI, 2D).  Replaces get_ItI (local_solve/_uniform_2D_ItI.py:120-186):
+ *   B = [G ; A[n_cb:, :]],  Binv = inv(B),
+ *   Y = Binv[:, :n_cb] P,   v = Binv[:, n_cb:] f_int,   T = QH Y,  h = QH v.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int dtype;          /* HPS_C128 or HPS_C64 */
+  int coef_complex;
+  int n_leaves, n_pts, n_cb, n_gauss, nsrc, n_ops;
+  const double* ops;  /* (n_ops, n_pts, n_pts) float64 */
+  const void* coeffs; /* (n_ops, n_leaves, n_pts) float64 or complex128 */
+  const void* source; /* (n_leaves, n_pts, nsrc) in dtype, or NULL */
+  const void* G;      /* (n_cb, n_pts) in dtype */
+  const void* P;      /* (n_cb, n_gauss) in dtype */
+  const void* QH;     /* (n_gauss, n_pts) in dtype */
+  void* Y;            /* out (n_leaves, n_pts, n_gauss) */
+  void* T;            /* out (n_leaves, n_gauss, n_gauss) */
+  void* v;            /* out (n_leaves, n_pts, nsrc) or NULL */
+  void* h;            /* out (n_leaves, n_gauss, nsrc) or NULL */
+  void* B_inv;        /* out (n_leaves, n_pts, n_pts) */
+  int* info;
+  void* workspace;
+  size_t workspace_bytes;
+} hps_leaf_iti_args;
+
+HPS_API size_t hps_local_solve_iti_workspace_size(const hps_leaf_iti_args* a);
+HPS_API int hps_local_solve_iti(const hps_leaf_iti_args* a, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * One merge level (DtN, quad or oct).  Replaces vmapped_uniform_quad_merge_DtN
+ * (merge/_uniform_2D_DtN.py:358-381) and _uniform_oct_merge_DtN
+ * (merge/_uniform_3D_DtN.py:127-187):
+ *   gather B, C, D, A-blocks from the children's T  (index maps),
+ *   D_inv = inv(D),  S = -D_inv C,  g~ = -D_inv dh,
+ *   T_out = A + B S,  h_out = h_ext + B g~.
+ * The exterior ordering of T_out / h_out / S columns is the final one
+ * (the reference's roll by -n_int, :343-346, is folded into ext_c/ext_l).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int dtype;
+  int n_merges;
+  int nch;            /* children per merge: 4 (2D) or 8 (3D) */
+  int nb;             /* boundary points of one child */
+  int n_int;          /* interface points of one merge */
+  int n_ext;          /* exterior points of one merge */
+  int nsrc;           /* 0 for no source */
+  const void* T_children; /* (n_merges*nch, nb, nb) */
+  const void* h_children; /* (n_merges*nch, nb, nsrc) or NULL */
+  const int* int_c;   /* (2*n_int) child of each copy of interface point i */
+  const int* int_l;   /* (2*n_int) local index in that child */
+  const int* ext_c;   /* (n_ext) */
+  const int* ext_l;   /* (n_ext) */
+  const int* loc;     /* (nch*n_int) local index of interface i in child c, -1 if absent */
+  void* S;            /* out (n_merges, n_int, n_ext) */
+  void* g_tilde;      /* out (n_merges, n_int, nsrc) or NULL */
+  void* T_out;        /* out (n_merges, n_ext, n_ext) */
+  void* h_out;        /* out (n_merges, n_ext, nsrc) or NULL */
+  void* D_inv;        /* out (n_merges, n_int, n_int), or NULL to keep it in the workspace */
+  void* BD_inv;       /* out (n_merges, n_ext, n_int) = B D_inv, or NULL (no-source up pass) */
+  int* info;          /* (n_merges) or NULL */
+  void* workspace;
+  size_t workspace_bytes;
+} hps_merge_args;
+
+HPS_API size_t hps_merge_level_dtn_workspace_size(const hps_merge_args* a);
+HPS_API int hps_merge_level_dtn(const hps_merge_args* a, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * One down-pass level.  Replaces _propagate_down_2D_DtN
+ * (down_pass/_uniform_2D_DtN.py:125-189), _propogate_down_2D_ItI
+ * (down_pass/_uniform_2D_ItI.py:121-192), _propogate_down_oct_DtN
+ * (down_pass/_uniform_3D_DtN.py:116-246):
+ *   g_int = S g_parent + g~ ;  child boundary data gathered through `code`
+ *   (code >= 0: parent exterior index, code < 0: interface -(code+1)).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int dtype;
+  int n_merges, nch, nb, n_int, n_ext, nsrc;
+  const void* S;        /* (n_merges, n_int, n_ext) */
+  const void* g_tilde;  /* (n_merges, n_int, nsrc) or NULL */
+  const void* g_parent; /* (n_merges, n_ext, nsrc) */
+  const int* code;      /* (nch*nb) */
+  void* g_int;          /* scratch/out (n_merges, n_int, nsrc) */
+  void* g_children;     /* out (n_merges*nch, nb, nsrc) */
+} hps_down_args;
+
+HPS_API int hps_down_level(const hps_down_args* a, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JAXHPS_GB300_H */

@@ -1,0 +1,79 @@
+"""``Domain``: discretization of the computational box (API mirror of
+src/jaxhps/_domain.py:38-97).
+
+Holds p, q, the root node, the number of uniform levels L (None for an
+adaptive tree), the leaf Chebyshev points ``interior_points``
+(n_leaves, p^d, d) and the root boundary Gauss points ``boundary_points``.
+Grid construction is host-side NumPy float64.
+"""
+
+from __future__ import annotations
+
+from typing import Callable, List
+
+import numpy as np
+
+from ._discretization_tree import DiscretizationNode2D, DiscretizationNode3D, get_all_leaves
+from . import _grid_creation_2D as g2
+
+
+class Domain:
+    def __init__(self, p: int, q: int, root, L: int | None = None):
+        self.p = int(p)
+        self.q = int(q)
+        self.root = root
+        self.L = None if L is None else int(L)
+        self.bool_2D = isinstance(root, DiscretizationNode2D)
+        if self.L is not None:
+            self.bool_uniform = True
+            if self.bool_2D:
+                self.interior_points = g2.compute_interior_Chebyshev_points_uniform_2D(root, self.L, self.p)
+                self.boundary_points = g2.compute_boundary_Gauss_points_uniform_2D(root, self.L, self.q)
+                self.n_leaves = 4 ** self.L
+            else:
+                from . import _grid_creation_3D as g3
+                self.interior_points = g3.compute_interior_Chebyshev_points_uniform_3D(root, self.L, self.p)
+                self.boundary_points = g3.compute_boundary_Gauss_points_uniform_3D(root, self.L, self.q)
+                self.n_leaves = 8 ** self.L
+        else:
+            self.bool_uniform = False
+            self.n_leaves = len(get_all_leaves(root))
+            if self.bool_2D:
+                self.interior_points = g2.compute_interior_Chebyshev_points_adaptive_2D(root, self.p)
+                self.boundary_points = g2.compute_boundary_Gauss_points_adaptive_2D(root, self.q)
+            else:
+                from . import _grid_creation_3D as g3
+                self.interior_points = g3.compute_interior_Chebyshev_points_adaptive_3D(root, self.p)
+                self.boundary_points = g3.compute_boundary_Gauss_points_adaptive_3D(root, self.q)
+
+    def get_adaptive_boundary_data_lst(self, f: Callable) -> List[np.ndarray]:
+        """Boundary data split per side (2D: S, E, N, W) or face (3D: -x, +x,
+        -y, +y, -z, +z) as in src/jaxhps/_domain.py:296-365."""
+        b = self.boundary_points
+        r = self.root
+        if self.bool_2D:
+            masks = [b[:, 1] == r.ymin, b[:, 0] == r.xmax, b[:, 1] == r.ymax, b[:, 0] == r.xmin]
+        else:
+            masks = [b[:, 0] == r.xmin, b[:, 0] == r.xmax, b[:, 1] == r.ymin, b[:, 1] == r.ymax,
+                     b[:, 2] == r.zmin, b[:, 2] == r.zmax]
+        return [f(b[m]) for m in masks]
+
+    @classmethod
+    def from_adaptive_discretization(cls, p: int, q: int, root, f, tol: float, use_level_restriction: bool = True,
+                                     use_l_2_norm: bool = False, proposer=None) -> "Domain":
+        """Adaptive refinement of ``root`` until every leaf resolves ``f``
+        to ``tol`` (src/jaxhps/_domain.py:367-434).  ``proposer`` is an
+        optional learned refinement proposal (jaxhps_gb300.refinement_mlp);
+        the interpolation criterion still decides every accepted leaf."""
+        fs = f if isinstance(f, list) else [f]
+        if isinstance(root, DiscretizationNode2D):
+            from ._adaptive_discretization_2D import generate_adaptive_mesh_level_restriction_2D as gen
+        else:
+            from ._adaptive_discretization_3D import generate_adaptive_mesh_level_restriction as gen
+        for fn in fs:
+            kw = dict(root=root, f_fn=fn, tol=tol, p=p, q=q, restrict_bool=use_level_restriction,
+                      l2_norm=use_l_2_norm)
+            if proposer is not None:
+                kw["proposer"] = proposer
+            gen(**kw)
+        return cls(p=p, q=q, root=root)

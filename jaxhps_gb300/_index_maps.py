@@ -1,0 +1,102 @@
+"""Host-side index maps that drive the merge gather and down-pass scatter
+kernels.
+
+A merge of ``nch`` children, each with ``nb`` boundary points, is described
+by one integer ``code`` per (child, local boundary point):
+``code >= 0`` is the point's index in the merged node's exterior (in the
+final, already rolled order), ``code < 0`` is interface unknown
+``-(code+1)``.  From ``code`` the DtN gather maps are derived: the two
+(child, local) copies of every interface point, the (child, local) of every
+exterior point, and a child x interface table of local indices.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from functools import lru_cache
+
+import numpy as np
+import torch
+
+
+@dataclass
+class MergeMaps:
+    nch: int
+    nb: int
+    n_int: int
+    n_ext: int
+    code: np.ndarray    # (nch, nb)
+    int_c: np.ndarray   # (n_int, 2)
+    int_l: np.ndarray   # (n_int, 2)
+    ext_c: np.ndarray   # (n_ext,)
+    ext_l: np.ndarray   # (n_ext,)
+    loc: np.ndarray     # (nch, n_int)
+
+    def device(self, dev):
+        key = str(dev)
+        cache = self.__dict__.setdefault("_dev", {})
+        if key not in cache:
+            def t(a):
+                return torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32), device=dev)
+            cache[key] = {k: t(getattr(self, k)) for k in ("code", "int_c", "int_l", "ext_c", "ext_l", "loc")}
+        return cache[key]
+
+
+def maps_from_code(code: np.ndarray, n_ext: int, n_int: int) -> MergeMaps:
+    nch, nb = code.shape
+    int_c = np.full((n_int, 2), -1, dtype=np.int64)
+    int_l = np.full((n_int, 2), -1, dtype=np.int64)
+    ext_c = np.full(n_ext, -1, dtype=np.int64)
+    ext_l = np.full(n_ext, -1, dtype=np.int64)
+    loc = np.full((nch, n_int), -1, dtype=np.int64)
+    fill = np.zeros(n_int, dtype=np.int64)
+    for c in range(nch):
+        for k in range(nb):
+            cd = code[c, k]
+            if cd >= 0:
+                assert ext_c[cd] < 0, "exterior point mapped twice"
+                ext_c[cd], ext_l[cd] = c, k
+            else:
+                i = -cd - 1
+                assert fill[i] < 2, "interface point shared by more than two children"
+                int_c[i, fill[i]], int_l[i, fill[i]] = c, k
+                fill[i] += 1
+                loc[c, i] = k
+    assert (ext_c >= 0).all(), "exterior point not covered"
+    assert (fill == 2).all(), "interface point without two sides"
+    return MergeMaps(nch, nb, n_int, n_ext, code, int_c, int_l, ext_c, ext_l, loc)
+
+
+@lru_cache(maxsize=None)
+def quad_merge_maps_dtn(nc: int) -> MergeMaps:
+    """2D quad merge of children a,b,c,d (SW,SE,NE,NW) with nc Gauss points
+    per child side.
+
+    Exterior order after the roll of merge/_uniform_2D_DtN.py:343-346:
+    [a_S, b_S, b_E, c_E, c_N, d_N, d_W, a_W].  Interfaces 5 (a|b), 6 (b|c),
+    7 (c|d), 8 (d|a) in the orientation of get_quadmerge_blocks_* (:384-437):
+    a's and b's own side order for 5 and 6 ... with the partner side flipped.
+    """
+    nb = 4 * nc
+    code = np.zeros((4, nb), dtype=np.int64)
+    t = np.arange(nc)
+    # exterior
+    code[0, 0:nc] = 0 * nc + t            # a_S
+    code[1, 0:nc] = 1 * nc + t            # b_S
+    code[1, nc:2 * nc] = 2 * nc + t       # b_E
+    code[2, nc:2 * nc] = 3 * nc + t       # c_E
+    code[2, 2 * nc:3 * nc] = 4 * nc + t   # c_N
+    code[3, 2 * nc:3 * nc] = 5 * nc + t   # d_N
+    code[3, 3 * nc:4 * nc] = 6 * nc + t   # d_W
+    code[0, 3 * nc:4 * nc] = 7 * nc + t   # a_W
+    # interfaces (value -(i+1))
+    i5, i6, i7, i8 = t, nc + t, 2 * nc + t, 3 * nc + t
+    code[0, nc + t] = -(i5 + 1)
+    code[1, 4 * nc - 1 - t] = -(i5 + 1)
+    code[1, 2 * nc + t] = -(i6 + 1)
+    code[2, nc - 1 - t] = -(i6 + 1)
+    code[2, 3 * nc + t] = -(i7 + 1)
+    code[3, 2 * nc - 1 - t] = -(i7 + 1)
+    code[3, t] = -(i8 + 1)
+    code[0, 3 * nc - 1 - t] = -(i8 + 1)
+    return maps_from_code(code, n_ext=8 * nc, n_int=4 * nc)

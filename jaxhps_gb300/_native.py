@@ -1,0 +1,230 @@
+"""ctypes binding of the native library (C ABI: include/jaxhps_gb300.h).
+
+The product path has no CPU fallback: if ``libjaxhps_gb300.so`` is missing
+or CUDA is unavailable, every stage raises.  Device memory comes from torch
+tensors; their ``data_ptr()`` values are passed straight to the C ABI along
+with torch's current CUDA stream.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import torch
+
+_LIB_PATH = Path(__file__).resolve().parent / "libjaxhps_gb300.so"
+_lock = threading.Lock()
+_lib = None
+
+HPS_F64, HPS_F32, HPS_C128, HPS_C64 = 0, 1, 2, 3
+
+TORCH_TO_HPS = {
+    torch.float64: HPS_F64,
+    torch.float32: HPS_F32,
+    torch.complex128: HPS_C128,
+    torch.complex64: HPS_C64,
+}
+
+
+class NativeError(RuntimeError):
+    """A native-library call returned a non-zero status."""
+
+
+vp = C.c_void_p
+ci = C.c_int
+cll = C.c_longlong
+csz = C.c_size_t
+
+
+class LeafDtnArgs(C.Structure):
+    _fields_ = [
+        ("dtype", ci), ("coef_complex", ci), ("n_leaves", ci), ("n_pts", ci), ("n_cb", ci),
+        ("n_gauss", ci), ("nsrc", ci), ("n_ops", ci),
+        ("ops", vp), ("coeffs", vp), ("source", vp), ("P", vp), ("Q", vp),
+        ("Y", vp), ("T", vp), ("v", vp), ("h", vp), ("Aii_inv", vp), ("info", vp),
+        ("workspace", vp), ("workspace_bytes", csz),
+    ]
+
+
+class LeafItiArgs(C.Structure):
+    _fields_ = [
+        ("dtype", ci), ("coef_complex", ci), ("n_leaves", ci), ("n_pts", ci), ("n_cb", ci),
+        ("n_gauss", ci), ("nsrc", ci), ("n_ops", ci),
+        ("ops", vp), ("coeffs", vp), ("source", vp), ("G", vp), ("P", vp), ("QH", vp),
+        ("Y", vp), ("T", vp), ("v", vp), ("h", vp), ("B_inv", vp), ("info", vp),
+        ("workspace", vp), ("workspace_bytes", csz),
+    ]
+
+
+class MergeArgs(C.Structure):
+    _fields_ = [
+        ("dtype", ci), ("n_merges", ci), ("nch", ci), ("nb", ci), ("n_int", ci), ("n_ext", ci),
+        ("nsrc", ci),
+        ("T_children", vp), ("h_children", vp),
+        ("int_c", vp), ("int_l", vp), ("ext_c", vp), ("ext_l", vp), ("loc", vp),
+        ("S", vp), ("g_tilde", vp), ("T_out", vp), ("h_out", vp), ("D_inv", vp), ("BD_inv", vp),
+        ("info", vp), ("workspace", vp), ("workspace_bytes", csz),
+    ]
+
+
+class DownArgs(C.Structure):
+    _fields_ = [
+        ("dtype", ci), ("n_merges", ci), ("nch", ci), ("nb", ci), ("n_int", ci), ("n_ext", ci),
+        ("nsrc", ci),
+        ("S", vp), ("g_tilde", vp), ("g_parent", vp), ("code", vp), ("g_int", vp), ("g_children", vp),
+    ]
+
+
+def _declare(lib):
+    P = C.POINTER
+    lib.hps_version.restype = C.c_char_p
+    lib.hps_last_error.argtypes = [C.c_char_p, csz]
+    lib.hps_last_error.restype = ci
+    lib.hps_gemm_batched.argtypes = [ci, ci, ci, ci, P(C.c_double), vp, cll, cll, vp, cll, cll, P(C.c_double),
+                                     vp, cll, cll, vp, cll, cll, ci, vp]
+    lib.hps_gemm_batched.restype = ci
+    lib.hps_inverse_workspace_size.argtypes = [ci, ci, ci]
+    lib.hps_inverse_workspace_size.restype = csz
+    lib.hps_inverse_batched.argtypes = [ci, ci, vp, cll, cll, vp, cll, cll, ci, vp, vp, csz, vp]
+    lib.hps_inverse_batched.restype = ci
+    lib.hps_convert.argtypes = [ci, ci, cll, vp, vp, vp]
+    lib.hps_convert.restype = ci
+    lib.hps_local_solve_dtn_workspace_size.argtypes = [P(LeafDtnArgs)]
+    lib.hps_local_solve_dtn_workspace_size.restype = csz
+    lib.hps_local_solve_dtn.argtypes = [P(LeafDtnArgs), vp]
+    lib.hps_local_solve_dtn.restype = ci
+    lib.hps_local_solve_iti_workspace_size.argtypes = [P(LeafItiArgs)]
+    lib.hps_local_solve_iti_workspace_size.restype = csz
+    lib.hps_local_solve_iti.argtypes = [P(LeafItiArgs), vp]
+    lib.hps_local_solve_iti.restype = ci
+    lib.hps_merge_level_dtn_workspace_size.argtypes = [P(MergeArgs)]
+    lib.hps_merge_level_dtn_workspace_size.restype = csz
+    lib.hps_merge_level_dtn.argtypes = [P(MergeArgs), vp]
+    lib.hps_merge_level_dtn.restype = ci
+    lib.hps_down_level.argtypes = [P(DownArgs), vp]
+    lib.hps_down_level.restype = ci
+
+
+EXPORTED_SYMBOLS = (
+    "hps_version", "hps_last_error", "hps_gemm_batched", "hps_inverse_workspace_size",
+    "hps_inverse_batched", "hps_convert", "hps_local_solve_dtn_workspace_size", "hps_local_solve_dtn",
+    "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
+    "hps_merge_level_dtn", "hps_down_level",
+)
+
+
+def load_library(path: Path | None = None):
+    """Loads (without building) the shared library; raises if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path is not None else _LIB_PATH
+        if not p.exists():
+            raise NativeError(
+                f"native library {p} not found: build it with `python -c \"import __graft_entry__ as g; g.build()\"`"
+            )
+        lib = C.CDLL(str(p))
+        _declare(lib)
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def lib():
+    """The loaded library, for GPU work.  Raises if CUDA is unavailable."""
+    if not torch.cuda.is_available():
+        raise NativeError("jaxhps_gb300 needs a CUDA device; no CPU fallback exists")
+    return load_library()
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        buf = C.create_string_buffer(1024)
+        load_library().hps_last_error(buf, 1024)
+        raise NativeError(f"{what} failed with status {status}: {buf.value.decode(errors='replace')}")
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def ptr(t) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+class Workspace:
+    """Grow-only device scratch buffer reused across calls."""
+
+    def __init__(self):
+        self.buf = None
+
+    def get(self, nbytes: int, device) -> torch.Tensor:
+        nbytes = max(int(nbytes), 256)
+        if self.buf is None or self.buf.numel() < nbytes or self.buf.device != torch.device(device):
+            self.buf = None
+            self.buf = torch.empty(nbytes, dtype=torch.uint8, device=device)
+        return self.buf
+
+
+_ws = Workspace()
+
+
+def workspace(nbytes: int, device) -> torch.Tensor:
+    return _ws.get(nbytes, device)
+
+
+def release_workspace() -> None:
+    _ws.buf = None
+
+
+# ---------------------------------------------------------------------------
+# thin wrappers over the primitives
+# ---------------------------------------------------------------------------
+
+
+def gemm(A, B, out, alpha=1.0, beta=0.0, Cmat=None, batch=None):
+    """out[b] = alpha A[b] @ B[b] + beta C[b] for 3D (or broadcast 2D) tensors,
+    all contiguous in their last two dims."""
+    L = lib()
+    dt = TORCH_TO_HPS[out.dtype]
+
+    def mat(t):
+        if t.dim() == 2:
+            return t.shape[0], t.shape[1], t.stride(0), 0
+        return t.shape[1], t.shape[2], t.stride(1), t.stride(0)
+
+    m, k, lda, sA = mat(A)
+    k2, n, ldb, sB = mat(B)
+    assert k == k2, (A.shape, B.shape)
+    mo, no, ldd, sD = mat(out)
+    assert (mo, no) == (m, n)
+    nb = batch if batch is not None else (out.shape[0] if out.dim() == 3 else 1)
+    al = (C.c_double * 2)(complex(alpha).real, complex(alpha).imag)
+    be = (C.c_double * 2)(complex(beta).real, complex(beta).imag)
+    if Cmat is not None:
+        _, _, ldc, sC = mat(Cmat)
+        cp = Cmat.data_ptr()
+    else:
+        ldc, sC, cp = 0, 0, None
+    check(L.hps_gemm_batched(dt, m, n, k, al, A.data_ptr(), lda, sA, B.data_ptr(), ldb, sB, be, cp, ldc, sC,
+                             out.data_ptr(), ldd, sD, nb, stream_ptr()), "hps_gemm_batched")
+    return out
+
+
+def inverse(A, out=None, info=None):
+    """Batched inverse of a (batch, n, n) tensor (out may be A)."""
+    L = lib()
+    if A.dim() == 2:
+        A = A.unsqueeze(0)
+    if out is None:
+        out = torch.empty_like(A)
+    b, n, _ = A.shape
+    dt = TORCH_TO_HPS[A.dtype]
+    wsb = L.hps_inverse_workspace_size(dt, n, b)
+    ws = workspace(wsb, A.device) if wsb else None
+    check(L.hps_inverse_batched(dt, n, A.data_ptr(), A.stride(1), A.stride(0), out.data_ptr(), out.stride(1),
+                                out.stride(0), b, ptr(info), ptr(ws), wsb, stream_ptr()), "hps_inverse_batched")
+    return out

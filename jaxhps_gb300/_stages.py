@@ -1,0 +1,331 @@
+"""GPU implementations of the reference's stage functions.
+
+Each function keeps the reference's name and argument meaning
+(local_solve/*.py, merge/*.py, down_pass/*.py) and runs its work through the
+native library's C ABI on torch-owned device memory.  Arrays may be given as
+NumPy arrays or torch tensors; results are torch tensors on ``device`` (the
+solver state is kept in HBM) except the final leaf solutions, which are
+moved to ``host_device`` when one is given.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from ._index_maps import quad_merge_maps_dtn
+
+REAL_TO_COMPLEX = {torch.float64: torch.complex128, torch.float32: torch.complex64}
+
+
+def _device(device) -> torch.device:
+    if device is None or (isinstance(device, str) and device == "cuda"):
+        return torch.device("cuda", torch.cuda.current_device())
+    return torch.device(device)
+
+
+def _as_tensor(a, dtype, device) -> torch.Tensor:
+    if isinstance(a, torch.Tensor):
+        return a.to(device=device, dtype=dtype).contiguous()
+    arr = np.asarray(a)
+    return torch.as_tensor(np.ascontiguousarray(arr)).to(device=device, dtype=dtype)
+
+
+def _is_complex(a) -> bool:
+    if a is None:
+        return False
+    if isinstance(a, torch.Tensor):
+        return a.is_complex()
+    return np.iscomplexobj(a)
+
+
+def _to_host(t: torch.Tensor, host_device):
+    if host_device is None:
+        return t
+    return t.to(torch.device(host_device))
+
+
+def _src3(src, n_leaves, n_pts, dtype, dev):
+    """Source as (n_leaves, n_pts, nsrc); returns (tensor, was_multi)."""
+    s = _as_tensor(src, dtype, dev)
+    if s.dim() == 2:
+        return s.unsqueeze(-1).contiguous(), False
+    return s, True
+
+
+def _coefficients(pde_problem, dev):
+    cs, ops = pde_problem.active_coefficients()
+    if not cs:
+        raise ValueError("PDEProblem has no differential operator coefficients")
+    cplx = any(_is_complex(c) for c in cs)
+    ctype = torch.complex128 if cplx else torch.float64
+    coeffs = torch.stack([_as_tensor(c, ctype, dev) for c in cs]).contiguous()
+    ops_t = torch.as_tensor(np.stack(ops)).to(device=dev, dtype=torch.float64).contiguous()
+    return ops_t, coeffs, cplx
+
+
+# ---------------------------------------------------------------------------
+# Leaf stage
+# ---------------------------------------------------------------------------
+
+
+def local_solve_stage_uniform_2D_DtN(pde_problem, host_device=None, device=None, dtype=torch.float64,
+                                     keep_inverse: bool = False):
+    """Leaf DtN solve for every leaf (reference local_solve/_uniform_2D_DtN.py:9-102).
+
+    Returns ``(Y, T, v, h)``: Y (n_leaves, p^2, 4q), T (n_leaves, 4q, 4q),
+    v (n_leaves, p^2[, nsrc]), h (n_leaves, 4q[, nsrc]).  With
+    ``keep_inverse`` the per-leaf ``inv(A_ii)`` is returned as a fifth item.
+    """
+    return _local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, device, dtype, keep_inverse)
+
+
+def _local_solve_dtn(pde_problem, P_np, Q_np, device, dtype, keep_inverse, source=None, want_source=True):
+    L = nat.lib()
+    dev = _device(device)
+    dom = pde_problem.domain
+    n_leaves = dom.n_leaves
+    n_pts = dom.interior_points.shape[1]
+    n_cb = P_np.shape[0]
+    ng = P_np.shape[1]
+    ops_t, coeffs, cplx = _coefficients(pde_problem, dev)
+    if cplx or _is_complex(pde_problem.source if source is None else source):
+        dtype = REAL_TO_COMPLEX.get(dtype, dtype)
+    P = _as_tensor(P_np, dtype, dev)
+    Q = _as_tensor(Q_np, dtype, dev)
+    src = pde_problem.source if source is None else source
+    multi = False
+    if want_source and src is not None:
+        f, multi = _src3(src, n_leaves, n_pts, dtype, dev)
+        ns = f.shape[-1]
+    else:
+        f, ns = None, 0
+    n_i = n_pts - n_cb
+    Y = torch.empty((n_leaves, n_pts, ng), dtype=dtype, device=dev)
+    T = torch.empty((n_leaves, ng, ng), dtype=dtype, device=dev)
+    v = torch.empty((n_leaves, n_pts, ns), dtype=dtype, device=dev) if ns else None
+    h = torch.empty((n_leaves, ng, ns), dtype=dtype, device=dev) if ns else None
+    Aii = torch.empty((n_leaves, n_i, n_i), dtype=dtype, device=dev)
+    info = torch.zeros(n_leaves, dtype=torch.int32, device=dev)
+    a = nat.LeafDtnArgs(
+        dtype=nat.TORCH_TO_HPS[dtype], coef_complex=int(cplx), n_leaves=n_leaves, n_pts=n_pts, n_cb=n_cb,
+        n_gauss=ng, nsrc=ns, n_ops=ops_t.shape[0], ops=ops_t.data_ptr(), coeffs=coeffs.data_ptr(),
+        source=nat.ptr(f), P=P.data_ptr(), Q=Q.data_ptr(), Y=Y.data_ptr(), T=T.data_ptr(), v=nat.ptr(v),
+        h=nat.ptr(h), Aii_inv=Aii.data_ptr(), info=info.data_ptr(), workspace=None, workspace_bytes=0)
+    wsb = L.hps_local_solve_dtn_workspace_size(C.byref(a))
+    ws = nat.workspace(wsb, dev)
+    a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
+    nat.check(L.hps_local_solve_dtn(C.byref(a), nat.stream_ptr()), "hps_local_solve_dtn")
+    if v is not None and not multi:
+        v, h = v[..., 0], h[..., 0]
+    out = (Y, T, v, h)
+    if keep_inverse:
+        out = out + (Aii,)
+    pde_problem._leaf_info = info
+    return out
+
+
+def local_solve_stage_uniform_3D_DtN(pde_problem, host_device=None, device=None, dtype=torch.float64,
+                                     keep_inverse: bool = False):
+    """Leaf DtN solve for 3D leaves (reference local_solve/_uniform_3D_DtN.py:13-106);
+    the leaf algebra is the same as 2D with p^3 points and 6q^2 Gauss nodes."""
+    return _local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, device, dtype, keep_inverse)
+
+
+def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None, dtype=torch.complex128,
+                                     keep_inverse: bool = False):
+    """Leaf ItI solve (reference local_solve/_uniform_2D_ItI.py:10-186).
+
+    Returns ``(Y, T, v, h)`` with T the impedance-to-impedance map."""
+    L = nat.lib()
+    dev = _device(device)
+    dom = pde_problem.domain
+    n_leaves = dom.n_leaves
+    n_pts = dom.interior_points.shape[1]
+    P_np = pde_problem.P
+    n_cb, ng = P_np.shape
+    ops_t, coeffs, cplx = _coefficients(pde_problem, dev)
+    dtype = REAL_TO_COMPLEX.get(dtype, dtype)
+    P = _as_tensor(P_np, dtype, dev)
+    G = _as_tensor(pde_problem.G, dtype, dev)
+    QH = _as_tensor(pde_problem.QH, dtype, dev)
+    multi = False
+    if pde_problem.source is not None:
+        f, multi = _src3(pde_problem.source, n_leaves, n_pts, dtype, dev)
+        ns = f.shape[-1]
+    else:
+        f, ns = None, 0
+    Y = torch.empty((n_leaves, n_pts, ng), dtype=dtype, device=dev)
+    T = torch.empty((n_leaves, ng, ng), dtype=dtype, device=dev)
+    v = torch.empty((n_leaves, n_pts, ns), dtype=dtype, device=dev) if ns else None
+    h = torch.empty((n_leaves, ng, ns), dtype=dtype, device=dev) if ns else None
+    Binv = torch.empty((n_leaves, n_pts, n_pts), dtype=dtype, device=dev)
+    info = torch.zeros(n_leaves, dtype=torch.int32, device=dev)
+    a = nat.LeafItiArgs(
+        dtype=nat.TORCH_TO_HPS[dtype], coef_complex=int(cplx), n_leaves=n_leaves, n_pts=n_pts, n_cb=n_cb,
+        n_gauss=ng, nsrc=ns, n_ops=ops_t.shape[0], ops=ops_t.data_ptr(), coeffs=coeffs.data_ptr(),
+        source=nat.ptr(f), G=G.data_ptr(), P=P.data_ptr(), QH=QH.data_ptr(), Y=Y.data_ptr(), T=T.data_ptr(),
+        v=nat.ptr(v), h=nat.ptr(h), B_inv=Binv.data_ptr(), info=info.data_ptr(), workspace=None,
+        workspace_bytes=0)
+    wsb = L.hps_local_solve_iti_workspace_size(C.byref(a))
+    ws = nat.workspace(wsb, dev)
+    a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
+    nat.check(L.hps_local_solve_iti(C.byref(a), nat.stream_ptr()), "hps_local_solve_iti")
+    if v is not None and not multi:
+        v, h = v[..., 0], h[..., 0]
+    out = (Y, T, v, h)
+    if keep_inverse:
+        out = out + (Binv,)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Merge stage
+# ---------------------------------------------------------------------------
+
+
+def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False):
+    """One batched merge level.  T_children: (n_merges*nch, nb, nb);
+    h_children: (n_merges*nch, nb, nsrc) or None.  Returns
+    (S, g_tilde, T_out, h_out, D_inv, BD_inv)."""
+    L = nat.lib()
+    dev = T_children.device
+    dtype = T_children.dtype
+    nch, nb, n_int, n_ext = maps.nch, maps.nb, maps.n_int, maps.n_ext
+    assert T_children.shape[1] == nb and T_children.shape[0] % nch == 0
+    n_m = T_children.shape[0] // nch
+    ns = 0 if h_children is None else h_children.shape[-1]
+    S = torch.empty((n_m, n_int, n_ext), dtype=dtype, device=dev)
+    T_out = torch.empty((n_m, n_ext, n_ext), dtype=dtype, device=dev)
+    g_t = torch.empty((n_m, n_int, ns), dtype=dtype, device=dev) if ns else None
+    h_out = torch.empty((n_m, n_ext, ns), dtype=dtype, device=dev) if ns else None
+    D_inv = torch.empty((n_m, n_int, n_int), dtype=dtype, device=dev) if keep_D_inv else None
+    BD_inv = torch.empty((n_m, n_ext, n_int), dtype=dtype, device=dev) if keep_BD_inv else None
+    info = torch.zeros(n_m, dtype=torch.int32, device=dev)
+    md = maps.device(dev)
+    a = nat.MergeArgs(
+        dtype=nat.TORCH_TO_HPS[dtype], n_merges=n_m, nch=nch, nb=nb, n_int=n_int, n_ext=n_ext, nsrc=ns,
+        T_children=T_children.data_ptr(), h_children=nat.ptr(h_children), int_c=md["int_c"].data_ptr(),
+        int_l=md["int_l"].data_ptr(), ext_c=md["ext_c"].data_ptr(), ext_l=md["ext_l"].data_ptr(),
+        loc=md["loc"].data_ptr(), S=S.data_ptr(), g_tilde=nat.ptr(g_t), T_out=T_out.data_ptr(),
+        h_out=nat.ptr(h_out), D_inv=nat.ptr(D_inv), BD_inv=nat.ptr(BD_inv), info=info.data_ptr(),
+        workspace=None, workspace_bytes=0)
+    wsb = L.hps_merge_level_dtn_workspace_size(C.byref(a))
+    ws = nat.workspace(wsb, dev)
+    a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
+    nat.check(L.hps_merge_level_dtn(C.byref(a), nat.stream_ptr()), "hps_merge_level_dtn")
+    return S, g_t, T_out, h_out, D_inv, BD_inv
+
+
+def merge_stage_uniform_2D_DtN(T_arr, h_arr, l: int, device=None, host_device=None, subtree_recomp: bool = False,
+                               return_T: bool = False, keep_D_inv: bool = False):
+    """Level loop of DtN quad merges (reference merge/_uniform_2D_DtN.py:13-203).
+
+    Returns ``(S_lst, g_tilde_lst)`` (leaf-adjacent level first, root last,
+    root with a leading batch axis of 1) and the top-level T when
+    ``return_T``.  With ``subtree_recomp`` returns only the top ``(T, h)``.
+    """
+    dev = _device(device)
+    T = T_arr if isinstance(T_arr, torch.Tensor) else _as_tensor(T_arr, torch.float64, dev)
+    T = T.to(dev).contiguous()
+    if T.dim() == 4:
+        T = T.reshape(-1, T.shape[-2], T.shape[-1])
+    multi = h_arr is not None and np.ndim(h_arr) == 3 if not isinstance(h_arr, torch.Tensor) else (
+        h_arr is not None and h_arr.dim() == 3)
+    h = None
+    if h_arr is not None:
+        h = h_arr if isinstance(h_arr, torch.Tensor) else _as_tensor(h_arr, T.dtype, dev)
+        h = h.to(device=dev, dtype=T.dtype)
+        if h.dim() == 2:
+            h = h.unsqueeze(-1)
+        h = h.reshape(T.shape[0], T.shape[1], -1).contiguous()
+    S_lst, g_lst, Dinv_lst = [], [], []
+    n_levels = max(int(l), 1)
+    for _ in range(n_levels):
+        nc = T.shape[1] // 4
+        maps = quad_merge_maps_dtn(nc)
+        S, g_t, T, h, D_inv, _ = merge_level_dtn(T, h, maps, keep_D_inv=keep_D_inv)
+        S_lst.append(S)
+        g_lst.append(g_t if (g_t is None or multi) else g_t[..., 0])
+        Dinv_lst.append(D_inv)
+    if subtree_recomp:
+        return T, (h if (h is None or multi) else h[..., 0])
+    out = (S_lst, g_lst)
+    if return_T:
+        out = out + (T[0],)
+    if keep_D_inv:
+        out = out + (Dinv_lst,)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Down pass
+# ---------------------------------------------------------------------------
+
+
+def down_level(S, g_tilde, g_parent, maps):
+    """One level of boundary-data propagation (n_merges parents -> nch*n_merges children)."""
+    L = nat.lib()
+    n_m, n_int, n_ext = S.shape
+    ns = g_parent.shape[-1]
+    dev, dtype = S.device, S.dtype
+    g_int = torch.empty((n_m, n_int, ns), dtype=dtype, device=dev)
+    g_ch = torch.empty((n_m * maps.nch, maps.nb, ns), dtype=dtype, device=dev)
+    md = maps.device(dev)
+    a = nat.DownArgs(dtype=nat.TORCH_TO_HPS[dtype], n_merges=n_m, nch=maps.nch, nb=maps.nb, n_int=n_int,
+                     n_ext=n_ext, nsrc=ns, S=S.data_ptr(), g_tilde=nat.ptr(g_tilde), g_parent=g_parent.data_ptr(),
+                     code=md["code"].data_ptr(), g_int=g_int.data_ptr(), g_children=g_ch.data_ptr())
+    nat.check(L.hps_down_level(C.byref(a), nat.stream_ptr()), "hps_down_level")
+    return g_ch
+
+
+def _down_pass_generic(boundary_data, S_lst, g_tilde_lst, Y_arr, v_arr, maps_fn, device, host_device):
+    dev = _device(device)
+    dtype = S_lst[0].dtype
+    g = boundary_data if isinstance(boundary_data, torch.Tensor) else _as_tensor(boundary_data, dtype, dev)
+    g = g.to(device=dev, dtype=dtype)
+    multi_g = g_tilde_lst[0] is not None and g_tilde_lst[0].dim() == 3
+    if g.dim() == 1:
+        g = g.unsqueeze(-1)
+    if g.dim() == 2:
+        g = g.unsqueeze(0)
+    g = g.contiguous()
+    ns = g.shape[-1]
+    for lvl in range(len(S_lst) - 1, -1, -1):
+        S = S_lst[lvl]
+        gt = g_tilde_lst[lvl]
+        if gt is not None and gt.dim() == 2:
+            gt = gt.unsqueeze(-1)
+        if gt is not None and gt.shape[-1] != ns:
+            if gt.shape[-1] == 1:
+                gt = gt.expand(-1, -1, ns)
+            else:
+                raise ValueError("boundary data and g_tilde have different numbers of sources")
+        gt = None if gt is None else gt.contiguous()
+        nc_child = S.shape[2] // 8
+        g = down_level(S, gt, g, maps_fn(nc_child))
+    if Y_arr is None:
+        return g if (ns > 1 or multi_g) else g[..., 0]
+    u = torch.empty((Y_arr.shape[0], Y_arr.shape[1], ns), dtype=dtype, device=dev)
+    if v_arr is not None:
+        v = v_arr if v_arr.dim() == 3 else v_arr.unsqueeze(-1)
+        if v.shape[-1] != ns:
+            v = v.expand(-1, -1, ns)
+        v = v.contiguous()
+        nat.gemm(Y_arr, g, u, 1.0, 1.0, Cmat=v)
+    else:
+        nat.gemm(Y_arr, g, u)
+    if ns == 1 and not multi_g and (v_arr is None or v_arr.dim() == 2):
+        u = u[..., 0]
+    return _to_host(u, host_device)
+
+
+def down_pass_uniform_2D_DtN(boundary_data, S_lst, g_tilde_lst, Y_arr, v_arr, device=None, host_device=None):
+    """Reference down_pass/_uniform_2D_DtN.py:7-122.  If ``Y_arr`` is None the
+    leaf boundary data is returned instead of the leaf solutions."""
+    return _down_pass_generic(boundary_data, S_lst, g_tilde_lst, Y_arr, v_arr, quad_merge_maps_dtn, device,
+                              host_device)

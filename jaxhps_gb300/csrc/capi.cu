@@ -1,0 +1,414 @@
+// C ABI of the native HPS library (declarations: include/jaxhps_gb300.h).
+//
+// Each stage entry point validates its arguments, carves the caller's
+// workspace, and enqueues the kernel sequence of that stage on the given
+// stream.  No device memory is allocated here.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+
+#include "../../include/jaxhps_gb300.h"
+#include "hps_common.cuh"
+#include "hps_internal.h"
+
+namespace hps {
+
+template <class T, class CT>
+cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col_split, int n_ops,
+                          const double* ops, const CT* coeffs, T* out_lo, long long ld_lo, long long s_lo,
+                          T* out_hi, long long ld_hi, long long s_hi, cudaStream_t st);
+template <class T>
+cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds, T* dst, long long ldd,
+                     long long sd, cudaStream_t st);
+template <class T>
+cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Tc, const T* hc,
+                         const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
+                         const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, cudaStream_t st);
+template <class T>
+cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, int ns, const int* code,
+                         const T* gpar, const T* gint, T* gch, cudaStream_t st);
+template <class S, class D>
+cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st);
+
+static thread_local std::string g_last_error;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Carves consecutive 256-byte aligned regions out of a workspace.
+struct Carver {
+  unsigned char* p;
+  size_t used = 0;
+  explicit Carver(void* base) : p(reinterpret_cast<unsigned char*>(base)) {}
+  void* take(size_t bytes) {
+    void* r = p ? p + used : nullptr;
+    used += al256(bytes);
+    return r;
+  }
+};
+
+#define HPS_CHECK(...)                                                             \
+  do {                                                                             \
+    cudaError_t _e = (__VA_ARGS__);                                                    \
+    if (_e != cudaSuccess) {                                                       \
+      set_error("%s failed: %s (%s:%d)", #__VA_ARGS__, cudaGetErrorString(_e), __FILE__, \
+                __LINE__);                                                         \
+      return HPS_ERR_CUDA;                                                         \
+    }                                                                              \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Leaf DtN
+// ---------------------------------------------------------------------------
+static size_t leaf_dtn_ws(const hps_leaf_dtn_args* a, Carver* cv) {
+  const size_t es = dtype_size(a->dtype);
+  const int n_i = a->n_pts - a->n_cb;
+  cv->take(es * (size_t)a->n_leaves * n_i * a->n_cb);      // A_ie
+  cv->take(es * (size_t)a->n_leaves * n_i * a->n_gauss);   // W = -A_ie P
+  cv->take(inverse_workspace_bytes(a->dtype, n_i, a->n_leaves));
+  return cv->used + 256;
+}
+
+template <class T>
+static int leaf_dtn_impl(const hps_leaf_dtn_args* a, cudaStream_t st) {
+  const int nl = a->n_leaves, np = a->n_pts, ncb = a->n_cb, ng = a->n_gauss, ns = a->nsrc;
+  const int ni = np - ncb;
+  unsigned char* wsb = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(a->workspace) + 255) & ~uintptr_t(255));
+  Carver cv(wsb);
+  T* Aie = (T*)cv.take(sizeof(T) * (size_t)nl * ni * ncb);
+  T* W = (T*)cv.take(sizeof(T) * (size_t)nl * ni * ng);
+  const size_t invb = inverse_workspace_bytes(a->dtype, ni, nl);
+  void* invws = cv.take(invb);
+  T* Aii = (T*)a->Aii_inv;
+  cudaError_t e;
+  if (a->coef_complex)
+    e = leaf_assemble<T, c128>(nl, np, ncb, ni, ncb, a->n_ops, a->ops, (const c128*)a->coeffs, Aie, ncb,
+                               (long long)ni * ncb, Aii, ni, (long long)ni * ni, st);
+  else
+    e = leaf_assemble<T, double>(nl, np, ncb, ni, ncb, a->n_ops, a->ops, (const double*)a->coeffs, Aie, ncb,
+                                 (long long)ni * ncb, Aii, ni, (long long)ni * ni, st);
+  HPS_CHECK(e);
+  HPS_CHECK(inverse_batched<T>(ni, Aii, ni, (long long)ni * ni, Aii, ni, (long long)ni * ni, nl, a->info, invws,
+                               invb, st));
+  const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
+  const T* P = (const T*)a->P;
+  const T* Q = (const T*)a->Q;
+  T* Y = (T*)a->Y;
+  // W = -A_ie P
+  HPS_CHECK(gemm_batched<T>(ni, ng, ncb, mone, Aie, ncb, (long long)ni * ncb, P, ng, 0, zero_, nullptr, 0, 0, W,
+                            ng, (long long)ni * ng, nl, st));
+  // Y[n_cb:] = A_ii^-1 W ;  Y[:n_cb] = P
+  HPS_CHECK(gemm_batched<T>(ni, ng, ni, one_, Aii, ni, (long long)ni * ni, W, ng, (long long)ni * ng, zero_,
+                            nullptr, 0, 0, Y + (size_t)ncb * ng, ng, (long long)np * ng, nl, st));
+  HPS_CHECK(set_rows<T>(nl, ncb, ng, P, ng, Y, ng, (long long)np * ng, st));
+  // T = Q Y
+  HPS_CHECK(gemm_batched<T>(ng, ng, np, one_, Q, np, 0, Y, ng, (long long)np * ng, zero_, nullptr, 0, 0,
+                            (T*)a->T, ng, (long long)ng * ng, nl, st));
+  if (ns > 0 && a->source && a->v) {
+    T* v = (T*)a->v;
+    const T* f = (const T*)a->source;
+    HPS_CHECK(gemm_batched<T>(ni, ns, ni, one_, Aii, ni, (long long)ni * ni, f + (size_t)ncb * ns, ns,
+                              (long long)np * ns, zero_, nullptr, 0, 0, v + (size_t)ncb * ns, ns,
+                              (long long)np * ns, nl, st));
+    HPS_CHECK(set_rows<T>(nl, ncb, ns, nullptr, 0, v, ns, (long long)np * ns, st));
+    if (a->h)
+      HPS_CHECK(gemm_batched<T>(ng, ns, np, one_, Q, np, 0, v, ns, (long long)np * ns, zero_, nullptr, 0, 0,
+                                (T*)a->h, ns, (long long)ng * ns, nl, st));
+  }
+  return HPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Leaf ItI
+// ---------------------------------------------------------------------------
+static size_t leaf_iti_ws(const hps_leaf_iti_args* a, Carver* cv) {
+  cv->take(inverse_workspace_bytes(a->dtype, a->n_pts, a->n_leaves));
+  return cv->used + 256;
+}
+
+template <class T>
+static int leaf_iti_impl(const hps_leaf_iti_args* a, cudaStream_t st) {
+  const int nl = a->n_leaves, np = a->n_pts, ncb = a->n_cb, ng = a->n_gauss, ns = a->nsrc;
+  const int ni = np - ncb;
+  unsigned char* wsb = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(a->workspace) + 255) & ~uintptr_t(255));
+  Carver cv(wsb);
+  const size_t invb = inverse_workspace_bytes(a->dtype, np, nl);
+  void* invws = cv.take(invb);
+  T* Bm = (T*)a->B_inv;
+  const long long sB = (long long)np * np;
+  HPS_CHECK(set_rows<T>(nl, ncb, np, (const T*)a->G, np, Bm, np, sB, st));
+  cudaError_t e;
+  if (a->coef_complex)
+    e = leaf_assemble<T, c128>(nl, np, ncb, ni, 0, a->n_ops, a->ops, (const c128*)a->coeffs, nullptr, 0, 0,
+                               Bm + (size_t)ncb * np, np, sB, st);
+  else
+    e = leaf_assemble<T, double>(nl, np, ncb, ni, 0, a->n_ops, a->ops, (const double*)a->coeffs, nullptr, 0, 0,
+                                 Bm + (size_t)ncb * np, np, sB, st);
+  HPS_CHECK(e);
+  HPS_CHECK(inverse_batched<T>(np, Bm, np, sB, Bm, np, sB, nl, a->info, invws, invb, st));
+  const T one_ = one<T>(), zero_ = zero<T>();
+  HPS_CHECK(gemm_batched<T>(np, ng, ncb, one_, Bm, np, sB, (const T*)a->P, ng, 0, zero_, nullptr, 0, 0,
+                            (T*)a->Y, ng, (long long)np * ng, nl, st));
+  HPS_CHECK(gemm_batched<T>(ng, ng, np, one_, (const T*)a->QH, np, 0, (const T*)a->Y, ng, (long long)np * ng,
+                            zero_, nullptr, 0, 0, (T*)a->T, ng, (long long)ng * ng, nl, st));
+  if (ns > 0 && a->source && a->v) {
+    HPS_CHECK(gemm_batched<T>(np, ns, ni, one_, Bm + ncb, np, sB, (const T*)a->source + (size_t)ncb * ns, ns,
+                              (long long)np * ns, zero_, nullptr, 0, 0, (T*)a->v, ns, (long long)np * ns, nl,
+                              st));
+    if (a->h)
+      HPS_CHECK(gemm_batched<T>(ng, ns, np, one_, (const T*)a->QH, np, 0, (const T*)a->v, ns,
+                                (long long)np * ns, zero_, nullptr, 0, 0, (T*)a->h, ns, (long long)ng * ns, nl,
+                                st));
+  }
+  return HPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Merge level (DtN)
+// ---------------------------------------------------------------------------
+static size_t merge_ws(const hps_merge_args* a, Carver* cv) {
+  const size_t es = dtype_size(a->dtype);
+  const size_t nm = (size_t)a->n_merges;
+  if (!a->D_inv) cv->take(es * nm * a->n_int * a->n_int);
+  cv->take(es * nm * a->n_int * a->n_ext);                       // C
+  cv->take(es * nm * a->n_ext * a->n_int);                       // B
+  cv->take(es * nm * a->n_int * (a->nsrc > 0 ? a->nsrc : 1));    // dh
+  cv->take(inverse_workspace_bytes(a->dtype, a->n_int, a->n_merges));
+  return cv->used + 256;
+}
+
+template <class T>
+static int merge_impl(const hps_merge_args* a, cudaStream_t st) {
+  const int nm = a->n_merges, ni = a->n_int, ne = a->n_ext, ns = a->nsrc;
+  unsigned char* wsb = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(a->workspace) + 255) & ~uintptr_t(255));
+  Carver cv(wsb);
+  T* D = a->D_inv ? (T*)a->D_inv : (T*)cv.take(sizeof(T) * (size_t)nm * ni * ni);
+  T* C = (T*)cv.take(sizeof(T) * (size_t)nm * ni * ne);
+  T* B = (T*)cv.take(sizeof(T) * (size_t)nm * ne * ni);
+  T* dh = (T*)cv.take(sizeof(T) * (size_t)nm * ni * (ns > 0 ? ns : 1));
+  const size_t invb = inverse_workspace_bytes(a->dtype, ni, nm);
+  void* invws = cv.take(invb);
+  const bool with_h = ns > 0 && a->h_children && a->h_out && a->g_tilde;
+  HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, with_h ? ns : 0, (const T*)a->T_children,
+                            with_h ? (const T*)a->h_children : nullptr, a->int_c, a->int_l, a->ext_c, a->ext_l,
+                            a->loc, D, C, B, (T*)a->T_out, dh, (T*)a->h_out, st));
+  HPS_CHECK(inverse_batched<T>(ni, D, ni, (long long)ni * ni, D, ni, (long long)ni * ni, nm, a->info, invws, invb,
+                               st));
+  const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
+  T* S = (T*)a->S;
+  HPS_CHECK(gemm_batched<T>(ni, ne, ni, mone, D, ni, (long long)ni * ni, C, ne, (long long)ni * ne, zero_, nullptr,
+                            0, 0, S, ne, (long long)ni * ne, nm, st));
+  HPS_CHECK(gemm_batched<T>(ne, ne, ni, one_, B, ni, (long long)ne * ni, S, ne, (long long)ni * ne, one_,
+                            (T*)a->T_out, ne, (long long)ne * ne, (T*)a->T_out, ne, (long long)ne * ne, nm, st));
+  if (with_h) {
+    HPS_CHECK(gemm_batched<T>(ni, ns, ni, mone, D, ni, (long long)ni * ni, dh, ns, (long long)ni * ns, zero_,
+                              nullptr, 0, 0, (T*)a->g_tilde, ns, (long long)ni * ns, nm, st));
+    HPS_CHECK(gemm_batched<T>(ne, ns, ni, one_, B, ni, (long long)ne * ni, (const T*)a->g_tilde, ns,
+                              (long long)ni * ns, one_, (T*)a->h_out, ns, (long long)ne * ns, (T*)a->h_out, ns,
+                              (long long)ne * ns, nm, st));
+  }
+  if (a->BD_inv)
+    HPS_CHECK(gemm_batched<T>(ne, ni, ni, one_, B, ni, (long long)ne * ni, D, ni, (long long)ni * ni, zero_,
+                              nullptr, 0, 0, (T*)a->BD_inv, ni, (long long)ne * ni, nm, st));
+  return HPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Down level
+// ---------------------------------------------------------------------------
+template <class T>
+static int down_impl(const hps_down_args* a, cudaStream_t st) {
+  const int nm = a->n_merges, ni = a->n_int, ne = a->n_ext, ns = a->nsrc;
+  const T one_ = one<T>();
+  HPS_CHECK(gemm_batched<T>(ni, ns, ne, one_, (const T*)a->S, ne, (long long)ni * ne, (const T*)a->g_parent, ns,
+                            (long long)ne * ns, one_, (const T*)a->g_tilde, ns, (long long)ni * ns, (T*)a->g_int,
+                            ns, (long long)ni * ns, nm, st));
+  HPS_CHECK(down_scatter<T>(nm, a->nch, a->nb, ne, ni, ns, a->code, (const T*)a->g_parent, (const T*)a->g_int,
+                            (T*)a->g_children, st));
+  return HPS_OK;
+}
+
+template <class T>
+static int gemm_entry(int m, int n, int k, const double* alpha, const void* A, long long lda, long long sA,
+                      const void* B, long long ldb, long long sB, const double* beta, const void* C, long long ldc,
+                      long long sC, void* D, long long ldd, long long sD, int batch, void* stream) {
+  const T al = make_scalar<T>(alpha ? alpha[0] : 1.0, alpha ? alpha[1] : 0.0);
+  const T be = make_scalar<T>(beta ? beta[0] : 0.0, beta ? beta[1] : 0.0);
+  HPS_CHECK(gemm_batched<T>(m, n, k, al, (const T*)A, lda, sA, (const T*)B, ldb, sB, be, (const T*)C, ldc, sC,
+                            (T*)D, ldd, sD, batch, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+template <class T>
+static int inverse_entry(int n, const void* A, long long lda, long long sA, void* X, long long ldx, long long sX,
+                         int batch, int* info, void* ws, size_t wsb, void* stream) {
+  HPS_CHECK(inverse_batched<T>(n, (const T*)A, lda, sA, (T*)X, ldx, sX, batch, info, ws, wsb,
+                               (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+}  // namespace hps
+
+using namespace hps;
+
+#define DISPATCH(dt, FN, ...)                                                  \
+  switch (dt) {                                                                \
+    case HPS_F64: return FN<double>(__VA_ARGS__);                              \
+    case HPS_F32: return FN<float>(__VA_ARGS__);                               \
+    case HPS_C128: return FN<c128>(__VA_ARGS__);                               \
+    case HPS_C64: return FN<c64>(__VA_ARGS__);                                 \
+    default: set_error("unknown dtype %d", (int)(dt)); return HPS_ERR_ARG;     \
+  }
+
+extern "C" {
+
+const char* hps_version(void) { return "jaxhps_gb300 0.1.0 (sm_103a)"; }
+
+int hps_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)g_last_error.size();
+}
+
+
+int hps_gemm_batched(int dtype, int m, int n, int k, const double* alpha, const void* A, long long lda,
+                     long long strideA, const void* B, long long ldb, long long strideB, const double* beta,
+                     const void* C, long long ldc, long long strideC, void* D, long long ldd, long long strideD,
+                     int batch, void* stream) {
+  if (m < 0 || n < 0 || k < 0 || batch < 0 || (!A && m * k > 0) || (!B && k * n > 0) || (!D && m * n > 0)) {
+    set_error("hps_gemm_batched: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  DISPATCH(dtype, gemm_entry, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc, strideC, D, ldd,
+           strideD, batch, stream)
+}
+
+size_t hps_inverse_workspace_size(int dtype, int n, int batch) {
+  return inverse_workspace_bytes(dtype, n, batch);
+}
+
+
+int hps_inverse_batched(int dtype, int n, const void* A, long long lda, long long strideA, void* X, long long ldx,
+                        long long strideX, int batch, int* info, void* workspace, size_t workspace_bytes,
+                        void* stream) {
+  if (n < 0 || batch < 0 || !A || !X) {
+    set_error("hps_inverse_batched: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (workspace_bytes < inverse_workspace_bytes(dtype, n, batch)) {
+    set_error("hps_inverse_batched: workspace too small (%zu < %zu)", workspace_bytes,
+              inverse_workspace_bytes(dtype, n, batch));
+    return HPS_ERR_WORKSPACE;
+  }
+  DISPATCH(dtype, inverse_entry, n, A, lda, strideA, X, ldx, strideX, batch, info, workspace, workspace_bytes,
+           stream)
+}
+
+int hps_convert(int ds, int dd, long long n, const void* src, void* dst, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!src || !dst || n < 0) {
+    set_error("hps_convert: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (ds == HPS_F64 && dd == HPS_F32) HPS_CHECK(convert<double, float>(n, (const double*)src, (float*)dst, st));
+  else if (ds == HPS_F32 && dd == HPS_F64) HPS_CHECK(convert<float, double>(n, (const float*)src, (double*)dst, st));
+  else if (ds == HPS_C128 && dd == HPS_C64) HPS_CHECK(convert<c128, c64>(n, (const c128*)src, (c64*)dst, st));
+  else if (ds == HPS_C64 && dd == HPS_C128) HPS_CHECK(convert<c64, c128>(n, (const c64*)src, (c128*)dst, st));
+  else {
+    set_error("hps_convert: unsupported pair %d -> %d", ds, dd);
+    return HPS_ERR_ARG;
+  }
+  return HPS_OK;
+}
+
+size_t hps_local_solve_dtn_workspace_size(const hps_leaf_dtn_args* a) {
+  Carver cv(nullptr);
+  return leaf_dtn_ws(a, &cv);
+}
+
+int hps_local_solve_dtn(const hps_leaf_dtn_args* a, void* stream) {
+  if (!a || a->n_leaves <= 0 || a->n_pts <= a->n_cb || a->n_cb <= 0 || a->n_gauss <= 0 || a->n_ops <= 0 ||
+      !a->ops || !a->coeffs || !a->P || !a->Q || !a->Y || !a->T || !a->Aii_inv) {
+    set_error("hps_local_solve_dtn: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (a->nsrc > 0 && (!a->source || !a->v || !a->h)) {
+    set_error("hps_local_solve_dtn: nsrc > 0 needs source, v and h");
+    return HPS_ERR_ARG;
+  }
+  if (a->workspace_bytes < hps_local_solve_dtn_workspace_size(a)) {
+    set_error("hps_local_solve_dtn: workspace too small (%zu < %zu)", a->workspace_bytes,
+              hps_local_solve_dtn_workspace_size(a));
+    return HPS_ERR_WORKSPACE;
+  }
+  DISPATCH(a->dtype, leaf_dtn_impl, a, (cudaStream_t)stream)
+}
+
+size_t hps_local_solve_iti_workspace_size(const hps_leaf_iti_args* a) {
+  Carver cv(nullptr);
+  return leaf_iti_ws(a, &cv);
+}
+
+int hps_local_solve_iti(const hps_leaf_iti_args* a, void* stream) {
+  if (!a || a->n_leaves <= 0 || a->n_pts <= a->n_cb || a->n_cb <= 0 || a->n_gauss <= 0 || a->n_ops <= 0 ||
+      !a->ops || !a->coeffs || !a->G || !a->P || !a->QH || !a->Y || !a->T || !a->B_inv ||
+      (a->dtype != HPS_C128 && a->dtype != HPS_C64)) {
+    set_error("hps_local_solve_iti: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (a->nsrc > 0 && (!a->source || !a->v || !a->h)) {
+    set_error("hps_local_solve_iti: nsrc > 0 needs source, v and h");
+    return HPS_ERR_ARG;
+  }
+  if (a->workspace_bytes < hps_local_solve_iti_workspace_size(a)) {
+    set_error("hps_local_solve_iti: workspace too small");
+    return HPS_ERR_WORKSPACE;
+  }
+  if (a->dtype == HPS_C128) return leaf_iti_impl<c128>(a, (cudaStream_t)stream);
+  return leaf_iti_impl<c64>(a, (cudaStream_t)stream);
+}
+
+size_t hps_merge_level_dtn_workspace_size(const hps_merge_args* a) {
+  Carver cv(nullptr);
+  return merge_ws(a, &cv);
+}
+
+int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
+  if (!a || a->n_merges <= 0 || a->nch <= 0 || a->nb <= 0 || a->n_int <= 0 || a->n_ext <= 0 || !a->T_children ||
+      !a->int_c || !a->int_l || !a->ext_c || !a->ext_l || !a->loc || !a->S || !a->T_out) {
+    set_error("hps_merge_level_dtn: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (a->workspace_bytes < hps_merge_level_dtn_workspace_size(a)) {
+    set_error("hps_merge_level_dtn: workspace too small (%zu < %zu)", a->workspace_bytes,
+              hps_merge_level_dtn_workspace_size(a));
+    return HPS_ERR_WORKSPACE;
+  }
+  DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream)
+}
+
+int hps_down_level(const hps_down_args* a, void* stream) {
+  if (!a || a->n_merges <= 0 || a->nsrc <= 0 || !a->S || !a->g_parent || !a->code || !a->g_int ||
+      !a->g_children) {
+    set_error("hps_down_level: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  DISPATCH(a->dtype, down_impl, a, (cudaStream_t)stream)
+}
+
+}  // extern "C"

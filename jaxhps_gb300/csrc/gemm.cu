@@ -1,0 +1,172 @@
+// Strided-batched GEMM on CUDA cores:  D = alpha * A @ B + beta * C
+// (row-major, every operand with its own leading dimension and batch
+// stride; a batch stride of 0 broadcasts one operand to the whole batch).
+//
+// This is the workhorse of every HPS stage: leaf operator products
+// (Y = A_ii^-1 (-A_ie P), T = Q Y), the Schur-complement products of the
+// merges (S = -D^-1 C, T = A + B S) and the down pass (g = S g + g~,
+// u = Y g + v).  Register-tiled, double-buffered through shared memory,
+// templated over the element type so the same code serves f64 / f32 /
+// complex128 / complex64.
+#include "hps_common.cuh"
+#include "hps_internal.h"
+
+namespace hps {
+
+template <class T, int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+gemm_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, long long lda, long long sA,
+            const T* __restrict__ B, long long ldb, long long sB, T beta, const T* C,
+            long long ldc, long long sC, T* D, long long ldd, long long sD, int use_c) {
+  constexpr int NTX = BN / TN;
+  constexpr int NTY = BM / TM;
+  constexpr int NT = NTX * NTY;
+  constexpr int LA = (BM * BK + NT - 1) / NT;
+  constexpr int LB = (BK * BN + NT - 1) / NT;
+  __shared__ T As[2][BK][BM + 1];
+  __shared__ T Bs[2][BK][BN];
+
+  const long long bz = blockIdx.z;
+  A += bz * sA;
+  B += bz * sB;
+  D += bz * sD;
+  if (use_c) C += bz * sC;
+  const int m0 = blockIdx.y * BM;
+  const int n0 = blockIdx.x * BN;
+  const int tid = threadIdx.x;
+  const int tx = tid % NTX;
+  const int ty = tid / NTX;
+
+  T ra[LA], rb[LB];
+  auto load_tiles = [&](int k0) {
+#pragma unroll
+    for (int l = 0; l < LA; ++l) {
+      int e = tid + l * NT;
+      T v = zero<T>();
+      if (e < BM * BK) {
+        int r = e / BK, c = e % BK;
+        int gm = m0 + r, gk = k0 + c;
+        if (gm < M && gk < K) v = A[(long long)gm * lda + gk];
+      }
+      ra[l] = v;
+    }
+#pragma unroll
+    for (int l = 0; l < LB; ++l) {
+      int e = tid + l * NT;
+      T v = zero<T>();
+      if (e < BK * BN) {
+        int r = e / BN, c = e % BN;
+        int gk = k0 + r, gn = n0 + c;
+        if (gk < K && gn < N) v = B[(long long)gk * ldb + gn];
+      }
+      rb[l] = v;
+    }
+  };
+  auto store_tiles = [&](int buf) {
+#pragma unroll
+    for (int l = 0; l < LA; ++l) {
+      int e = tid + l * NT;
+      if (e < BM * BK) As[buf][e % BK][e / BK] = ra[l];
+    }
+#pragma unroll
+    for (int l = 0; l < LB; ++l) {
+      int e = tid + l * NT;
+      if (e < BK * BN) Bs[buf][e / BN][e % BN] = rb[l];
+    }
+  };
+
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = zero<T>();
+
+  const int ktiles = (K + BK - 1) / BK;
+  if (ktiles > 0) {
+    load_tiles(0);
+    store_tiles(0);
+    __syncthreads();
+  }
+  for (int kt = 0; kt < ktiles; ++kt) {
+    const int buf = kt & 1;
+    if (kt + 1 < ktiles) load_tiles((kt + 1) * BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[buf][kk][ty + i * NTY];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[buf][kk][tx + j * NTX];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma_(a[i], b[j], acc[i][j]);
+    }
+    if (kt + 1 < ktiles) {
+      store_tiles(buf ^ 1);
+      __syncthreads();
+    }
+  }
+
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int gm = m0 + ty + i * NTY;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int gn = n0 + tx + j * NTX;
+      if (gn >= N) continue;
+      T v = mul(alpha, acc[i][j]);
+      if (use_c) v = fma_(beta, C[(long long)gm * ldc + gn], v);
+      D[(long long)gm * ldd + gn] = v;
+    }
+  }
+}
+
+template <class T, int BM, int BN, int BK, int TM, int TN>
+static cudaError_t launch_gemm_cfg(int M, int N, int K, T alpha, const T* A, long long lda, long long sA,
+                                   const T* B, long long ldb, long long sB, T beta, const T* C,
+                                   long long ldc, long long sC, T* D, long long ldd, long long sD,
+                                   int batch, cudaStream_t st) {
+  const int use_c = (C != nullptr);
+  constexpr int NT = (BM / TM) * (BN / TN);
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, nb);
+    gemm_kernel<T, BM, BN, BK, TM, TN><<<grid, NT, 0, st>>>(
+        M, N, K, alpha, A + b0 * sA, lda, sA, B + b0 * sB, ldb, sB, beta,
+        use_c ? C + b0 * sC : nullptr, ldc, sC, D + b0 * sD, ldd, sD, use_c);
+  }
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda, long long sA,
+                         const T* B, long long ldb, long long sB, T beta, const T* C, long long ldc,
+                         long long sC, T* D, long long ldd, long long sD, int batch, cudaStream_t st) {
+  if (M <= 0 || N <= 0 || batch <= 0) return cudaSuccess;
+  if (sizeof(T) == 4) {
+    const long long tiles128 = (long long)((M + 127) / 128) * ((N + 127) / 128) * batch;
+    if (M >= 96 && N >= 96 && tiles128 >= 120)
+      return launch_gemm_cfg<T, 128, 128, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
+                                                   ldc, sC, D, ldd, sD, batch, st);
+    return launch_gemm_cfg<T, 64, 64, 8, 4, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
+                                               sC, D, ldd, sD, batch, st);
+  }
+  if (sizeof(T) == 16 && M <= 32 && N <= 32)
+    return launch_gemm_cfg<T, 32, 32, 8, 2, 2>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
+                                               sC, D, ldd, sD, batch, st);
+  return launch_gemm_cfg<T, 64, 64, 8, 4, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
+                                             sC, D, ldd, sD, batch, st);
+}
+
+#define HPS_INST_GEMM(T)                                                                          \
+  template cudaError_t gemm_batched<T>(int, int, int, T, const T*, long long, long long, const T*, \
+                                       long long, long long, T, const T*, long long, long long,    \
+                                       T*, long long, long long, int, cudaStream_t);
+HPS_INST_GEMM(float)
+HPS_INST_GEMM(double)
+HPS_INST_GEMM(c64)
+HPS_INST_GEMM(c128)
+
+}  // namespace hps

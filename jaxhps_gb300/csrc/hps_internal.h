@@ -1,0 +1,33 @@
+// Internal (C++) interfaces shared between the translation units of the
+// native library.  The public boundary is the C ABI in include/jaxhps_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "hps_common.cuh"
+
+namespace hps {
+
+// D = alpha*A@B + beta*C over a strided batch (row-major).  C may be null
+// (then beta is ignored) and may alias D.
+template <class T>
+cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda, long long sA,
+                         const T* B, long long ldb, long long sB, T beta, const T* C, long long ldc,
+                         long long sC, T* D, long long ldd, long long sD, int batch, cudaStream_t st);
+
+// Batched inverse by Gauss-Jordan elimination with partial (row) pivoting.
+// X may alias A.  info[b] = 0 on success, k+1 if the k-th pivot was zero.
+size_t inverse_workspace_bytes(int dtype, int n, int batch);
+template <class T>
+cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
+                            long long sX, int batch, int* info, void* ws, size_t ws_bytes,
+                            cudaStream_t st);
+
+// Largest n served by the register-resident single-CTA kernel.
+int inverse_small_nmax(int dtype);
+
+// Records an error message for hps_last_error().
+void set_error(const char* fmt, ...);
+
+}  // namespace hps

@@ -1,0 +1,280 @@
+// HPS data-movement kernels: leaf operator assembly, merge block gather
+// and down-pass scatter.  The index bookkeeping of the reference (child
+// side orderings, interface flips, the exterior roll after a merge) is
+// precomputed on the host as small integer maps and applied here, so one
+// kernel serves 2D quad merges and 3D oct merges alike.
+#include "hps_common.cuh"
+#include "hps_internal.h"
+
+namespace hps {
+
+// ---------------------------------------------------------------------------
+// Leaf operator assembly  (reference: local_solve/_uniform_2D_DtN.py:182-225)
+//
+// For interior row i (global row row0+i) of every leaf l:
+//   A[l][row0+i][j] = sum_o coeff[o][l][row0+i] * ops[o][row0+i][j]
+// Columns j < col_split go to out_lo[l][i][j], the rest to
+// out_hi[l][i][j-col_split].  One CTA per (row, leaf group); the operator
+// rows are staged in shared memory once and reused for the whole group.
+// ---------------------------------------------------------------------------
+template <class T, class CT>
+__global__ void leaf_assemble_kernel(int n_leaves, int n_pts, int row0, int col_split, int n_ops,
+                                     const double* __restrict__ ops, const CT* __restrict__ coeffs,
+                                     T* out_lo, long long ld_lo, long long s_lo, T* out_hi,
+                                     long long ld_hi, long long s_hi, int leaves_per_cta, int l_base) {
+  extern __shared__ double ds[];  // [n_ops][n_pts]
+  const int i = blockIdx.x;
+  const int row = row0 + i;
+  for (int e = threadIdx.x; e < n_ops * n_pts; e += blockDim.x) {
+    const int o = e / n_pts, j = e % n_pts;
+    ds[e] = ops[((long long)o * n_pts + row) * n_pts + j];
+  }
+  __syncthreads();
+  const int l0 = l_base + blockIdx.y * leaves_per_cta;
+  const int l1 = min(n_leaves, l0 + leaves_per_cta);
+  for (int l = l0; l < l1; ++l) {
+    for (int j = threadIdx.x; j < n_pts; j += blockDim.x) {
+      CT acc;
+      if constexpr (sizeof(CT) == 8) {
+        acc = 0.0;
+        for (int o = 0; o < n_ops; ++o)
+          acc = fma(coeffs[((long long)o * n_leaves + l) * n_pts + row], ds[o * n_pts + j], acc);
+      } else {
+        acc = c128{0.0, 0.0};
+        for (int o = 0; o < n_ops; ++o) {
+          const CT c = coeffs[((long long)o * n_leaves + l) * n_pts + row];
+          const double d = ds[o * n_pts + j];
+          acc.x = fma(c.x, d, acc.x);
+          acc.y = fma(c.y, d, acc.y);
+        }
+      }
+      T v;
+      if constexpr (sizeof(CT) == 8) v = from_real<T>(acc);
+      else v = from_c128<T>(acc);
+      if (j < col_split) out_lo[l * s_lo + (long long)i * ld_lo + j] = v;
+      else out_hi[l * s_hi + (long long)i * ld_hi + (j - col_split)] = v;
+    }
+  }
+}
+
+template <class T, class CT>
+cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col_split, int n_ops,
+                          const double* ops, const CT* coeffs, T* out_lo, long long ld_lo, long long s_lo,
+                          T* out_hi, long long ld_hi, long long s_hi, cudaStream_t st) {
+  const int lpc = 32;
+  const size_t smem = sizeof(double) * (size_t)n_ops * n_pts;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(leaf_assemble_kernel<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+  const int gy = (n_leaves + lpc - 1) / lpc;
+  for (int y0 = 0; y0 < gy; y0 += 65535) {
+    const int ny = gy - y0 < 65535 ? gy - y0 : 65535;
+    dim3 grid(n_rows, ny);
+    leaf_assemble_kernel<T, CT><<<grid, 256, smem, st>>>(n_leaves, n_pts, row0, col_split, n_ops, ops, coeffs,
+                                                         out_lo, ld_lo, s_lo, out_hi, ld_hi, s_hi, lpc,
+                                                         y0 * lpc);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// dst[b][r][c] = src[r][c] (or 0 when src is null) for r < rows, c < cols.
+// Used for the Chebyshev-boundary rows of Y (= P) and of v (= 0).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void set_rows_kernel(int rows, int cols, const T* src, long long lds, T* dst, long long ldd,
+                                long long sd) {
+  const long long b = blockIdx.y;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols; e += gridDim.x * blockDim.x) {
+    const int r = e / cols, c = e % cols;
+    dst[b * sd + (long long)r * ldd + c] = src ? src[(long long)r * lds + c] : zero<T>();
+  }
+}
+
+template <class T>
+cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds, T* dst, long long ldd,
+                     long long sd, cudaStream_t st) {
+  if (batch <= 0 || rows <= 0 || cols <= 0) return cudaSuccess;
+  int gx = (rows * cols + 255) / 256;
+  if (gx > 64) gx = 64;
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    set_rows_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(rows, cols, src, lds, dst + b0 * sd, ldd, sd);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Merge gather  (reference: merge/_uniform_2D_DtN.py:206-475,
+// merge/_schur_complement.py:182-237, 3D: merge/_schur_complement.py:293-774)
+//
+// Children of merge m are nodes m*nch .. m*nch+nch-1, each with a boundary
+// of nb points.  Index maps (shared by all merges of a level):
+//   int_c/int_l [2*n_int] : the two (child, local) copies of interface i
+//   ext_c/ext_l [n_ext]   : (child, local) of exterior point e (final order)
+//   loc [nch*n_int]       : local index of interface i in child c, or -1
+// Outputs per merge:
+//   D[i][j]  = sum over the children holding both i and j of T_c[i][j]
+//   C[i][e]  = T_c(e)[i][e]        B[e][j] = T_c(e)[e][j]
+//   Tout[e][f] = T_c[e][f] if e, f on the same child else 0   (the A blocks)
+//   dh[i]    = sum of the two children's h at i,   hext[e] = h_c(e)[e]
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int ns, const T* __restrict__ Tc,
+                                    const T* __restrict__ hc, const int* __restrict__ int_c,
+                                    const int* __restrict__ int_l, const int* __restrict__ ext_c,
+                                    const int* __restrict__ ext_l, const int* __restrict__ loc, T* D, T* C,
+                                    T* B, T* Tout, T* dh, T* hext, long long m_base) {
+  const long long m = blockIdx.y + m_base;
+  const int seg = blockIdx.z;
+  const long long nbb = (long long)nb * nb;
+  const T* Tm = Tc + m * nch * nbb;
+  const T* hm = hc ? hc + m * nch * (long long)nb * ns : nullptr;
+  long long cnt;
+  switch (seg) {
+    case 0: cnt = (long long)n_int * n_int; break;
+    case 1: cnt = (long long)n_int * n_ext; break;
+    case 2: cnt = (long long)n_ext * n_int; break;
+    case 3: cnt = (long long)n_ext * n_ext; break;
+    case 4: cnt = hm ? (long long)n_int * ns : 0; break;
+    default: cnt = hm ? (long long)n_ext * ns : 0; break;
+  }
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt;
+       e += (long long)gridDim.x * blockDim.x) {
+    T v = zero<T>();
+    if (seg == 0) {
+      const int i = (int)(e / n_int), j = (int)(e % n_int);
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int c = int_c[2 * i + t];
+        if (c < 0) continue;
+        const int lj = loc[c * n_int + j];
+        if (lj >= 0) v = add(v, Tm[c * nbb + (long long)int_l[2 * i + t] * nb + lj]);
+      }
+      D[m * n_int * (long long)n_int + e] = v;
+    } else if (seg == 1) {
+      const int i = (int)(e / n_ext), x = (int)(e % n_ext);
+      const int c = ext_c[x];
+      const int li = loc[c * n_int + i];
+      if (li >= 0) v = Tm[c * nbb + (long long)li * nb + ext_l[x]];
+      C[m * n_int * (long long)n_ext + e] = v;
+    } else if (seg == 2) {
+      const int x = (int)(e / n_int), j = (int)(e % n_int);
+      const int c = ext_c[x];
+      const int lj = loc[c * n_int + j];
+      if (lj >= 0) v = Tm[c * nbb + (long long)ext_l[x] * nb + lj];
+      B[m * n_ext * (long long)n_int + e] = v;
+    } else if (seg == 3) {
+      const int x = (int)(e / n_ext), y = (int)(e % n_ext);
+      const int c = ext_c[x];
+      if (ext_c[y] == c) v = Tm[c * nbb + (long long)ext_l[x] * nb + ext_l[y]];
+      Tout[m * n_ext * (long long)n_ext + e] = v;
+    } else if (seg == 4) {
+      const int i = (int)(e / ns), s = (int)(e % ns);
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        const int c = int_c[2 * i + t];
+        if (c < 0) continue;
+        v = add(v, hm[(c * (long long)nb + int_l[2 * i + t]) * ns + s]);
+      }
+      dh[m * n_int * (long long)ns + e] = v;
+    } else {
+      const int x = (int)(e / ns), s = (int)(e % ns);
+      v = hm[(ext_c[x] * (long long)nb + ext_l[x]) * ns + s];
+      hext[m * n_ext * (long long)ns + e] = v;
+    }
+  }
+}
+
+template <class T>
+cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Tc, const T* hc,
+                         const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
+                         const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, cudaStream_t st) {
+  long long big = (long long)n_ext * n_ext;
+  int gx = (int)((big + 255) / 256);
+  if (gx > 512) gx = 512;
+  for (int m0 = 0; m0 < n_merges; m0 += 65535) {
+    const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    merge_gather_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Tc, hc, int_c, int_l,
+                                                            ext_c, ext_l, loc, D, C, B, Tout, dh, hext, m0);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Down-pass scatter  (reference: down_pass/_uniform_2D_DtN.py:125-189)
+// child boundary point (c, k) takes parent exterior value code>=0 or
+// interface value -(code+1).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void down_scatter_kernel(int nch, int nb, int n_ext, int n_int, int ns, const int* __restrict__ code,
+                                    const T* __restrict__ gpar, const T* __restrict__ gint, T* gch,
+                                    long long m_base) {
+  const long long m = blockIdx.y + m_base;
+  const long long cnt = (long long)nch * nb * ns;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(e % ns);
+    const int ck = (int)(e / ns);  // c*nb + k
+    const int cd = code[ck];
+    const T v = (cd >= 0) ? gpar[(m * n_ext + cd) * ns + s] : gint[(m * n_int + (-cd - 1)) * ns + s];
+    gch[m * cnt + e] = v;
+  }
+}
+
+template <class T>
+cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, int ns, const int* code,
+                         const T* gpar, const T* gint, T* gch, cudaStream_t st) {
+  long long cnt = (long long)nch * nb * ns;
+  int gx = (int)((cnt + 255) / 256);
+  if (gx > 256) gx = 256;
+  for (int m0 = 0; m0 < n_merges; m0 += 65535) {
+    const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    down_scatter_kernel<T><<<dim3(gx, nm), 256, 0, st>>>(nch, nb, n_ext, n_int, ns, code, gpar, gint, gch, m0);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Element-type conversion (f64 <-> f32, c128 <-> c64)
+// ---------------------------------------------------------------------------
+template <class S, class D>
+__global__ void convert_kernel(long long n, const S* __restrict__ src, D* __restrict__ dst) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    if constexpr (sizeof(S) == sizeof(D) * 2 && sizeof(D) == 4) dst[e] = (D)src[e];
+    else if constexpr (sizeof(D) == sizeof(S) * 2 && sizeof(S) == 4) dst[e] = (D)src[e];
+    else if constexpr (sizeof(S) == 16) dst[e] = D{(float)src[e].x, (float)src[e].y};
+    else dst[e] = D{(double)src[e].x, (double)src[e].y};
+  }
+}
+
+template <class S, class D>
+cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  long long g = (n + 255) / 256;
+  if (g > 4096) g = 4096;
+  convert_kernel<S, D><<<(int)g, 256, 0, st>>>(n, src, dst);
+  return cudaGetLastError();
+}
+
+// explicit instantiations
+#define HPS_INST_K(T)                                                                                          \
+  template cudaError_t leaf_assemble<T, double>(int, int, int, int, int, int, const double*, const double*, T*, \
+                                                long long, long long, T*, long long, long long, cudaStream_t);  \
+  template cudaError_t leaf_assemble<T, c128>(int, int, int, int, int, int, const double*, const c128*, T*,     \
+                                              long long, long long, T*, long long, long long, cudaStream_t);    \
+  template cudaError_t set_rows<T>(int, int, int, const T*, long long, T*, long long, long long, cudaStream_t); \
+  template cudaError_t merge_gather<T>(int, int, int, int, int, int, const T*, const T*, const int*, const int*, \
+                                       const int*, const int*, const int*, T*, T*, T*, T*, T*, T*, cudaStream_t); \
+  template cudaError_t down_scatter<T>(int, int, int, int, int, int, const int*, const T*, const T*, T*,        \
+                                       cudaStream_t);
+HPS_INST_K(float)
+HPS_INST_K(double)
+HPS_INST_K(c64)
+HPS_INST_K(c128)
+template cudaError_t convert<double, float>(long long, const double*, float*, cudaStream_t);
+template cudaError_t convert<float, double>(long long, const float*, double*, cudaStream_t);
+template cudaError_t convert<c128, c64>(long long, const c128*, c64*, cudaStream_t);
+template cudaError_t convert<c64, c128>(long long, const c64*, c128*, cudaStream_t);
+
+}  // namespace hps

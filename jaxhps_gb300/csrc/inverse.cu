@@ -1,0 +1,514 @@
+// Batched matrix inverse by Gauss-Jordan elimination with partial pivoting.
+//
+// The reference forms every leaf and merge operator through explicit
+// inverses (jnp.linalg.inv at local_solve/_uniform_2D_DtN.py:257,
+// local_solve/_uniform_2D_ItI.py:167, merge/_schur_complement.py:107,146);
+// this file is the GPU replacement for those calls.
+//
+// Pivoting is "implicit": rows are never moved.  Column k is eliminated
+// with the largest-magnitude entry among rows not yet used as pivots; the
+// in-place tableau then holds inv(A) up to a row/column relabelling that is
+// undone on write-out:  inv(A)[k][j] = M[piv[k]][rinv[j]].
+//
+// Two implementations:
+//  * inv_reg_kernel  - one 512-thread CTA per matrix, the whole matrix held
+//    in registers (block-cyclic over a 32x16 thread grid).  Two barriers
+//    per pivot; the rank-1 update reads one column and one scaled row from
+//    shared memory.  Serves n <= 208 (f32), 128 (f64, c64), 64 (c128).
+//  * blocked GJE     - panels of BP columns: one CTA per matrix selects the
+//    pivots of the panel (tableau restricted to the panel columns), then
+//    the block sweep is applied to the rest of the matrix by two batched
+//    GEMMs and a row scatter:
+//        M[Rbar,Cbar] += U G,   M[R,Cbar] = E G,
+//    with U = new panel (pivot rows zeroed), G = pivot rows (panel columns
+//    zeroed), E = inv(A[R,C]) (the panel's pivot rows after elimination).
+#include <stdio.h>
+
+#include "hps_common.cuh"
+#include "hps_internal.h"
+
+namespace hps {
+
+// --------------------------------------------------------------------------
+// Register-resident single-CTA kernel
+// --------------------------------------------------------------------------
+template <class T, int NMAX>
+__global__ void __launch_bounds__(512, 1)
+inv_reg_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* X, long long ldx,
+               long long sX, int* info) {
+  constexpr int TY = 32, TX = 16;
+  constexpr int RM = (NMAX + TY - 1) / TY;
+  constexpr int RN = (NMAX + TX - 1) / TX;
+  __shared__ T colbuf[2][NMAX];
+  __shared__ T rowbuf[2][NMAX];
+  __shared__ int piv[NMAX];
+  __shared__ int colof[NMAX];
+  __shared__ unsigned char used[NMAX];
+  __shared__ int s_info;
+
+  const long long bb = blockIdx.x;
+  const T* Ab = A + bb * sA;
+  const int tid = threadIdx.x;
+  const int ty = tid / TX, tx = tid % TX, lane = tid & 31;
+
+  T m[RM][RN];
+#pragma unroll
+  for (int a = 0; a < RM; ++a)
+#pragma unroll
+    for (int c = 0; c < RN; ++c) {
+      const int i = ty + TY * a, j = tx + TX * c;
+      m[a][c] = (i < n && j < n) ? Ab[(long long)i * lda + j] : zero<T>();
+    }
+  for (int i = tid; i < NMAX; i += blockDim.x) used[i] = (i < n) ? 0 : 1;
+  if (tid == 0) s_info = 0;
+  __syncthreads();
+
+  for (int k = 0; k < n; ++k) {
+    const int buf = k & 1;
+    const int kx = k % TX, kc = k / TX;
+    // (1) publish column k
+    if (tx == kx) {
+#pragma unroll
+      for (int a = 0; a < RM; ++a) {
+        const int i = ty + TY * a;
+        T v = zero<T>();
+#pragma unroll
+        for (int c = 0; c < RN; ++c)
+          if (c == kc) v = m[a][c];
+        if (i < n) colbuf[buf][i] = v;
+      }
+    }
+    __syncthreads();
+    // (2) pivot row: every warp computes the same argmax redundantly
+    double best = -1.0;
+    int bi = n;
+    for (int i = lane; i < n; i += 32) {
+      if (!used[i]) {
+        double mg = pivmag(colbuf[buf][i]);
+        if (mg != mg) mg = __longlong_as_double(0x7ff0000000000000LL);
+        if (mg > best) {
+          best = mg;
+          bi = i;
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    const int r = bi;
+    T pinv = zero<T>();
+    if (best > 0.0) {
+      pinv = rcp_(colbuf[buf][r]);
+    } else if (tid == 0 && s_info == 0) {
+      s_info = k + 1;
+    }
+    // (3) publish the scaled pivot row
+    const int ry = r % TY, ra = r / TY;
+    if (ty == ry) {
+#pragma unroll
+      for (int a = 0; a < RM; ++a) {
+        if (a != ra) continue;
+#pragma unroll
+        for (int c = 0; c < RN; ++c) {
+          const int j = tx + TX * c;
+          if (j < n) rowbuf[buf][j] = mul(m[a][c], pinv);
+        }
+      }
+    }
+    __syncthreads();
+    // (4) rank-1 update of the register tile, then row r / column k fix-ups
+    T rj[RN];
+#pragma unroll
+    for (int c = 0; c < RN; ++c) {
+      const int j = tx + TX * c;
+      rj[c] = (j < n) ? rowbuf[buf][j] : zero<T>();
+    }
+#pragma unroll
+    for (int a = 0; a < RM; ++a) {
+      const int i = ty + TY * a;
+      const T ci = (i < n) ? colbuf[buf][i] : zero<T>();
+#pragma unroll
+      for (int c = 0; c < RN; ++c) m[a][c] = fms_(ci, rj[c], m[a][c]);
+    }
+    if (ty == ry) {
+#pragma unroll
+      for (int a = 0; a < RM; ++a)
+        if (a == ra) {
+#pragma unroll
+          for (int c = 0; c < RN; ++c) m[a][c] = rj[c];
+        }
+    }
+    if (tx == kx) {
+#pragma unroll
+      for (int a = 0; a < RM; ++a) {
+        const int i = ty + TY * a;
+        T nv = (i < n) ? neg(mul(colbuf[buf][i], pinv)) : zero<T>();
+        if (i == r) nv = pinv;
+#pragma unroll
+        for (int c = 0; c < RN; ++c)
+          if (c == kc) m[a][c] = nv;
+      }
+    }
+    if (tid == 0) {
+      used[r] = 1;
+      piv[k] = r;
+      colof[r] = k;
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && info) info[bb] = s_info;
+  T* Xb = X + bb * sX;
+#pragma unroll
+  for (int a = 0; a < RM; ++a)
+#pragma unroll
+    for (int c = 0; c < RN; ++c) {
+      const int i = ty + TY * a, j = tx + TX * c;
+      if (i < n && j < n) Xb[(long long)colof[i] * ldx + piv[j]] = m[a][c];
+    }
+}
+
+// --------------------------------------------------------------------------
+// Blocked Gauss-Jordan (global-memory tableau)
+// --------------------------------------------------------------------------
+constexpr int BP = 32;       // panel width
+constexpr int PANEL_NT = 512;
+
+struct GjeWs {
+  // per-matrix region sizes (elements / bytes), each 256-byte aligned
+  size_t mat, pan, u, g, h, e, piv, rinv, used, per;
+};
+
+static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static GjeWs gje_layout(size_t es, int n) {
+  GjeWs w;
+  w.mat = al256(es * (size_t)n * n);
+  w.pan = al256(es * (size_t)n * (BP + 1));
+  w.u = al256(es * (size_t)n * BP);
+  w.g = al256(es * (size_t)BP * n);
+  w.h = al256(es * (size_t)BP * n);
+  w.e = al256(es * (size_t)BP * BP);
+  w.piv = al256(4 * (size_t)n);
+  w.rinv = al256(4 * (size_t)n);
+  w.used = al256((size_t)n);
+  w.per = w.mat + w.pan + w.u + w.g + w.h + w.e + w.piv + w.rinv + w.used;
+  return w;
+}
+
+template <class T>
+__global__ void gje_copy_in_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* Mat,
+                                   unsigned char* used) {
+  const long long b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long i = e / n, j = e % n;
+    Mat[b * nn + e] = A[b * sA + i * lda + j];
+  }
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) used[b * n + i] = 0;
+}
+
+template <class T>
+__global__ void __launch_bounds__(PANEL_NT)
+gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G, T* E, int* piv,
+                 unsigned char* used, int* info) {
+  const long long b = blockIdx.x;
+  const long long nn = (long long)n * n;
+  T* M = Mat + b * nn;
+  int* pv = piv + b * n;
+  unsigned char* us = used + b * n;
+  constexpr int ldp = BP + 1;
+  extern __shared__ unsigned char smraw[];
+  T* P = use_smem ? reinterpret_cast<T*>(smraw) : Pw + b * (long long)n * ldp;
+  __shared__ T rowr[BP];
+  __shared__ int Rs[BP];
+  __shared__ double wbest[PANEL_NT / 32];
+  __shared__ int widx[PANEL_NT / 32];
+  __shared__ int s_r;
+  __shared__ double s_best;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  for (int e = tid; e < n * bw; e += PANEL_NT) {
+    const int i = e / bw, c = e % bw;
+    P[i * ldp + c] = M[(long long)i * n + k0 + c];
+  }
+  __syncthreads();
+
+  for (int c = 0; c < bw; ++c) {
+    double best = -1.0;
+    int bi = n;
+    for (int i = tid; i < n; i += PANEL_NT) {
+      if (!us[i]) {
+        double mg = pivmag(P[i * ldp + c]);
+        if (mg != mg) mg = __longlong_as_double(0x7ff0000000000000LL);
+        if (mg > best) {
+          best = mg;
+          bi = i;
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      wbest[warp] = best;
+      widx[warp] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double bb = wbest[0];
+      int bx = widx[0];
+      for (int w = 1; w < PANEL_NT / 32; ++w)
+        if (wbest[w] > bb || (wbest[w] == bb && widx[w] < bx)) {
+          bb = wbest[w];
+          bx = widx[w];
+        }
+      s_r = bx;
+      s_best = bb;
+      us[bx] = 2;  // pivot of the current panel
+      pv[k0 + c] = bx;
+      Rs[c] = bx;
+      if (!(bb > 0.0) && info && info[b] == 0) info[b] = k0 + c + 1;
+    }
+    __syncthreads();
+    const int r = s_r;
+    const T pinv = (s_best > 0.0) ? rcp_(P[r * ldp + c]) : zero<T>();
+    for (int c2 = tid; c2 < bw; c2 += PANEL_NT) rowr[c2] = mul(P[r * ldp + c2], pinv);
+    __syncthreads();
+    for (int i = tid; i < n; i += PANEL_NT) {
+      T* row = P + i * ldp;
+      if (i == r) {
+        for (int c2 = 0; c2 < bw; ++c2) row[c2] = rowr[c2];
+        row[c] = pinv;
+      } else {
+        const T f = row[c];
+        for (int c2 = 0; c2 < bw; ++c2) row[c2] = fms_(f, rowr[c2], row[c2]);
+        row[c] = neg(mul(f, pinv));
+      }
+    }
+    __syncthreads();
+  }
+
+  // outputs: new panel back into M, U (pivot rows zeroed), E, G
+  T* Ub = U + b * (long long)n * BP;
+  T* Gb = G + b * (long long)BP * n;
+  T* Eb = E + b * (long long)BP * BP;
+  for (int e = tid; e < n * bw; e += PANEL_NT) {
+    const int i = e / bw, c = e % bw;
+    const T v = P[i * ldp + c];
+    M[(long long)i * n + k0 + c] = v;
+    Ub[(long long)i * BP + c] = (us[i] == 2) ? zero<T>() : v;
+  }
+  for (int e = tid; e < bw * bw; e += PANEL_NT) {
+    const int c1 = e / bw, c2 = e % bw;
+    Eb[c1 * BP + c2] = P[Rs[c1] * ldp + c2];
+  }
+  for (long long e = tid; e < (long long)bw * n; e += PANEL_NT) {
+    const int c1 = (int)(e / n), j = (int)(e % n);
+    Gb[(long long)c1 * n + j] = (j >= k0 && j < k0 + bw) ? zero<T>() : M[(long long)Rs[c1] * n + j];
+  }
+  __syncthreads();
+  for (int c = tid; c < bw; c += PANEL_NT) us[Rs[c]] = 1;
+}
+
+template <class T>
+__global__ void gje_scatter_rows_kernel(int n, int k0, int bw, T* Mat, const T* H, const int* piv) {
+  const long long b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)bw * n;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e / n), j = (int)(e % n);
+    if (j >= k0 && j < k0 + bw) continue;
+    const int r = piv[b * n + k0 + c];
+    Mat[b * nn + (long long)r * n + j] = H[b * (long long)BP * n + (long long)c * n + j];
+  }
+}
+
+__global__ void gje_rinv_kernel(int n, const int* piv, int* rinv) {
+  const long long b = blockIdx.y;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    rinv[b * n + piv[b * n + k]] = k;
+}
+
+template <class T>
+__global__ void gje_permute_out_kernel(int n, const T* Mat, const int* piv, const int* rinv, T* X,
+                                       long long ldx, long long sX) {
+  const long long b = blockIdx.y;
+  const long long nn = (long long)n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(e / n), j = (int)(e % n);
+    X[b * sX + (long long)k * ldx + j] =
+        Mat[b * nn + (long long)piv[b * n + k] * n + rinv[b * n + j]];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Dispatch
+// --------------------------------------------------------------------------
+int inverse_small_nmax(int dtype) {
+  switch (dtype) {
+    case F32: return 208;
+    case F64: return 128;
+    case C64: return 128;
+    case C128: return 64;
+  }
+  return 0;
+}
+
+size_t inverse_workspace_bytes(int dtype, int n, int batch) {
+  if (n <= inverse_small_nmax(dtype)) return 0;
+  const size_t es = dtype_size(dtype);
+  return gje_layout(es, n).per * (size_t)batch + 256;
+}
+
+template <class T, int NMAX>
+static cudaError_t launch_reg(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
+                             long long sX, int batch, int* info, cudaStream_t st) {
+  for (int b0 = 0; b0 < batch; b0 += 1 << 30) {
+    const int nb = batch - b0;
+    inv_reg_kernel<T, NMAX><<<nb, 512, 0, st>>>(n, A + (long long)b0 * sA, lda, sA,
+                                                X + (long long)b0 * sX, ldx, sX,
+                                                info ? info + b0 : nullptr);
+  }
+  return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t inverse_small(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
+                                 long long sX, int batch, int* info, cudaStream_t st);
+
+template <>
+cudaError_t inverse_small<float>(int n, const float* A, long long lda, long long sA, float* X,
+                                 long long ldx, long long sX, int batch, int* info, cudaStream_t st) {
+  if (n <= 32) return launch_reg<float, 32>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  if (n <= 64) return launch_reg<float, 64>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  if (n <= 128) return launch_reg<float, 128>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  return launch_reg<float, 208>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+}
+template <>
+cudaError_t inverse_small<double>(int n, const double* A, long long lda, long long sA, double* X,
+                                  long long ldx, long long sX, int batch, int* info, cudaStream_t st) {
+  if (n <= 32) return launch_reg<double, 32>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  if (n <= 64) return launch_reg<double, 64>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  return launch_reg<double, 128>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+}
+template <>
+cudaError_t inverse_small<c64>(int n, const c64* A, long long lda, long long sA, c64* X,
+                               long long ldx, long long sX, int batch, int* info, cudaStream_t st) {
+  if (n <= 32) return launch_reg<c64, 32>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  if (n <= 64) return launch_reg<c64, 64>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  return launch_reg<c64, 128>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+}
+template <>
+cudaError_t inverse_small<c128>(int n, const c128* A, long long lda, long long sA, c128* X,
+                                long long ldx, long long sX, int batch, int* info, cudaStream_t st) {
+  if (n <= 32) return launch_reg<c128, 32>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  return launch_reg<c128, 64>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+}
+
+template <class T>
+cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
+                            long long sX, int batch, int* info, void* ws, size_t ws_bytes,
+                            cudaStream_t st) {
+  if (n <= 0 || batch <= 0) return cudaSuccess;
+  if (info) cudaMemsetAsync(info, 0, sizeof(int) * (size_t)batch, st);
+  const int dtype = DTypeOf<T>::value;
+  if (n <= inverse_small_nmax(dtype)) return inverse_small<T>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+
+  const size_t es = sizeof(T);
+  const GjeWs L = gje_layout(es, n);
+  if (ws == nullptr || ws_bytes < L.per * (size_t)batch) {
+    set_error("inverse: workspace too small (%zu < %zu)", ws_bytes, L.per * (size_t)batch);
+    return cudaErrorInvalidValue;
+  }
+  unsigned char* base = reinterpret_cast<unsigned char*>(ws);
+  base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(base) + 255) & ~uintptr_t(255));
+  T* Mat = reinterpret_cast<T*>(base);
+  base += L.mat * batch;
+  T* Pw = reinterpret_cast<T*>(base);
+  base += L.pan * batch;
+  T* U = reinterpret_cast<T*>(base);
+  base += L.u * batch;
+  T* G = reinterpret_cast<T*>(base);
+  base += L.g * batch;
+  T* H = reinterpret_cast<T*>(base);
+  base += L.h * batch;
+  T* E = reinterpret_cast<T*>(base);
+  base += L.e * batch;
+  int* piv = reinterpret_cast<int*>(base);
+  base += L.piv * batch;
+  int* rinv = reinterpret_cast<int*>(base);
+  base += L.rinv * batch;
+  unsigned char* used = base;
+
+  const long long nn = (long long)n * n;
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = (batch - b0) < 65535 ? (batch - b0) : 65535;
+    int gx = (int)((nn + 255) / 256);
+    if (gx > 1024) gx = 1024;
+    gje_copy_in_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(n, A + (long long)b0 * sA, lda, sA,
+                                                        Mat + (long long)b0 * nn, used + (long long)b0 * n);
+  }
+  const size_t pan_smem = es * (size_t)n * (BP + 1);
+  const int use_smem = pan_smem <= 160 * 1024;
+  if (use_smem)
+    cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)pan_smem);
+  const T one_ = one<T>();
+  for (int k0 = 0; k0 < n; k0 += BP) {
+    const int bw = (n - k0) < BP ? (n - k0) : BP;
+    gje_panel_kernel<T><<<batch, PANEL_NT, use_smem ? pan_smem : 0, st>>>(
+        n, k0, bw, Mat, Pw, use_smem, U, G, E, piv, used, info);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // H = E G
+    e = gemm_batched<T>(bw, n, bw, one_, E, BP, BP * BP, G, n, (long long)BP * n, zero<T>(), nullptr, 0,
+                        0, H, n, (long long)BP * n, batch, st);
+    if (e != cudaSuccess) return e;
+    // Mat += U G
+    e = gemm_batched<T>(n, n, bw, one_, U, BP, (long long)n * BP, G, n, (long long)BP * n, one_, Mat, n,
+                        nn, Mat, n, nn, batch, st);
+    if (e != cudaSuccess) return e;
+    for (int b0 = 0; b0 < batch; b0 += 65535) {
+      const int nb = (batch - b0) < 65535 ? (batch - b0) : 65535;
+      int gx = (bw * n + 255) / 256;
+      gje_scatter_rows_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(
+          n, k0, bw, Mat + (long long)b0 * nn, H + (long long)b0 * BP * n, piv + (long long)b0 * n);
+    }
+  }
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = (batch - b0) < 65535 ? (batch - b0) : 65535;
+    gje_rinv_kernel<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(n, piv + (long long)b0 * n,
+                                                               rinv + (long long)b0 * n);
+    int gx = (int)((nn + 255) / 256);
+    if (gx > 2048) gx = 2048;
+    gje_permute_out_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(
+        n, Mat + (long long)b0 * nn, piv + (long long)b0 * n, rinv + (long long)b0 * n,
+        X + (long long)b0 * sX, ldx, sX);
+  }
+  return cudaGetLastError();
+}
+
+#define HPS_INST_INV(T)                                                                       \
+  template cudaError_t inverse_batched<T>(int, const T*, long long, long long, T*, long long, \
+                                          long long, int, int*, void*, size_t, cudaStream_t);
+HPS_INST_INV(float)
+HPS_INST_INV(double)
+HPS_INST_INV(c64)
+HPS_INST_INV(c128)
+
+}  // namespace hps

@@ -1,0 +1,573 @@
+"""FP64 CPU oracle for the HPS build/solve path (TEST INFRASTRUCTURE ONLY).
+
+This module is a plain NumPy/SciPy restatement of the reference
+(meliao/jaxhps) algorithm for the leaf-solve -> merge -> down-pass path.
+It exists only to check the CUDA product path: it may be imported by
+``tests/``, by ``__graft_entry__.smoke()`` and by ``bench.py``'s CPU
+baseline leg, and by nothing else.  The product package never imports it.
+
+Parity pinning: the reference (JAX, un-pinned ``jax>=0.4``) cannot be run in
+this environment, and its test-suite stores no golden vectors.  The oracle is
+pinned instead against the reference's own analytic known-answer tests
+(polynomial data reproduced to 1e-12, ``tests/test_accuracy/*``), which the
+CPU test-suite re-runs against this module.  Raw bitwise parity with JAX's
+``jnp.linalg.inv`` output is therefore *unpinned*; agreement is to rounding.
+
+Every function cites the reference file:line it restates (paths relative to
+the reference project root).  The code is written per-leaf / per-merge with
+explicit loops where that keeps the index bookkeeping readable.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+# ---------------------------------------------------------------------------
+# Quadrature  (src/jaxhps/quadrature/_discretization.py, _differentiation.py,
+#              _interpolation.py)
+# ---------------------------------------------------------------------------
+
+
+def chebyshev_points(n: int) -> np.ndarray:
+    """Chebyshev-Lobatto points on [-1, 1], left end first.
+
+    Restates quadrature/_discretization.py:12-37:
+    ``out[i] = cos(pi * (n-1-i)/(n-1))``.
+    """
+    angles = np.flipud(np.pi * (np.arange(n, dtype=np.float64) / (n - 1)))
+    return np.cos(angles)
+
+
+def gauss_points(n: int) -> np.ndarray:
+    """Gauss-Legendre nodes (quadrature/_discretization.py:104-116)."""
+    return np.polynomial.legendre.leggauss(n)[0]
+
+
+def affine_transform(pts: np.ndarray, ab) -> np.ndarray:
+    """Map [-1,1] -> [a,b] (quadrature/_discretization.py:89-101)."""
+    a, b = ab
+    return 0.5 * (b - a) * pts + 0.5 * (a + b)
+
+
+def differentiation_matrix_1D(x: np.ndarray) -> np.ndarray:
+    """Chebyshev spectral differentiation matrix (Trefethen, Spectral Methods
+    in MATLAB ch.6), as in quadrature/_differentiation.py:8-47."""
+    p = x.shape[0]
+    c = np.ones(p)
+    c[0] = 2.0
+    c[-1] = 2.0
+    c[1::2] *= -1.0
+    dx = x[:, None] - x[None, :]
+    d = np.outer(c, 1.0 / c) / (dx + np.eye(p))
+    d = d - np.diag(d.sum(axis=1))
+    return d
+
+
+def barycentric_matrix_1D(from_pts: np.ndarray, to_pts: np.ndarray) -> np.ndarray:
+    """Barycentric Lagrange interpolation matrix (to x from).
+
+    Restates quadrature/_interpolation.py:17-114, including the exact-match
+    rows that become unit rows.
+    """
+    n = from_pts.shape[0]
+    w = np.ones(n)
+    for j in range(n):
+        for k in range(n):
+            if j != k:
+                w[j] *= from_pts[k] - from_pts[j]
+    m = np.zeros((to_pts.shape[0], n))
+    for i, t in enumerate(to_pts):
+        hit = np.nonzero(t == from_pts)[0]
+        if hit.size:
+            m[i, hit[0]] = 1.0
+            continue
+        terms = 1.0 / (w * (t - from_pts))
+        m[i] = terms / terms.sum()
+    return m
+
+
+# ---------------------------------------------------------------------------
+# 2D leaf grid ordering  (src/jaxhps/_grid_creation_2D.py)
+# ---------------------------------------------------------------------------
+
+
+def ext_first_order_2D(n: int) -> np.ndarray:
+    """Permutation from meshgrid(x, flipud(y), 'ij') flat order to the
+    exterior-first order of _grid_creation_2D.py:203-233.
+
+    Flat index ``j = ix*n + iy`` with ``iy=0`` the north row.  Boundary runs
+    counter-clockwise from the SW corner: south (W->E, n points), east
+    (S->N, n-1), north (E->W, n-1, ends on the NW corner), west (N->S, n-2);
+    then the interior in increasing flat index.
+    """
+    order = []
+    order += [ix * n + (n - 1) for ix in range(n)]               # south
+    order += [(n - 1) * n + iy for iy in range(n - 2, -1, -1)]   # east
+    order += [ix * n + 0 for ix in range(n - 2, -1, -1)]         # north
+    order += [0 * n + iy for iy in range(1, n - 1)]              # west
+    seen = set(order)
+    order += [j for j in range(n * n) if j not in seen]
+    return np.array(order, dtype=np.int64)
+
+
+def quad_children_bounds(b):
+    """SW, SE, NE, NW children (_grid_creation_2D.py:34-46)."""
+    xmin, xmax, ymin, ymax = b
+    xm = (xmin + xmax) / 2
+    ym = (ymin + ymax) / 2
+    return [
+        (xmin, xm, ymin, ym),
+        (xm, xmax, ymin, ym),
+        (xm, xmax, ym, ymax),
+        (xmin, xm, ym, ymax),
+    ]
+
+
+def uniform_leaf_bounds_2D(root_bounds, L: int) -> np.ndarray:
+    """Leaf boxes in the reference's uniform order (_grid_creation_2D.py:18-31,
+    repeated SW/SE/NE/NW subdivision flattened level by level)."""
+    boxes = [tuple(root_bounds)]
+    for _ in range(L):
+        nxt = []
+        for b in boxes:
+            nxt += quad_children_bounds(b)
+        boxes = nxt
+    return np.array(boxes, dtype=np.float64)
+
+
+def leaf_points_2D(bounds: np.ndarray, p: int) -> np.ndarray:
+    """Chebyshev points of each leaf, exterior first
+    (_grid_creation_2D.py:49-68)."""
+    c = chebyshev_points(p)
+    r = ext_first_order_2D(p)
+    out = np.empty((bounds.shape[0], p * p, 2))
+    for i, (xmin, xmax, ymin, ymax) in enumerate(bounds):
+        xs = affine_transform(c, (xmin, xmax))
+        ys = affine_transform(c, (ymin, ymax))
+        X, Y = np.meshgrid(xs, np.flipud(ys), indexing="ij")
+        pts = np.stack([X.ravel(), Y.ravel()], axis=-1)
+        out[i] = pts[r]
+    return out
+
+
+def boundary_gauss_points_2D(root_bounds, L: int, q: int) -> np.ndarray:
+    """Root boundary Gauss points: S (x up), E (y up), N (x down), W (y down)
+    (_grid_creation_2D.py:76-124)."""
+    xmin, xmax, ymin, ymax = root_bounds
+    g = gauss_points(q)
+    n = 2 ** L
+    xb = np.linspace(xmin, xmax, n + 1)
+    yb = np.linspace(ymin, ymax, n + 1)
+    xg = np.concatenate([affine_transform(g, xb[i:i + 2]) for i in range(n)])
+    yg = np.concatenate([affine_transform(g, yb[i:i + 2]) for i in range(n)])
+    return np.concatenate([
+        np.stack([xg, np.full_like(xg, ymin)], -1),
+        np.stack([np.full_like(yg, xmax), yg], -1),
+        np.stack([xg[::-1], np.full_like(xg, ymax)], -1),
+        np.stack([np.full_like(yg, xmin), yg[::-1]], -1),
+    ])
+
+
+# ---------------------------------------------------------------------------
+# 2D operators  (src/jaxhps/_precompute_operators_2D.py)
+# ---------------------------------------------------------------------------
+
+
+def diff_operators_2D(p: int, half_side_len: float):
+    """D_x, D_y, D_xx, D_yy, D_xy in exterior-first order
+    (_precompute_operators_2D.py:16-44)."""
+    r = ext_first_order_2D(p)
+    d = differentiation_matrix_1D(chebyshev_points(p)) / half_side_len
+    dx = np.kron(d, np.eye(p))[np.ix_(r, r)]
+    dy = -np.kron(np.eye(p), d)[np.ix_(r, r)]
+    return dx, dy, dx @ dx, dy @ dy, dx @ dy
+
+
+def P_2D_DtN(p: int, q: int) -> np.ndarray:
+    """Gauss (4q) -> Chebyshev boundary (4(p-1)); corners averaged
+    (_precompute_operators_2D.py:48-79)."""
+    P = barycentric_matrix_1D(gauss_points(q), chebyshev_points(p))
+    out = np.zeros((4 * (p - 1), 4 * q))
+    out[0:p, 0:q] = P
+    out[p - 1:2 * p - 1, q:2 * q] = P
+    out[2 * (p - 1):3 * p - 2, 2 * q:3 * q] = P
+    out[3 * (p - 1):, 3 * q:] = P[:-1]
+    out[0, 3 * q:] = P[-1]
+    for r in (0, p - 1, 2 * (p - 1), 3 * (p - 1)):
+        out[r] /= 2.0
+    return out
+
+
+def P_2D_ItI(p: int, q: int) -> np.ndarray:
+    """kron(I_4, P[:-1]) (_precompute_operators_2D.py:83-99)."""
+    P = barycentric_matrix_1D(gauss_points(q), chebyshev_points(p))
+    return np.kron(np.eye(4), P[:-1])
+
+
+def N_matrix_2D(dx, dy, p):
+    """Outward normal derivative on the 4p doubled-corner Chebyshev boundary
+    (_precompute_operators_2D.py:132-163)."""
+    N = np.zeros((4 * p, p * p))
+    N[:p] = -dy[:p]
+    N[p:2 * p] = dx[p - 1:2 * p - 1]
+    N[2 * p:3 * p] = dy[2 * p - 2:3 * p - 2]
+    N[3 * p:4 * p - 1] = -dx[3 * p - 3:4 * p - 4]
+    N[4 * p - 1] = -dx[0]
+    return N
+
+
+def N_tilde_matrix_2D(dx, dy, p):
+    """Normal derivative at the 4(p-1) boundary points
+    (_precompute_operators_2D.py:166-192)."""
+    N = np.zeros((4 * (p - 1), p * p))
+    N[:p - 1] = -dy[:p - 1]
+    N[p - 1:2 * (p - 1)] = dx[p - 1:2 * (p - 1)]
+    N[2 * (p - 1):3 * (p - 1)] = dy[2 * (p - 1):3 * (p - 1)]
+    N[3 * (p - 1):] = -dx[3 * (p - 1):4 * (p - 1)]
+    return N
+
+
+def Q_2D_DtN(p, q, dx, dy):
+    """Interior -> outward normal derivative at the 4q Gauss nodes
+    (_precompute_operators_2D.py:102-129)."""
+    Qi = barycentric_matrix_1D(chebyshev_points(p), gauss_points(q))
+    return np.kron(np.eye(4), Qi) @ N_matrix_2D(dx, dy, p)
+
+
+def QH_2D_ItI(p, q, dx, dy, eta):
+    """Outgoing impedance u_n - i eta u at the Gauss nodes
+    (_precompute_operators_2D.py:195-240)."""
+    H = N_matrix_2D(dx, dy, p).astype(np.complex128)
+    I = np.eye(p)
+    H[:p, :p] -= 1j * eta * I
+    H[p:2 * p, p - 1:2 * p - 1] -= 1j * eta * I
+    H[2 * p:3 * p, 2 * p - 2:3 * p - 2] -= 1j * eta * I
+    H[3 * p:4 * p - 1, 3 * p - 3:4 * p - 4] -= 1j * eta * np.eye(p - 1)
+    H[4 * p - 1, 0] -= 1j * eta
+    Qi = barycentric_matrix_1D(chebyshev_points(p), gauss_points(q))
+    return np.kron(np.eye(4), Qi) @ H
+
+
+def G_2D_ItI(dx, dy, p, eta):
+    """Incoming impedance u_n + i eta u at the 4(p-1) Chebyshev boundary
+    points (_precompute_operators_2D.py:243-265)."""
+    G = N_tilde_matrix_2D(dx, dy, p).astype(np.complex128)
+    m = G.shape[0]
+    G[:m, :m] += 1j * eta * np.eye(m)
+    return G
+
+
+# ---------------------------------------------------------------------------
+# Leaf stage  (src/jaxhps/local_solve/_uniform_2D_DtN.py, _uniform_2D_ItI.py)
+# ---------------------------------------------------------------------------
+
+
+def assemble_operator(coeffs: dict, ops: dict, n_leaves: int, n_pts: int):
+    """A = sum_k diag(c_k) D_k per leaf (local_solve/_uniform_2D_DtN.py:182-218).
+
+    ``coeffs`` maps operator names to (n_leaves, n_pts) arrays (or None),
+    ``ops`` maps the same names to (n_pts, n_pts) matrices.
+    """
+    dtype = np.result_type(*[c for c in coeffs.values() if c is not None])
+    A = np.zeros((n_leaves, n_pts, n_pts), dtype=np.result_type(dtype, np.float64))
+    for name, c in coeffs.items():
+        if c is None:
+            continue
+        A += c[:, :, None] * ops[name][None, :, :]
+    return A
+
+
+def leaf_dtn(A: np.ndarray, f: np.ndarray, P: np.ndarray, Q: np.ndarray):
+    """Leaf DtN solve for each leaf (local_solve/_uniform_2D_DtN.py:228-273).
+
+    A: (n_leaves, n, n); f: (n_leaves, n, nsrc).  Returns Y, T, v, h.
+    """
+    n_cb = P.shape[0]
+    nl, n, _ = A.shape
+    ns = f.shape[-1]
+    Y = np.empty((nl, n, P.shape[1]), dtype=A.dtype)
+    v = np.zeros((nl, n, ns), dtype=np.result_type(A.dtype, f.dtype))
+    for i in range(nl):
+        Aii_inv = np.linalg.inv(A[i, n_cb:, n_cb:])
+        Aie = A[i, n_cb:, :n_cb]
+        L2 = np.vstack([np.eye(n_cb), -Aii_inv @ Aie])
+        Y[i] = L2 @ P
+        v[i, n_cb:] = Aii_inv @ f[i, n_cb:]
+    T = np.einsum("ab,lbc->lac", Q, Y)
+    h = np.einsum("ab,lbc->lac", Q, v)
+    return Y, T, v, h
+
+
+def leaf_iti(A: np.ndarray, f: np.ndarray, P: np.ndarray, QH: np.ndarray,
+             G: np.ndarray):
+    """Leaf ItI solve (local_solve/_uniform_2D_ItI.py:120-186)."""
+    n_cb = P.shape[0]
+    nl, n, _ = A.shape
+    ns = f.shape[-1]
+    Y = np.empty((nl, n, P.shape[1]), dtype=np.complex128)
+    v = np.empty((nl, n, ns), dtype=np.complex128)
+    for i in range(nl):
+        B = np.zeros((n, n), dtype=np.complex128)
+        B[:n_cb] = G
+        B[n_cb:] = A[i, n_cb:]
+        Binv = np.linalg.inv(B)
+        Y[i] = Binv[:, :n_cb] @ P
+        v[i] = Binv[:, n_cb:] @ f[i, n_cb:]
+    T = np.einsum("ab,lbc->lac", QH, Y)
+    h = np.einsum("ab,lbc->lac", QH, v)
+    return Y, T, v, h
+
+
+# ---------------------------------------------------------------------------
+# Quad merge, DtN  (src/jaxhps/merge/_uniform_2D_DtN.py:206-475,
+#                   merge/_schur_complement.py:117-237)
+# ---------------------------------------------------------------------------
+
+
+def _quad_side_indices(nc: int):
+    """Per-child index lists of merge/_uniform_2D_DtN.py:384-437.
+
+    Returns dict child -> (outer, first_interface, second_interface) with the
+    interface labels used by the reference (5: a|b, 6: b|c, 7: c|d, 8: d|a).
+    """
+    ix = np.arange(4 * nc)
+    a = (np.concatenate([ix[-nc:], ix[:nc]]), ix[nc:2 * nc], ix[2 * nc:3 * nc][::-1])
+    b = (ix[:2 * nc], ix[2 * nc:3 * nc], ix[3 * nc:][::-1])
+    c = (ix[:nc][::-1], ix[nc:3 * nc], ix[3 * nc:])
+    d = (ix[:nc], ix[nc:2 * nc][::-1], ix[2 * nc:])
+    return a, b, c, d
+
+
+def _sub(T, i, j):
+    return T[np.ix_(i, j)]
+
+
+def quad_merge_dtn(Ta, Tb, Tc, Td, ha, hb, hc, hd):
+    """One DtN quad merge (merge/_uniform_2D_DtN.py:206-348).
+
+    h* have shape (4nc, nsrc).  Returns S, T, h_out, g_tilde with the
+    exterior already rolled by -nc (:343-346).
+    """
+    nc = Ta.shape[0] // 4
+    (a1, a5, a8), (b2, b6, b5), (c6, c3, c7), (d8, d7, d4) = _quad_side_indices(nc)
+    z_ei = np.zeros((2 * nc, nc))
+    z_ie = np.zeros((nc, 2 * nc))
+    z_ii = np.zeros((nc, nc))
+    B = np.block([
+        [_sub(Ta, a1, a5), z_ei, z_ei, _sub(Ta, a1, a8)],
+        [_sub(Tb, b2, b5), _sub(Tb, b2, b6), z_ei, z_ei],
+        [z_ei, _sub(Tc, c3, c6), _sub(Tc, c3, c7), z_ei],
+        [z_ei, z_ei, _sub(Td, d4, d7), _sub(Td, d4, d8)],
+    ])
+    C = np.block([
+        [_sub(Ta, a5, a1), _sub(Tb, b5, b2), z_ie, z_ie],
+        [z_ie, _sub(Tb, b6, b2), _sub(Tc, c6, c3), z_ie],
+        [z_ie, z_ie, _sub(Tc, c7, c3), _sub(Td, d7, d4)],
+        [_sub(Ta, a8, a1), z_ie, z_ie, _sub(Td, d8, d4)],
+    ])
+    D = np.block([
+        [_sub(Ta, a5, a5) + _sub(Tb, b5, b5), _sub(Tb, b5, b6), z_ii, _sub(Ta, a5, a8)],
+        [_sub(Tb, b6, b5), _sub(Tb, b6, b6) + _sub(Tc, c6, c6), _sub(Tc, c6, c7), z_ii],
+        [z_ii, _sub(Tc, c7, c6), _sub(Tc, c7, c7) + _sub(Td, d7, d7), _sub(Td, d7, d8)],
+        [_sub(Ta, a8, a5), z_ii, _sub(Td, d8, d7), _sub(Td, d8, d8) + _sub(Ta, a8, a8)],
+    ])
+    dh = np.concatenate([ha[a5] + hb[b5], hb[b6] + hc[c6], hc[c7] + hd[d7], hd[d8] + ha[a8]])
+    h_ext = np.concatenate([ha[a1], hb[b2], hc[c3], hd[d4]])
+    Dinv = np.linalg.inv(D)
+    S = -Dinv @ C
+    T = B @ S
+    A_blocks = [_sub(Ta, a1, a1), _sub(Tb, b2, b2), _sub(Tc, c3, c3), _sub(Td, d4, d4)]
+    for k, Ak in enumerate(A_blocks):
+        sl = slice(2 * nc * k, 2 * nc * (k + 1))
+        T[sl, sl] += Ak
+    g_tilde = -Dinv @ dh
+    h_out = h_ext + B @ g_tilde
+    h_out = np.roll(h_out, -nc, axis=0)
+    T = np.roll(np.roll(T, -nc, axis=0), -nc, axis=1)
+    S = np.roll(S, -nc, axis=1)
+    return S, T, h_out, g_tilde
+
+
+def quad_merge_iti(Ra, Rb, Rc, Rd, ha, hb, hc, hd):
+    """One ItI quad merge (merge/_uniform_2D_ItI.py:182-375 with
+    merge/_schur_complement.py:6-41, 78-114, 182-237)."""
+    nc = Ra.shape[0] // 4
+    (a1, a5, a8), (b2, b6, b5), (c6, c3, c7), (d8, d7, d4) = _quad_side_indices(nc)
+    z_ei = np.zeros((2 * nc, nc))
+    z_ie = np.zeros((nc, 2 * nc))
+    z_ii = np.zeros((nc, nc))
+    B = np.block([
+        [_sub(Ra, a1, a5), _sub(Ra, a1, a8), z_ei, z_ei, z_ei, z_ei, z_ei, z_ei],
+        [z_ei, z_ei, z_ei, z_ei, _sub(Rb, b2, b5), _sub(Rb, b2, b6), z_ei, z_ei],
+        [z_ei, z_ei, _sub(Rc, c3, c6), _sub(Rc, c3, c7), z_ei, z_ei, z_ei, z_ei],
+        [z_ei, z_ei, z_ei, z_ei, z_ei, z_ei, _sub(Rd, d4, d7), _sub(Rd, d4, d8)],
+    ])
+    C = np.block([
+        [z_ie, _sub(Rb, b5, b2), z_ie, z_ie],
+        [z_ie, z_ie, z_ie, _sub(Rd, d8, d4)],
+        [z_ie, _sub(Rb, b6, b2), z_ie, z_ie],
+        [z_ie, z_ie, z_ie, _sub(Rd, d7, d4)],
+        [_sub(Ra, a5, a1), z_ie, z_ie, z_ie],
+        [z_ie, z_ie, _sub(Rc, c6, c3), z_ie],
+        [z_ie, z_ie, _sub(Rc, c7, c3), z_ie],
+        [_sub(Ra, a8, a1), z_ie, z_ie, z_ie],
+    ])
+    D12 = np.block([
+        [_sub(Rb, b5, b5), _sub(Rb, b5, b6), z_ii, z_ii],
+        [z_ii, z_ii, _sub(Rd, d8, d7), _sub(Rd, d8, d8)],
+        [_sub(Rb, b6, b5), _sub(Rb, b6, b6), z_ii, z_ii],
+        [z_ii, z_ii, _sub(Rd, d7, d7), _sub(Rd, d7, d8)],
+    ])
+    D21 = np.block([
+        [_sub(Ra, a5, a5), _sub(Ra, a5, a8), z_ii, z_ii],
+        [z_ii, z_ii, _sub(Rc, c6, c6), _sub(Rc, c6, c7)],
+        [z_ii, z_ii, _sub(Rc, c7, c6), _sub(Rc, c7, c7)],
+        [_sub(Ra, a8, a5), _sub(Ra, a8, a8), z_ii, z_ii],
+    ])
+    h_int = np.concatenate([hb[b5], hd[d8], hb[b6], hd[d7], ha[a5], hc[c6], hc[c7], ha[a8]])
+    h_ext = np.concatenate([ha[a1], hb[b2], hc[c3], hd[d4]])
+    n = D12.shape[0]
+    W = np.eye(n) - D12 @ D21
+    Winv = np.linalg.inv(W)
+    Dinv = np.zeros((2 * n, 2 * n), dtype=np.complex128)
+    Dinv[:n, :n] = Winv
+    Dinv[:n, n:] = -Winv @ D12
+    Dinv[n:, :n] = -D21 @ Winv
+    Dinv[n:, n:] = np.eye(n) + D21 @ Winv @ D12
+    S = -Dinv @ C
+    T = B @ S
+    for k, Ak in enumerate([_sub(Ra, a1, a1), _sub(Rb, b2, b2), _sub(Rc, c3, c3), _sub(Rd, d4, d4)]):
+        sl = slice(2 * nc * k, 2 * nc * (k + 1))
+        T[sl, sl] += Ak
+    g_tilde = -Dinv @ h_int
+    h_out = h_ext + B @ g_tilde
+    h_out = np.roll(h_out, -nc, axis=0)
+    T = np.roll(np.roll(T, -nc, axis=0), -nc, axis=1)
+    S = np.roll(S, -nc, axis=1)
+    r = np.concatenate([np.arange(0, nc), np.arange(4 * nc, 5 * nc), np.arange(5 * nc, 6 * nc),
+                        np.arange(2 * nc, 3 * nc), np.arange(3 * nc, 4 * nc), np.arange(6 * nc, 7 * nc),
+                        np.arange(7 * nc, 8 * nc), np.arange(nc, 2 * nc)])
+    return S[r], T, h_out, g_tilde[r]
+
+
+def merge_stage(T, h, L: int, iti: bool = False):
+    """Level loop of merge_stage_uniform_2D_{DtN,ItI}
+    (merge/_uniform_2D_DtN.py:96-203; merge/_uniform_2D_ItI.py:98-179).
+
+    T: (n_leaves, 4q, 4q); h: (n_leaves, 4q, nsrc).  Returns S_lst,
+    g_tilde_lst (leaf-adjacent level first, root last, root with a leading
+    batch axis of 1) and the top-level T.
+    """
+    fn = quad_merge_iti if iti else quad_merge_dtn
+    S_lst, g_lst = [], []
+    n_levels = max(L, 1)
+    for _ in range(n_levels):
+        nm = T.shape[0] // 4
+        outs = [fn(*T[4 * m:4 * m + 4], *h[4 * m:4 * m + 4]) for m in range(nm)]
+        S_lst.append(np.stack([o[0] for o in outs]))
+        g_lst.append(np.stack([o[3] for o in outs]))
+        T = np.stack([o[1] for o in outs])
+        h = np.stack([o[2] for o in outs])
+    return S_lst, g_lst, T[0], h[0]
+
+
+# ---------------------------------------------------------------------------
+# Down pass  (src/jaxhps/down_pass/_uniform_2D_DtN.py:7-189,
+#             down_pass/_uniform_2D_ItI.py:8-192)
+# ---------------------------------------------------------------------------
+
+
+def _propagate_down_dtn(S, g, gt):
+    nc = g.shape[0] // 8
+    gi = S @ g + gt
+    g5, g6, g7, g8 = gi[:nc], gi[nc:2 * nc], gi[2 * nc:3 * nc], gi[3 * nc:]
+    ga = np.concatenate([g[:nc], g5, g8[::-1], g[7 * nc:]])
+    gb = np.concatenate([g[nc:3 * nc], g6, g5[::-1]])
+    gc = np.concatenate([g6[::-1], g[3 * nc:5 * nc], g7])
+    gd = np.concatenate([g8, g7[::-1], g[5 * nc:7 * nc]])
+    return np.stack([ga, gb, gc, gd])
+
+
+def _propagate_down_iti(S, g, gt):
+    nc = g.shape[0] // 8
+    t = S @ g + gt
+    ta5 = t[:nc]
+    tb5 = t[nc:2 * nc][::-1]
+    tb6 = t[2 * nc:3 * nc]
+    tc6 = t[3 * nc:4 * nc][::-1]
+    tc7 = t[4 * nc:5 * nc]
+    td7 = t[5 * nc:6 * nc][::-1]
+    td8 = t[6 * nc:7 * nc]
+    ta8 = t[7 * nc:][::-1]
+    ga = np.concatenate([g[:nc], ta5, ta8, g[7 * nc:]])
+    gb = np.concatenate([g[nc:3 * nc], tb6, tb5])
+    gc = np.concatenate([tc6, g[3 * nc:5 * nc], tc7])
+    gd = np.concatenate([td8, td7, g[5 * nc:7 * nc]])
+    return np.stack([ga, gb, gc, gd])
+
+
+def down_pass(bdry, S_lst, g_lst, Y, v, iti: bool = False):
+    """bdry: (n_bdry, nsrc).  Returns leaf solutions (n_leaves, n_pts, nsrc)."""
+    fn = _propagate_down_iti if iti else _propagate_down_dtn
+    g = bdry[None]
+    for lvl in range(len(S_lst) - 1, -1, -1):
+        S, gt = S_lst[lvl], g_lst[lvl]
+        g = np.concatenate([fn(S[m], g[m], gt[m]) for m in range(S.shape[0])])
+    return np.einsum("ijk,ikl->ijl", Y, g) + v
+
+
+# ---------------------------------------------------------------------------
+# Whole-problem driver (uniform 2D)
+# ---------------------------------------------------------------------------
+
+
+class Problem2D:
+    """FP64 oracle problem for a uniform 2D quadtree.
+
+    Coefficient arrays are (n_leaves, p^2) on the leaf points in the
+    reference's order; ``source`` is (n_leaves, p^2) or (n_leaves, p^2, nsrc).
+    Mirrors PDEProblem (_pdeproblem.py:26-234) for the uniform 2D case.
+    """
+
+    OPS = ("D_xx", "D_xy", "D_yy", "D_x", "D_y", "I")
+
+    def __init__(self, root_bounds, L, p, q, coeffs, source, iti=False, eta=None):
+        self.root = tuple(float(x) for x in root_bounds)
+        self.L, self.p, self.q = L, p, q
+        self.iti, self.eta = iti, eta
+        self.bounds = uniform_leaf_bounds_2D(self.root, L)
+        self.points = leaf_points_2D(self.bounds, p)
+        self.boundary_points = boundary_gauss_points_2D(self.root, L, q)
+        half = (self.root[1] - self.root[0]) / (2 ** (L + 1))
+        dx, dy, dxx, dyy, dxy = diff_operators_2D(p, half)
+        self.ops = {"D_xx": dxx, "D_xy": dxy, "D_yy": dyy, "D_x": dx, "D_y": dy,
+                    "I": np.eye(p * p)}
+        if iti:
+            self.P = P_2D_ItI(p, q)
+            self.QH = QH_2D_ItI(p, q, dx, dy, eta)
+            self.G = G_2D_ItI(dx, dy, p, eta)
+        else:
+            self.P = P_2D_DtN(p, q)
+            self.Q = Q_2D_DtN(p, q, dx, dy)
+        self.coeffs = {k: (None if coeffs.get(k) is None else np.asarray(coeffs[k]))
+                       for k in self.OPS}
+        src = np.asarray(source)
+        self.multi = src.ndim == 3
+        self.source = src if self.multi else src[..., None]
+
+    def build(self):
+        nl = self.bounds.shape[0]
+        A = assemble_operator(self.coeffs, self.ops, nl, self.p ** 2)
+        if self.iti:
+            self.Y, T, self.v, h = leaf_iti(A, self.source, self.P, self.QH, self.G)
+        else:
+            self.Y, T, self.v, h = leaf_dtn(A, self.source, self.P, self.Q)
+        self.T_leaf, self.h_leaf = T, h
+        self.S_lst, self.g_lst, self.T_top, self.h_top = merge_stage(T, h, self.L, self.iti)
+        return self
+
+    def solve(self, bdry):
+        b = np.asarray(bdry)
+        b2 = b if b.ndim == 2 else b[:, None]
+        u = down_pass(b2, self.S_lst, self.g_lst, self.Y, self.v, self.iti)
+        return u if self.multi else u[..., 0]

@@ -1,0 +1,91 @@
+"""GPU tests of the batched primitives behind the C ABI: GEMM and the
+Gauss-Jordan inverse (register-resident and blocked paths), every dtype."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+DT = {
+    "f64": (torch.float64, np.float64, 1e-12),
+    "f32": (torch.float32, np.float32, 2e-5),
+    "c128": (torch.complex128, np.complex128, 1e-12),
+    "c64": (torch.complex64, np.complex64, 2e-5),
+}
+
+
+def _rand(rng, shape, npdt):
+    a = rng.standard_normal(shape)
+    if np.issubdtype(npdt, np.complexfloating):
+        a = a + 1j * rng.standard_normal(shape)
+    return a.astype(npdt)
+
+
+@pytest.mark.parametrize("dt", list(DT))
+@pytest.mark.parametrize("m,n,k,batch", [(1, 1, 1, 1), (56, 56, 256, 7), (130, 129, 67, 3), (300, 200, 5, 2),
+                                         (5, 9, 0, 2)])
+def test_gemm_batched(cuda, dt, m, n, k, batch):
+    from jaxhps_gb300 import _native as nat
+
+    tdt, npdt, tol = DT[dt]
+    rng = np.random.default_rng(m * 7 + n)
+    A = _rand(rng, (batch, m, k), npdt)
+    B = _rand(rng, (batch, k, n), npdt)
+    Cm = _rand(rng, (batch, m, n), npdt)
+    tA, tB, tC = (torch.as_tensor(x, device=cuda) for x in (A, B, Cm))
+    out = torch.empty((batch, m, n), dtype=tdt, device=cuda)
+    nat.gemm(tA, tB, out, alpha=-0.5, beta=2.0, Cmat=tC)
+    ref = -0.5 * A.astype(np.complex128) @ B + 2.0 * Cm
+    scale = max(1.0, np.abs(ref).max()) * max(1, k) ** 0.5
+    assert np.abs(out.cpu().numpy() - ref).max() <= tol * scale * 10
+    # broadcast A (stride 0) and in-place C == D
+    nat.gemm(tA[0], tB, tC, alpha=1.0, beta=1.0, Cmat=tC)
+    ref2 = A[0] @ B + Cm
+    assert np.abs(tC.cpu().numpy() - ref2).max() <= tol * scale * 10
+
+
+@pytest.mark.parametrize("dt", list(DT))
+@pytest.mark.parametrize("n,batch", [(1, 3), (5, 4), (36, 9), (64, 2), (100, 3), (129, 2), (196, 3), (233, 2)])
+def test_inverse_batched(cuda, dt, n, batch):
+    from jaxhps_gb300 import _native as nat
+
+    tdt, npdt, tol = DT[dt]
+    rng = np.random.default_rng(n)
+    A = _rand(rng, (batch, n, n), npdt) + (2 * np.sqrt(n)) * np.eye(n, dtype=npdt)
+    # permute rows so that pivoting is exercised
+    A = A[:, rng.permutation(n), :]
+    tA = torch.as_tensor(A, device=cuda)
+    info = torch.zeros(batch, dtype=torch.int32, device=cuda)
+    X = nat.inverse(tA, info=info).cpu().numpy()
+    assert (info.cpu().numpy() == 0).all()
+    res = np.abs(X.astype(np.complex128) @ A - np.eye(n)).max()
+    assert res < tol * 50 * n, res
+    # in place
+    nat.inverse(tA, out=tA)
+    assert np.allclose(tA.cpu().numpy(), X, atol=tol * 10, rtol=tol * 10)
+
+
+@pytest.mark.parametrize("n", [40, 300])
+def test_inverse_reports_singular(cuda, n):
+    from jaxhps_gb300 import _native as nat
+
+    A = np.zeros((2, n, n))
+    A[0] = np.eye(n)
+    A[1] = np.eye(n)
+    A[1, :, 3] = 0.0  # singular: zero column
+    tA = torch.as_tensor(A, device=cuda)
+    info = torch.zeros(2, dtype=torch.int32, device=cuda)
+    nat.inverse(tA, info=info)
+    inf = info.cpu().numpy()
+    assert inf[0] == 0 and inf[1] > 0
+
+
+def test_inverse_large_blocked(cuda):
+    from jaxhps_gb300 import _native as nat
+
+    n = 1100
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((1, n, n)) + np.sqrt(n) * np.eye(n)
+    X = nat.inverse(torch.as_tensor(A, device=cuda)).cpu().numpy()
+    assert np.abs(X[0] @ A[0] - np.eye(n)).max() < 1e-10

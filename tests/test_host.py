@@ -1,0 +1,171 @@
+"""CPU tests of the host side: operators, grids, index maps, the C ABI's
+exported symbols and the API's argument validation.  No GPU work here."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import jaxhps_gb300 as hps
+from jaxhps_gb300 import _grid_creation_2D as g2
+from jaxhps_gb300 import _index_maps as im
+from jaxhps_gb300 import _precompute_operators_2D as op2
+from jaxhps_gb300 import _quadrature as qd
+from oracle import hps_oracle as O
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.mark.parametrize("p,q", [(6, 4), (8, 6), (16, 14)])
+def test_operators_match_oracle(p, q):
+    half = 0.37
+    mine = op2.precompute_diff_operators_2D(p, half)
+    ref = O.diff_operators_2D(p, half)
+    for a, b in zip(mine, ref):
+        assert np.allclose(a, b, atol=1e-12 * np.abs(b).max())
+    assert np.allclose(op2.precompute_P_2D_DtN(p, q), O.P_2D_DtN(p, q), atol=1e-14)
+    assert np.allclose(op2.precompute_Q_2D_DtN(p, q, mine[0], mine[1]), O.Q_2D_DtN(p, q, ref[0], ref[1]),
+                       rtol=1e-12, atol=1e-10)
+    assert np.allclose(op2.precompute_P_2D_ItI(p, q), O.P_2D_ItI(p, q), atol=1e-14)
+    N = op2.precompute_N_matrix_2D(mine[0], mine[1], p)
+    assert np.allclose(op2.precompute_QH_2D_ItI(N, p, q, 2.5), O.QH_2D_ItI(p, q, ref[0], ref[1], 2.5),
+                       rtol=1e-12, atol=1e-10)
+    Nt = op2.precompute_N_tilde_matrix_2D(mine[0], mine[1], p)
+    assert np.allclose(op2.precompute_G_2D_ItI(Nt, 2.5), O.G_2D_ItI(ref[0], ref[1], p, 2.5), atol=1e-10)
+
+
+def test_quadrature_matches_oracle():
+    for n in (2, 3, 7, 16):
+        assert np.allclose(qd.chebyshev_points(n), O.chebyshev_points(n), atol=0)
+        x = qd.chebyshev_points(n)
+        assert np.allclose(qd.differentiation_matrix_1D(x), O.differentiation_matrix_1D(x), atol=1e-13)
+    a, b = qd.gauss_points(7), np.linspace(-1, 1, 11)
+    assert np.allclose(qd.barycentric_lagrange_interpolation_matrix_1D(a, b), O.barycentric_matrix_1D(a, b),
+                       atol=1e-14)
+    c = qd.chebyshev_points(5)
+    assert np.allclose(qd.barycentric_lagrange_interpolation_matrix_1D(c, c), np.eye(5))
+    w = qd.chebyshev_weights(9, (-1.0, 1.0))
+    assert abs(w.sum() - 2.0) < 1e-14
+    assert abs(w @ qd.chebyshev_points(9) ** 2 - 2 / 3) < 1e-14
+
+
+@pytest.mark.parametrize("L,p,q", [(0, 5, 3), (2, 6, 4), (3, 8, 6)])
+def test_grids_match_oracle(L, p, q):
+    root = hps.DiscretizationNode2D(-1.0, 2.0, 0.5, 3.5)
+    dom = hps.Domain(p=p, q=q, root=root, L=L)
+    assert np.allclose(dom.interior_points, O.leaf_points_2D(O.uniform_leaf_bounds_2D(root.bounds, L), p))
+    assert np.allclose(dom.boundary_points, O.boundary_gauss_points_2D(root.bounds, L, q))
+    assert list(g2.rearrange_indices_ext_int(p)) == list(O.ext_first_order_2D(p))
+    assert dom.n_leaves == 4 ** L
+
+
+def _emulate_merge(Ts, hs, maps):
+    """NumPy restatement of the merge gather + Schur complement driven by the
+    index maps (what hps_merge_level_dtn computes)."""
+    Tm, hm = np.stack(Ts), np.stack(hs)
+    ni, ne = maps.n_int, maps.n_ext
+    D = np.zeros((ni, ni))
+    for i in range(ni):
+        for t in range(2):
+            c, l = maps.int_c[i, t], maps.int_l[i, t]
+            for j in range(ni):
+                lj = maps.loc[c, j]
+                if lj >= 0:
+                    D[i, j] += Tm[c, l, lj]
+    C = np.zeros((ni, ne))
+    B = np.zeros((ne, ni))
+    A = np.zeros((ne, ne))
+    for x in range(ne):
+        c, l = maps.ext_c[x], maps.ext_l[x]
+        for i in range(ni):
+            li = maps.loc[c, i]
+            if li >= 0:
+                C[i, x] = Tm[c, li, l]
+                B[x, i] = Tm[c, l, li]
+        for y in range(ne):
+            if maps.ext_c[y] == c:
+                A[x, y] = Tm[c, l, maps.ext_l[y]]
+    dh = hm[maps.int_c[:, 0], maps.int_l[:, 0]] + hm[maps.int_c[:, 1], maps.int_l[:, 1]]
+    hext = hm[maps.ext_c, maps.ext_l]
+    Dinv = np.linalg.inv(D)
+    S = -Dinv @ C
+    gt = -Dinv @ dh
+    return S, A + B @ S, hext + B @ gt, gt
+
+
+@pytest.mark.parametrize("nc", [1, 3, 6])
+def test_quad_merge_maps_reproduce_oracle(nc):
+    rng = np.random.default_rng(nc)
+    n = 4 * nc
+    Ts = [rng.standard_normal((n, n)) + 4 * np.eye(n) for _ in range(4)]
+    hs = [rng.standard_normal((n, 2)) for _ in range(4)]
+    S, T, h, gt = O.quad_merge_dtn(*Ts, *hs)
+    maps = im.quad_merge_maps_dtn(nc)
+    S2, T2, h2, gt2 = _emulate_merge(Ts, hs, maps)
+    assert np.allclose(S, S2) and np.allclose(T, T2) and np.allclose(h, h2) and np.allclose(gt, gt2)
+
+
+@pytest.mark.parametrize("nc", [1, 4])
+def test_down_scatter_maps_reproduce_oracle(nc):
+    rng = np.random.default_rng(7)
+    S = rng.standard_normal((4 * nc, 8 * nc))
+    g = rng.standard_normal((8 * nc, 3))
+    gt = rng.standard_normal((4 * nc, 3))
+    ref = O._propagate_down_dtn(S, g, gt)
+    maps = im.quad_merge_maps_dtn(nc)
+    gi = S @ g + gt
+    out = np.empty((4, 4 * nc, 3))
+    for c in range(4):
+        for k in range(4 * nc):
+            cd = maps.code[c, k]
+            out[c, k] = g[cd] if cd >= 0 else gi[-cd - 1]
+    assert np.allclose(out, ref)
+
+
+def _declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        txt = h.read_text()
+        names |= set(re.findall(r"^\s*(?:[\w\*\s]+?)\b(hps_\w+)\s*\(", txt, flags=re.M))
+    return names
+
+
+def test_library_exports_header_symbols():
+    from jaxhps_gb300 import _build, _native
+
+    _build.build()
+    lib = ctypes.CDLL(str(_native._LIB_PATH))
+    declared = _declared_symbols()
+    assert len(declared) >= 10
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+    assert set(_native.EXPORTED_SYMBOLS) <= declared
+    lib.hps_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.hps_version()
+
+
+def test_gpu_path_fails_loudly_without_cuda(monkeypatch):
+    import torch
+    from jaxhps_gb300 import _native
+
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
+    with pytest.raises(_native.NativeError):
+        _native.lib()
+
+
+def test_pdeproblem_validation():
+    root = hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0)
+    dom = hps.Domain(p=6, q=4, root=root, L=1)
+    ones = np.ones(dom.interior_points.shape[:2])
+    with pytest.raises(ValueError):
+        hps.PDEProblem(dom, source=ones, D_xx_coefficients=ones, D_z_coefficients=ones)
+    with pytest.raises(ValueError):
+        hps.PDEProblem(dom, source=ones, D_xx_coefficients=ones[:2])
+    with pytest.raises(ValueError):
+        hps.PDEProblem(dom, source=ones, D_xx_coefficients=ones, use_ItI=True)
+    pde = hps.PDEProblem(dom, source=ones, D_xx_coefficients=ones, D_yy_coefficients=ones)
+    cs, ops = pde.active_coefficients()
+    assert len(cs) == 2 and ops[0] is pde.D_xx and ops[1] is pde.D_yy
+    assert pde.Y is None and pde.S_lst == []
