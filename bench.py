@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""HPS build+solve benchmark on one GB300.
+
+Workload (default): 2D variable-coefficient problem on [-1,1]^2,
+L = d_xx + d_yy + c(x,y), c = 1 + 0.5 * sum of 4 Gaussian bumps (seeded
+centres in [-0.8,0.8]^2, width 0.2); uniform quadtree L=7 (16384 leaves),
+p=16, q=14, DtN; 64 right-hand sides, each a seeded sum of 8 Gaussian
+sources (width 0.1) with Dirichlet data b_j (x^2 - y^2).
+
+One step = build_solver + solve of all 64 right-hand sides.
+Metric: leaves/s = n_leaves / (t_build + t_solve).
+
+  value : inputs already resident in HBM, result left in HBM.
+  e2e   : through the public API with pinned host inputs; the host->device
+          copies of coefficients/source/boundary data and the device->host
+          copy of the solution are inside the timed region.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
+restatement of the reference algorithm (the FP64 oracle; the reference's
+own JAX code cannot be installed on these machines) on a bounded sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = dict(name="2D var-coeff DtN, uniform quadtree", L=7, p=16, q=14, nsrc=64)
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+
+def bump_centres(seed=0):
+    return np.random.default_rng(seed).uniform(-0.8, 0.8, (4, 2))
+
+
+def coefficient_c(x, z):
+    r2 = ((x[..., None, :] - z) ** 2).sum(-1)
+    return 1.0 + 0.5 * np.exp(-r2 / 0.2 ** 2).sum(-1)
+
+
+def source_params(nsrc, seed=1):
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(-1, 1, (nsrc, 8))
+    zs = rng.uniform(-0.8, 0.8, (nsrc, 8, 2))
+    b = rng.uniform(-1, 1, nsrc)
+    return a, zs, b
+
+
+def make_inputs(L, p, q, nsrc, device):
+    """Domain, coefficient arrays and sources, generated on `device`."""
+    import torch
+
+    import jaxhps_gb300 as hps
+
+    root = hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0)
+    dom = hps.Domain(p=p, q=q, root=root, L=L)
+    x = torch.as_tensor(dom.interior_points, device=device)
+    z = torch.as_tensor(bump_centres(), device=device)
+    c = 1.0 + 0.5 * torch.exp(-((x[..., None, :] - z) ** 2).sum(-1) / 0.2 ** 2).sum(-1)
+    a, zs, b = (torch.as_tensor(t, device=device) for t in source_params(nsrc))
+    f = torch.empty(x.shape[:2] + (nsrc,), dtype=torch.float64, device=device)
+    for j in range(nsrc):
+        f[..., j] = (a[j] * torch.exp(-((x[..., None, :] - zs[j]) ** 2).sum(-1) / 0.1 ** 2)).sum(-1)
+    bp = torch.as_tensor(dom.boundary_points, device=device)
+    g = (bp[:, 0] ** 2 - bp[:, 1] ** 2)[:, None] * b[None, :]
+    ones = torch.ones_like(c)
+    return dom, dict(D_xx_coefficients=ones, D_yy_coefficients=ones, I_coefficients=c), f, g
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+CLOCK_Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+           "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+           "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={CLOCK_Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [t.strip() for t in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        load = [s for s in sm if mx and s > 0.5 * mx] or sm
+        return {"sm_mhz": float(np.median(load)) if load else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle timing (bounded sample of the same workload)
+# ---------------------------------------------------------------------------
+
+
+def cpu_oracle_sample(L_sample=5, p=16, q=14, nsrc=64):
+    from oracle import hps_oracle as O
+
+    root = (-1.0, 1.0, -1.0, 1.0)
+    pts = O.leaf_points_2D(O.uniform_leaf_bounds_2D(root, L_sample), p)
+    c = coefficient_c(pts, bump_centres())
+    a, zs, b = source_params(nsrc)
+    r2 = ((pts[:, :, None, None, :] - zs[None, None]) ** 2).sum(-1)
+    f = (a[None, None] * np.exp(-r2 / 0.1 ** 2)).sum(-1)
+    ones = np.ones_like(c)
+    t0 = time.perf_counter()
+    pr = O.Problem2D(root, L_sample, p, q, {"D_xx": ones, "D_yy": ones, "I": c}, f).build()
+    bp = pr.boundary_points
+    g = (bp[:, 0] ** 2 - bp[:, 1] ** 2)[:, None] * b[None, :]
+    pr.solve(g)
+    dt = time.perf_counter() - t0
+    n = 4 ** L_sample
+    return n / dt, dt, n
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# main
+# ---------------------------------------------------------------------------
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt, n = cpu_oracle_sample(args.ref_L)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    sample = (f"FP64 NumPy/SciPy oracle (CPU restatement of the reference algorithm), build+solve of the same "
+              f"problem at L={args.ref_L} ({4 ** args.ref_L} leaves, p=16, q=14, 64 RHS)")
+    line = {
+        "impl": "reference", "metric": "build+solve leaves/s", "value": value, "unit": "leaves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD["name"], **{k: WORKLOAD[k] for k in
+                                                                                    ("L", "p", "q", "nsrc")}},
+        "cpu_baseline": {"value": value, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "leaves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's JAX package cannot be installed offline here; its algorithm is timed as the "
+                "oracle port",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["float64", "float32", "mixed"])
+    ap.add_argument("--fp64-steps", dest="fp64_steps", type=int, default=1)
+    ap.add_argument("--L", type=int, default=WORKLOAD["L"])
+    ap.add_argument("--ref-L", dest="ref_L", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--breakdown", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import jaxhps_gb300 as hps
+    from jaxhps_gb300 import _native as nat
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    L, p, q, ns = args.L, WORKLOAD["p"], WORKLOAD["q"], WORKLOAD["nsrc"]
+    dom, coeffs, f, g = make_inputs(L, p, q, ns, dev)
+    n_leaves = dom.n_leaves
+    pde = hps.PDEProblem(dom, source=f, **coeffs)
+
+    def step():
+        pde.reset()
+        hps.build_solver(pde, precision=args.precision)
+        return hps.solve(pde, g, host_device=None)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = nat.launch_count()
+    nat.profile_begin(nat.KC_GEMM, nat.KC_INVERSE, nat.KC_MOVE, nat.KC_RESIDUAL)
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        u = step()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    classes = nat.profile_end()
+    launches = nat.launch_count() - launches0
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * n_leaves / (ms_per_step / 1e3)
+    iters = len(pde._state.history) if getattr(pde, "_state", None) is not None else None
+
+    # the plain FP64 GPU path on the same problem: its rate, and the error of
+    # this run's solution against it
+    err, fp64 = None, None
+    if args.precision != "float64":
+        pde64 = hps.PDEProblem(dom, source=f, **coeffs)
+        hps.build_solver(pde64, precision="float64")
+        u64 = hps.solve(pde64, g, host_device=None)
+        err = float(((u - u64).abs().max() / u64.abs().max()).item())
+        if args.fp64_steps > 0:
+            torch.cuda.synchronize()
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record()
+            for _ in range(args.fp64_steps):
+                pde64.reset()
+                hps.build_solver(pde64, precision="float64")
+                u64 = hps.solve(pde64, g, host_device=None)
+            a1.record()
+            torch.cuda.synchronize()
+            ms64 = a0.elapsed_time(a1) / args.fp64_steps
+            fp64 = {"value": n_leaves / (ms64 / 1e3), "unit": "leaves/s", "ms_per_step": ms64,
+                    "speedup_of_this_path": ms64 / ms_per_step}
+        del pde64, u64
+        nat.release_workspace()
+        torch.cuda.empty_cache()
+
+    # e2e through the public API from pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        hf = f.cpu().pin_memory()
+        hg = g.cpu().pin_memory()
+        hco = {k: v.cpu().pin_memory() for k, v in coeffs.items()}
+        h2d = hf.numel() * 8 + hg.numel() * 8 + sum(v.numel() * 8 for v in hco.values())
+        d2h = n_leaves * p * p * ns * 8
+        pde_h = hps.PDEProblem(dom, source=hf, **hco)
+
+        def estep():
+            pde_h.reset()
+            hps.build_solver(pde_h, precision=args.precision)
+            return hps.solve(pde_h, hg, host_device="cpu")
+
+        estep()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 2)):
+            uh = estep()
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / max(1, args.steps // 2)
+        e2e = {"value": world * n_leaves / te, "unit": "leaves/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": te * 1e3}
+        del pde_h, uh
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    names = {nat.KC_GEMM: "gemm_kernel", nat.KC_INVERSE: "inverse (inv_reg_kernel / gje_panel_kernel)",
+             nat.KC_MOVE: "gather/scatter/assembly", nat.KC_RESIDUAL: "residual_2d_kernel (FP64)"}
+    breakdown = {names[c]: {"ms_per_step": v[0] / args.steps, "share": v[0] / ms, "launches_per_step":
+                            v[1] / args.steps} for c, v in classes.items()}
+    dom_cls = max(classes, key=lambda c: classes[c][0])
+    k_ms, k_n, k_work = classes[dom_cls]
+    avg_ms = k_ms / max(k_n, 1)
+    if dom_cls in (nat.KC_MOVE, nat.KC_RESIDUAL):
+        if dom_cls == nat.KC_RESIDUAL:
+            # algorithmic bytes of one residual launch: read u_int, g, f, coefficients; write r (FP32), flux
+            n_i = p * p - 4 * (p - 1)
+            per = n_leaves * ns * (n_i * 8 + 4 * q * 8 + p * p * 8 + n_i * 4 + 4 * q * 8) + 3 * n_leaves * p * p * 8
+        else:
+            per = k_work / max(k_n, 1)
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = per / (avg_ms / 1e3) / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": None, "kernel": names[dom_cls], "bytes_per_launch": per,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured" if peaks else "fallback 6800 GB/s"}
+        if dom_cls == nat.KC_RESIDUAL:
+            roofline["flops_per_launch"] = k_work / max(k_n, 1)
+            roofline["fp64_tflops"] = k_work / (k_ms / 1e3) / 1e12
+    else:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        achieved = k_work / (k_ms / 1e3) / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "traffic": None, "kernel": names[dom_cls],
+                    "flops_per_launch": k_work / max(k_n, 1),
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured" if peaks else "fallback"}
+    roofline["avg_launch_ms"] = avg_ms
+    roofline["share_of_step"] = k_ms / ms
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, dt, n = cpu_oracle_sample(args.ref_L)
+        cpu = {"value": v, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"FP64 oracle build+solve at L={args.ref_L} ({n} leaves, p=16, q=14, 64 RHS), {dt:.1f} s"}
+
+    dtype = {"float64": "f64", "float32": "f32", "mixed": "f32+f64-refinement"}[args.precision]
+    line = {
+        "metric": "build+solve leaves/s", "value": value, "unit": "leaves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+        "config": {"workload": WORKLOAD["name"], "L": L, "n_leaves": n_leaves, "p": p, "q": q, "nsrc": ns,
+                   "precision": args.precision, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "l2": "inputs larger than L2 (operator set is several GB)"},
+        "rel_err_vs_fp64": err, "refinement_iterations": iters, "fp64_path": fp64,
+        "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernel_classes": breakdown,
+        "cpu_baseline": cpu, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -57,6 +57,19 @@ enum {
 /* Library version string (static storage). */
 HPS_API const char* hps_version(void);
 
+/* Number of CUDA kernels this library has enqueued since it was loaded. */
+HPS_API long long hps_launch_count(void);
+
+/* Live profiler.  hps_profile_begin(mask) arms CUDA-event timing of every
+ * later launch whose kernel class c has bit (1 << c) set in mask (classes:
+ * 1 GEMM, 2 inverse, 3 gather/scatter/assembly, 4 refinement residual),
+ * recorded on the launch's own stream.  hps_profile_end() synchronises on
+ * those events and fills arrays of 8 entries indexed by class: summed kernel
+ * time (ms), number of launches and summed algorithmic work (flops for 1, 2,
+ * 4; bytes for 3), then disarms. */
+HPS_API int hps_profile_begin(int class_mask);
+HPS_API int hps_profile_end(double* total_ms, long long* launches, double* work);
+
 /* Copies the last error message of this thread into buf (NUL-terminated).
  * Returns the full message length. */
 HPS_API int hps_last_error(char* buf, size_t len);
@@ -183,6 +196,7 @@ typedef struct {
   void* h_out;        /* out (n_merges, n_ext, nsrc) or NULL */
   void* D_inv;        /* out (n_merges, n_int, n_int), or NULL to keep it in the workspace */
   void* BD_inv;       /* out (n_merges, n_ext, n_int) = B D_inv, or NULL (no-source up pass) */
+  void* B_out;        /* out (n_merges, n_ext, n_int) = B, or NULL (kept for the refinement up pass) */
   int* info;          /* (n_merges) or NULL */
   void* workspace;
   size_t workspace_bytes;
@@ -211,6 +225,67 @@ typedef struct {
 } hps_down_args;
 
 HPS_API int hps_down_level(const hps_down_args* a, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * One up-pass level for new leaf data without rebuilding (the reference's
+ * up_pass_uniform_2D_DtN / _ItI, up_pass/_uniform_2D_DtN.py:8-173):
+ *   dh = h_a + h_b on every interface,  g~ = -D_inv dh,
+ *   h_out = h_ext + B g~.
+ * Uses the D_inv and B kept from the merge stage.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int dtype;
+  int n_merges, nch, nb, n_int, n_ext, nsrc;
+  const void* h_children; /* (n_merges*nch, nb, nsrc) */
+  const int *int_c, *int_l, *ext_c, *ext_l;
+  const void* D_inv;      /* (n_merges, n_int, n_int) */
+  const void* B;          /* (n_merges, n_ext, n_int) */
+  void* dh;               /* scratch (n_merges, n_int, nsrc) */
+  void* g_tilde;          /* out (n_merges, n_int, nsrc) */
+  void* h_out;            /* out (n_merges, n_ext, nsrc) */
+} hps_up_args;
+
+HPS_API int hps_up_level(const hps_up_args* a, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Iterative refinement (mixed precision).  No reference counterpart: the
+ * reference solves in FP64 only.  These compute, in FP64, the residual of
+ * the discrete system that the HPS solver solves directly:
+ *   leaf rows       r_int = f_int - A_ii u_int - A_ie P g   (get_DtN's system,
+ *                   local_solve/_uniform_2D_DtN.py:228-273)
+ *   interface rows  flux continuity of Q u across shared Gauss nodes
+ *                   (the merge equations, merge/_schur_complement.py:182-237)
+ *   boundary rows   g - g_given on the domain boundary.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int n_leaves, p, q, nsrc, n_ops;
+  int op_kind[10];         /* host values: 0 D_xx, 1 D_xy, 2 D_yy, 3 D_x, 4 D_y, 5 I */
+  const double* coeffs;    /* (n_ops, n_leaves, p*p) on the exterior-first leaf points */
+  const double* inv_half;  /* (n_leaves) 2 / leaf side length */
+  const double* D1;        /* (p, p) Chebyshev differentiation on [-1, 1] */
+  const double* D2;        /* (p, p) D1 @ D1 */
+  const double* Pside;     /* (p, q) Gauss -> Chebyshev interpolation on one side */
+  const double* Qside;     /* (q, p) Chebyshev -> Gauss interpolation on one side */
+  const int* perm;         /* (p*p) meshgrid index of every exterior-first point */
+  const double* u_int;     /* (n_leaves, n_i, nsrc) interior values */
+  const double* g;         /* (n_leaves, 4q, nsrc) leaf boundary Gauss values */
+  const double* f;         /* (n_leaves, p*p, nsrc) source */
+  float* r_int;            /* out (n_leaves, n_i, nsrc) leaf-row residual, rounded to FP32 */
+  double* r_int64;         /* out, same in FP64, or NULL */
+  double* flux;            /* out (n_leaves, 4q, nsrc) outward normal derivative at the Gauss nodes */
+  double* u_full;          /* out (n_leaves, p*p, nsrc) full leaf solution, or NULL */
+} hps_residual2d_args;
+
+HPS_API int hps_residual_2d(const hps_residual2d_args* a, void* stream);
+
+/* hcorr[node] = (flux[node] + flux[nbr[node]]) / 2 (0 where nbr < 0);
+ * r_bdry[b] = g_given[b] - g_state[bdry_node[b]].  Node = leaf*4q + k. */
+HPS_API int hps_flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr,
+                             int n_bdry, const int* bdry_node, const double* g_given, const double* g_state,
+                             float* r_bdry, void* stream);
+
+/* y += x elementwise (x FP32, y FP64). */
+HPS_API int hps_accumulate(long long n, const float* x, double* y, void* stream);
 
 #ifdef __cplusplus
 }

@@ -65,7 +65,23 @@ class MergeArgs(C.Structure):
         ("T_children", vp), ("h_children", vp),
         ("int_c", vp), ("int_l", vp), ("ext_c", vp), ("ext_l", vp), ("loc", vp),
         ("S", vp), ("g_tilde", vp), ("T_out", vp), ("h_out", vp), ("D_inv", vp), ("BD_inv", vp),
-        ("info", vp), ("workspace", vp), ("workspace_bytes", csz),
+        ("B_out", vp), ("info", vp), ("workspace", vp), ("workspace_bytes", csz),
+    ]
+
+
+class UpArgs(C.Structure):
+    _fields_ = [
+        ("dtype", ci), ("n_merges", ci), ("nch", ci), ("nb", ci), ("n_int", ci), ("n_ext", ci), ("nsrc", ci),
+        ("h_children", vp), ("int_c", vp), ("int_l", vp), ("ext_c", vp), ("ext_l", vp),
+        ("D_inv", vp), ("B", vp), ("dh", vp), ("g_tilde", vp), ("h_out", vp),
+    ]
+
+
+class Residual2DArgs(C.Structure):
+    _fields_ = [
+        ("n_leaves", ci), ("p", ci), ("q", ci), ("nsrc", ci), ("n_ops", ci), ("op_kind", ci * 10),
+        ("coeffs", vp), ("inv_half", vp), ("D1", vp), ("D2", vp), ("Pside", vp), ("Qside", vp), ("perm", vp),
+        ("u_int", vp), ("g", vp), ("f", vp), ("r_int", vp), ("r_int64", vp), ("flux", vp), ("u_full", vp),
     ]
 
 
@@ -80,6 +96,11 @@ class DownArgs(C.Structure):
 def _declare(lib):
     P = C.POINTER
     lib.hps_version.restype = C.c_char_p
+    lib.hps_launch_count.restype = cll
+    lib.hps_profile_begin.argtypes = [ci]
+    lib.hps_profile_begin.restype = ci
+    lib.hps_profile_end.argtypes = [P(C.c_double), P(cll), P(C.c_double)]
+    lib.hps_profile_end.restype = ci
     lib.hps_last_error.argtypes = [C.c_char_p, csz]
     lib.hps_last_error.restype = ci
     lib.hps_gemm_batched.argtypes = [ci, ci, ci, ci, P(C.c_double), vp, cll, cll, vp, cll, cll, P(C.c_double),
@@ -105,13 +126,22 @@ def _declare(lib):
     lib.hps_merge_level_dtn.restype = ci
     lib.hps_down_level.argtypes = [P(DownArgs), vp]
     lib.hps_down_level.restype = ci
+    lib.hps_up_level.argtypes = [P(UpArgs), vp]
+    lib.hps_up_level.restype = ci
+    lib.hps_residual_2d.argtypes = [P(Residual2DArgs), vp]
+    lib.hps_residual_2d.restype = ci
+    lib.hps_flux_combine.argtypes = [cll, ci, vp, vp, vp, ci, vp, vp, vp, vp, vp]
+    lib.hps_flux_combine.restype = ci
+    lib.hps_accumulate.argtypes = [cll, vp, vp, vp]
+    lib.hps_accumulate.restype = ci
 
 
 EXPORTED_SYMBOLS = (
-    "hps_version", "hps_last_error", "hps_gemm_batched", "hps_inverse_workspace_size",
+    "hps_version", "hps_launch_count", "hps_profile_begin", "hps_profile_end", "hps_last_error", "hps_gemm_batched", "hps_inverse_workspace_size",
     "hps_inverse_batched", "hps_convert", "hps_local_solve_dtn_workspace_size", "hps_local_solve_dtn",
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
-    "hps_merge_level_dtn", "hps_down_level",
+    "hps_merge_level_dtn", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
+    "hps_accumulate",
 )
 
 
@@ -145,6 +175,28 @@ def check(status: int, what: str) -> None:
         buf = C.create_string_buffer(1024)
         load_library().hps_last_error(buf, 1024)
         raise NativeError(f"{what} failed with status {status}: {buf.value.decode(errors='replace')}")
+
+
+def launch_count() -> int:
+    """Kernels enqueued by the native library so far (process-wide)."""
+    return int(load_library().hps_launch_count())
+
+
+KC_GEMM, KC_INVERSE, KC_MOVE, KC_RESIDUAL = 1, 2, 3, 4
+
+
+def profile_begin(*kernel_classes: int) -> None:
+    mask = 0
+    for c in kernel_classes:
+        mask |= 1 << c
+    check(load_library().hps_profile_begin(mask), "hps_profile_begin")
+
+
+def profile_end():
+    """{class: (summed kernel ms, launches, summed algorithmic work)} since profile_begin."""
+    ms, n, w = (C.c_double * 8)(), (C.c_longlong * 8)(), (C.c_double * 8)()
+    check(load_library().hps_profile_end(ms, n, w), "hps_profile_end")
+    return {c: (ms[c], n[c], w[c]) for c in range(1, 8) if n[c]}
 
 
 def stream_ptr() -> int:

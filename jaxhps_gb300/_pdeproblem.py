@@ -22,10 +22,10 @@ COEFF_NAMES_3D = ("D_xx", "D_xy", "D_yy", "D_xz", "D_yz", "D_zz", "D_x", "D_y", 
 
 
 def _to_numpy(a):
-    if a is None:
-        return None
-    if hasattr(a, "detach"):
-        return a.detach().cpu().numpy()
+    """Inputs are kept as given (NumPy arrays or torch tensors, possibly in
+    pinned host memory); lists are converted to NumPy."""
+    if a is None or hasattr(a, "shape"):
+        return a
     return np.asarray(a)
 
 
@@ -138,6 +138,6 @@ class PDEProblem:
 
 def check_input_shapes(expected_shape, coeffs: dict) -> None:
     for name, arr in coeffs.items():
-        if arr is not None and tuple(np.shape(arr)) != tuple(expected_shape):
-            raise ValueError(f"{name}_coefficients has shape {tuple(np.shape(arr))} but should have shape "
+        if arr is not None and tuple(arr.shape) != tuple(expected_shape):
+            raise ValueError(f"{name}_coefficients has shape {tuple(arr.shape)} but should have shape "
                              f"{tuple(expected_shape)} to match the Domain's interior points.")

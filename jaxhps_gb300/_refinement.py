@@ -1,0 +1,274 @@
+"""Mixed-precision build and iteratively refined solve (uniform 2D DtN).
+
+Build (FP32): leaf inverses inv(A_ii), the interior rows of Y, and for every
+merge level S, inv(D) and B — the operators of a complete FP32 HPS direct
+solver, used here as an approximate inverse M of the discrete system J.
+
+Solve: x = (interior values u_int of every leaf, Gauss boundary values g of
+every leaf) in FP64, starting from zero, iterating
+
+    r  = b - J x                 FP64 residual (hps_residual_2d,
+                                 hps_flux_combine)
+    dx = M r                     FP32: leaf inverse, up pass (hps_up_level),
+                                 down pass (hps_down_level)
+    x += dx                      FP64 (hps_accumulate)
+
+until max|du| <= tol * max|u|.  J is the system the reference's FP64 direct
+solver solves exactly: leaf collocation rows (local_solve/_uniform_2D_DtN.py:
+228-273), continuity of the outward normal derivative across interfaces
+(the merge equations, merge/_schur_complement.py:182-237) and the Dirichlet
+data on the domain boundary.  The fixed point is therefore the FP64 discrete
+solution; each iteration contracts the error by roughly the FP32 solver's
+relative accuracy.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from . import _stages as st
+from ._grid_creation_2D import rearrange_indices_ext_int, uniform_leaf_bounds_2D
+from ._index_maps import quad_merge_maps_dtn
+from ._pdeproblem import COEFF_NAMES_2D
+from ._quadrature import (
+    affine_transform,
+    barycentric_lagrange_interpolation_matrix_1D,
+    chebyshev_points,
+    differentiation_matrix_1D,
+    gauss_points,
+)
+
+OP_KIND_2D = {name: i for i, name in enumerate(COEFF_NAMES_2D)}
+
+
+def leaf_gauss_nodes_2D(bounds: np.ndarray, q: int) -> np.ndarray:
+    """(n_leaves, 4q, 2) Gauss nodes of every leaf boundary in leaf order:
+    S (x up), E (y up), N (x down), W (y down)."""
+    gp = gauss_points(q)
+    xmin, xmax, ymin, ymax = (bounds[:, i:i + 1] for i in range(4))
+    xs = 0.5 * (xmax - xmin) * gp[None] + 0.5 * (xmin + xmax)
+    ys = 0.5 * (ymax - ymin) * gp[None] + 0.5 * (ymin + ymax)
+    S = np.stack([xs, np.broadcast_to(ymin, xs.shape)], -1)
+    E = np.stack([np.broadcast_to(xmax, ys.shape), ys], -1)
+    N = np.stack([xs[:, ::-1], np.broadcast_to(ymax, xs.shape)], -1)
+    W = np.stack([np.broadcast_to(xmin, ys.shape), ys[:, ::-1]], -1)
+    return np.concatenate([S, E, N, W], axis=1)
+
+
+def node_maps(leaf_nodes: np.ndarray, boundary_points: np.ndarray, scale: float):
+    """Pairs every leaf boundary Gauss node with the coinciding node of the
+    neighbouring leaf (-1 on the domain boundary), and maps every root
+    boundary point to its leaf node.  Nodes are matched by coordinates."""
+    n_leaves, nb, d = leaf_nodes.shape
+    flat = leaf_nodes.reshape(-1, d)
+    key = np.round(flat / scale * 1e10).astype(np.int64)
+    uniq, inv, counts = np.unique(key, axis=0, return_inverse=True, return_counts=True)
+    inv = inv.reshape(-1)
+    order = np.argsort(inv, kind="stable")
+    starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    nbr = np.full(flat.shape[0], -1, dtype=np.int64)
+    if counts.max() > 2:
+        raise ValueError("a Gauss node is shared by more than two leaves (non-conforming mesh)")
+    two = np.nonzero(counts == 2)[0]
+    a = order[starts[two]]
+    b = order[starts[two] + 1]
+    nbr[a] = b
+    nbr[b] = a
+    bkey = np.round(boundary_points / scale * 1e10).astype(np.int64)
+    lookup = {tuple(k): i for i, k in enumerate(uniq)}
+    bnode = np.empty(len(bkey), dtype=np.int64)
+    for j, k in enumerate(bkey):
+        u = lookup.get(tuple(k))
+        if u is None or counts[u] != 1:
+            raise ValueError("root boundary point does not match a single leaf boundary node")
+        bnode[j] = order[starts[u]]
+    return nbr, bnode
+
+
+@dataclass
+class MixedState:
+    mixed: bool
+    n_leaves: int
+    p: int
+    q: int
+    Y_int: torch.Tensor          # (n_leaves, n_i, 4q) FP32 view
+    Aii_inv: torch.Tensor        # (n_leaves, n_i, n_i) FP32
+    Q_int: torch.Tensor          # (4q, n_i) FP32
+    S_lst: List[torch.Tensor]
+    Dinv_lst: List[torch.Tensor]
+    B_lst: List[torch.Tensor]
+    coeffs: torch.Tensor         # (n_ops, n_leaves, p^2) FP64
+    op_kind: List[int]
+    f: torch.Tensor              # (n_leaves, p^2, nsrc) FP64
+    multi: bool
+    consts: dict
+    nbr: torch.Tensor
+    bnode: torch.Tensor
+    tol: float = 1e-12
+    max_iters: int = 30
+    history: list = field(default_factory=list)
+
+
+def _domain_constants(dom, dev):
+    """Residual-kernel constants and the leaf node pairing of a uniform 2D
+    domain, computed once per (domain, device) and cached on the Domain."""
+    cache = dom.__dict__.setdefault("_refine_cache", {})
+    key = str(dev)
+    if key in cache:
+        return cache[key]
+    p, q, n_leaves = dom.p, dom.q, dom.n_leaves
+    half = (dom.root.xmax - dom.root.xmin) / (2 ** (dom.L + 1))
+    cheb = chebyshev_points(p)
+    D1 = differentiation_matrix_1D(cheb)
+    bounds = uniform_leaf_bounds_2D(dom.root.bounds, dom.L)
+    nodes = leaf_gauss_nodes_2D(bounds, q)
+    nbr, bnode = node_maps(nodes, dom.boundary_points, scale=dom.root.xmax - dom.root.xmin)
+    consts = {
+        "inv_half": torch.full((n_leaves,), 1.0 / half, dtype=torch.float64, device=dev),
+        "D1": torch.as_tensor(D1, device=dev),
+        "D2": torch.as_tensor(D1 @ D1, device=dev),
+        "Pside": torch.as_tensor(barycentric_lagrange_interpolation_matrix_1D(gauss_points(q), cheb), device=dev),
+        "Qside": torch.as_tensor(barycentric_lagrange_interpolation_matrix_1D(cheb, gauss_points(q)), device=dev),
+        "perm": torch.as_tensor(rearrange_indices_ext_int(p).astype(np.int32), device=dev),
+        "nbr": torch.as_tensor(nbr.astype(np.int32), device=dev),
+        "bnode": torch.as_tensor(bnode.astype(np.int32), device=dev),
+    }
+    cache[key] = consts
+    return consts
+
+
+def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12, max_iters: int = 30):
+    dom = pde_problem.domain
+    if pde_problem.use_ItI or not dom.bool_2D or not dom.bool_uniform:
+        raise NotImplementedError("mixed precision is implemented for uniform 2D DtN problems")
+    if pde_problem.source is None:
+        raise ValueError("mixed precision needs the source at build time")
+    dev = st._device(device)
+    p, q, n_leaves = dom.p, dom.q, dom.n_leaves
+    n_cb = 4 * (p - 1)
+    Y, T, _, _, Aii = st._local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, dev, torch.float32,
+                                          keep_inverse=True, want_source=False)
+    S_lst, Dinv_lst, B_lst = [], [], []
+    Tc = T
+    for _ in range(max(dom.L, 1)):
+        maps = quad_merge_maps_dtn(Tc.shape[1] // 4)
+        S, _, Tc, _, Dinv, _, B = st.merge_level_dtn(Tc, None, maps, keep_D_inv=True, keep_B=True)
+        S_lst.append(S)
+        Dinv_lst.append(Dinv)
+        B_lst.append(B)
+    del T
+
+    cs, names = [], []
+    for name in COEFF_NAMES_2D:
+        c = getattr(pde_problem, f"{name}_coefficients")
+        if c is not None:
+            cs.append(st._as_tensor(c, torch.float64, dev))
+            names.append(name)
+    if any(st._is_complex(c) for c in cs):
+        raise NotImplementedError("mixed precision with complex coefficients is not implemented")
+    coeffs = torch.stack(cs).contiguous()
+    f, multi = st._src3(pde_problem.source, n_leaves, p * p, torch.float64, dev)
+
+    consts = _domain_constants(dom, dev)
+    Q32 = torch.as_tensor(np.ascontiguousarray(pde_problem.Q[:, n_cb:]), device=dev, dtype=torch.float32)
+    state = MixedState(
+        mixed=True, n_leaves=n_leaves, p=p, q=q, Y_int=Y[:, n_cb:, :], Aii_inv=Aii, Q_int=Q32, S_lst=S_lst,
+        Dinv_lst=Dinv_lst, B_lst=B_lst, coeffs=coeffs, op_kind=[OP_KIND_2D[n] for n in names], f=f, multi=multi,
+        consts=consts, nbr=consts["nbr"], bnode=consts["bnode"], tol=tol, max_iters=max_iters)
+    pde_problem._state = state
+    pde_problem._precision = "mixed"
+    pde_problem.Y = Y
+    pde_problem.S_lst = S_lst
+    pde_problem.D_inv_lst = Dinv_lst
+    pde_problem.g_tilde_lst = []
+    if return_top_T:
+        return Tc[0]
+    return None
+
+
+def _residual(state: MixedState, u_int, g, r32, flux, u_full=None):
+    c = state.consts
+    a = nat.Residual2DArgs(
+        n_leaves=state.n_leaves, p=state.p, q=state.q, nsrc=u_int.shape[-1], n_ops=len(state.op_kind),
+        coeffs=state.coeffs.data_ptr(), inv_half=c["inv_half"].data_ptr(), D1=c["D1"].data_ptr(),
+        D2=c["D2"].data_ptr(), Pside=c["Pside"].data_ptr(), Qside=c["Qside"].data_ptr(), perm=c["perm"].data_ptr(),
+        u_int=u_int.data_ptr(), g=g.data_ptr(), f=state.f.data_ptr(), r_int=r32.data_ptr(), r_int64=None,
+        flux=flux.data_ptr(), u_full=nat.ptr(u_full))
+    for i, k in enumerate(state.op_kind):
+        a.op_kind[i] = k
+    nat.check(nat.lib().hps_residual_2d(C.byref(a), nat.stream_ptr()), "hps_residual_2d")
+
+
+def correction(state: MixedState, r32, hcorr, rb32):
+    """dx = M r with the FP32 operators: returns (du_int, dg) in FP32."""
+    v = torch.empty_like(r32)
+    nat.gemm(state.Aii_inv, r32, v)
+    h = torch.empty_like(hcorr)
+    nat.gemm(state.Q_int, v, h, 1.0, 1.0, Cmat=hcorr)
+    g_t_lst = []
+    hc = h
+    for lvl, (Dinv, B) in enumerate(zip(state.Dinv_lst, state.B_lst)):
+        maps = quad_merge_maps_dtn(B.shape[1] // 8)
+        g_t, hc = st.up_level(hc, Dinv, B, maps)
+        g_t_lst.append(g_t)
+    gch = rb32.unsqueeze(0)
+    for lvl in range(len(state.S_lst) - 1, -1, -1):
+        S = state.S_lst[lvl]
+        gch = st.down_level(S, g_t_lst[lvl], gch, quad_merge_maps_dtn(S.shape[2] // 8))
+    du = v  # du_int = Y_int dg + v   (in place on v)
+    nat.gemm(state.Y_int, gch, du, 1.0, 1.0, Cmat=v)
+    return du, gch
+
+
+def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=None, max_iters=None):
+    state: MixedState = pde_problem._state
+    if source is not None:
+        raise ValueError("the mixed-precision solver takes the source at build time")
+    L = nat.lib()
+    dev = state.Aii_inv.device
+    tol = state.tol if tol is None else tol
+    max_iters = state.max_iters if max_iters is None else max_iters
+    ns = state.f.shape[-1]
+    g_given = boundary_data if isinstance(boundary_data, torch.Tensor) else torch.as_tensor(np.asarray(boundary_data))
+    g_given = g_given.to(device=dev, dtype=torch.float64)
+    if g_given.dim() == 1:
+        g_given = g_given.unsqueeze(-1)
+    if g_given.shape[-1] != ns:
+        if g_given.shape[-1] == 1:
+            g_given = g_given.expand(-1, ns)
+        else:
+            raise ValueError("boundary data and source have different numbers of right-hand sides")
+    g_given = g_given.contiguous()
+    nl, p, q = state.n_leaves, state.p, state.q
+    n_i = p * p - 4 * (p - 1)
+    u_int = torch.zeros((nl, n_i, ns), dtype=torch.float64, device=dev)
+    g = torch.zeros((nl, 4 * q, ns), dtype=torch.float64, device=dev)
+    r32 = torch.empty((nl, n_i, ns), dtype=torch.float32, device=dev)
+    flux = torch.empty((nl, 4 * q, ns), dtype=torch.float64, device=dev)
+    hcorr = torch.empty((nl, 4 * q, ns), dtype=torch.float32, device=dev)
+    rb32 = torch.empty((g_given.shape[0], ns), dtype=torch.float32, device=dev)
+    state.history = []
+    for it in range(max_iters):
+        _residual(state, u_int, g, r32, flux)
+        nat.check(L.hps_flux_combine(nl * 4 * q, ns, state.nbr.data_ptr(), flux.data_ptr(), hcorr.data_ptr(),
+                                     g_given.shape[0], state.bnode.data_ptr(), g_given.data_ptr(), g.data_ptr(),
+                                     rb32.data_ptr(), nat.stream_ptr()), "hps_flux_combine")
+        du, dg = correction(state, r32, hcorr, rb32)
+        nat.check(L.hps_accumulate(du.numel(), du.data_ptr(), u_int.data_ptr(), nat.stream_ptr()), "hps_accumulate")
+        nat.check(L.hps_accumulate(dg.numel(), dg.data_ptr(), g.data_ptr(), nat.stream_ptr()), "hps_accumulate")
+        step = float(du.abs().max().item())
+        size = float(u_int.abs().max().item())
+        state.history.append(step / max(size, 1e-300))
+        if step <= tol * size:
+            break
+    u = torch.empty((nl, p * p, ns), dtype=torch.float64, device=dev)
+    _residual(state, u_int, g, r32, flux, u_full=u)
+    if not state.multi:
+        u = u[..., 0]
+    return st._to_host(u, host_device)

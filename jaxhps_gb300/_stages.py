@@ -188,10 +188,11 @@ def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None,
 # ---------------------------------------------------------------------------
 
 
-def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False):
+def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False,
+                    keep_B=False):
     """One batched merge level.  T_children: (n_merges*nch, nb, nb);
     h_children: (n_merges*nch, nb, nsrc) or None.  Returns
-    (S, g_tilde, T_out, h_out, D_inv, BD_inv)."""
+    (S, g_tilde, T_out, h_out, D_inv, BD_inv) and B when ``keep_B``."""
     L = nat.lib()
     dev = T_children.device
     dtype = T_children.dtype
@@ -205,6 +206,7 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
     h_out = torch.empty((n_m, n_ext, ns), dtype=dtype, device=dev) if ns else None
     D_inv = torch.empty((n_m, n_int, n_int), dtype=dtype, device=dev) if keep_D_inv else None
     BD_inv = torch.empty((n_m, n_ext, n_int), dtype=dtype, device=dev) if keep_BD_inv else None
+    B = torch.empty((n_m, n_ext, n_int), dtype=dtype, device=dev) if keep_B else None
     info = torch.zeros(n_m, dtype=torch.int32, device=dev)
     md = maps.device(dev)
     a = nat.MergeArgs(
@@ -212,13 +214,36 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
         T_children=T_children.data_ptr(), h_children=nat.ptr(h_children), int_c=md["int_c"].data_ptr(),
         int_l=md["int_l"].data_ptr(), ext_c=md["ext_c"].data_ptr(), ext_l=md["ext_l"].data_ptr(),
         loc=md["loc"].data_ptr(), S=S.data_ptr(), g_tilde=nat.ptr(g_t), T_out=T_out.data_ptr(),
-        h_out=nat.ptr(h_out), D_inv=nat.ptr(D_inv), BD_inv=nat.ptr(BD_inv), info=info.data_ptr(),
-        workspace=None, workspace_bytes=0)
+        h_out=nat.ptr(h_out), D_inv=nat.ptr(D_inv), BD_inv=nat.ptr(BD_inv), B_out=nat.ptr(B),
+        info=info.data_ptr(), workspace=None, workspace_bytes=0)
     wsb = L.hps_merge_level_dtn_workspace_size(C.byref(a))
     ws = nat.workspace(wsb, dev)
     a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
     nat.check(L.hps_merge_level_dtn(C.byref(a), nat.stream_ptr()), "hps_merge_level_dtn")
+    if keep_B:
+        return S, g_t, T_out, h_out, D_inv, BD_inv, B
     return S, g_t, T_out, h_out, D_inv, BD_inv
+
+
+def up_level(h_children, D_inv, B, maps):
+    """One up-pass level with stored D_inv and B (reference up_pass/_uniform_2D_DtN.py:8-173):
+    returns (g_tilde, h_out)."""
+    L = nat.lib()
+    n_m, n_int, _ = D_inv.shape
+    n_ext = B.shape[1]
+    ns = h_children.shape[-1]
+    dev, dtype = D_inv.device, D_inv.dtype
+    dh = torch.empty((n_m, n_int, ns), dtype=dtype, device=dev)
+    g_t = torch.empty((n_m, n_int, ns), dtype=dtype, device=dev)
+    h_out = torch.empty((n_m, n_ext, ns), dtype=dtype, device=dev)
+    md = maps.device(dev)
+    a = nat.UpArgs(dtype=nat.TORCH_TO_HPS[dtype], n_merges=n_m, nch=maps.nch, nb=maps.nb, n_int=n_int, n_ext=n_ext,
+                   nsrc=ns, h_children=h_children.data_ptr(), int_c=md["int_c"].data_ptr(),
+                   int_l=md["int_l"].data_ptr(), ext_c=md["ext_c"].data_ptr(), ext_l=md["ext_l"].data_ptr(),
+                   D_inv=D_inv.data_ptr(), B=B.data_ptr(), dh=dh.data_ptr(), g_tilde=g_t.data_ptr(),
+                   h_out=h_out.data_ptr())
+    nat.check(L.hps_up_level(C.byref(a), nat.stream_ptr()), "hps_up_level")
+    return g_t, h_out
 
 
 def merge_stage_uniform_2D_DtN(T_arr, h_arr, l: int, device=None, host_device=None, subtree_recomp: bool = False,

@@ -7,6 +7,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
+#include <vector>
 #include <string>
 
 #include "../../include/jaxhps_gb300.h"
@@ -31,8 +33,54 @@ cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, in
                          const T* gpar, const T* gint, T* gch, cudaStream_t st);
 template <class S, class D>
 cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st);
+cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds, const double* coeffs,
+                        const double* inv_half, const double* D1, const double* D2, const double* Pside,
+                        const double* Qside, const int* perm, const double* u_int, const double* g,
+                        const double* f, float* r_int, double* r_int64, double* flux, double* u_full,
+                        int need_uy, cudaStream_t st);
+cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr, int n_bdry,
+                         const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
+                         cudaStream_t st);
+cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st);
 
 static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// ---- live profiler: event pairs around the launches of the armed classes ----
+constexpr int N_KC = 8;
+struct Profiler {
+  unsigned mask = 0;
+  std::vector<cudaEvent_t> ev;  // 2 per slot
+  std::vector<int> slot_cls;
+  int used = 0;
+  double work[N_KC] = {0};
+  long long launches[N_KC] = {0};
+};
+static Profiler g_prof;
+
+ProfScope::ProfScope(int cls, cudaStream_t s, double w) : on(false), st(s), slot(-1) {
+  if (cls <= 0 || cls >= N_KC || !(g_prof.mask & (1u << cls))) return;
+  if (g_prof.used * 2 + 2 > (int)g_prof.ev.size()) {
+    for (int i = 0; i < 256; ++i) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return;
+      g_prof.ev.push_back(e);
+    }
+  }
+  slot = g_prof.used++;
+  if ((int)g_prof.slot_cls.size() < g_prof.used) g_prof.slot_cls.resize(g_prof.used);
+  g_prof.slot_cls[slot] = cls;
+  on = true;
+  g_prof.work[cls] += w;
+  g_prof.launches[cls] += 1;
+  cudaEventRecord(g_prof.ev[2 * slot], st);
+}
+
+ProfScope::~ProfScope() {
+  if (on) cudaEventRecord(g_prof.ev[2 * slot + 1], st);
+}
 
 void set_error(const char* fmt, ...) {
   char buf[1024];
@@ -198,6 +246,7 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st) {
   T* D = a->D_inv ? (T*)a->D_inv : (T*)cv.take(sizeof(T) * (size_t)nm * ni * ni);
   T* C = (T*)cv.take(sizeof(T) * (size_t)nm * ni * ne);
   T* B = (T*)cv.take(sizeof(T) * (size_t)nm * ne * ni);
+  if (a->B_out) B = (T*)a->B_out;
   T* dh = (T*)cv.take(sizeof(T) * (size_t)nm * ni * (ns > 0 ? ns : 1));
   const size_t invb = inverse_workspace_bytes(a->dtype, ni, nm);
   void* invws = cv.take(invb);
@@ -260,6 +309,22 @@ static int inverse_entry(int n, const void* A, long long lda, long long sA, void
   return HPS_OK;
 }
 
+template <class T>
+static int up_impl(const hps_up_args* a, cudaStream_t st) {
+  const int nm = a->n_merges, ni = a->n_int, ne = a->n_ext, ns = a->nsrc;
+  const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
+  HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, ns, nullptr, (const T*)a->h_children, a->int_c, a->int_l,
+                            a->ext_c, a->ext_l, nullptr, nullptr, nullptr, nullptr, nullptr, (T*)a->dh,
+                            (T*)a->h_out, st));
+  HPS_CHECK(gemm_batched<T>(ni, ns, ni, mone, (const T*)a->D_inv, ni, (long long)ni * ni, (const T*)a->dh, ns,
+                            (long long)ni * ns, zero_, nullptr, 0, 0, (T*)a->g_tilde, ns, (long long)ni * ns, nm,
+                            st));
+  HPS_CHECK(gemm_batched<T>(ne, ns, ni, one_, (const T*)a->B, ni, (long long)ne * ni, (const T*)a->g_tilde, ns,
+                            (long long)ni * ns, one_, (T*)a->h_out, ns, (long long)ne * ns, (T*)a->h_out, ns,
+                            (long long)ne * ns, nm, st));
+  return HPS_OK;
+}
+
 }  // namespace hps
 
 using namespace hps;
@@ -277,6 +342,40 @@ extern "C" {
 
 const char* hps_version(void) { return "jaxhps_gb300 0.1.0 (sm_103a)"; }
 
+long long hps_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int hps_profile_begin(int class_mask) {
+  g_prof.mask = (unsigned)class_mask;
+  g_prof.used = 0;
+  for (int c = 0; c < N_KC; ++c) {
+    g_prof.work[c] = 0.0;
+    g_prof.launches[c] = 0;
+  }
+  return HPS_OK;
+}
+
+int hps_profile_end(double* total_ms, long long* launches, double* work) {
+  double tot[N_KC] = {0};
+  for (int i = 0; i < g_prof.used; ++i) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(g_prof.ev[2 * i + 1]) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, g_prof.ev[2 * i], g_prof.ev[2 * i + 1]) != cudaSuccess) {
+      set_error("hps_profile_end: event query failed");
+      g_prof.mask = 0;
+      return HPS_ERR_CUDA;
+    }
+    tot[g_prof.slot_cls[i]] += ms;
+  }
+  for (int c = 0; c < N_KC; ++c) {
+    if (total_ms) total_ms[c] = tot[c];
+    if (launches) launches[c] = g_prof.launches[c];
+    if (work) work[c] = g_prof.work[c];
+  }
+  g_prof.mask = 0;
+  g_prof.used = 0;
+  return HPS_OK;
+}
+
 int hps_last_error(char* buf, size_t len) {
   if (buf && len) {
     strncpy(buf, g_last_error.c_str(), len - 1);
@@ -284,7 +383,6 @@ int hps_last_error(char* buf, size_t len) {
   }
   return (int)g_last_error.size();
 }
-
 
 int hps_gemm_batched(int dtype, int m, int n, int k, const double* alpha, const void* A, long long lda,
                      long long strideA, const void* B, long long ldb, long long strideB, const double* beta,
@@ -400,6 +498,69 @@ int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
     return HPS_ERR_WORKSPACE;
   }
   DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream)
+}
+
+int hps_up_level(const hps_up_args* a, void* stream) {
+  if (!a || a->n_merges <= 0 || a->nsrc <= 0 || !a->h_children || !a->D_inv || !a->B || !a->dh || !a->g_tilde ||
+      !a->h_out || !a->int_c || !a->int_l || !a->ext_c || !a->ext_l) {
+    set_error("hps_up_level: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  DISPATCH(a->dtype, up_impl, a, (cudaStream_t)stream)
+}
+
+int hps_residual_2d(const hps_residual2d_args* a, void* stream) {
+  if (!a || a->n_leaves <= 0 || a->p < 3 || a->q <= 0 || a->nsrc <= 0 || a->n_ops <= 0 ||
+      !a->coeffs || !a->inv_half || !a->D1 || !a->D2 || !a->Pside || !a->Qside || !a->perm || !a->u_int || !a->g ||
+      !a->f || !a->r_int || !a->flux) {
+    set_error("hps_residual_2d: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (a->n_leaves > 2147483647 || (a->nsrc + 15) / 16 > 65535) {
+    set_error("hps_residual_2d: too many right-hand sides");
+    return HPS_ERR_ARG;
+  }
+  // op kinds packed 4 bits each; D_xy needs the u_y field on the whole grid
+  if (a->n_ops > 10) {
+    set_error("hps_residual_2d: at most 10 operators");
+    return HPS_ERR_ARG;
+  }
+  unsigned long long kinds = 0;
+  int need_uy = 0;
+  for (int o = 0; o < a->n_ops; ++o) {
+    if (a->op_kind[o] < 0 || a->op_kind[o] > 5) {
+      set_error("hps_residual_2d: bad op kind %d", a->op_kind[o]);
+      return HPS_ERR_ARG;
+    }
+    kinds |= (unsigned long long)a->op_kind[o] << (4 * o);
+    if (a->op_kind[o] == 1) need_uy = 1;
+  }
+  HPS_CHECK(residual_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, a->coeffs, a->inv_half, a->D1, a->D2,
+                        a->Pside, a->Qside, a->perm, a->u_int, a->g, a->f, a->r_int, a->r_int64, a->flux, a->u_full,
+                        need_uy, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr, int n_bdry,
+                     const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
+                     void* stream) {
+  if (n_nodes <= 0 || nsrc <= 0 || !nbr || !flux || !hcorr || (n_bdry > 0 && (!bdry_node || !g_given || !g_state ||
+                                                                              !r_bdry))) {
+    set_error("hps_flux_combine: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(flux_combine(n_nodes, nsrc, nbr, flux, hcorr, n_bdry, bdry_node, g_given, g_state, r_bdry,
+                         (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_accumulate(long long n, const float* x, double* y, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) {
+    set_error("hps_accumulate: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(accumulate(n, x, y, (cudaStream_t)stream));
+  return HPS_OK;
 }
 
 int hps_down_level(const hps_down_args* a, void* stream) {

@@ -133,6 +133,9 @@ static cudaError_t launch_gemm_cfg(int M, int N, int K, T alpha, const T* A, lon
   for (int b0 = 0; b0 < batch; b0 += 65535) {
     int nb = batch - b0 < 65535 ? batch - b0 : 65535;
     dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, nb);
+    const double cplx = (sizeof(T) == 16 || (sizeof(T) == 8 && DTypeOf<T>::value == C64)) ? 4.0 : 1.0;
+    ProfScope ps(KC_GEMM, st, 2.0 * cplx * M * (double)N * K * nb);
+    note_launch();
     gemm_kernel<T, BM, BN, BK, TM, TN><<<grid, NT, 0, st>>>(
         M, N, K, alpha, A + b0 * sA, lda, sA, B + b0 * sB, ldb, sB, beta,
         use_c ? C + b0 * sC : nullptr, ldc, sC, D + b0 * sD, ldd, sD, use_c);

@@ -93,11 +93,26 @@ __device__ __forceinline__ c128 rcp_(c128 a) {
 }
 
 // Pivot magnitude: |a| for reals, |re|+|im| for complex (the LAPACK
-// cabs1 convention used by i?amax).
-__device__ __forceinline__ double pivmag(float a) { return fabsf(a); }
+// cabs1 convention used by i?amax), computed in the element's own real
+// precision (FP64 arithmetic is a small fraction of FP32 throughput on
+// GB300, so single-precision kernels never touch it).
+template <class T> struct MagOf;
+template <> struct MagOf<float> { using type = float; };
+template <> struct MagOf<c64> { using type = float; };
+template <> struct MagOf<double> { using type = double; };
+template <> struct MagOf<c128> { using type = double; };
+
+__device__ __forceinline__ float pivmag(float a) { return fabsf(a); }
 __device__ __forceinline__ double pivmag(double a) { return fabs(a); }
-__device__ __forceinline__ double pivmag(c64 a) { return (double)(fabsf(a.x) + fabsf(a.y)); }
+__device__ __forceinline__ float pivmag(c64 a) { return fabsf(a.x) + fabsf(a.y); }
 __device__ __forceinline__ double pivmag(c128 a) { return fabs(a.x) + fabs(a.y); }
+
+// NaN magnitudes are promoted to +inf so that a NaN pivot column is picked
+// (and propagates) instead of leaving no candidate.
+__device__ __forceinline__ float nan_to_inf(float m) { return (m != m) ? __int_as_float(0x7f800000) : m; }
+__device__ __forceinline__ double nan_to_inf(double m) {
+  return (m != m) ? __longlong_as_double(0x7ff0000000000000LL) : m;
+}
 
 // Conversions from the FP64 host-precision inputs.
 template <class T> __device__ __forceinline__ T from_real(double v);

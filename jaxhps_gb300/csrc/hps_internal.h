@@ -27,6 +27,24 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
 // Largest n served by the register-resident single-CTA kernel.
 int inverse_small_nmax(int dtype);
 
+// Number of kernels this library has launched (process-wide), reported by
+// hps_launch_count().  Every launch site calls note_launch().
+void note_launch();
+
+// Kernel classes for the live profiler (hps_profile_begin/end).
+enum KernelClass : int { KC_GEMM = 1, KC_INVERSE = 2, KC_MOVE = 3, KC_RESIDUAL = 4 };
+
+// RAII scope placed around one kernel launch: when the profiler is armed for
+// `cls`, records a CUDA event pair on `st` around the launch and adds the
+// launch's algorithmic flop (or byte) count.
+struct ProfScope {
+  bool on;
+  cudaStream_t st;
+  int slot;
+  ProfScope(int cls, cudaStream_t st, double work);
+  ~ProfScope();
+};
+
 // Records an error message for hps_last_error().
 void set_error(const char* fmt, ...);
 

@@ -70,6 +70,8 @@ cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col
   for (int y0 = 0; y0 < gy; y0 += 65535) {
     const int ny = gy - y0 < 65535 ? gy - y0 : 65535;
     dim3 grid(n_rows, ny);
+    ProfScope ps(KC_MOVE, st, (double)sizeof(T) * n_rows * (double)n_pts * (ny * lpc < n_leaves - y0 * lpc ? ny * lpc : n_leaves - y0 * lpc));
+    note_launch();
     leaf_assemble_kernel<T, CT><<<grid, 256, smem, st>>>(n_leaves, n_pts, row0, col_split, n_ops, ops, coeffs,
                                                          out_lo, ld_lo, s_lo, out_hi, ld_hi, s_hi, lpc,
                                                          y0 * lpc);
@@ -99,6 +101,7 @@ cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds,
   if (gx > 64) gx = 64;
   for (int b0 = 0; b0 < batch; b0 += 65535) {
     const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    note_launch();
     set_rows_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(rows, cols, src, lds, dst + b0 * sd, ldd, sd);
   }
   return cudaGetLastError();
@@ -128,14 +131,14 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
   const long long m = blockIdx.y + m_base;
   const int seg = blockIdx.z;
   const long long nbb = (long long)nb * nb;
-  const T* Tm = Tc + m * nch * nbb;
+  const T* Tm = Tc ? Tc + m * nch * nbb : nullptr;
   const T* hm = hc ? hc + m * nch * (long long)nb * ns : nullptr;
   long long cnt;
   switch (seg) {
-    case 0: cnt = (long long)n_int * n_int; break;
-    case 1: cnt = (long long)n_int * n_ext; break;
-    case 2: cnt = (long long)n_ext * n_int; break;
-    case 3: cnt = (long long)n_ext * n_ext; break;
+    case 0: cnt = Tm ? (long long)n_int * n_int : 0; break;
+    case 1: cnt = Tm ? (long long)n_int * n_ext : 0; break;
+    case 2: cnt = Tm ? (long long)n_ext * n_int : 0; break;
+    case 3: cnt = Tm ? (long long)n_ext * n_ext : 0; break;
     case 4: cnt = hm ? (long long)n_int * ns : 0; break;
     default: cnt = hm ? (long long)n_ext * ns : 0; break;
   }
@@ -190,11 +193,14 @@ template <class T>
 cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Tc, const T* hc,
                          const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
                          const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, cudaStream_t st) {
-  long long big = (long long)n_ext * n_ext;
+  long long big = Tc ? (long long)n_ext * n_ext : (long long)n_ext * ns;
   int gx = (int)((big + 255) / 256);
   if (gx > 512) gx = 512;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    const double outs = Tc ? ((double)n_int * n_int + 2.0 * n_int * n_ext + (double)n_ext * n_ext) : 0.0;
+    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (outs + (double)(n_int + n_ext) * ns));
+    note_launch();
     merge_gather_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Tc, hc, int_c, int_l,
                                                             ext_c, ext_l, loc, D, C, B, Tout, dh, hext, m0);
   }
@@ -230,6 +236,8 @@ cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, in
   if (gx > 256) gx = 256;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (double)cnt);
+    note_launch();
     down_scatter_kernel<T><<<dim3(gx, nm), 256, 0, st>>>(nch, nb, n_ext, n_int, ns, code, gpar, gint, gch, m0);
   }
   return cudaGetLastError();
@@ -253,6 +261,7 @@ cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   long long g = (n + 255) / 256;
   if (g > 4096) g = 4096;
+  note_launch();
   convert_kernel<S, D><<<(int)g, 256, 0, st>>>(n, src, dst);
   return cudaGetLastError();
 }

@@ -80,12 +80,12 @@ inv_reg_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* X
     }
     __syncthreads();
     // (2) pivot row: every warp computes the same argmax redundantly
-    double best = -1.0;
+    using MagT = typename MagOf<T>::type;
+    MagT best = -1;
     int bi = n;
     for (int i = lane; i < n; i += 32) {
       if (!used[i]) {
-        double mg = pivmag(colbuf[buf][i]);
-        if (mg != mg) mg = __longlong_as_double(0x7ff0000000000000LL);
+        const MagT mg = nan_to_inf(pivmag(colbuf[buf][i]));
         if (mg > best) {
           best = mg;
           bi = i;
@@ -94,7 +94,7 @@ inv_reg_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* X
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
       if (ob > best || (ob == best && oi < bi)) {
         best = ob;
@@ -103,7 +103,7 @@ inv_reg_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* X
     }
     const int r = bi;
     T pinv = zero<T>();
-    if (best > 0.0) {
+    if (best > 0) {
       pinv = rcp_(colbuf[buf][r]);
     } else if (tid == 0 && s_info == 0) {
       s_info = k + 1;
@@ -177,7 +177,7 @@ inv_reg_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* X
 // Blocked Gauss-Jordan (global-memory tableau)
 // --------------------------------------------------------------------------
 constexpr int BP = 32;       // panel width
-constexpr int PANEL_NT = 512;
+constexpr int PANEL_NT = 1024;
 
 struct GjeWs {
   // per-matrix region sizes (elements / bytes), each 256-byte aligned
@@ -189,7 +189,7 @@ static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 static GjeWs gje_layout(size_t es, int n) {
   GjeWs w;
   w.mat = al256(es * (size_t)n * n);
-  w.pan = al256(es * (size_t)n * (BP + 1));
+  w.pan = al256(es * (size_t)n * BP);
   w.u = al256(es * (size_t)n * BP);
   w.g = al256(es * (size_t)BP * n);
   w.h = al256(es * (size_t)BP * n);
@@ -215,39 +215,48 @@ __global__ void gje_copy_in_kernel(int n, const T* __restrict__ A, long long lda
     for (int i = threadIdx.x; i < n; i += blockDim.x) used[b * n + i] = 0;
 }
 
+// Panel pivot selection: Gauss-Jordan restricted to the bw panel columns
+// k0..k0+bw-1 over all n rows, rows already used as pivots excluded.
+// One CTA per matrix.  The panel lives in shared memory column-major
+// (P[c*ldp + i], consecutive threads on consecutive rows: conflict-free)
+// when it fits, otherwise in a global workspace with the same layout.
+// Outputs: the new panel written back into Mat, U (panel with this block's
+// pivot rows zeroed), E (the block's pivot rows = inv(A[R,C])), G (pivot
+// rows of Mat outside the panel columns), piv[k0..k0+bw-1].
 template <class T>
 __global__ void __launch_bounds__(PANEL_NT)
 gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G, T* E, int* piv,
                  unsigned char* used, int* info) {
+  using MagT = typename MagOf<T>::type;
   const long long b = blockIdx.x;
   const long long nn = (long long)n * n;
   T* M = Mat + b * nn;
   int* pv = piv + b * n;
   unsigned char* us = used + b * n;
-  constexpr int ldp = BP + 1;
   extern __shared__ unsigned char smraw[];
-  T* P = use_smem ? reinterpret_cast<T*>(smraw) : Pw + b * (long long)n * ldp;
+  const int ldp = n;
+  T* P = use_smem ? reinterpret_cast<T*>(smraw) : Pw + b * (long long)n * BP;
   __shared__ T rowr[BP];
   __shared__ int Rs[BP];
-  __shared__ double wbest[PANEL_NT / 32];
+  __shared__ MagT wbest[PANEL_NT / 32];
   __shared__ int widx[PANEL_NT / 32];
   __shared__ int s_r;
-  __shared__ double s_best;
+  __shared__ MagT s_best;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int e = tid; e < n * bw; e += PANEL_NT) {
     const int i = e / bw, c = e % bw;
-    P[i * ldp + c] = M[(long long)i * n + k0 + c];
+    P[c * ldp + i] = M[(long long)i * n + k0 + c];
   }
   __syncthreads();
 
   for (int c = 0; c < bw; ++c) {
-    double best = -1.0;
+    const T* col = P + c * ldp;
+    MagT best = -1;
     int bi = n;
     for (int i = tid; i < n; i += PANEL_NT) {
       if (!us[i]) {
-        double mg = pivmag(P[i * ldp + c]);
-        if (mg != mg) mg = __longlong_as_double(0x7ff0000000000000LL);
+        const MagT mg = nan_to_inf(pivmag(col[i]));
         if (mg > best) {
           best = mg;
           bi = i;
@@ -256,7 +265,7 @@ gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G,
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
       if (ob > best || (ob == best && oi < bi)) {
         best = ob;
@@ -268,35 +277,40 @@ gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G,
       widx[warp] = bi;
     }
     __syncthreads();
-    if (tid == 0) {
-      double bb = wbest[0];
-      int bx = widx[0];
-      for (int w = 1; w < PANEL_NT / 32; ++w)
-        if (wbest[w] > bb || (wbest[w] == bb && widx[w] < bx)) {
-          bb = wbest[w];
-          bx = widx[w];
+    if (warp == 0) {
+      best = lane < PANEL_NT / 32 ? wbest[lane] : (MagT)-1;
+      bi = lane < PANEL_NT / 32 ? widx[lane] : n;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
         }
-      s_r = bx;
-      s_best = bb;
-      us[bx] = 2;  // pivot of the current panel
-      pv[k0 + c] = bx;
-      Rs[c] = bx;
-      if (!(bb > 0.0) && info && info[b] == 0) info[b] = k0 + c + 1;
+      }
+      if (lane == 0) {
+        s_r = bi;
+        s_best = best;
+        us[bi] = 2;  // pivot of the current panel
+        pv[k0 + c] = bi;
+        Rs[c] = bi;
+        if (!(best > 0) && info && info[b] == 0) info[b] = k0 + c + 1;
+      }
     }
     __syncthreads();
     const int r = s_r;
-    const T pinv = (s_best > 0.0) ? rcp_(P[r * ldp + c]) : zero<T>();
-    for (int c2 = tid; c2 < bw; c2 += PANEL_NT) rowr[c2] = mul(P[r * ldp + c2], pinv);
+    const T pinv = (s_best > 0) ? rcp_(col[r]) : zero<T>();
+    if (tid < bw) rowr[tid] = mul(P[tid * ldp + r], pinv);
     __syncthreads();
     for (int i = tid; i < n; i += PANEL_NT) {
-      T* row = P + i * ldp;
       if (i == r) {
-        for (int c2 = 0; c2 < bw; ++c2) row[c2] = rowr[c2];
-        row[c] = pinv;
+        for (int c2 = 0; c2 < bw; ++c2) P[c2 * ldp + i] = rowr[c2];
+        P[c * ldp + i] = pinv;
       } else {
-        const T f = row[c];
-        for (int c2 = 0; c2 < bw; ++c2) row[c2] = fms_(f, rowr[c2], row[c2]);
-        row[c] = neg(mul(f, pinv));
+        const T f = P[c * ldp + i];
+        for (int c2 = 0; c2 < bw; ++c2) P[c2 * ldp + i] = fms_(f, rowr[c2], P[c2 * ldp + i]);
+        P[c * ldp + i] = neg(mul(f, pinv));
       }
     }
     __syncthreads();
@@ -308,13 +322,13 @@ gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G,
   T* Eb = E + b * (long long)BP * BP;
   for (int e = tid; e < n * bw; e += PANEL_NT) {
     const int i = e / bw, c = e % bw;
-    const T v = P[i * ldp + c];
+    const T v = P[c * ldp + i];
     M[(long long)i * n + k0 + c] = v;
     Ub[(long long)i * BP + c] = (us[i] == 2) ? zero<T>() : v;
   }
   for (int e = tid; e < bw * bw; e += PANEL_NT) {
     const int c1 = e / bw, c2 = e % bw;
-    Eb[c1 * BP + c2] = P[Rs[c1] * ldp + c2];
+    Eb[c1 * BP + c2] = P[c2 * ldp + Rs[c1]];
   }
   for (long long e = tid; e < (long long)bw * n; e += PANEL_NT) {
     const int c1 = (int)(e / n), j = (int)(e % n);
@@ -380,6 +394,9 @@ static cudaError_t launch_reg(int n, const T* A, long long lda, long long sA, T*
                              long long sX, int batch, int* info, cudaStream_t st) {
   for (int b0 = 0; b0 < batch; b0 += 1 << 30) {
     const int nb = batch - b0;
+    const double cplx = (DTypeOf<T>::value == C64 || DTypeOf<T>::value == C128) ? 4.0 : 1.0;
+    ProfScope ps(KC_INVERSE, st, 2.0 * cplx * (double)n * n * n * nb);
+    note_launch();
     inv_reg_kernel<T, NMAX><<<nb, 512, 0, st>>>(n, A + (long long)b0 * sA, lda, sA,
                                                 X + (long long)b0 * sX, ldx, sX,
                                                 info ? info + b0 : nullptr);
@@ -460,17 +477,24 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
     const int nb = (batch - b0) < 65535 ? (batch - b0) : 65535;
     int gx = (int)((nn + 255) / 256);
     if (gx > 1024) gx = 1024;
+    note_launch();
     gje_copy_in_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(n, A + (long long)b0 * sA, lda, sA,
                                                         Mat + (long long)b0 * nn, used + (long long)b0 * n);
   }
-  const size_t pan_smem = es * (size_t)n * (BP + 1);
-  const int use_smem = pan_smem <= 160 * 1024;
+  // Panel width: the widest of 32/16/8/4 whose panel fits in shared memory;
+  // wider panels mean fewer (rank-bw) trailing GEMM updates.
+  int bwmax = BP;
+  while (bwmax > 4 && es * (size_t)n * bwmax > 200 * 1024) bwmax /= 2;
+  const size_t pan_smem = es * (size_t)n * bwmax;
+  const int use_smem = pan_smem <= 200 * 1024;
+  if (!use_smem) bwmax = BP;
   if (use_smem)
-    cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)pan_smem);
+    cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pan_smem);
   const T one_ = one<T>();
-  for (int k0 = 0; k0 < n; k0 += BP) {
-    const int bw = (n - k0) < BP ? (n - k0) : BP;
+  for (int k0 = 0; k0 < n; k0 += bwmax) {
+    const int bw = (n - k0) < bwmax ? (n - k0) : bwmax;
+    ProfScope ps(KC_INVERSE, st, 2.0 * (double)n * bw * bw * batch);
+    note_launch();
     gje_panel_kernel<T><<<batch, PANEL_NT, use_smem ? pan_smem : 0, st>>>(
         n, k0, bw, Mat, Pw, use_smem, U, G, E, piv, used, info);
     cudaError_t e = cudaGetLastError();
@@ -486,16 +510,19 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
     for (int b0 = 0; b0 < batch; b0 += 65535) {
       const int nb = (batch - b0) < 65535 ? (batch - b0) : 65535;
       int gx = (bw * n + 255) / 256;
+      note_launch();
       gje_scatter_rows_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(
           n, k0, bw, Mat + (long long)b0 * nn, H + (long long)b0 * BP * n, piv + (long long)b0 * n);
     }
   }
   for (int b0 = 0; b0 < batch; b0 += 65535) {
     const int nb = (batch - b0) < 65535 ? (batch - b0) : 65535;
+    note_launch();
     gje_rinv_kernel<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(n, piv + (long long)b0 * n,
                                                                rinv + (long long)b0 * n);
     int gx = (int)((nn + 255) / 256);
     if (gx > 2048) gx = 2048;
+    note_launch();
     gje_permute_out_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(
         n, Mat + (long long)b0 * nn, piv + (long long)b0 * n, rinv + (long long)b0 * n,
         X + (long long)b0 * sX, ldx, sX);

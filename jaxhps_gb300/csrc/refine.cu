@@ -1,0 +1,277 @@
+// FP64 residual of the discrete HPS system and the bookkeeping kernels of
+// mixed-precision iterative refinement.
+//
+// The HPS direct solver (leaf solves, merges, down pass) solves, for every
+// leaf, the collocation equations at the interior Chebyshev points
+//     A_ii u_int + A_ie (P g) = f_int                       (leaf rows)
+// together with continuity of the outward normal derivative (Q u) across
+// every interior interface Gauss node and the Dirichlet data on the domain
+// boundary.  With the solver operators built in FP32, refinement iterates
+//     r = b - J x   (FP64, this file),   x += HPS_fp32(r)
+// until x is the FP64 discrete solution.  The residual uses the tensor
+// structure of the spectral operators: derivatives are 1D Chebyshev
+// differentiation along one grid axis (p MACs per point and operator)
+// instead of dense p^2 x p^2 products.
+#include "hps_common.cuh"
+#include "hps_internal.h"
+
+namespace hps {
+
+// op kinds (2D), matching the reference's coefficient stacking order
+// (local_solve/_uniform_2D_DtN.py:59-68)
+enum OpKind2D : int { OP_XX = 0, OP_XY = 1, OP_YY = 2, OP_X = 3, OP_Y = 4, OP_I = 5 };
+
+constexpr int RES_SC = 16;   // right-hand sides per CTA
+constexpr int RES_NT = 256;
+
+// One CTA per (leaf, chunk of RES_SC right-hand sides).
+// Grid values are kept in shared memory in the natural meshgrid layout
+// u[(ix*p + iy)*RES_SC + s]  (iy = 0 is the north row, y decreasing).
+__global__ void __launch_bounds__(RES_NT)
+residual_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
+                   const double* __restrict__ coeffs, const double* __restrict__ inv_half,
+                   const double* __restrict__ D1g, const double* __restrict__ D2g,
+                   const double* __restrict__ Pside_g, const double* __restrict__ Qside_g,
+                   const int* __restrict__ perm_g, const double* __restrict__ u_int,
+                   const double* __restrict__ g, const double* __restrict__ f, float* r_int, double* r_int64,
+                   double* flux, double* u_full, int need_uy) {
+  extern __shared__ double sm[];
+  const int pp = p * p;
+  const int ncb = 4 * (p - 1);
+  const int ni = pp - ncb;
+  const int nq = 4 * q;
+  double* u = sm;                         // pp * SC
+  double* uy = u + pp * RES_SC;           // pp * SC (only when D_xy is active)
+  double* gs = uy + (need_uy ? pp * RES_SC : 0);  // nq * SC
+  double* nd = gs + nq * RES_SC;          // 4p * SC
+  double* D1 = nd + 4 * p * RES_SC;       // p*p
+  double* D2 = D1 + pp;                   // p*p
+  double* Ps = D2 + pp;                   // p*q
+  double* Qs = Ps + p * q;                // q*p
+  int* perm = reinterpret_cast<int*>(Qs + q * p);  // pp
+
+  const long long l = blockIdx.x;
+  const int s0 = blockIdx.y * RES_SC;
+  const int sc = min(RES_SC, nsrc - s0);
+  const int tid = threadIdx.x;
+  const double ih = inv_half[l];
+  const double ih2 = ih * ih;
+
+  for (int e = tid; e < pp; e += RES_NT) {
+    D1[e] = D1g[e];
+    D2[e] = D2g[e];
+    perm[e] = perm_g[e];
+  }
+  for (int e = tid; e < p * q; e += RES_NT) {
+    Ps[e] = Pside_g[e];
+    Qs[e] = Qside_g[e];
+  }
+  for (int e = tid; e < nq * RES_SC; e += RES_NT) {
+    const int k = e / RES_SC, s = e % RES_SC;
+    gs[e] = (s < sc) ? g[(l * nq + k) * nsrc + s0 + s] : 0.0;
+  }
+  __syncthreads();
+  // interior values
+  for (int e = tid; e < ni * RES_SC; e += RES_NT) {
+    const int i = e / RES_SC, s = e % RES_SC;
+    u[perm[ncb + i] * RES_SC + s] = (s < sc) ? u_int[(l * ni + i) * nsrc + s0 + s] : 0.0;
+  }
+  // Chebyshev boundary values u_b = P g: side t-th point interpolated from
+  // the side's q Gauss values; the four corners average their two sides
+  // (_precompute_operators_2D.py:48-79).
+  for (int e = tid; e < ncb * RES_SC; e += RES_NT) {
+    const int k = e / RES_SC, s = e % RES_SC;
+    double acc = 0.0;
+    int cnt = 0;
+#pragma unroll
+    for (int side = 0; side < 4; ++side) {
+      int t = k - side * (p - 1);
+      if (side == 3 && k == 0) t = p - 1;
+      if (t < 0 || t > p - 1) continue;
+      if (side == 3 && t == p - 1 && k != 0) continue;
+      double v = 0.0;
+      for (int j = 0; j < q; ++j) v = fma(Ps[t * q + j], gs[(side * q + j) * RES_SC + s], v);
+      acc += v;
+      ++cnt;
+    }
+    u[perm[k] * RES_SC + s] = (cnt == 2) ? 0.5 * acc : acc;
+  }
+  __syncthreads();
+  if (need_uy) {
+    for (int e = tid; e < pp * RES_SC; e += RES_NT) {
+      const int idx = e / RES_SC, s = e % RES_SC;
+      const int ix = idx / p, iy = idx % p;
+      double v = 0.0;
+      for (int k = 0; k < p; ++k) v = fma(D1[iy * p + k], u[(ix * p + k) * RES_SC + s], v);
+      uy[e] = -ih * v;
+    }
+    __syncthreads();
+  }
+  // leaf rows: r = f - sum_o c_o * (D_o u) at the interior points
+  for (int e = tid; e < ni * RES_SC; e += RES_NT) {
+    const int i = e / RES_SC, s = e % RES_SC;
+    if (s >= sc) continue;
+    const int idx = perm[ncb + i];
+    const int ix = idx / p, iy = idx % p;
+    const long long pt = (long long)l * pp + ncb + i;
+    double acc = f[pt * nsrc + s0 + s];
+    for (int o = 0; o < n_ops; ++o) {
+      const double c = coeffs[(long long)o * n_leaves * pp + pt];
+      double fld = 0.0;
+      switch ((int)((kinds >> (4 * o)) & 15ull)) {
+        case OP_XX:
+          for (int j = 0; j < p; ++j) fld = fma(D2[ix * p + j], u[(j * p + iy) * RES_SC + s], fld);
+          fld *= ih2;
+          break;
+        case OP_YY:
+          for (int j = 0; j < p; ++j) fld = fma(D2[iy * p + j], u[(ix * p + j) * RES_SC + s], fld);
+          fld *= ih2;
+          break;
+        case OP_X:
+          for (int j = 0; j < p; ++j) fld = fma(D1[ix * p + j], u[(j * p + iy) * RES_SC + s], fld);
+          fld *= ih;
+          break;
+        case OP_Y:
+          for (int j = 0; j < p; ++j) fld = fma(D1[iy * p + j], u[(ix * p + j) * RES_SC + s], fld);
+          fld *= -ih;
+          break;
+        case OP_XY:
+          for (int j = 0; j < p; ++j) fld = fma(D1[ix * p + j], uy[(j * p + iy) * RES_SC + s], fld);
+          fld *= ih;
+          break;
+        default:
+          fld = u[idx * RES_SC + s];
+      }
+      acc = fma(-c, fld, acc);
+    }
+    const long long o = ((long long)l * ni + i) * nsrc + s0 + s;
+    r_int[o] = (float)acc;
+    if (r_int64) r_int64[o] = acc;
+  }
+  // outward normal derivatives at the Chebyshev points of each side
+  // (rows of N, _precompute_operators_2D.py:132-163):
+  //  S: -u_y on iy=p-1 (W->E)   E: u_x on ix=p-1 (S->N)
+  //  N:  u_y on iy=0   (E->W)   W: -u_x on ix=0  (N->S)
+  for (int e = tid; e < 4 * p * RES_SC; e += RES_NT) {
+    const int st = e / RES_SC, s = e % RES_SC;
+    const int side = st / p, t = st % p;
+    double v = 0.0;
+    if (side == 0) {
+      for (int k = 0; k < p; ++k) v = fma(D1[(p - 1) * p + k], u[(t * p + k) * RES_SC + s], v);
+      v *= ih;  // -u_y = +ih * sum D1[iy=p-1][k] u
+    } else if (side == 1) {
+      const int iy = p - 1 - t;
+      for (int j = 0; j < p; ++j) v = fma(D1[(p - 1) * p + j], u[(j * p + iy) * RES_SC + s], v);
+      v *= ih;
+    } else if (side == 2) {
+      const int ix = p - 1 - t;
+      for (int k = 0; k < p; ++k) v = fma(D1[k], u[(ix * p + k) * RES_SC + s], v);
+      v *= -ih;
+    } else {
+      const int iy = t;
+      for (int j = 0; j < p; ++j) v = fma(D1[j], u[(j * p + iy) * RES_SC + s], v);
+      v *= -ih;
+    }
+    nd[e] = v;
+  }
+  __syncthreads();
+  for (int e = tid; e < nq * RES_SC; e += RES_NT) {
+    const int k = e / RES_SC, s = e % RES_SC;
+    if (s >= sc) continue;
+    const int side = k / q, j = k % q;
+    double v = 0.0;
+    for (int t = 0; t < p; ++t) v = fma(Qs[j * p + t], nd[(side * p + t) * RES_SC + s], v);
+    flux[((long long)l * nq + k) * nsrc + s0 + s] = v;
+  }
+  if (u_full) {
+    for (int e = tid; e < pp * RES_SC; e += RES_NT) {
+      const int k = e / RES_SC, s = e % RES_SC;
+      if (s < sc) u_full[((long long)l * pp + k) * nsrc + s0 + s] = u[perm[k] * RES_SC + s];
+    }
+  }
+}
+
+size_t residual_2d_smem(int p, int q, int need_uy) {
+  const int pp = p * p;
+  size_t d = (size_t)pp * RES_SC * (need_uy ? 2 : 1) + (size_t)4 * q * RES_SC + (size_t)4 * p * RES_SC +
+             2 * (size_t)pp + 2 * (size_t)p * q;
+  return d * sizeof(double) + (size_t)pp * sizeof(int);
+}
+
+cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds, const double* coeffs,
+                        const double* inv_half, const double* D1, const double* D2, const double* Pside,
+                        const double* Qside, const int* perm, const double* u_int, const double* g,
+                        const double* f, float* r_int, double* r_int64, double* flux, double* u_full,
+                        int need_uy, cudaStream_t st) {
+  const size_t smem = residual_2d_smem(p, q, need_uy);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(residual_2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid(n_leaves, (nsrc + RES_SC - 1) / RES_SC);
+  const double work = 2.0 * n_leaves * (double)nsrc * (p * p * (double)p * (n_ops + 2) + 8.0 * p * q);
+  ProfScope ps(KC_RESIDUAL, st, work);
+  note_launch();
+  residual_2d_kernel<<<grid, RES_NT, smem, st>>>(n_leaves, p, q, nsrc, n_ops, kinds, coeffs, inv_half, D1, D2,
+                                                 Pside, Qside, perm, u_int, g, f, r_int, r_int64, flux, u_full,
+                                                 need_uy);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Interface flux mismatch and boundary-data residual.
+//   hcorr[l][k] = (F[l][k] + F[nbr(l,k)]) / 2   for interior interface nodes,
+//               0                               on the domain boundary;
+//   r_bdry[b]   = g_given[b] - g[bdry_node(b)].
+// Adding -R/2 = hcorr to the h of both leaves at a node enforces the flux
+// residual R = -(F_a + F_b) in the next merge up-pass.
+// ---------------------------------------------------------------------------
+__global__ void flux_combine_kernel(long long n_nodes, int nsrc, const int* __restrict__ nbr,
+                                    const double* __restrict__ flux, float* hcorr, int n_bdry,
+                                    const int* __restrict__ bdry_node, const double* __restrict__ g_given,
+                                    const double* __restrict__ g_state, float* r_bdry) {
+  const long long total = n_nodes * nsrc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long node = e / nsrc;
+    const int s = (int)(e % nsrc);
+    const int nb = nbr[node];
+    hcorr[e] = (nb >= 0) ? (float)(0.5 * (flux[e] + flux[(long long)nb * nsrc + s])) : 0.0f;
+  }
+  const long long tb = (long long)n_bdry * nsrc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tb;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / nsrc;
+    const int s = (int)(e % nsrc);
+    r_bdry[e] = (float)(g_given[e] - g_state[(long long)bdry_node[b] * nsrc + s]);
+  }
+}
+
+cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr, int n_bdry,
+                         const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
+                         cudaStream_t st) {
+  long long g = (n_nodes * nsrc + 255) / 256;
+  if (g > 8192) g = 8192;
+  if (g < 1) g = 1;
+  ProfScope ps(KC_MOVE, st, (double)n_nodes * nsrc * (8.0 + 8.0 + 4.0) + (double)n_bdry * nsrc * 20.0);
+  note_launch();
+  flux_combine_kernel<<<(int)g, 256, 0, st>>>(n_nodes, nsrc, nbr, flux, hcorr, n_bdry, bdry_node, g_given, g_state,
+                                              r_bdry);
+  return cudaGetLastError();
+}
+
+// y[i] += x[i] (x FP32, y FP64), for n elements; returns nothing.
+__global__ void accumulate_kernel(long long n, const float* __restrict__ x, double* y) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    y[e] += (double)x[e];
+}
+
+cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st) {
+  long long g = (n + 255) / 256;
+  if (g > 8192) g = 8192;
+  if (g < 1) g = 1;
+  ProfScope ps(KC_MOVE, st, 20.0 * (double)n);
+  note_launch();
+  accumulate_kernel<<<(int)g, 256, 0, st>>>(n, x, y);
+  return cudaGetLastError();
+}
+
+}  // namespace hps

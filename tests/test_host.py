@@ -169,3 +169,49 @@ def test_pdeproblem_validation():
     cs, ops = pde.active_coefficients()
     assert len(cs) == 2 and ops[0] is pde.D_xx and ops[1] is pde.D_yy
     assert pde.Y is None and pde.S_lst == []
+
+
+@pytest.mark.parametrize("L,q", [(1, 4), (3, 6)])
+def test_leaf_node_maps(L, q):
+    from jaxhps_gb300 import _refinement as rf
+
+    root = hps.DiscretizationNode2D(-1.0, 1.0, -2.0, 0.0)
+    dom = hps.Domain(p=q + 2, q=q, root=root, L=L)
+    nodes = rf.leaf_gauss_nodes_2D(g2.uniform_leaf_bounds_2D(root.bounds, L), q)
+    nbr, bnode = rf.node_maps(nodes, dom.boundary_points, scale=2.0)
+    flat = nodes.reshape(-1, 2)
+    inner = nbr >= 0
+    # symmetric pairing of coinciding nodes
+    assert (nbr[nbr[inner]] == np.nonzero(inner)[0]).all()
+    assert np.allclose(flat[inner], flat[nbr[inner]])
+    # every interior edge node paired, every boundary node mapped once
+    assert (~inner).sum() == dom.boundary_points.shape[0]
+    assert np.allclose(flat[bnode], dom.boundary_points)
+    assert len(set(bnode.tolist())) == len(bnode)
+
+
+def test_oracle_solution_is_zero_of_refinement_residual():
+    """The refinement drives r = b - J x to zero.  At the oracle's FP64
+    solution the leaf rows and the interface flux mismatch vanish."""
+    from jaxhps_gb300 import _refinement as rf
+
+    L, p, q = 2, 8, 6
+    rng = np.random.default_rng(5)
+    root = (-1.0, 1.0, -1.0, 1.0)
+    pts = O.leaf_points_2D(O.uniform_leaf_bounds_2D(root, L), p)
+    c = 1 + 0.3 * np.sin(pts[..., 0] * 2)
+    ones = np.ones_like(c)
+    f = rng.standard_normal(pts.shape[:2])
+    pr = O.Problem2D(root, L, p, q, {"D_xx": ones, "D_yy": ones, "I": c}, f).build()
+    bp = pr.boundary_points
+    u = pr.solve(np.cos(bp[:, 0]) * bp[:, 1])
+    A = O.assemble_operator(pr.coeffs, pr.ops, 4 ** L, p * p)
+    ncb = 4 * (p - 1)
+    r1 = f[:, ncb:] - np.einsum("lij,lj->li", A[:, ncb:, :], u)
+    assert np.abs(r1).max() < 1e-10 * np.abs(f).max()
+    F = np.einsum("ij,lj->li", pr.Q, u)
+    nodes = rf.leaf_gauss_nodes_2D(O.uniform_leaf_bounds_2D(root, L), q)
+    nbr, _ = rf.node_maps(nodes, bp, scale=2.0)
+    Ff = F.reshape(-1)
+    inner = nbr >= 0
+    assert np.abs(Ff[inner] + Ff[nbr[inner]]).max() < 1e-9 * np.abs(F).max()
