@@ -269,7 +269,7 @@ typedef struct {
   const int* perm;         /* (p*p) meshgrid index of every exterior-first point */
   const double* u_int;     /* (n_leaves, n_i, nsrc) interior values */
   const double* g;         /* (n_leaves, 4q, nsrc) leaf boundary Gauss values */
-  const double* f;         /* (n_leaves, p*p, nsrc) source */
+  const double* f;         /* (n_leaves, p*p, nsrc) source, or NULL for a zero source */
   float* r_int;            /* out (n_leaves, n_i, nsrc) leaf-row residual, rounded to FP32 */
   double* r_int64;         /* out, same in FP64, or NULL */
   double* flux;            /* out (n_leaves, 4q, nsrc) outward normal derivative at the Gauss nodes */
@@ -278,14 +278,32 @@ typedef struct {
 
 HPS_API int hps_residual_2d(const hps_residual2d_args* a, void* stream);
 
+/* Incremental update of the residual for corrections du (n_leaves, n_i, nsrc)
+ * and dg (n_leaves, 4q, nsrc), both FP32:
+ *   a->r_int64 -= (A du_full)_int   (FP64, in/out; a->r_int gets its FP32 copy)
+ *   a->flux    += Q du_full          (FP64, in/out)
+ * with du_full = [P dg ; du], evaluated in double-float (FP32-pair)
+ * arithmetic on the FP32 pipe. */
+HPS_API int hps_residual_update_2d(const hps_residual2d_args* a, const float* du, const float* dg, void* stream);
+
+/* u_full = [P g ; u_int] per leaf (FP64), exterior-first leaf order. */
+HPS_API int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
+                              const double* g, double* u_full, void* stream);
+
+/* r32 = f[:, n_cb:, :] rounded to FP32 (the residual at zero). */
+HPS_API int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32,
+                             void* stream);
+
 /* hcorr[node] = (flux[node] + flux[nbr[node]]) / 2 (0 where nbr < 0);
- * r_bdry[b] = g_given[b] - g_state[bdry_node[b]].  Node = leaf*4q + k. */
+ * r_bdry[b] = g_given[b] - g_state[bdry_node[b]] (g_given NULL: zero data).
+ * Node = leaf*4q + k. */
 HPS_API int hps_flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr,
                              int n_bdry, const int* bdry_node, const double* g_given, const double* g_state,
                              float* r_bdry, void* stream);
 
 /* y += x elementwise (x FP32, y FP64). */
 HPS_API int hps_accumulate(long long n, const float* x, double* y, void* stream);
+
 
 #ifdef __cplusplus
 }

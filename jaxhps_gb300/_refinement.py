@@ -143,7 +143,63 @@ def _domain_constants(dom, dev):
     return consts
 
 
-def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12, max_iters: int = 30):
+def _coefficient_stack(pde_problem, dev):
+    cs, names = [], []
+    for name in COEFF_NAMES_2D:
+        c = getattr(pde_problem, f"{name}_coefficients")
+        if c is not None:
+            if st._is_complex(c):
+                raise NotImplementedError("mixed precision with complex coefficients is not implemented")
+            cs.append(st._as_tensor(c, torch.float64, dev))
+            names.append(name)
+    return torch.stack(cs).contiguous(), names
+
+
+def _refine_leaf_operators(dom, coeffs, op_kind, consts, Y, Aii_inv, Q_int):
+    """One refinement step of the FP32 leaf solution operators.
+
+    Y_int solves A_ii Y_int = W, W = -A_ie P.  With the FP32 solution Y0,
+    R = W - A_ii Y0 and T0 = Q [P ; Y0] are evaluated in double-float
+    arithmetic (hps_residual_update_2d applied to the 4q Gauss-data columns),
+    then Y_int = Y0 + inv(A_ii) R and T = T0 + Q_int inv(A_ii) R in FP32.
+    FP32 evaluation of W and Q Y cancels terms ~1e8 times larger than the
+    DtN map's smallest eigenvalues (the near-constant modes); this step
+    restores those modes to FP32 rounding level.  Returns the refined T."""
+    n_leaves, n_pts, nq = Y.shape
+    p, q = dom.p, dom.q
+    n_cb = 4 * (p - 1)
+    dev = Y.device
+    Y0 = Y[:, n_cb:, :].contiguous()
+    dg = torch.eye(nq, dtype=torch.float32, device=dev).expand(n_leaves, nq, nq).contiguous()
+    r64 = torch.zeros(Y0.shape, dtype=torch.float64, device=dev)
+    r32 = torch.empty(Y0.shape, dtype=torch.float32, device=dev)
+    T0 = torch.zeros((n_leaves, nq, nq), dtype=torch.float64, device=dev)
+    a = nat.Residual2DArgs(
+        n_leaves=n_leaves, p=p, q=q, nsrc=nq, n_ops=len(op_kind), coeffs=coeffs.data_ptr(),
+        inv_half=consts["inv_half"].data_ptr(), D1=consts["D1"].data_ptr(), D2=consts["D2"].data_ptr(),
+        Pside=consts["Pside"].data_ptr(), Qside=consts["Qside"].data_ptr(), perm=consts["perm"].data_ptr(),
+        u_int=None, g=None, f=None, r_int=r32.data_ptr(), r_int64=r64.data_ptr(), flux=T0.data_ptr(), u_full=None)
+    for i, k in enumerate(op_kind):
+        a.op_kind[i] = k
+    nat.check(nat.lib().hps_residual_update_2d(C.byref(a), Y0.data_ptr(), dg.data_ptr(), nat.stream_ptr()),
+              "hps_residual_update_2d")
+    dY = torch.empty_like(r32)
+    nat.gemm(Aii_inv, r32, dY)                      # dY = inv(A_ii) R
+    Y_int = Y[:, n_cb:, :]
+    nat.gemm(Aii_inv, r32, Y_int, 1.0, 1.0, Cmat=Y0)  # Y_int = Y0 + dY
+    T = torch.empty((n_leaves, nq, nq), dtype=torch.float32, device=dev)
+    nat.check(nat.lib().hps_convert(nat.HPS_F64, nat.HPS_F32, T0.numel(), T0.data_ptr(), T.data_ptr(),
+                                    nat.stream_ptr()), "hps_convert")
+    nat.gemm(Q_int, dY, T, 1.0, 1.0, Cmat=T)        # T = T0 + Q_int dY
+    return T
+
+
+def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12, max_iters: int = 30,
+                leaf_dtype=torch.float32, merge_dtype=torch.float32, top_fp64_levels: int = 0,
+                leaf_refine: bool = True):
+    """FP32 build of the solver operators (see module docstring).  leaf_dtype /
+    merge_dtype / top_fp64_levels select the arithmetic of the leaf stage, of
+    the merges and of the top merge levels; the stored operators are FP32."""
     dom = pde_problem.domain
     if pde_problem.use_ItI or not dom.bool_2D or not dom.bool_uniform:
         raise NotImplementedError("mixed precision is implemented for uniform 2D DtN problems")
@@ -152,30 +208,29 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     dev = st._device(device)
     p, q, n_leaves = dom.p, dom.q, dom.n_leaves
     n_cb = 4 * (p - 1)
-    Y, T, _, _, Aii = st._local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, dev, torch.float32,
+    Y, T, _, _, Aii = st._local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, dev, leaf_dtype,
                                           keep_inverse=True, want_source=False)
+    Y, Aii = Y.float(), Aii.float()
+    coeffs, names = _coefficient_stack(pde_problem, dev)
+    consts = _domain_constants(dom, dev)
+    if leaf_refine and leaf_dtype == torch.float32:
+        T = _refine_leaf_operators(dom, coeffs, [OP_KIND_2D[n] for n in names], consts, Y, Aii,
+                                   torch.as_tensor(np.ascontiguousarray(pde_problem.Q[:, n_cb:]), device=dev,
+                                                   dtype=torch.float32))
     S_lst, Dinv_lst, B_lst = [], [], []
-    Tc = T
-    for _ in range(max(dom.L, 1)):
+    Tc = T.to(merge_dtype)
+    for lvl in range(max(dom.L, 1)):
         maps = quad_merge_maps_dtn(Tc.shape[1] // 4)
+        if lvl == dom.L - top_fp64_levels:
+            Tc = Tc.double()
         S, _, Tc, _, Dinv, _, B = st.merge_level_dtn(Tc, None, maps, keep_D_inv=True, keep_B=True)
-        S_lst.append(S)
-        Dinv_lst.append(Dinv)
-        B_lst.append(B)
+        S_lst.append(S.float())
+        Dinv_lst.append(Dinv.float())
+        B_lst.append(B.float())
     del T
 
-    cs, names = [], []
-    for name in COEFF_NAMES_2D:
-        c = getattr(pde_problem, f"{name}_coefficients")
-        if c is not None:
-            cs.append(st._as_tensor(c, torch.float64, dev))
-            names.append(name)
-    if any(st._is_complex(c) for c in cs):
-        raise NotImplementedError("mixed precision with complex coefficients is not implemented")
-    coeffs = torch.stack(cs).contiguous()
     f, multi = st._src3(pde_problem.source, n_leaves, p * p, torch.float64, dev)
 
-    consts = _domain_constants(dom, dev)
     Q32 = torch.as_tensor(np.ascontiguousarray(pde_problem.Q[:, n_cb:]), device=dev, dtype=torch.float32)
     state = MixedState(
         mixed=True, n_leaves=n_leaves, p=p, q=q, Y_int=Y[:, n_cb:, :], Aii_inv=Aii, Q_int=Q32, S_lst=S_lst,
@@ -192,17 +247,30 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     return None
 
 
-def _residual(state: MixedState, u_int, g, r32, flux, u_full=None):
+def _res_args(state: MixedState, u_int, g, r32, flux, r64=None, u_full=None, zero_source=False):
     c = state.consts
     a = nat.Residual2DArgs(
-        n_leaves=state.n_leaves, p=state.p, q=state.q, nsrc=u_int.shape[-1], n_ops=len(state.op_kind),
+        n_leaves=state.n_leaves, p=state.p, q=state.q, nsrc=r32.shape[-1], n_ops=len(state.op_kind),
         coeffs=state.coeffs.data_ptr(), inv_half=c["inv_half"].data_ptr(), D1=c["D1"].data_ptr(),
         D2=c["D2"].data_ptr(), Pside=c["Pside"].data_ptr(), Qside=c["Qside"].data_ptr(), perm=c["perm"].data_ptr(),
-        u_int=u_int.data_ptr(), g=g.data_ptr(), f=state.f.data_ptr(), r_int=r32.data_ptr(), r_int64=None,
-        flux=flux.data_ptr(), u_full=nat.ptr(u_full))
+        u_int=nat.ptr(u_int), g=nat.ptr(g), f=None if zero_source else state.f.data_ptr(),
+        r_int=r32.data_ptr(), r_int64=nat.ptr(r64), flux=flux.data_ptr(), u_full=nat.ptr(u_full))
     for i, k in enumerate(state.op_kind):
         a.op_kind[i] = k
+    return a
+
+
+def _residual(state: MixedState, u_int, g, r32, flux, u_full=None, zero_source=False, r64=None):
+    """FP64 residual of the discrete system at (u_int, g); zero_source drops f."""
+    a = _res_args(state, u_int, g, r32, flux, r64=r64, u_full=u_full, zero_source=zero_source)
     nat.check(nat.lib().hps_residual_2d(C.byref(a), nat.stream_ptr()), "hps_residual_2d")
+
+
+def _residual_update(state: MixedState, du, dg, r64, r32, flux):
+    """r64 -= (A du)_int, flux += Q du_full (double-float arithmetic)."""
+    a = _res_args(state, None, None, r32, flux, r64=r64)
+    nat.check(nat.lib().hps_residual_update_2d(C.byref(a), du.data_ptr(), dg.data_ptr(), nat.stream_ptr()),
+              "hps_residual_update_2d")
 
 
 def correction(state: MixedState, r32, hcorr, rb32):
@@ -250,25 +318,36 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
     u_int = torch.zeros((nl, n_i, ns), dtype=torch.float64, device=dev)
     g = torch.zeros((nl, 4 * q, ns), dtype=torch.float64, device=dev)
     r32 = torch.empty((nl, n_i, ns), dtype=torch.float32, device=dev)
-    flux = torch.empty((nl, 4 * q, ns), dtype=torch.float64, device=dev)
+    r64 = torch.empty((nl, n_i, ns), dtype=torch.float64, device=dev)
+    flux = torch.zeros((nl, 4 * q, ns), dtype=torch.float64, device=dev)
     hcorr = torch.empty((nl, 4 * q, ns), dtype=torch.float32, device=dev)
     rb32 = torch.empty((g_given.shape[0], ns), dtype=torch.float32, device=dev)
+    sp = nat.stream_ptr()
+    # residual at x = 0 is b itself
+    nat.check(L.hps_interior_f32(nl, p * p, 4 * (p - 1), ns, state.f.data_ptr(), r32.data_ptr(), sp),
+              "hps_interior_f32")
     state.history = []
     for it in range(max_iters):
-        _residual(state, u_int, g, r32, flux)
         nat.check(L.hps_flux_combine(nl * 4 * q, ns, state.nbr.data_ptr(), flux.data_ptr(), hcorr.data_ptr(),
                                      g_given.shape[0], state.bnode.data_ptr(), g_given.data_ptr(), g.data_ptr(),
-                                     rb32.data_ptr(), nat.stream_ptr()), "hps_flux_combine")
+                                     rb32.data_ptr(), sp), "hps_flux_combine")
         du, dg = correction(state, r32, hcorr, rb32)
-        nat.check(L.hps_accumulate(du.numel(), du.data_ptr(), u_int.data_ptr(), nat.stream_ptr()), "hps_accumulate")
-        nat.check(L.hps_accumulate(dg.numel(), dg.data_ptr(), g.data_ptr(), nat.stream_ptr()), "hps_accumulate")
+        nat.check(L.hps_accumulate(du.numel(), du.data_ptr(), u_int.data_ptr(), sp), "hps_accumulate")
+        nat.check(L.hps_accumulate(dg.numel(), dg.data_ptr(), g.data_ptr(), sp), "hps_accumulate")
         step = float(du.abs().max().item())
         size = float(u_int.abs().max().item())
         state.history.append(step / max(size, 1e-300))
         if step <= tol * size:
             break
+        if it == 0:
+            # the first correction is the size of the solution: recompute the
+            # residual from scratch in FP64
+            _residual(state, u_int, g, r32, flux, r64=r64)
+        else:
+            _residual_update(state, du, dg, r64, r32, flux)
     u = torch.empty((nl, p * p, ns), dtype=torch.float64, device=dev)
-    _residual(state, u_int, g, r32, flux, u_full=u)
+    nat.check(L.hps_assemble_u_2d(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_int.data_ptr(), g.data_ptr(),
+                                  u.data_ptr(), sp), "hps_assemble_u_2d")
     if not state.multi:
         u = u[..., 0]
     return st._to_host(u, host_device)

@@ -42,6 +42,13 @@ cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const doub
                          const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
                          cudaStream_t st);
 cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st);
+cudaError_t jx_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
+                         const double* coeffs, const double* inv_half, const double* D1, const double* D2,
+                         const double* Pside, const double* Qside, const int* perm, const float* du, const float* dg,
+                         double* r_int, float* r32, double* flux, int need_uy, cudaStream_t st);
+cudaError_t assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
+                          const double* g, double* u_full, cudaStream_t st);
+cudaError_t interior_f32(long long n_leaves, int pp, int ncb, int nsrc, const double* f, float* r32, cudaStream_t st);
 
 static thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};
@@ -509,10 +516,68 @@ int hps_up_level(const hps_up_args* a, void* stream) {
   DISPATCH(a->dtype, up_impl, a, (cudaStream_t)stream)
 }
 
+static int pack_op_kinds(const hps_residual2d_args* a, unsigned long long* kinds, int* need_uy) {
+  // op kinds packed 4 bits each; D_xy needs the u_y field on the whole grid
+  if (a->n_ops > 10) {
+    set_error("residual: at most 10 operators");
+    return HPS_ERR_ARG;
+  }
+  *kinds = 0;
+  *need_uy = 0;
+  for (int o = 0; o < a->n_ops; ++o) {
+    if (a->op_kind[o] < 0 || a->op_kind[o] > 5) {
+      set_error("residual: bad op kind %d", a->op_kind[o]);
+      return HPS_ERR_ARG;
+    }
+    *kinds |= (unsigned long long)a->op_kind[o] << (4 * o);
+    if (a->op_kind[o] == 1) *need_uy = 1;
+  }
+  return HPS_OK;
+}
+
+int hps_residual_update_2d(const hps_residual2d_args* a, const float* du, const float* dg, void* stream) {
+  if (!a || a->n_leaves <= 0 || a->p < 3 || a->q <= 0 || a->nsrc <= 0 || a->n_ops <= 0 || !a->coeffs ||
+      !a->inv_half || !a->D1 || !a->D2 || !a->Pside || !a->Qside || !a->perm || !du || !dg || !a->r_int ||
+      !a->r_int64 || !a->flux) {
+    set_error("hps_residual_update_2d: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if ((a->nsrc + 15) / 16 > 65535) {
+    set_error("hps_residual_update_2d: too many right-hand sides");
+    return HPS_ERR_ARG;
+  }
+  unsigned long long kinds = 0;
+  int need_uy = 0;
+  if (pack_op_kinds(a, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
+  HPS_CHECK(jx_update_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, a->coeffs, a->inv_half, a->D1, a->D2,
+                         a->Pside, a->Qside, a->perm, du, dg, a->r_int64, a->r_int, a->flux, need_uy,
+                         (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
+                      const double* g, double* u_full, void* stream) {
+  if (n_leaves <= 0 || p < 3 || q <= 0 || nsrc <= 0 || !Pside || !u_int || !g || !u_full) {
+    set_error("hps_assemble_u_2d: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(assemble_u_2d(n_leaves, p, q, nsrc, Pside, u_int, g, u_full, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32, void* stream) {
+  if (n_leaves <= 0 || n_pts <= n_cb || nsrc <= 0 || !f || !r32) {
+    set_error("hps_interior_f32: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(interior_f32(n_leaves, n_pts, n_cb, nsrc, f, r32, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
 int hps_residual_2d(const hps_residual2d_args* a, void* stream) {
   if (!a || a->n_leaves <= 0 || a->p < 3 || a->q <= 0 || a->nsrc <= 0 || a->n_ops <= 0 ||
       !a->coeffs || !a->inv_half || !a->D1 || !a->D2 || !a->Pside || !a->Qside || !a->perm || !a->u_int || !a->g ||
-      !a->f || !a->r_int || !a->flux) {
+      !a->r_int || !a->flux) {
     set_error("hps_residual_2d: invalid arguments");
     return HPS_ERR_ARG;
   }
@@ -520,21 +585,9 @@ int hps_residual_2d(const hps_residual2d_args* a, void* stream) {
     set_error("hps_residual_2d: too many right-hand sides");
     return HPS_ERR_ARG;
   }
-  // op kinds packed 4 bits each; D_xy needs the u_y field on the whole grid
-  if (a->n_ops > 10) {
-    set_error("hps_residual_2d: at most 10 operators");
-    return HPS_ERR_ARG;
-  }
   unsigned long long kinds = 0;
   int need_uy = 0;
-  for (int o = 0; o < a->n_ops; ++o) {
-    if (a->op_kind[o] < 0 || a->op_kind[o] > 5) {
-      set_error("hps_residual_2d: bad op kind %d", a->op_kind[o]);
-      return HPS_ERR_ARG;
-    }
-    kinds |= (unsigned long long)a->op_kind[o] << (4 * o);
-    if (a->op_kind[o] == 1) need_uy = 1;
-  }
+  if (pack_op_kinds(a, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
   HPS_CHECK(residual_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, a->coeffs, a->inv_half, a->D1, a->D2,
                         a->Pside, a->Qside, a->perm, a->u_int, a->g, a->f, a->r_int, a->r_int64, a->flux, a->u_full,
                         need_uy, (cudaStream_t)stream));
@@ -544,8 +597,7 @@ int hps_residual_2d(const hps_residual2d_args* a, void* stream) {
 int hps_flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr, int n_bdry,
                      const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
                      void* stream) {
-  if (n_nodes <= 0 || nsrc <= 0 || !nbr || !flux || !hcorr || (n_bdry > 0 && (!bdry_node || !g_given || !g_state ||
-                                                                              !r_bdry))) {
+  if (n_nodes <= 0 || nsrc <= 0 || !nbr || !flux || !hcorr || (n_bdry > 0 && (!bdry_node || !g_state || !r_bdry))) {
     set_error("hps_flux_combine: invalid arguments");
     return HPS_ERR_ARG;
   }

@@ -114,7 +114,7 @@ residual_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lon
     const int idx = perm[ncb + i];
     const int ix = idx / p, iy = idx % p;
     const long long pt = (long long)l * pp + ncb + i;
-    double acc = f[pt * nsrc + s0 + s];
+    double acc = f ? f[pt * nsrc + s0 + s] : 0.0;
     for (int o = 0; o < n_ops; ++o) {
       const double c = coeffs[(long long)o * n_leaves * pp + pt];
       double fld = 0.0;
@@ -241,7 +241,7 @@ __global__ void flux_combine_kernel(long long n_nodes, int nsrc, const int* __re
        e += (long long)gridDim.x * blockDim.x) {
     const long long b = e / nsrc;
     const int s = (int)(e % nsrc);
-    r_bdry[e] = (float)(g_given[e] - g_state[(long long)bdry_node[b] * nsrc + s]);
+    r_bdry[e] = (float)((g_given ? g_given[e] : 0.0) - g_state[(long long)bdry_node[b] * nsrc + s]);
   }
 }
 
@@ -271,6 +271,277 @@ cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st) 
   ProfScope ps(KC_MOVE, st, 20.0 * (double)n);
   note_launch();
   accumulate_kernel<<<(int)g, 256, 0, st>>>(n, x, y);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Incremental residual update in double-float arithmetic.
+//
+// After the first FP64 residual, refinement keeps the residual current by
+//     r_int -= (A du)_int,   flux += Q du_full,
+// where du (FP32 interior values) and dg (FP32 Gauss boundary values) are the
+// FP32 corrections.  Products and sums use unevaluated pairs of FP32 numbers
+// (hi + lo, ~48-bit significands) with the error-free transformations
+// TwoProd (by FMA) and TwoSum (Knuth), so the work runs on the FP32 pipe;
+// every correction after the first is at most a few percent of the solution,
+// so the pair arithmetic's rounding enters the residual far below FP64 level.
+// ---------------------------------------------------------------------------
+struct df32 {
+  float hi, lo;
+};
+
+__device__ __forceinline__ df32 df_split(double x) {
+  const float h = __double2float_rn(x);
+  return df32{h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_join(float s, float e) { return (double)s + (double)e; }
+
+// (s, e) += a * b ; s carries the running sum, e the low-order terms
+__device__ __forceinline__ void df_mac(float& s, float& e, df32 a, df32 b) {
+  const float p = a.hi * b.hi;
+  float pe = fmaf(a.hi, b.hi, -p);
+  pe = fmaf(a.hi, b.lo, pe);
+  pe = fmaf(a.lo, b.hi, pe);
+  const float t = s + p;
+  const float bb = t - s;
+  const float err = (s - (t - bb)) + (p - bb);
+  s = t;
+  e += err + pe;
+}
+
+__global__ void __launch_bounds__(RES_NT)
+jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
+                    const double* __restrict__ coeffs, const double* __restrict__ inv_half,
+                    const double* __restrict__ D1g, const double* __restrict__ D2g,
+                    const double* __restrict__ Pside_g, const double* __restrict__ Qside_g,
+                    const int* __restrict__ perm_g, const float* __restrict__ du, const float* __restrict__ dg,
+                    double* r_int, float* r32, double* flux, int need_uy) {
+  extern __shared__ float smf[];
+  const int pp = p * p;
+  const int ncb = 4 * (p - 1);
+  const int ni = pp - ncb;
+  const int nq = 4 * q;
+  df32* u = reinterpret_cast<df32*>(smf);          // pp * SC
+  df32* uy = u + pp * RES_SC;                       // pp * SC when D_xy is active
+  df32* nd = uy + (need_uy ? pp * RES_SC : 0);      // 4p * SC
+  df32* D1 = nd + 4 * p * RES_SC;
+  df32* D2 = D1 + pp;
+  df32* Ps = D2 + pp;
+  df32* Qs = Ps + p * q;
+  float* gs = reinterpret_cast<float*>(Qs + q * p);  // nq * SC
+  int* perm = reinterpret_cast<int*>(gs + nq * RES_SC);
+
+  const long long l = blockIdx.x;
+  const int s0 = blockIdx.y * RES_SC;
+  const int sc = min(RES_SC, nsrc - s0);
+  const int tid = threadIdx.x;
+  const double ih = inv_half[l];
+  const double ih2 = ih * ih;
+
+  for (int e = tid; e < pp; e += RES_NT) {
+    D1[e] = df_split(D1g[e]);
+    D2[e] = df_split(D2g[e]);
+    perm[e] = perm_g[e];
+  }
+  for (int e = tid; e < p * q; e += RES_NT) {
+    Ps[e] = df_split(Pside_g[e]);
+    Qs[e] = df_split(Qside_g[e]);
+  }
+  for (int e = tid; e < nq * RES_SC; e += RES_NT) {
+    const int k = e / RES_SC, s = e % RES_SC;
+    gs[e] = (s < sc) ? dg[(l * nq + k) * nsrc + s0 + s] : 0.f;
+  }
+  __syncthreads();
+  for (int e = tid; e < ni * RES_SC; e += RES_NT) {
+    const int i = e / RES_SC, s = e % RES_SC;
+    u[perm[ncb + i] * RES_SC + s] = df32{(s < sc) ? du[(l * ni + i) * nsrc + s0 + s] : 0.f, 0.f};
+  }
+  for (int e = tid; e < ncb * RES_SC; e += RES_NT) {
+    const int k = e / RES_SC, s = e % RES_SC;
+    float hs = 0.f, he = 0.f;
+    int cnt = 0;
+#pragma unroll
+    for (int side = 0; side < 4; ++side) {
+      int t = k - side * (p - 1);
+      if (side == 3 && k == 0) t = p - 1;
+      if (t < 0 || t > p - 1) continue;
+      if (side == 3 && t == p - 1 && k != 0) continue;
+      for (int j = 0; j < q; ++j) df_mac(hs, he, Ps[t * q + j], df32{gs[(side * q + j) * RES_SC + s], 0.f});
+      ++cnt;
+    }
+    if (cnt == 2) {
+      hs *= 0.5f;
+      he *= 0.5f;
+    }
+    const double v = df_join(hs, he);
+    u[perm[k] * RES_SC + s] = df_split(v);
+  }
+  __syncthreads();
+  if (need_uy) {
+    for (int e = tid; e < pp * RES_SC; e += RES_NT) {
+      const int idx = e / RES_SC, s = e % RES_SC;
+      const int ix = idx / p, iy = idx % p;
+      float hs = 0.f, he = 0.f;
+      for (int k = 0; k < p; ++k) df_mac(hs, he, D1[iy * p + k], u[(ix * p + k) * RES_SC + s]);
+      uy[e] = df_split(-ih * df_join(hs, he));
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < ni * RES_SC; e += RES_NT) {
+    const int i = e / RES_SC, s = e % RES_SC;
+    if (s >= sc) continue;
+    const int idx = perm[ncb + i];
+    const int ix = idx / p, iy = idx % p;
+    const long long pt = (long long)l * pp + ncb + i;
+    double acc = 0.0;
+    for (int o = 0; o < n_ops; ++o) {
+      const double c = coeffs[(long long)o * n_leaves * pp + pt];
+      float hs = 0.f, he = 0.f;
+      double scale = 1.0;
+      switch ((int)((kinds >> (4 * o)) & 15ull)) {
+        case OP_XX:
+          for (int j = 0; j < p; ++j) df_mac(hs, he, D2[ix * p + j], u[(j * p + iy) * RES_SC + s]);
+          scale = ih2;
+          break;
+        case OP_YY:
+          for (int j = 0; j < p; ++j) df_mac(hs, he, D2[iy * p + j], u[(ix * p + j) * RES_SC + s]);
+          scale = ih2;
+          break;
+        case OP_X:
+          for (int j = 0; j < p; ++j) df_mac(hs, he, D1[ix * p + j], u[(j * p + iy) * RES_SC + s]);
+          scale = ih;
+          break;
+        case OP_Y:
+          for (int j = 0; j < p; ++j) df_mac(hs, he, D1[iy * p + j], u[(ix * p + j) * RES_SC + s]);
+          scale = -ih;
+          break;
+        case OP_XY:
+          for (int j = 0; j < p; ++j) df_mac(hs, he, D1[ix * p + j], uy[(j * p + iy) * RES_SC + s]);
+          scale = ih;
+          break;
+        default:
+          hs = u[idx * RES_SC + s].hi;
+          he = u[idx * RES_SC + s].lo;
+      }
+      acc = fma(c * scale, df_join(hs, he), acc);
+    }
+    const long long o = ((long long)l * ni + i) * nsrc + s0 + s;
+    const double r = r_int[o] - acc;
+    r_int[o] = r;
+    r32[o] = (float)r;
+  }
+  for (int e = tid; e < 4 * p * RES_SC; e += RES_NT) {
+    const int st = e / RES_SC, s = e % RES_SC;
+    const int side = st / p, t = st % p;
+    float hs = 0.f, he = 0.f;
+    double sg;
+    if (side == 0) {
+      for (int k = 0; k < p; ++k) df_mac(hs, he, D1[(p - 1) * p + k], u[(t * p + k) * RES_SC + s]);
+      sg = ih;
+    } else if (side == 1) {
+      const int iy = p - 1 - t;
+      for (int j = 0; j < p; ++j) df_mac(hs, he, D1[(p - 1) * p + j], u[(j * p + iy) * RES_SC + s]);
+      sg = ih;
+    } else if (side == 2) {
+      const int ix = p - 1 - t;
+      for (int k = 0; k < p; ++k) df_mac(hs, he, D1[k], u[(ix * p + k) * RES_SC + s]);
+      sg = -ih;
+    } else {
+      for (int j = 0; j < p; ++j) df_mac(hs, he, D1[j], u[(j * p + t) * RES_SC + s]);
+      sg = -ih;
+    }
+    nd[e] = df_split(sg * df_join(hs, he));
+  }
+  __syncthreads();
+  for (int e = tid; e < nq * RES_SC; e += RES_NT) {
+    const int k = e / RES_SC, s = e % RES_SC;
+    if (s >= sc) continue;
+    const int side = k / q, j = k % q;
+    float hs = 0.f, he = 0.f;
+    for (int t = 0; t < p; ++t) df_mac(hs, he, Qs[j * p + t], nd[(side * p + t) * RES_SC + s]);
+    flux[((long long)l * nq + k) * nsrc + s0 + s] += df_join(hs, he);
+  }
+}
+
+size_t jx_update_2d_smem(int p, int q, int need_uy) {
+  const int pp = p * p;
+  size_t pairs = (size_t)pp * RES_SC * (need_uy ? 2 : 1) + (size_t)4 * p * RES_SC + 2 * (size_t)pp +
+                 2 * (size_t)p * q;
+  return pairs * sizeof(df32) + (size_t)4 * q * RES_SC * sizeof(float) + (size_t)pp * sizeof(int);
+}
+
+cudaError_t jx_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
+                         const double* coeffs, const double* inv_half, const double* D1, const double* D2,
+                         const double* Pside, const double* Qside, const int* perm, const float* du, const float* dg,
+                         double* r_int, float* r32, double* flux, int need_uy, cudaStream_t st) {
+  const size_t smem = jx_update_2d_smem(p, q, need_uy);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(jx_update_2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid(n_leaves, (nsrc + RES_SC - 1) / RES_SC);
+  const int ni = p * p - 4 * (p - 1);
+  const double work = 2.0 * n_leaves * (double)nsrc * ((double)ni * p * n_ops + 8.0 * p * q);
+  ProfScope ps(KC_RESIDUAL, st, work);
+  note_launch();
+  jx_update_2d_kernel<<<grid, RES_NT, smem, st>>>(n_leaves, p, q, nsrc, n_ops, kinds, coeffs, inv_half, D1, D2, Pside,
+                                                  Qside, perm, du, dg, r_int, r32, flux, need_uy);
+  return cudaGetLastError();
+}
+
+// u_full[l][k] = (P g)[k] on the Chebyshev boundary and u_int on the interior
+// (FP64), written in the exterior-first leaf order.
+__global__ void assemble_u_2d_kernel(int n_leaves, int p, int q, int nsrc, const double* __restrict__ Pside,
+                                     const double* __restrict__ u_int, const double* __restrict__ g, double* u_full) {
+  const int pp = p * p, ncb = 4 * (p - 1), ni = pp - ncb, nq = 4 * q;
+  const long long l = blockIdx.x;
+  for (int e = threadIdx.x; e < pp * nsrc; e += blockDim.x) {
+    const int k = e / nsrc, s = e % nsrc;
+    double v;
+    if (k >= ncb) {
+      v = u_int[(l * ni + (k - ncb)) * nsrc + s];
+    } else {
+      double acc = 0.0;
+      int cnt = 0;
+      for (int side = 0; side < 4; ++side) {
+        int t = k - side * (p - 1);
+        if (side == 3 && k == 0) t = p - 1;
+        if (t < 0 || t > p - 1) continue;
+        if (side == 3 && t == p - 1 && k != 0) continue;
+        for (int j = 0; j < q; ++j) acc = fma(Pside[t * q + j], g[(l * nq + side * q + j) * nsrc + s], acc);
+        ++cnt;
+      }
+      v = (cnt == 2) ? 0.5 * acc : acc;
+    }
+    u_full[(l * pp + k) * nsrc + s] = v;
+  }
+}
+
+cudaError_t assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
+                          const double* g, double* u_full, cudaStream_t st) {
+  ProfScope ps(KC_MOVE, st, 8.0 * n_leaves * (double)p * p * nsrc * 2.0);
+  note_launch();
+  assemble_u_2d_kernel<<<n_leaves, 256, 0, st>>>(n_leaves, p, q, nsrc, Pside, u_int, g, u_full);
+  return cudaGetLastError();
+}
+
+// r32[l][i][s] = f[l][n_cb + i][s]  (the residual at x = 0, rounded to FP32)
+__global__ void interior_f32_kernel(long long n_leaves, int pp, int ncb, int nsrc, const double* __restrict__ f,
+                                    float* r32) {
+  const int ni = pp - ncb;
+  const long long n = n_leaves * ni * nsrc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const long long l = e / ((long long)ni * nsrc);
+    const long long rem = e % ((long long)ni * nsrc);
+    r32[e] = (float)f[l * pp * nsrc + (long long)ncb * nsrc + rem];
+  }
+}
+
+cudaError_t interior_f32(long long n_leaves, int pp, int ncb, int nsrc, const double* f, float* r32, cudaStream_t st) {
+  long long n = n_leaves * (pp - ncb) * nsrc;
+  long long g = (n + 255) / 256;
+  if (g > 8192) g = 8192;
+  if (g < 1) g = 1;
+  note_launch();
+  interior_f32_kernel<<<(int)g, 256, 0, st>>>(n_leaves, pp, ncb, nsrc, f, r32);
   return cudaGetLastError();
 }
 

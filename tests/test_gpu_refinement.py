@@ -75,3 +75,35 @@ def test_mixed_matches_fp64_oracle(cuda, L, p, q, nsrc, extra):
     hist = pde._state.history
     assert err < 1e-10, (err, hist)
     assert len(hist) < pde._state.max_iters
+
+
+@pytest.mark.parametrize("extra", [False, True])
+def test_incremental_residual_matches_fp64(cuda, extra):
+    """r(x) - J dx evaluated in double-float equals the FP64 residual r(x + dx)."""
+    L, p, q, ns = 2, 10, 8, 5
+    dom, pde, ref = _setup(L, p, q, ns, extra, seed=3)
+    hps.build_solver(pde, precision="mixed")
+    state = pde._state
+    rng = np.random.default_rng(4)
+    nl, ncb = dom.n_leaves, 4 * (p - 1)
+    ni = p * p - ncb
+    u = torch.as_tensor(rng.standard_normal((nl, ni, ns)), device=cuda)
+    g = torch.as_tensor(rng.standard_normal((nl, 4 * q, ns)), device=cuda)
+    du = torch.as_tensor(1e-2 * rng.standard_normal((nl, ni, ns)), device=cuda, dtype=torch.float32)
+    dg = torch.as_tensor(1e-2 * rng.standard_normal((nl, 4 * q, ns)), device=cuda, dtype=torch.float32)
+    r32 = torch.empty((nl, ni, ns), dtype=torch.float32, device=cuda)
+    r64 = torch.empty((nl, ni, ns), dtype=torch.float64, device=cuda)
+    flux = torch.empty((nl, 4 * q, ns), dtype=torch.float64, device=cuda)
+    rf._residual(state, u, g, r32, flux, r64=r64)
+    rf._residual_update(state, du, dg, r64, r32, flux)
+    r64b = torch.empty_like(r64)
+    flux_b = torch.empty_like(flux)
+    rf._residual(state, u + du.double(), g + dg.double(), r32, flux_b, r64=r64b)
+    # the update's rounding is relative to the size of A du, not of r
+    ref_d = torch.empty_like(r64)
+    fl_d = torch.empty_like(flux)
+    rf._residual(state, du.double(), dg.double(), r32, fl_d, r64=ref_d, zero_source=True)
+    scale_r = float(ref_d.abs().max())
+    scale_f = float(fl_d.abs().max())
+    assert float((r64 - r64b).abs().max()) < 1e-10 * scale_r
+    assert float((flux - flux_b).abs().max()) < 1e-10 * scale_f

@@ -215,3 +215,4 @@ def test_oracle_solution_is_zero_of_refinement_residual():
     Ff = F.reshape(-1)
     inner = nbr >= 0
     assert np.abs(Ff[inner] + Ff[nbr[inner]]).max() < 1e-9 * np.abs(F).max()
+
