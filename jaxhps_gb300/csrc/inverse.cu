@@ -174,6 +174,201 @@ inv_reg_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* X
 }
 
 // --------------------------------------------------------------------------
+// Shared-memory blocked kernel: one 512-thread CTA per matrix, the tableau
+// in shared memory.  Panels of KB columns: the panel's pivots are chosen by
+// Gauss-Jordan restricted to the panel columns (three barriers per column),
+// then one rank-KB block-sweep update of the other columns with register
+// tiles (RA rows x RN columns per thread, KB-long dot products):
+//     M[i][j] = (i in R ? 0 : M[i][j]) + sum_k Z[i][k] G[k][j]
+// where Z = the panel after elimination and G = the pivot rows before it.
+// --------------------------------------------------------------------------
+constexpr int SB_NT = 512;
+constexpr int SB_TY = 16, SB_TX = 32;
+
+template <class T>
+size_t inv_sblock_smem(int n, int KB) {
+  const int ldm = n + 1;
+  return sizeof(T) * ((size_t)n * ldm + (size_t)KB * n) + sizeof(int) * 2 * (size_t)n + (size_t)n + 16;
+}
+
+template <class T, int KB, int RN>
+__global__ void __launch_bounds__(SB_NT, 1)
+inv_sblock_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* X, long long ldx, long long sX,
+                  int* info) {
+  using MagT = typename MagOf<T>::type;
+  constexpr int RA = 4;
+  extern __shared__ __align__(16) unsigned char sbraw[];
+  const int ldm = n + 1;
+  T* M = reinterpret_cast<T*>(sbraw);
+  T* G = M + (size_t)n * ldm;
+  int* piv = reinterpret_cast<int*>(G + (size_t)KB * n);
+  int* colof = piv + n;
+  unsigned char* used = reinterpret_cast<unsigned char*>(colof + n);
+  __shared__ T rowr[KB];
+  __shared__ int Rs[KB];
+  __shared__ MagT wbest[SB_NT / 32];
+  __shared__ int widx[SB_NT / 32];
+  __shared__ int s_r;
+  __shared__ T s_pinv;
+  __shared__ int s_info;
+
+  const long long bb = blockIdx.x;
+  const T* Ab = A + bb * sA;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ty = tid / SB_TX, tx = tid % SB_TX;
+
+  for (int e = tid; e < n * n; e += SB_NT) {
+    const int i = e / n, j = e % n;
+    M[i * ldm + j] = Ab[(long long)i * lda + j];
+  }
+  for (int i = tid; i < n; i += SB_NT) used[i] = 0;
+  if (tid == 0) s_info = 0;
+  __syncthreads();
+
+  for (int k0 = 0; k0 < n; k0 += KB) {
+    const int bw = min(KB, n - k0);
+    // ---- panel: Gauss-Jordan restricted to columns k0 .. k0+bw-1
+    for (int c = 0; c < bw; ++c) {
+      const int col = k0 + c;
+      MagT best = -1;
+      int bi = n;
+      for (int i = tid; i < n; i += SB_NT) {
+        if (!used[i]) {
+          const MagT mg = nan_to_inf(pivmag(M[i * ldm + col]));
+          if (mg > best) {
+            best = mg;
+            bi = i;
+          }
+        }
+      }
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        wbest[warp] = best;
+        widx[warp] = bi;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        best = lane < SB_NT / 32 ? wbest[lane] : (MagT)-1;
+        bi = lane < SB_NT / 32 ? widx[lane] : n;
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+          const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+          }
+        }
+        const T pv = (best > 0) ? rcp_(M[bi * ldm + col]) : zero<T>();
+        if (lane < bw) rowr[lane] = mul(M[bi * ldm + k0 + lane], pv);
+        if (lane == 0) {
+          s_r = bi;
+          s_pinv = pv;
+          used[bi] = 2;
+          Rs[c] = bi;
+          piv[col] = bi;
+          colof[bi] = col;
+          if (!(best > 0) && s_info == 0) s_info = col + 1;
+        }
+      }
+      __syncthreads();
+      const int r = s_r;
+      const T pinv = s_pinv;  // read from shared: row r is rewritten below
+      // one thread per row: no two threads touch the same row of the panel;
+      // the row is staged in registers so its loads are issued together
+      T rr[KB];
+#pragma unroll
+      for (int c2 = 0; c2 < KB; ++c2) rr[c2] = (c2 < bw) ? rowr[c2] : zero<T>();
+      for (int i = tid; i < n; i += SB_NT) {
+        T* Mi = M + i * ldm + k0;
+        T rv[KB];
+#pragma unroll
+        for (int c2 = 0; c2 < KB; ++c2) rv[c2] = (c2 < bw) ? Mi[c2] : zero<T>();
+        T f = zero<T>();
+#pragma unroll
+        for (int c2 = 0; c2 < KB; ++c2)
+          if (c2 == c) f = rv[c2];
+        if (i == r) {
+#pragma unroll
+          for (int c2 = 0; c2 < KB; ++c2) rv[c2] = (c2 == c) ? pinv : rr[c2];
+        } else {
+#pragma unroll
+          for (int c2 = 0; c2 < KB; ++c2) rv[c2] = (c2 == c) ? neg(mul(f, pinv)) : fms_(f, rr[c2], rv[c2]);
+        }
+#pragma unroll
+        for (int c2 = 0; c2 < KB; ++c2)
+          if (c2 < bw) Mi[c2] = rv[c2];
+      }
+      __syncthreads();
+    }
+    // ---- pivot rows outside the panel, before the sweep
+    for (int e = tid; e < bw * n; e += SB_NT) {
+      const int k = e / n, j = e % n;
+      G[k * n + j] = (j >= k0 && j < k0 + bw) ? zero<T>() : M[Rs[k] * ldm + j];
+    }
+    __syncthreads();
+    // ---- rank-bw block sweep of the non-panel columns
+    for (int a0 = ty * RA; a0 < n; a0 += SB_TY * RA) {
+      T acc[RA][RN];
+      bool isR[RA];
+#pragma unroll
+      for (int a = 0; a < RA; ++a) {
+        const int i = a0 + a;
+        isR[a] = (i < n) && used[i] == 2;
+#pragma unroll
+        for (int b = 0; b < RN; ++b) {
+          const int j = tx + SB_TX * b;
+          acc[a][b] = (i < n && j < n && !isR[a]) ? M[i * ldm + j] : zero<T>();
+        }
+      }
+      for (int k = 0; k < bw; ++k) {
+        T z[RA], gk[RN];
+#pragma unroll
+        for (int a = 0; a < RA; ++a) z[a] = (a0 + a < n) ? M[(a0 + a) * ldm + k0 + k] : zero<T>();
+#pragma unroll
+        for (int b = 0; b < RN; ++b) {
+          const int j = tx + SB_TX * b;
+          gk[b] = (j < n) ? G[k * n + j] : zero<T>();
+        }
+#pragma unroll
+        for (int a = 0; a < RA; ++a)
+#pragma unroll
+          for (int b = 0; b < RN; ++b) acc[a][b] = fma_(z[a], gk[b], acc[a][b]);
+      }
+#pragma unroll
+      for (int a = 0; a < RA; ++a) {
+        const int i = a0 + a;
+        if (i >= n) continue;
+#pragma unroll
+        for (int b = 0; b < RN; ++b) {
+          const int j = tx + SB_TX * b;
+          if (j < n && (j < k0 || j >= k0 + bw)) M[i * ldm + j] = acc[a][b];
+        }
+      }
+    }
+    __syncthreads();
+    if (tid < bw) used[Rs[tid]] = 1;
+    __syncthreads();
+  }
+  if (tid == 0 && info) info[bb] = s_info;
+  // inv(A)[k][j] = M[piv[k]][rinv[j]], written row by row (coalesced);
+  // colof is rinv: colof[piv[j]] = j
+  T* Xb = X + bb * sX;
+  for (int e = tid; e < n * n; e += SB_NT) {
+    const int k = e / n, j = e % n;
+    Xb[(long long)k * ldx + j] = M[piv[k] * ldm + colof[j]];
+  }
+}
+
+// --------------------------------------------------------------------------
 // Blocked Gauss-Jordan (global-memory tableau)
 // --------------------------------------------------------------------------
 constexpr int BP = 32;       // panel width
@@ -373,6 +568,35 @@ __global__ void gje_permute_out_kernel(int n, const T* Mat, const int* piv, cons
 // --------------------------------------------------------------------------
 // Dispatch
 // --------------------------------------------------------------------------
+// Shared-memory blocked kernel: chooses RN (= columns per thread / 32) and
+// launches when the tableau fits in shared memory.
+constexpr size_t SB_SMEM_MAX = 220 * 1024;
+
+template <class T>
+static bool sblock_fits(int n) {
+  return n > 64 && n <= 256 && inv_sblock_smem<T>(n, 16) <= SB_SMEM_MAX;
+}
+
+template <class T, int RN>
+static cudaError_t launch_sblock_rn(int n, const T* A, long long lda, long long sA, T* X, long long ldx, long long sX,
+                                    int batch, int* info, cudaStream_t st) {
+  const size_t smem = inv_sblock_smem<T>(n, 16);
+  cudaFuncSetAttribute(inv_sblock_kernel<T, 16, RN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const double cplx = (DTypeOf<T>::value == C64 || DTypeOf<T>::value == C128) ? 4.0 : 1.0;
+  ProfScope ps(KC_INVERSE, st, 2.0 * cplx * (double)n * n * n * batch);
+  note_launch();
+  inv_sblock_kernel<T, 16, RN><<<batch, SB_NT, smem, st>>>(n, A, lda, sA, X, ldx, sX, info);
+  return cudaGetLastError();
+}
+
+template <class T>
+static cudaError_t launch_sblock(int n, const T* A, long long lda, long long sA, T* X, long long ldx, long long sX,
+                                 int batch, int* info, cudaStream_t st) {
+  if (n <= 128) return launch_sblock_rn<T, 4>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  if (n <= 192) return launch_sblock_rn<T, 6>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  return launch_sblock_rn<T, 8>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+}
+
 int inverse_small_nmax(int dtype) {
   switch (dtype) {
     case F32: return 208;
@@ -385,6 +609,9 @@ int inverse_small_nmax(int dtype) {
 
 size_t inverse_workspace_bytes(int dtype, int n, int batch) {
   if (n <= inverse_small_nmax(dtype)) return 0;
+  if ((dtype == F32 && sblock_fits<float>(n)) || (dtype == F64 && sblock_fits<double>(n)) ||
+      (dtype == C64 && sblock_fits<c64>(n)))
+    return 0;
   const size_t es = dtype_size(dtype);
   return gje_layout(es, n).per * (size_t)batch + 256;
 }
@@ -444,6 +671,9 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
   if (n <= 0 || batch <= 0) return cudaSuccess;
   if (info) cudaMemsetAsync(info, 0, sizeof(int) * (size_t)batch, st);
   const int dtype = DTypeOf<T>::value;
+  if constexpr (sizeof(T) <= 8) {
+    if (sblock_fits<T>(n)) return launch_sblock<T>(n, A, lda, sA, X, ldx, sX, batch, info, st);
+  }
   if (n <= inverse_small_nmax(dtype)) return inverse_small<T>(n, A, lda, sA, X, ldx, sX, batch, info, st);
 
   const size_t es = sizeof(T);

@@ -46,7 +46,8 @@ def test_gemm_batched(cuda, dt, m, n, k, batch):
 
 
 @pytest.mark.parametrize("dt", list(DT))
-@pytest.mark.parametrize("n,batch", [(1, 3), (5, 4), (36, 9), (64, 2), (100, 3), (129, 2), (196, 3), (233, 2)])
+@pytest.mark.parametrize("n,batch", [(1, 3), (5, 4), (36, 9), (64, 2), (65, 2), (100, 3), (129, 2), (160, 2),
+                                     (161, 2), (196, 3), (233, 2)])
 def test_inverse_batched(cuda, dt, n, batch):
     from jaxhps_gb300 import _native as nat
 
@@ -59,8 +60,9 @@ def test_inverse_batched(cuda, dt, n, batch):
     info = torch.zeros(batch, dtype=torch.int32, device=cuda)
     X = nat.inverse(tA, info=info).cpu().numpy()
     assert (info.cpu().numpy() == 0).all()
-    res = np.abs(X.astype(np.complex128) @ A - np.eye(n)).max()
-    assert res < tol * 50 * n, res
+    Xe = np.linalg.inv(A.astype(np.complex128))
+    rel = np.abs(X - Xe).max() / np.abs(Xe).max()
+    assert rel < tol * 20, rel
     # in place
     nat.inverse(tA, out=tA)
     assert np.allclose(tA.cpu().numpy(), X, atol=tol * 10, rtol=tol * 10)
