@@ -205,6 +205,14 @@ typedef struct {
 HPS_API size_t hps_merge_level_dtn_workspace_size(const hps_merge_args* a);
 HPS_API int hps_merge_level_dtn(const hps_merge_args* a, void* stream);
 
+/* One ItI merge level.  Replaces vmapped_uniform_quad_merge_ItI
+ * (merge/_uniform_2D_ItI.py:182-405): the interface unknowns are the
+ * children's incoming impedances on both sides of every interface, in the
+ * reference's final order; int_c/int_l hold (own, partner) pairs per unknown
+ * (loc is unused).  D = I + R-coupling is inverted directly; the rest is as
+ * hps_merge_level_dtn.  Workspace: hps_merge_level_dtn_workspace_size(). */
+HPS_API int hps_merge_level_iti(const hps_merge_args* a, void* stream);
+
 /* ---------------------------------------------------------------------------
  * One down-pass level.  Replaces _propagate_down_2D_DtN
  * (down_pass/_uniform_2D_DtN.py:125-189), _propogate_down_2D_ItI

@@ -100,3 +100,53 @@ def quad_merge_maps_dtn(nc: int) -> MergeMaps:
     code[3, t] = -(i8 + 1)
     code[0, 3 * nc - 1 - t] = -(i8 + 1)
     return maps_from_code(code, n_ext=8 * nc, n_int=4 * nc)
+
+
+@dataclass
+class ItiMergeMaps:
+    """ItI quad merge: interface unknowns are the children's incoming
+    impedances on each side of every interface (8nc of them), ordered
+    [a5, b5, b6, c6, c7, d7, d8, a8] as after the row reordering of
+    merge/_uniform_2D_ItI.py:360-373.  Unknown u lives at (unk_c, unk_l);
+    its equation involves the partner child across the interface
+    (par_c, par_l)."""
+    nch: int
+    nb: int
+    n_int: int
+    n_ext: int
+    code: np.ndarray
+    int_c: np.ndarray   # (n_int, 2): [own child, partner child]
+    int_l: np.ndarray   # (n_int, 2): [own local, partner local]
+    ext_c: np.ndarray
+    ext_l: np.ndarray
+    loc: np.ndarray     # unused by the ItI gather (kept for a uniform interface)
+
+    device = MergeMaps.device
+
+
+@lru_cache(maxsize=None)
+def quad_merge_maps_iti(nc: int) -> ItiMergeMaps:
+    dtn = quad_merge_maps_dtn(nc)
+    t = np.arange(nc)
+    # (child, local) of each unknown block, in the reference's final order
+    blocks = [
+        (0, nc + t),               # a5: a's E side
+        (1, 4 * nc - 1 - t),       # b5: b's W side, reversed
+        (1, 2 * nc + t),           # b6: b's N side
+        (2, nc - 1 - t),           # c6: c's S side, reversed
+        (2, 3 * nc + t),           # c7: c's W side
+        (3, 2 * nc - 1 - t),       # d7: d's E side, reversed
+        (3, t),                    # d8: d's S side
+        (0, 3 * nc - 1 - t),       # a8: a's N side, reversed
+    ]
+    partner = [1, 0, 3, 2, 5, 4, 7, 6]
+    n_int = 8 * nc
+    own_c = np.concatenate([np.full(nc, c) for c, _ in blocks])
+    own_l = np.concatenate([l for _, l in blocks])
+    par_c = np.concatenate([np.full(nc, blocks[partner[b]][0]) for b in range(8)])
+    par_l = np.concatenate([blocks[partner[b]][1] for b in range(8)])
+    code = dtn.code.copy()
+    for u in range(n_int):
+        code[own_c[u], own_l[u]] = -(u + 1)
+    return ItiMergeMaps(4, 4 * nc, n_int, 8 * nc, code, np.stack([own_c, par_c], 1), np.stack([own_l, par_l], 1),
+                        dtn.ext_c, dtn.ext_l, np.full((4, n_int), -1, dtype=np.int64))

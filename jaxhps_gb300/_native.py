@@ -124,6 +124,8 @@ def _declare(lib):
     lib.hps_merge_level_dtn_workspace_size.restype = csz
     lib.hps_merge_level_dtn.argtypes = [P(MergeArgs), vp]
     lib.hps_merge_level_dtn.restype = ci
+    lib.hps_merge_level_iti.argtypes = [P(MergeArgs), vp]
+    lib.hps_merge_level_iti.restype = ci
     lib.hps_down_level.argtypes = [P(DownArgs), vp]
     lib.hps_down_level.restype = ci
     lib.hps_up_level.argtypes = [P(UpArgs), vp]
@@ -146,7 +148,7 @@ EXPORTED_SYMBOLS = (
     "hps_version", "hps_launch_count", "hps_profile_begin", "hps_profile_end", "hps_last_error", "hps_gemm_batched", "hps_inverse_workspace_size",
     "hps_inverse_batched", "hps_convert", "hps_local_solve_dtn_workspace_size", "hps_local_solve_dtn",
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
-    "hps_merge_level_dtn", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
+    "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32",
 )
 

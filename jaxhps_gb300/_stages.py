@@ -189,7 +189,7 @@ def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None,
 
 
 def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False,
-                    keep_B=False):
+                    keep_B=False, iti=False):
     """One batched merge level.  T_children: (n_merges*nch, nb, nb);
     h_children: (n_merges*nch, nb, nsrc) or None.  Returns
     (S, g_tilde, T_out, h_out, D_inv, BD_inv) and B when ``keep_B``."""
@@ -219,7 +219,10 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
     wsb = L.hps_merge_level_dtn_workspace_size(C.byref(a))
     ws = nat.workspace(wsb, dev)
     a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
-    nat.check(L.hps_merge_level_dtn(C.byref(a), nat.stream_ptr()), "hps_merge_level_dtn")
+    if iti:
+        nat.check(L.hps_merge_level_iti(C.byref(a), nat.stream_ptr()), "hps_merge_level_iti")
+    else:
+        nat.check(L.hps_merge_level_dtn(C.byref(a), nat.stream_ptr()), "hps_merge_level_dtn")
     if keep_B:
         return S, g_t, T_out, h_out, D_inv, BD_inv, B
     return S, g_t, T_out, h_out, D_inv, BD_inv

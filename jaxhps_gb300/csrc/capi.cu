@@ -29,6 +29,10 @@ cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, in
                          const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
                          const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, cudaStream_t st);
 template <class T>
+cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Rc, const T* hc,
+                             const int* int_c, const int* int_l, const int* ext_c, const int* ext_l, T* D, T* C, T* B,
+                             T* Tout, T* dh, T* hext, cudaStream_t st);
+template <class T>
 cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, int ns, const int* code,
                          const T* gpar, const T* gint, T* gch, cudaStream_t st);
 template <class S, class D>
@@ -245,7 +249,7 @@ static size_t merge_ws(const hps_merge_args* a, Carver* cv) {
 }
 
 template <class T>
-static int merge_impl(const hps_merge_args* a, cudaStream_t st) {
+static int merge_impl(const hps_merge_args* a, cudaStream_t st, bool iti) {
   const int nm = a->n_merges, ni = a->n_int, ne = a->n_ext, ns = a->nsrc;
   unsigned char* wsb = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(a->workspace) + 255) & ~uintptr_t(255));
@@ -258,9 +262,14 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st) {
   const size_t invb = inverse_workspace_bytes(a->dtype, ni, nm);
   void* invws = cv.take(invb);
   const bool with_h = ns > 0 && a->h_children && a->h_out && a->g_tilde;
-  HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, with_h ? ns : 0, (const T*)a->T_children,
-                            with_h ? (const T*)a->h_children : nullptr, a->int_c, a->int_l, a->ext_c, a->ext_l,
-                            a->loc, D, C, B, (T*)a->T_out, dh, (T*)a->h_out, st));
+  if (iti)
+    HPS_CHECK(merge_gather_iti<T>(nm, a->nch, a->nb, ni, ne, with_h ? ns : 0, (const T*)a->T_children,
+                                  with_h ? (const T*)a->h_children : nullptr, a->int_c, a->int_l, a->ext_c, a->ext_l,
+                                  D, C, B, (T*)a->T_out, dh, (T*)a->h_out, st));
+  else
+    HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, with_h ? ns : 0, (const T*)a->T_children,
+                              with_h ? (const T*)a->h_children : nullptr, a->int_c, a->int_l, a->ext_c, a->ext_l,
+                              a->loc, D, C, B, (T*)a->T_out, dh, (T*)a->h_out, st));
   HPS_CHECK(inverse_batched<T>(ni, D, ni, (long long)ni * ni, D, ni, (long long)ni * ni, nm, a->info, invws, invb,
                                st));
   const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
@@ -504,7 +513,21 @@ int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
               hps_merge_level_dtn_workspace_size(a));
     return HPS_ERR_WORKSPACE;
   }
-  DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream)
+  DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream, false)
+}
+
+int hps_merge_level_iti(const hps_merge_args* a, void* stream) {
+  if (!a || a->n_merges <= 0 || a->nch <= 0 || a->nb <= 0 || a->n_int <= 0 || a->n_ext <= 0 || !a->T_children ||
+      !a->int_c || !a->int_l || !a->ext_c || !a->ext_l || !a->S || !a->T_out) {
+    set_error("hps_merge_level_iti: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (a->workspace_bytes < hps_merge_level_dtn_workspace_size(a)) {
+    set_error("hps_merge_level_iti: workspace too small (%zu < %zu)", a->workspace_bytes,
+              hps_merge_level_dtn_workspace_size(a));
+    return HPS_ERR_WORKSPACE;
+  }
+  DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream, true)
 }
 
 int hps_up_level(const hps_up_args* a, void* stream) {

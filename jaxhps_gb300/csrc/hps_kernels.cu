@@ -208,6 +208,105 @@ cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, in
 }
 
 // ---------------------------------------------------------------------------
+// ItI merge gather  (reference: merge/_uniform_2D_ItI.py:182-375 with
+// merge/_schur_complement.py:6-41, 78-114)
+//
+// Interface unknown u is child own_c[u]'s incoming impedance at local point
+// own_l[u]; its equation is  t_u + (R t + h)_{partner}[par_l[u]] = 0  with
+// the partner child par_c[u] across the interface.  int_c/int_l hold
+// (own, partner) pairs.  Outputs as for the DtN gather, with
+//   D[u][v] = delta_uv + R_{par(u)}[par_l(u)][own_l(v)]  if own_c(v) == par_c(u)
+//   C[u][e] = R_{par(u)}[par_l(u)][ext_l(e)]            if ext_c(e) == par_c(u)
+//   B[e][v] = R_{c(e)}[ext_l(e)][own_l(v)]              if own_c(v) == ext_c(e)
+//   dh[u]   = h_{par(u)}[par_l(u)]
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void merge_gather_iti_kernel(int nch, int nb, int n_int, int n_ext, int ns, const T* __restrict__ Rc,
+                                        const T* __restrict__ hc, const int* __restrict__ int_c,
+                                        const int* __restrict__ int_l, const int* __restrict__ ext_c,
+                                        const int* __restrict__ ext_l, T* D, T* C, T* B, T* Tout, T* dh, T* hext,
+                                        long long m_base) {
+  const long long m = blockIdx.y + m_base;
+  const int seg = blockIdx.z;
+  const long long nbb = (long long)nb * nb;
+  const T* Rm = Rc + m * nch * nbb;
+  const T* hm = hc ? hc + m * nch * (long long)nb * ns : nullptr;
+  long long cnt;
+  switch (seg) {
+    case 0: cnt = (long long)n_int * n_int; break;
+    case 1: cnt = (long long)n_int * n_ext; break;
+    case 2: cnt = (long long)n_ext * n_int; break;
+    case 3: cnt = (long long)n_ext * n_ext; break;
+    case 4: cnt = hm ? (long long)n_int * ns : 0; break;
+    default: cnt = hm ? (long long)n_ext * ns : 0; break;
+  }
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt;
+       e += (long long)gridDim.x * blockDim.x) {
+    T v = zero<T>();
+    if (seg == 0) {
+      const int u = (int)(e / n_int), w = (int)(e % n_int);
+      const int pc = int_c[2 * u + 1];
+      if (int_c[2 * w] == pc) v = Rm[pc * nbb + (long long)int_l[2 * u + 1] * nb + int_l[2 * w]];
+      if (u == w) v = add(v, one<T>());
+      D[m * n_int * (long long)n_int + e] = v;
+    } else if (seg == 1) {
+      const int u = (int)(e / n_ext), x = (int)(e % n_ext);
+      const int pc = int_c[2 * u + 1];
+      if (ext_c[x] == pc) v = Rm[pc * nbb + (long long)int_l[2 * u + 1] * nb + ext_l[x]];
+      C[m * n_int * (long long)n_ext + e] = v;
+    } else if (seg == 2) {
+      const int x = (int)(e / n_int), w = (int)(e % n_int);
+      const int c = ext_c[x];
+      if (int_c[2 * w] == c) v = Rm[c * nbb + (long long)ext_l[x] * nb + int_l[2 * w]];
+      B[m * n_ext * (long long)n_int + e] = v;
+    } else if (seg == 3) {
+      const int x = (int)(e / n_ext), y = (int)(e % n_ext);
+      const int c = ext_c[x];
+      if (ext_c[y] == c) v = Rm[c * nbb + (long long)ext_l[x] * nb + ext_l[y]];
+      Tout[m * n_ext * (long long)n_ext + e] = v;
+    } else if (seg == 4) {
+      const int u = (int)(e / ns), s = (int)(e % ns);
+      v = hm[(int_c[2 * u + 1] * (long long)nb + int_l[2 * u + 1]) * ns + s];
+      dh[m * n_int * (long long)ns + e] = v;
+    } else {
+      const int x = (int)(e / ns), s = (int)(e % ns);
+      v = hm[(ext_c[x] * (long long)nb + ext_l[x]) * ns + s];
+      hext[m * n_ext * (long long)ns + e] = v;
+    }
+  }
+}
+
+template <class T>
+cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Rc, const T* hc,
+                             const int* int_c, const int* int_l, const int* ext_c, const int* ext_l, T* D, T* C, T* B,
+                             T* Tout, T* dh, T* hext, cudaStream_t st) {
+  long long big = (long long)(n_ext > n_int ? n_ext : n_int) * (n_ext > n_int ? n_ext : n_int);
+  int gx = (int)((big + 255) / 256);
+  if (gx > 512) gx = 512;
+  for (int m0 = 0; m0 < n_merges; m0 += 65535) {
+    const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * ((double)n_int * n_int + 2.0 * n_int * n_ext +
+                                                       (double)n_ext * n_ext + (double)(n_int + n_ext) * ns));
+    note_launch();
+    merge_gather_iti_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Rc, hc, int_c, int_l, ext_c,
+                                                                ext_l, D, C, B, Tout, dh, hext, m0);
+  }
+  return cudaGetLastError();
+}
+template cudaError_t merge_gather_iti<c64>(int, int, int, int, int, int, const c64*, const c64*, const int*,
+                                           const int*, const int*, const int*, c64*, c64*, c64*, c64*, c64*, c64*,
+                                           cudaStream_t);
+template cudaError_t merge_gather_iti<c128>(int, int, int, int, int, int, const c128*, const c128*, const int*,
+                                            const int*, const int*, const int*, c128*, c128*, c128*, c128*, c128*,
+                                            c128*, cudaStream_t);
+template cudaError_t merge_gather_iti<float>(int, int, int, int, int, int, const float*, const float*, const int*,
+                                             const int*, const int*, const int*, float*, float*, float*, float*,
+                                             float*, float*, cudaStream_t);
+template cudaError_t merge_gather_iti<double>(int, int, int, int, int, int, const double*, const double*, const int*,
+                                              const int*, const int*, const int*, double*, double*, double*, double*,
+                                              double*, double*, cudaStream_t);
+
+// ---------------------------------------------------------------------------
 // Down-pass scatter  (reference: down_pass/_uniform_2D_DtN.py:125-189)
 // child boundary point (c, k) takes parent exterior value code>=0 or
 // interface value -(code+1).

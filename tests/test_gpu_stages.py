@@ -113,3 +113,61 @@ def test_float32_build_is_close(cuda):
     u = hps.solve(pde, g)
     ur = ref.build().solve(g)
     assert _rel(u, ur) < 1e-3
+
+
+def _iti_problem(L, p, q, nsrc=None, seed=0, eta=4.0):
+    rng = np.random.default_rng(seed)
+    rootn = hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0)
+    dom = hps.Domain(p=p, q=q, root=rootn, L=L)
+    x = dom.interior_points
+    k = 6.0
+    qv = 0.5 * np.exp(-((x[..., 0] - 0.2) ** 2 + (x[..., 1] + 0.3) ** 2) / 0.05)
+    ones = np.ones_like(qv)
+    Icoef = k ** 2 * (1 + qv)
+    shape = x.shape[:2] + ((nsrc,) if nsrc else ())
+    f = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    pde = hps.PDEProblem(dom, source=f, D_xx_coefficients=ones, D_yy_coefficients=ones, I_coefficients=Icoef,
+                         use_ItI=True, eta=eta)
+    ref = O.Problem2D(rootn.bounds, L, p, q, {"D_xx": ones, "D_yy": ones, "I": Icoef}, f, iti=True, eta=eta)
+    return dom, pde, ref
+
+
+@pytest.mark.parametrize("L,p,q,nsrc", [(1, 8, 6, None), (2, 10, 8, 3), (3, 8, 6, None)])
+def test_iti_build_solve_matches_oracle(cuda, L, p, q, nsrc):
+    dom, pde, ref = _iti_problem(L, p, q, nsrc)
+    T_top = hps.build_solver(pde, return_top_T=True)
+    bp = dom.boundary_points
+    g = np.exp(1j * bp[:, 0]) + bp[:, 1]
+    if nsrc:
+        g = np.stack([g * (k + 1) for k in range(nsrc)], -1)
+    u = hps.solve(pde, g)
+    ref.build()
+    ur = ref.solve(g)
+    assert tuple(u.shape) == ur.shape
+    assert _rel(u, ur) < 1e-11
+    assert _rel(T_top, ref.T_top) < 1e-11
+    for a, b in zip(pde.S_lst, ref.S_lst):
+        assert _rel(a, b) < 1e-10
+
+
+def test_iti_polynomial_known_answer_gpu(cuda):
+    """ItI analytic case with complex coefficients (tests/test_accuracy/cases.py:212-265)
+    through the GPU path: u = x^3 + 3y^2, (Delta + 1 + 0.1i) u = f."""
+    PI2 = np.pi / 2
+    root = hps.DiscretizationNode2D(-PI2, PI2, -PI2, PI2)
+    L, p, q, eta = 2, 10, 8, 1.0
+    dom = hps.Domain(p=p, q=q, root=root, L=L)
+    x = dom.interior_points
+    cc = 1.0 + 0.1j
+    u_ex = x[..., 0] ** 3 + 3 * x[..., 1] ** 2
+    f = 6 * x[..., 0] + 6 + cc * u_ex
+    ones = np.ones(x.shape[:2])
+    pde = hps.PDEProblem(dom, source=f, D_xx_coefficients=ones, D_yy_coefficients=ones, I_coefficients=cc * ones,
+                         use_ItI=True, eta=eta)
+    hps.build_solver(pde)
+    bp = dom.boundary_points
+    n = bp.shape[0] // 4
+    dn = np.concatenate([-6 * bp[:n, 1], 3 * bp[n:2 * n, 0] ** 2, 6 * bp[2 * n:3 * n, 1], -3 * bp[3 * n:, 0] ** 2])
+    imp = dn + 1j * eta * (bp[:, 0] ** 3 + 3 * bp[:, 1] ** 2)
+    u = hps.solve(pde, imp).numpy()
+    assert np.abs(u - u_ex).max() < 1e-9

@@ -216,3 +216,59 @@ def test_oracle_solution_is_zero_of_refinement_residual():
     inner = nbr >= 0
     assert np.abs(Ff[inner] + Ff[nbr[inner]]).max() < 1e-9 * np.abs(F).max()
 
+
+
+def _emulate_merge_iti(Rs, hs, maps):
+    """NumPy restatement of the ItI merge gather + Schur complement driven by
+    the index maps (what hps_merge_level_iti computes)."""
+    Rm, hm = np.stack(Rs), np.stack(hs)
+    ni, ne = maps.n_int, maps.n_ext
+    oc, pc = maps.int_c[:, 0], maps.int_c[:, 1]
+    ol, pl = maps.int_l[:, 0], maps.int_l[:, 1]
+    D = np.eye(ni, dtype=complex)
+    C = np.zeros((ni, ne), dtype=complex)
+    B = np.zeros((ne, ni), dtype=complex)
+    A = np.zeros((ne, ne), dtype=complex)
+    for u in range(ni):
+        for v in range(ni):
+            if oc[v] == pc[u]:
+                D[u, v] += Rm[pc[u], pl[u], ol[v]]
+        for x in range(ne):
+            if maps.ext_c[x] == pc[u]:
+                C[u, x] = Rm[pc[u], pl[u], maps.ext_l[x]]
+    for x in range(ne):
+        c, l = maps.ext_c[x], maps.ext_l[x]
+        for v in range(ni):
+            if oc[v] == c:
+                B[x, v] = Rm[c, l, ol[v]]
+        for y in range(ne):
+            if maps.ext_c[y] == c:
+                A[x, y] = Rm[c, l, maps.ext_l[y]]
+    dh = hm[pc, pl]
+    hext = hm[maps.ext_c, maps.ext_l]
+    Dinv = np.linalg.inv(D)
+    S = -Dinv @ C
+    gt = -Dinv @ dh
+    return S, A + B @ S, hext + B @ gt, gt
+
+
+@pytest.mark.parametrize("nc", [1, 3])
+def test_quad_merge_maps_iti_reproduce_oracle(nc):
+    rng = np.random.default_rng(11 + nc)
+    n = 4 * nc
+    Rs = [0.3 * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) for _ in range(4)]
+    hs = [rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2)) for _ in range(4)]
+    S, T, h, gt = O.quad_merge_iti(*Rs, *hs)
+    maps = im.quad_merge_maps_iti(nc)
+    S2, T2, h2, gt2 = _emulate_merge_iti(Rs, hs, maps)
+    assert np.allclose(S, S2) and np.allclose(T, T2) and np.allclose(h, h2) and np.allclose(gt, gt2)
+    # the down-pass scatter with the same code reproduces the oracle's ItI propagation
+    g = rng.standard_normal((8 * nc, 2)) + 0j
+    ref = O._propagate_down_iti(S, g, gt)
+    gi = S @ g + gt
+    out = np.empty((4, 4 * nc, 2), dtype=complex)
+    for c in range(4):
+        for k in range(4 * nc):
+            cd = maps.code[c, k]
+            out[c, k] = g[cd] if cd >= 0 else gi[-cd - 1]
+    assert np.allclose(out, ref)
