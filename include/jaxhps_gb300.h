@@ -100,6 +100,24 @@ HPS_API int hps_inverse_batched(int dtype, int n, const void* A, long long lda, 
                         long long ldx, long long strideX, int batch, int* info, void* workspace,
                         size_t workspace_bytes, void* stream);
 
+/* Size of the fixed scratch behind hps_inverse_batched_static: 64 MiB. */
+#define HPS_STATIC_SCRATCH_BYTES (64u << 20)
+
+/* hps_inverse_batched without a workspace argument, for callers that cannot
+ * allocate device memory (no cudaMalloc available to them, or all device
+ * memory owned by a pool that only hands out their inputs and outputs).
+ * No counterpart in the reference: it exists for such callers only.
+ * Scratch is a static device array of HPS_STATIC_SCRATCH_BYTES that every
+ * GPU loading the library holds until exit; the call allocates nothing.
+ * Returns HPS_ERR_WORKSPACE when hps_inverse_workspace_size(dtype, n, batch)
+ * exceeds that size.  All calls share the array: calls that overlap on the
+ * GPU (other streams or host threads, same device) race.  The first call on
+ * a device looks up the array's address and should come before any stream
+ * capture. */
+HPS_API int hps_inverse_batched_static(int dtype, int n, const void* A, long long lda, long long strideA,
+                                       void* X, long long ldx, long long strideX, int batch, int* info,
+                                       void* stream);
+
 /* Element-type conversion of n contiguous elements (f64<->f32, c128<->c64). */
 HPS_API int hps_convert(int dtype_src, int dtype_dst, long long n, const void* src, void* dst, void* stream);
 
