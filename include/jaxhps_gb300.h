@@ -210,7 +210,8 @@ typedef struct {
   const int* loc;     /* (nch*n_int) local index of interface i in child c, -1 if absent */
   void* S;            /* out (n_merges, n_int, n_ext) */
   void* g_tilde;      /* out (n_merges, n_int, nsrc) or NULL */
-  void* T_out;        /* out (n_merges, n_ext, n_ext) */
+  void* T_out;        /* out (n_merges, n_ext, n_ext), or NULL: the merged map is not formed
+                         (a top level whose map nobody reads) */
   void* h_out;        /* out (n_merges, n_ext, nsrc) or NULL */
   void* D_inv;        /* out (n_merges, n_int, n_int), or NULL to keep it in the workspace */
   void* BD_inv;       /* out (n_merges, n_ext, n_int) = B D_inv, or NULL (no-source up pass) */

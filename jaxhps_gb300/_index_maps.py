@@ -150,3 +150,38 @@ def quad_merge_maps_iti(nc: int) -> ItiMergeMaps:
         code[own_c[u], own_l[u]] = -(u + 1)
     return ItiMergeMaps(4, 4 * nc, n_int, 8 * nc, code, np.stack([own_c, par_c], 1), np.stack([own_l, par_l], 1),
                         dtn.ext_c, dtn.ext_l, np.full((4, n_int), -1, dtype=np.int64))
+
+
+# Octree children a..h as (x, y, z) half bits (_grid_creation_3D.py:28-74).
+OCT_CHILD_BITS = ((0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1), (0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0))
+# Interfaces in the reference's label order 9..20 (merge/_schur_complement.py:293-774):
+# a|b, b|c, c|d, d|a, e|f, f|g, g|h, h|e, a|e, b|f, c|g, d|h.
+OCT_INTERFACES = ((0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7))
+
+
+@lru_cache(maxsize=None)
+def oct_merge_maps_dtn(nf: int) -> MergeMaps:
+    """3D oct merge of children a..h, each face holding nf Gauss points.
+
+    Child faces are -x, +x, -y, +y, -z, +z (nf points each, same in-face
+    order on both sides of an interface, so no flips).  The merged exterior
+    is face by face, each face made of the four touching children's faces in
+    2D quad order of the face (the re-ordering of
+    merge/_uniform_3D_DtN.py:442-541).  Interface i holds the nf points of
+    OCT_INTERFACES[i]."""
+    from ._grid_creation_3D import FACE_TRAVERSAL
+
+    nb = 6 * nf
+    code = np.zeros((8, nb), dtype=np.int64)
+    t = np.arange(nf)
+    for F in range(6):
+        axis, side = F // 2, F % 2
+        kids = [c for c in FACE_TRAVERSAL[axis] if OCT_CHILD_BITS[c][axis] == side]
+        for j, c in enumerate(kids):
+            code[c, F * nf + t] = F * 4 * nf + j * nf + t
+    for i, (c0, c1) in enumerate(OCT_INTERFACES):
+        axis = next(k for k in range(3) if OCT_CHILD_BITS[c0][k] != OCT_CHILD_BITS[c1][k])
+        lo, hi = (c0, c1) if OCT_CHILD_BITS[c0][axis] == 0 else (c1, c0)
+        code[lo, (2 * axis + 1) * nf + t] = -(i * nf + t + 1)
+        code[hi, (2 * axis) * nf + t] = -(i * nf + t + 1)
+    return maps_from_code(code, n_ext=24 * nf, n_int=12 * nf)

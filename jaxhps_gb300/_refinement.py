@@ -219,11 +219,13 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
                                                    dtype=torch.float32))
     S_lst, Dinv_lst, B_lst = [], [], []
     Tc = T.to(merge_dtype)
-    for lvl in range(max(dom.L, 1)):
+    n_levels = max(dom.L, 1)
+    for lvl in range(n_levels):
         maps = quad_merge_maps_dtn(Tc.shape[1] // 4)
         if lvl == dom.L - top_fp64_levels:
             Tc = Tc.double()
-        S, _, Tc, _, Dinv, _, B = st.merge_level_dtn(Tc, None, maps, keep_D_inv=True, keep_B=True)
+        need_T = lvl < n_levels - 1 or return_top_T
+        S, _, Tc, _, Dinv, _, B = st.merge_level_dtn(Tc, None, maps, keep_D_inv=True, keep_B=True, need_T=need_T)
         S_lst.append(S.float())
         Dinv_lst.append(Dinv.float())
         B_lst.append(B.float())

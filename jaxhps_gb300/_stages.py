@@ -189,10 +189,11 @@ def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None,
 
 
 def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False,
-                    keep_B=False, iti=False):
+                    keep_B=False, iti=False, need_T=True):
     """One batched merge level.  T_children: (n_merges*nch, nb, nb);
     h_children: (n_merges*nch, nb, nsrc) or None.  Returns
-    (S, g_tilde, T_out, h_out, D_inv, BD_inv) and B when ``keep_B``."""
+    (S, g_tilde, T_out, h_out, D_inv, BD_inv) and B when ``keep_B``.
+    With ``need_T=False`` the merged map is not formed (T_out is None)."""
     L = nat.lib()
     dev = T_children.device
     dtype = T_children.dtype
@@ -201,7 +202,7 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
     n_m = T_children.shape[0] // nch
     ns = 0 if h_children is None else h_children.shape[-1]
     S = torch.empty((n_m, n_int, n_ext), dtype=dtype, device=dev)
-    T_out = torch.empty((n_m, n_ext, n_ext), dtype=dtype, device=dev)
+    T_out = torch.empty((n_m, n_ext, n_ext), dtype=dtype, device=dev) if need_T else None
     g_t = torch.empty((n_m, n_int, ns), dtype=dtype, device=dev) if ns else None
     h_out = torch.empty((n_m, n_ext, ns), dtype=dtype, device=dev) if ns else None
     D_inv = torch.empty((n_m, n_int, n_int), dtype=dtype, device=dev) if keep_D_inv else None
@@ -213,7 +214,7 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
         dtype=nat.TORCH_TO_HPS[dtype], n_merges=n_m, nch=nch, nb=nb, n_int=n_int, n_ext=n_ext, nsrc=ns,
         T_children=T_children.data_ptr(), h_children=nat.ptr(h_children), int_c=md["int_c"].data_ptr(),
         int_l=md["int_l"].data_ptr(), ext_c=md["ext_c"].data_ptr(), ext_l=md["ext_l"].data_ptr(),
-        loc=md["loc"].data_ptr(), S=S.data_ptr(), g_tilde=nat.ptr(g_t), T_out=T_out.data_ptr(),
+        loc=md["loc"].data_ptr(), S=S.data_ptr(), g_tilde=nat.ptr(g_t), T_out=nat.ptr(T_out),
         h_out=nat.ptr(h_out), D_inv=nat.ptr(D_inv), BD_inv=nat.ptr(BD_inv), B_out=nat.ptr(B),
         info=info.data_ptr(), workspace=None, workspace_bytes=0)
     wsb = L.hps_merge_level_dtn_workspace_size(C.byref(a))
@@ -249,14 +250,11 @@ def up_level(h_children, D_inv, B, maps):
     return g_t, h_out
 
 
-def merge_stage_uniform_2D_DtN(T_arr, h_arr, l: int, device=None, host_device=None, subtree_recomp: bool = False,
-                               return_T: bool = False, keep_D_inv: bool = False):
-    """Level loop of DtN quad merges (reference merge/_uniform_2D_DtN.py:13-203).
-
-    Returns ``(S_lst, g_tilde_lst)`` (leaf-adjacent level first, root last,
-    root with a leading batch axis of 1) and the top-level T when
-    ``return_T``.  With ``subtree_recomp`` returns only the top ``(T, h)``.
-    """
+def merge_stage_generic(T_arr, h_arr, n_levels: int, maps_fn, device=None, subtree_recomp: bool = False,
+                        return_T: bool = False, keep_D_inv: bool = False):
+    """Level loop shared by the quad and oct DtN merge stages.  ``maps_fn(nb)``
+    gives the merge maps for children with ``nb`` boundary points.  The top
+    level's merged map is formed only when it is returned."""
     dev = _device(device)
     T = T_arr if isinstance(T_arr, torch.Tensor) else _as_tensor(T_arr, torch.float64, dev)
     T = T.to(dev).contiguous()
@@ -272,11 +270,10 @@ def merge_stage_uniform_2D_DtN(T_arr, h_arr, l: int, device=None, host_device=No
             h = h.unsqueeze(-1)
         h = h.reshape(T.shape[0], T.shape[1], -1).contiguous()
     S_lst, g_lst, Dinv_lst = [], [], []
-    n_levels = max(int(l), 1)
-    for _ in range(n_levels):
-        nc = T.shape[1] // 4
-        maps = quad_merge_maps_dtn(nc)
-        S, g_t, T, h, D_inv, _ = merge_level_dtn(T, h, maps, keep_D_inv=keep_D_inv)
+    for lvl in range(n_levels):
+        maps = maps_fn(T.shape[1])
+        need_T = lvl < n_levels - 1 or return_T or subtree_recomp
+        S, g_t, T, h, D_inv, _ = merge_level_dtn(T, h, maps, keep_D_inv=keep_D_inv, need_T=need_T)
         S_lst.append(S)
         g_lst.append(g_t if (g_t is None or multi) else g_t[..., 0])
         Dinv_lst.append(D_inv)
@@ -288,6 +285,18 @@ def merge_stage_uniform_2D_DtN(T_arr, h_arr, l: int, device=None, host_device=No
     if keep_D_inv:
         out = out + (Dinv_lst,)
     return out
+
+
+def merge_stage_uniform_2D_DtN(T_arr, h_arr, l: int, device=None, host_device=None, subtree_recomp: bool = False,
+                               return_T: bool = False, keep_D_inv: bool = False):
+    """Level loop of DtN quad merges (reference merge/_uniform_2D_DtN.py:13-203).
+
+    Returns ``(S_lst, g_tilde_lst)`` (leaf-adjacent level first, root last,
+    root with a leading batch axis of 1) and the top-level T when
+    ``return_T``.  With ``subtree_recomp`` returns only the top ``(T, h)``.
+    """
+    return merge_stage_generic(T_arr, h_arr, max(int(l), 1), lambda nb: quad_merge_maps_dtn(nb // 4), device,
+                               subtree_recomp, return_T, keep_D_inv)
 
 
 # ---------------------------------------------------------------------------
@@ -311,7 +320,11 @@ def down_level(S, g_tilde, g_parent, maps):
     return g_ch
 
 
-def _down_pass_generic(boundary_data, S_lst, g_tilde_lst, Y_arr, v_arr, maps_fn, device, host_device):
+def _down_pass_generic(boundary_data, S_lst, g_tilde_lst, Y_arr, v_arr, maps_fn, device, host_device,
+                       ext_per_unit: int = 8):
+    """Down pass over the stored levels; ``maps_fn(n)`` gives the merge maps of
+    a level whose parents have ``ext_per_unit * n`` exterior points (8nc in
+    2D, 24nf in 3D)."""
     dev = _device(device)
     dtype = S_lst[0].dtype
     g = boundary_data if isinstance(boundary_data, torch.Tensor) else _as_tensor(boundary_data, dtype, dev)
@@ -334,7 +347,7 @@ def _down_pass_generic(boundary_data, S_lst, g_tilde_lst, Y_arr, v_arr, maps_fn,
             else:
                 raise ValueError("boundary data and g_tilde have different numbers of sources")
         gt = None if gt is None else gt.contiguous()
-        nc_child = S.shape[2] // 8
+        nc_child = S.shape[2] // ext_per_unit
         g = down_level(S, gt, g, maps_fn(nc_child))
     if Y_arr is None:
         return g if (ns > 1 or multi_g) else g[..., 0]

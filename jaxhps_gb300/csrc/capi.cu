@@ -276,8 +276,9 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st, bool iti) {
   T* S = (T*)a->S;
   HPS_CHECK(gemm_batched<T>(ni, ne, ni, mone, D, ni, (long long)ni * ni, C, ne, (long long)ni * ne, zero_, nullptr,
                             0, 0, S, ne, (long long)ni * ne, nm, st));
-  HPS_CHECK(gemm_batched<T>(ne, ne, ni, one_, B, ni, (long long)ne * ni, S, ne, (long long)ni * ne, one_,
-                            (T*)a->T_out, ne, (long long)ne * ne, (T*)a->T_out, ne, (long long)ne * ne, nm, st));
+  if (a->T_out)
+    HPS_CHECK(gemm_batched<T>(ne, ne, ni, one_, B, ni, (long long)ne * ni, S, ne, (long long)ni * ne, one_,
+                              (T*)a->T_out, ne, (long long)ne * ne, (T*)a->T_out, ne, (long long)ne * ne, nm, st));
   if (with_h) {
     HPS_CHECK(gemm_batched<T>(ni, ns, ni, mone, D, ni, (long long)ni * ni, dh, ns, (long long)ni * ns, zero_,
                               nullptr, 0, 0, (T*)a->g_tilde, ns, (long long)ni * ns, nm, st));
@@ -504,7 +505,7 @@ size_t hps_merge_level_dtn_workspace_size(const hps_merge_args* a) {
 
 int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
   if (!a || a->n_merges <= 0 || a->nch <= 0 || a->nb <= 0 || a->n_int <= 0 || a->n_ext <= 0 || !a->T_children ||
-      !a->int_c || !a->int_l || !a->ext_c || !a->ext_l || !a->loc || !a->S || !a->T_out) {
+      !a->int_c || !a->int_l || !a->ext_c || !a->ext_l || !a->loc || !a->S) {
     set_error("hps_merge_level_dtn: invalid arguments");
     return HPS_ERR_ARG;
   }
@@ -518,7 +519,7 @@ int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
 
 int hps_merge_level_iti(const hps_merge_args* a, void* stream) {
   if (!a || a->n_merges <= 0 || a->nch <= 0 || a->nb <= 0 || a->n_int <= 0 || a->n_ext <= 0 || !a->T_children ||
-      !a->int_c || !a->int_l || !a->ext_c || !a->ext_l || !a->S || !a->T_out) {
+      !a->int_c || !a->int_l || !a->ext_c || !a->ext_l || !a->S) {
     set_error("hps_merge_level_iti: invalid arguments");
     return HPS_ERR_ARG;
   }

@@ -21,15 +21,26 @@ template <class T, class CT>
 __global__ void leaf_assemble_kernel(int n_leaves, int n_pts, int row0, int col_split, int n_ops,
                                      const double* __restrict__ ops, const CT* __restrict__ coeffs,
                                      T* out_lo, long long ld_lo, long long s_lo, T* out_hi,
-                                     long long ld_hi, long long s_hi, int leaves_per_cta, int l_base) {
-  extern __shared__ double ds[];  // [n_ops][n_pts]
+                                     long long ld_hi, long long s_hi, int leaves_per_cta, int l_base,
+                                     int staged) {
+  extern __shared__ double ds_smem[];  // [n_ops][n_pts] when staged
   const int i = blockIdx.x;
   const int row = row0 + i;
-  for (int e = threadIdx.x; e < n_ops * n_pts; e += blockDim.x) {
-    const int o = e / n_pts, j = e % n_pts;
-    ds[e] = ops[((long long)o * n_pts + row) * n_pts + j];
+  const double* ds;
+  long long ds_ld;   // stride between operators
+  if (staged) {
+    for (int e = threadIdx.x; e < n_ops * n_pts; e += blockDim.x) {
+      const int o = e / n_pts, j = e % n_pts;
+      ds_smem[e] = ops[((long long)o * n_pts + row) * n_pts + j];
+    }
+    __syncthreads();
+    ds = ds_smem;
+    ds_ld = n_pts;
+  } else {
+    // rows too long for shared memory (large 3D leaves): read them from L2
+    ds = ops + (long long)row * n_pts;
+    ds_ld = (long long)n_pts * n_pts;
   }
-  __syncthreads();
   const int l0 = l_base + blockIdx.y * leaves_per_cta;
   const int l1 = min(n_leaves, l0 + leaves_per_cta);
   for (int l = l0; l < l1; ++l) {
@@ -38,12 +49,12 @@ __global__ void leaf_assemble_kernel(int n_leaves, int n_pts, int row0, int col_
       if constexpr (sizeof(CT) == 8) {
         acc = 0.0;
         for (int o = 0; o < n_ops; ++o)
-          acc = fma(coeffs[((long long)o * n_leaves + l) * n_pts + row], ds[o * n_pts + j], acc);
+          acc = fma(coeffs[((long long)o * n_leaves + l) * n_pts + row], ds[o * ds_ld + j], acc);
       } else {
         acc = c128{0.0, 0.0};
         for (int o = 0; o < n_ops; ++o) {
           const CT c = coeffs[((long long)o * n_leaves + l) * n_pts + row];
-          const double d = ds[o * n_pts + j];
+          const double d = ds[o * ds_ld + j];
           acc.x = fma(c.x, d, acc.x);
           acc.y = fma(c.y, d, acc.y);
         }
@@ -62,7 +73,9 @@ cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col
                           const double* ops, const CT* coeffs, T* out_lo, long long ld_lo, long long s_lo,
                           T* out_hi, long long ld_hi, long long s_hi, cudaStream_t st) {
   const int lpc = 32;
-  const size_t smem = sizeof(double) * (size_t)n_ops * n_pts;
+  size_t smem = sizeof(double) * (size_t)n_ops * n_pts;
+  const int staged = smem <= 200 * 1024;
+  if (!staged) smem = 0;
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(leaf_assemble_kernel<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
@@ -74,7 +87,7 @@ cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col
     note_launch();
     leaf_assemble_kernel<T, CT><<<grid, 256, smem, st>>>(n_leaves, n_pts, row0, col_split, n_ops, ops, coeffs,
                                                          out_lo, ld_lo, s_lo, out_hi, ld_hi, s_hi, lpc,
-                                                         y0 * lpc);
+                                                         y0 * lpc, staged);
   }
   return cudaGetLastError();
 }
@@ -138,7 +151,7 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
     case 0: cnt = Tm ? (long long)n_int * n_int : 0; break;
     case 1: cnt = Tm ? (long long)n_int * n_ext : 0; break;
     case 2: cnt = Tm ? (long long)n_ext * n_int : 0; break;
-    case 3: cnt = Tm ? (long long)n_ext * n_ext : 0; break;
+    case 3: cnt = (Tm && Tout) ? (long long)n_ext * n_ext : 0; break;
     case 4: cnt = hm ? (long long)n_int * ns : 0; break;
     default: cnt = hm ? (long long)n_ext * ns : 0; break;
   }
@@ -198,7 +211,8 @@ cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, in
   if (gx > 512) gx = 512;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
-    const double outs = Tc ? ((double)n_int * n_int + 2.0 * n_int * n_ext + (double)n_ext * n_ext) : 0.0;
+    const double outs =
+        Tc ? ((double)n_int * n_int + 2.0 * n_int * n_ext + (Tout ? (double)n_ext * n_ext : 0.0)) : 0.0;
     ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (outs + (double)(n_int + n_ext) * ns));
     note_launch();
     merge_gather_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Tc, hc, int_c, int_l,
@@ -236,7 +250,7 @@ __global__ void merge_gather_iti_kernel(int nch, int nb, int n_int, int n_ext, i
     case 0: cnt = (long long)n_int * n_int; break;
     case 1: cnt = (long long)n_int * n_ext; break;
     case 2: cnt = (long long)n_ext * n_int; break;
-    case 3: cnt = (long long)n_ext * n_ext; break;
+    case 3: cnt = Tout ? (long long)n_ext * n_ext : 0; break;
     case 4: cnt = hm ? (long long)n_int * ns : 0; break;
     default: cnt = hm ? (long long)n_ext * ns : 0; break;
   }
@@ -286,7 +300,8 @@ cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
     ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * ((double)n_int * n_int + 2.0 * n_int * n_ext +
-                                                       (double)n_ext * n_ext + (double)(n_int + n_ext) * ns));
+                                                       (Tout ? (double)n_ext * n_ext : 0.0) +
+                                                       (double)(n_int + n_ext) * ns));
     note_launch();
     merge_gather_iti_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Rc, hc, int_c, int_l, ext_c,
                                                                 ext_l, D, C, B, Tout, dh, hext, m0);

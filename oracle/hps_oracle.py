@@ -571,3 +571,317 @@ class Problem2D:
         b2 = b if b.ndim == 2 else b[:, None]
         u = down_pass(b2, self.S_lst, self.g_lst, self.Y, self.v, self.iti)
         return u if self.multi else u[..., 0]
+
+
+# ---------------------------------------------------------------------------
+# 3D uniform DtN  (src/jaxhps/_grid_creation_3D.py, _precompute_operators_3D.py,
+#                  local_solve/_uniform_3D_DtN.py, merge/_uniform_3D_DtN.py,
+#                  merge/_schur_complement.py:293-774,
+#                  down_pass/_uniform_3D_DtN.py)
+# ---------------------------------------------------------------------------
+
+
+def ext_first_order_3D(p: int) -> np.ndarray:
+    """Raster indices (ix p^2 + iy p + iz) in exterior-first order
+    (_grid_creation_3D.py:420-458): x faces, then y faces without the x
+    faces, then z faces without both, then the interior."""
+    idx = np.arange(p ** 3)
+    left, right = idx // p ** 2 == 0, idx // p ** 2 == p - 1
+    mask = left | right
+    bottom = ((idx // p) % p == 0) & ~mask
+    top = ((idx // p) % p == p - 1) & ~mask
+    mask = mask | bottom | top
+    front = (idx % p == 0) & ~mask
+    back = (idx % p == p - 1) & ~mask
+    mask = mask | front | back
+    return np.concatenate([idx[left], idx[right], idx[bottom], idx[top], idx[front], idx[back], idx[~mask]])
+
+
+def oct_children_bounds(b):
+    """Children a..h of an octree node (_grid_creation_3D.py:28-74)."""
+    x0, x1, y0, y1, z0, z1 = b
+    xm, ym, zm = (x0 + x1) / 2, (y0 + y1) / 2, (z0 + z1) / 2
+    return np.array([
+        [x0, xm, y0, ym, zm, z1], [xm, x1, y0, ym, zm, z1], [xm, x1, ym, y1, zm, z1], [x0, xm, ym, y1, zm, z1],
+        [x0, xm, y0, ym, z0, zm], [xm, x1, y0, ym, z0, zm], [xm, x1, ym, y1, z0, zm], [x0, xm, ym, y1, z0, zm],
+    ])
+
+
+def uniform_leaf_bounds_3D(root_bounds, L: int) -> np.ndarray:
+    b = np.asarray([root_bounds], dtype=np.float64)
+    for _ in range(L):
+        b = np.concatenate([oct_children_bounds(x) for x in b])
+    return b
+
+
+def leaf_points_3D(bounds: np.ndarray, p: int) -> np.ndarray:
+    """meshgrid(x, y, z, 'ij') then exterior-first (_grid_creation_3D.py:77-116)."""
+    c = chebyshev_points(p)
+    r = ext_first_order_3D(p)
+    out = []
+    for b in np.atleast_2d(bounds):
+        X, Y, Z = np.meshgrid(affine_transform(c, b[0:2]), affine_transform(c, b[2:4]),
+                              affine_transform(c, b[4:6]), indexing="ij")
+        out.append(np.stack([X.ravel(), Y.ravel(), Z.ravel()], -1)[r])
+    return np.stack(out)
+
+
+def boundary_gauss_points_3D(root_bounds, L: int, q: int) -> np.ndarray:
+    """Root boundary Gauss points (_grid_creation_3D.py:119-236): each face's
+    panel list is the 2D quad subdivision of its two coordinates repeated L
+    times; Gauss points meshgrid 'ij' inside a panel."""
+    x0, x1, y0, y1, z0, z1 = root_bounds
+    g = gauss_points(q)
+
+    def panels(u0, u1, v0, v1):
+        b = np.array([[u0, u1, v0, v1]])
+        for _ in range(L):
+            b = np.concatenate([quad_children_bounds(x) for x in b])
+        pts = []
+        for u0_, u1_, v0_, v1_ in b:
+            U, V = np.meshgrid(affine_transform(g, (u0_, u1_)), affine_transform(g, (v0_, v1_)), indexing="ij")
+            pts.append(np.stack([U.ravel(), V.ravel()], -1))
+        return np.concatenate(pts)
+
+    yz, xz, xy = panels(y0, y1, z0, z1), panels(x0, x1, z0, z1), panels(x0, x1, y0, y1)
+    n = yz.shape[0]
+    f = [np.column_stack([np.full(n, x0), yz]), np.column_stack([np.full(n, x1), yz]),
+         np.column_stack([xz[:, 0], np.full(n, y0), xz[:, 1]]), np.column_stack([xz[:, 0], np.full(n, y1), xz[:, 1]]),
+         np.column_stack([xy, np.full(n, z0)]), np.column_stack([xy, np.full(n, z1)])]
+    return np.concatenate(f)
+
+
+def face_idxes_3D(p: int, face: int) -> np.ndarray:
+    """get_face_1_idxes .. get_face_6_idxes (_precompute_operators_3D.py:220-320),
+    ``face`` = 0..5 for the reference's faces 1..6."""
+    if face == 0:
+        return np.arange(p ** 2)
+    if face == 1:
+        return np.arange(p ** 2) + p ** 2
+    if face == 2:
+        return np.concatenate([np.arange(p), np.arange(2 * p ** 2, 3 * p ** 2 - 2 * p), np.arange(p ** 2, p ** 2 + p)])
+    if face == 3:
+        return np.concatenate([np.arange(p * (p - 1), p ** 2), np.arange(3 * p ** 2 - 2 * p, 4 * p ** 2 - 4 * p),
+                               np.arange(2 * p ** 2 - p, 2 * p ** 2)])
+    if face == 4:
+        first_col = np.arange(0, p ** 2, p)
+        last_col = np.arange(p ** 2, 2 * p ** 2, p)
+        first_row = np.arange(2 * p ** 2, 3 * p ** 2 - 2 * p, p)
+        last_row = np.arange(3 * p ** 2 - 2 * p, 4 * p ** 2 - 4 * p, p)
+        interior = np.arange(4 * p ** 2 - 4 * p, 4 * p ** 2 - 4 * p + (p - 2) ** 2)
+    else:
+        first_col = np.arange(p - 1, p ** 2, p)
+        last_col = np.arange(p ** 2 + p - 1, 2 * p ** 2, p)
+        first_row = np.arange(2 * p ** 2 + p - 1, 3 * p ** 2 - 2 * p, p)
+        last_row = np.arange(3 * p ** 2 - 2 * p + p - 1, 4 * p ** 2 - 4 * p, p)
+        u = p ** 3 - (p - 2) ** 3
+        interior = np.arange(u - (p - 2) ** 2, u)
+    out = [first_col]
+    for i in range(p - 2):
+        out += [first_row[i:i + 1], interior[i * (p - 2):(i + 1) * (p - 2)], last_row[i:i + 1]]
+    out.append(last_col)
+    return np.concatenate(out)
+
+
+def diff_operators_3D(p: int, half_side_len: float):
+    """(_precompute_operators_3D.py:17-61) -> dx, dy, dz, dxx, dyy, dzz, dxy, dxz, dyz."""
+    r = ext_first_order_3D(p)
+    D = differentiation_matrix_1D(chebyshev_points(p)) / half_side_len
+    I = np.eye(p)
+    dx = np.kron(D, np.kron(I, I))[r][:, r]
+    dy = np.kron(I, np.kron(D, I))[r][:, r]
+    dz = np.kron(I, np.kron(I, D))[r][:, r]
+    return dx, dy, dz, dx @ dx, dy @ dy, dz @ dz, dx @ dy, dx @ dz, dy @ dz
+
+
+def _bary2D(fx, fy, tx, ty):
+    return np.kron(barycentric_matrix_1D(fx, tx), barycentric_matrix_1D(fy, ty))
+
+
+def P_3D_DtN(p: int, q: int) -> np.ndarray:
+    """(_precompute_operators_3D.py:64-147): per-face 2D interpolation, the 8
+    corner rows divided by 3 and the 12 edge row ranges divided by 2."""
+    g, c = gauss_points(q), chebyshev_points(p)
+    B = _bary2D(g, g, c, c)
+    P = np.zeros((p ** 3 - (p - 2) ** 3, 6 * q ** 2))
+    for f in range(6):
+        P[face_idxes_3D(p, f), f * q ** 2:(f + 1) * q ** 2] = B
+    corners = np.array([0, p - 1, p ** 2 - p, p ** 2 - 1, p ** 2, p ** 2 + p - 1, 2 * p ** 2 - p, 2 * p ** 2 - 1])
+    P[corners] /= 3
+    edges = np.concatenate([
+        np.arange(1, p - 1), np.arange(p ** 2 + 1, p ** 2 + p - 1), np.arange(p ** 2 - p + 1, p ** 2 - 1),
+        np.arange(2 * p ** 2 - p + 1, 2 * p ** 2 - 1), np.arange(1, p - 1) * p, np.arange(p, p ** 2 - p, p) + p ** 2,
+        np.arange(2 * p ** 2, 3 * p ** 2 - 2 * p, p), np.arange(3 * p ** 2 - 2 * p, 4 * p ** 2 - 4 * p, p),
+        np.arange(2 * p - 1, p ** 2 - p, p), np.arange(p ** 2 + 2 * p - 1, 2 * p ** 2 - p, p),
+        np.arange(2 * p ** 2 + p - 1, 3 * p ** 2 - 2 * p, p), np.arange(3 * p ** 2 - 2 * p + p - 1, 4 * p ** 2 - 4 * p, p),
+    ])
+    P[edges] /= 2
+    return P
+
+
+def Q_3D_DtN(p: int, q: int, dx, dy, dz) -> np.ndarray:
+    """(_precompute_operators_3D.py:150-210): N rows = -/+ d/dn on each face,
+    then kron(I_6, cheby->gauss 2D interpolation) @ N."""
+    N = np.concatenate([-dx[face_idxes_3D(p, 0)], dx[face_idxes_3D(p, 1)], -dy[face_idxes_3D(p, 2)],
+                        dy[face_idxes_3D(p, 3)], -dz[face_idxes_3D(p, 4)], dz[face_idxes_3D(p, 5)]])
+    g, c = gauss_points(q), chebyshev_points(p)
+    return np.kron(np.eye(6), _bary2D(c, c, g, g)) @ N
+
+
+# Oct merge bookkeeping (merge/_uniform_3D_DtN.py:190-380): for each child
+# a..h, the faces (0..5 = reference faces 1..6) forming its part of the merged
+# exterior, and its three interfaces as (label, face).  Labels 9..20 are the
+# reference's interface numbers.
+_OCT_CHILD = (
+    ((0, 2, 5), ((9, 1), (12, 3), (17, 4))),     # a
+    ((1, 2, 5), ((9, 0), (10, 3), (18, 4))),     # b
+    ((1, 3, 5), ((10, 2), (11, 0), (19, 4))),    # c
+    ((0, 3, 5), ((11, 1), (12, 2), (20, 4))),    # d
+    ((0, 2, 4), ((13, 1), (16, 3), (17, 5))),    # e
+    ((1, 2, 4), ((13, 0), (14, 3), (18, 5))),    # f
+    ((1, 3, 4), ((14, 2), (15, 0), (19, 5))),    # g
+    ((0, 3, 4), ((15, 1), (16, 2), (20, 5))),    # h
+)
+# Merged-face assembly order of the children's sub-blocks (get_rearrange_indices, :442-541).
+_OCT_FACE_CHILDREN = ((4, 7, 3, 0), (5, 6, 2, 1), (4, 5, 1, 0), (7, 6, 2, 3), (4, 5, 6, 7), (0, 1, 2, 3))
+
+
+def oct_merge_dtn(Ts, hs):
+    """One DtN oct merge (merge/_uniform_3D_DtN.py:127-187 with
+    _schur_complement.py:293-774 and the re-ordering of :442-541).
+
+    Ts: 8 child T (6nf, 6nf); hs: 8 child h (6nf, nsrc).  Returns S, T,
+    h_out, g_tilde, all in the reference's final orders."""
+    nf = Ts[0].shape[0] // 6
+    ix = np.arange(6 * nf)
+
+    def face(f):
+        return ix[f * nf:(f + 1) * nf]
+
+    ext_sets = [np.concatenate([face(f) for f in ch[0]]) for ch in _OCT_CHILD]
+    int_sets = [{lab: face(f) for lab, f in ch[1]} for ch in _OCT_CHILD]
+    n_ext, n_int = 24 * nf, 12 * nf
+    dt = np.result_type(*Ts)
+    B = np.zeros((n_ext, n_int), dtype=dt)
+    C = np.zeros((n_int, n_ext), dtype=dt)
+    D = np.zeros((n_int, n_int), dtype=dt)
+    ns = hs[0].shape[1]
+    dh = np.zeros((n_int, ns), dtype=dt)
+    h_ext = np.zeros((n_ext, ns), dtype=dt)
+
+    def isl(lab):
+        return slice((lab - 9) * nf, (lab - 8) * nf)
+
+    for c in range(8):
+        es = slice(3 * nf * c, 3 * nf * (c + 1))
+        h_ext[es] = hs[c][ext_sets[c]]
+        for lab, idx in int_sets[c].items():
+            B[es, isl(lab)] = Ts[c][np.ix_(ext_sets[c], idx)]
+            C[isl(lab), es] = Ts[c][np.ix_(idx, ext_sets[c])]
+            dh[isl(lab)] += hs[c][idx]
+            for lab2, idx2 in int_sets[c].items():
+                D[isl(lab), isl(lab2)] += Ts[c][np.ix_(idx, idx2)]
+    Dinv = np.linalg.inv(D)
+    S = -Dinv @ C
+    T = B @ S
+    for c in range(8):
+        es = slice(3 * nf * c, 3 * nf * (c + 1))
+        T[es, es] += Ts[c][np.ix_(ext_sets[c], ext_sets[c])]
+    g_tilde = -Dinv @ dh
+    h_out = h_ext + B @ g_tilde
+    # region c = [x-face block, y-face block, z-face block] of 3 nf each
+    r = []
+    for F, kids in enumerate(_OCT_FACE_CHILDREN):
+        for c in kids:
+            r.append(np.arange(3 * nf * c + (F // 2) * nf, 3 * nf * c + (F // 2 + 1) * nf))
+    r = np.concatenate(r)
+    return S[:, r], T[np.ix_(r, r)], h_out[r], g_tilde
+
+
+def merge_stage_3D(T, h, L: int):
+    """Level loop of merge_stage_uniform_3D_DtN (merge/_uniform_3D_DtN.py:12-124)."""
+    S_lst, g_lst = [], []
+    for _ in range(L):
+        nm = T.shape[0] // 8
+        outs = [oct_merge_dtn(T[8 * m:8 * m + 8], h[8 * m:8 * m + 8]) for m in range(nm)]
+        S_lst.append(np.stack([o[0] for o in outs]))
+        g_lst.append(np.stack([o[3] for o in outs]))
+        T = np.stack([o[1] for o in outs])
+        h = np.stack([o[2] for o in outs])
+    return S_lst, g_lst, T[0], h[0]
+
+
+# Child boundary assembly of _propogate_down_oct_DtN (down_pass/_uniform_3D_DtN.py:116-246):
+# per child, per own face, either ("b", merged face, block) or ("i", label).
+_OCT_DOWN = (
+    (("b", 0, 3), ("i", 9), ("b", 2, 3), ("i", 12), ("i", 17), ("b", 5, 0)),
+    (("i", 9), ("b", 1, 3), ("b", 2, 2), ("i", 10), ("i", 18), ("b", 5, 1)),
+    (("i", 11), ("b", 1, 2), ("i", 10), ("b", 3, 2), ("i", 19), ("b", 5, 2)),
+    (("b", 0, 2), ("i", 11), ("i", 12), ("b", 3, 3), ("i", 20), ("b", 5, 3)),
+    (("b", 0, 0), ("i", 13), ("b", 2, 0), ("i", 16), ("b", 4, 0), ("i", 17)),
+    (("i", 13), ("b", 1, 0), ("b", 2, 1), ("i", 14), ("b", 4, 1), ("i", 18)),
+    (("i", 15), ("b", 1, 1), ("i", 14), ("b", 3, 1), ("b", 4, 2), ("i", 19)),
+    (("b", 0, 1), ("i", 15), ("i", 16), ("b", 3, 0), ("b", 4, 3), ("i", 20)),
+)
+
+
+def _propagate_down_oct(S, g, gt):
+    nf = g.shape[0] // 24
+    gi = S @ g + gt
+    out = []
+    for spec in _OCT_DOWN:
+        parts = []
+        for s in spec:
+            if s[0] == "b":
+                o = s[1] * 4 * nf + s[2] * nf
+                parts.append(g[o:o + nf])
+            else:
+                parts.append(gi[(s[1] - 9) * nf:(s[1] - 8) * nf])
+        out.append(np.concatenate(parts))
+    return np.stack(out)
+
+
+def down_pass_3D(bdry, S_lst, g_lst, Y, v):
+    g = bdry[None]
+    for lvl in range(len(S_lst) - 1, -1, -1):
+        S, gt = S_lst[lvl], g_lst[lvl]
+        g = np.concatenate([_propagate_down_oct(S[m], g[m], gt[m]) for m in range(S.shape[0])])
+    return np.einsum("ijk,ikl->ijl", Y, g) + v
+
+
+class Problem3D:
+    """FP64 oracle problem for a uniform 3D octree (DtN).  Coefficients are
+    (n_leaves, p^3) arrays on the leaf points; ``source`` (n_leaves, p^3[, nsrc])."""
+
+    OPS = ("D_xx", "D_xy", "D_yy", "D_xz", "D_yz", "D_zz", "D_x", "D_y", "D_z", "I")
+
+    def __init__(self, root_bounds, L, p, q, coeffs, source):
+        self.root = tuple(float(x) for x in root_bounds)
+        self.L, self.p, self.q = L, p, q
+        self.bounds = uniform_leaf_bounds_3D(self.root, L)
+        self.points = leaf_points_3D(self.bounds, p)
+        self.boundary_points = boundary_gauss_points_3D(self.root, L, q)
+        half = (self.root[1] - self.root[0]) / (2 ** (L + 1))
+        dx, dy, dz, dxx, dyy, dzz, dxy, dxz, dyz = diff_operators_3D(p, half)
+        self.ops = {"D_xx": dxx, "D_xy": dxy, "D_yy": dyy, "D_xz": dxz, "D_yz": dyz, "D_zz": dzz,
+                    "D_x": dx, "D_y": dy, "D_z": dz, "I": np.eye(p ** 3)}
+        self.P = P_3D_DtN(p, q)
+        self.Q = Q_3D_DtN(p, q, dx, dy, dz)
+        self.coeffs = {k: (None if coeffs.get(k) is None else np.asarray(coeffs[k])) for k in self.OPS}
+        src = np.asarray(source)
+        self.multi = src.ndim == 3
+        self.source = src if self.multi else src[..., None]
+
+    def build(self):
+        nl = self.bounds.shape[0]
+        A = assemble_operator(self.coeffs, self.ops, nl, self.p ** 3)
+        self.Y, T, self.v, h = leaf_dtn(A, self.source, self.P, self.Q)
+        self.T_leaf, self.h_leaf = T, h
+        self.S_lst, self.g_lst, self.T_top, self.h_top = merge_stage_3D(T, h, self.L)
+        return self
+
+    def solve(self, bdry):
+        b = np.asarray(bdry)
+        b2 = b if b.ndim == 2 else b[:, None]
+        u = down_pass_3D(b2, self.S_lst, self.g_lst, self.Y, self.v)
+        return u if self.multi else u[..., 0]

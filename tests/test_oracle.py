@@ -143,3 +143,33 @@ def test_merge_iti_known_answer(L):
     fin = imp_data(bp, eta, +1)
     assert np.allclose(pr.T_top @ fin + pr.h_top[:, 0], imp_data(bp, eta, -1), atol=1e-9, rtol=0)
     assert np.allclose(pr.solve(fin), u_cc(pts), atol=1e-10, rtol=0)
+
+
+@pytest.mark.parametrize("L,p,q", [(1, 6, 4), (2, 6, 4)])
+def test_oct_merge_known_answer(L, p, q):
+    """3D analytic case: u = x^3 - 3 x y^2 + z^2 (Laplacian 2) is a degree-3
+    polynomial, reproduced by the discretization for p >= 4, q >= 4 up to
+    rounding through the leaf, oct-merge and down-pass restatements."""
+    root = (-1.0, 1.0, -0.5, 1.5, 0.0, 2.0)
+    pts = O.leaf_points_3D(O.uniform_leaf_bounds_3D(root, L), p)
+    x, y, z = pts[..., 0], pts[..., 1], pts[..., 2]
+    ones = np.ones_like(x)
+    pr = O.Problem3D(root, L, p, q, {"D_xx": ones, "D_yy": ones, "D_zz": ones}, 2 * ones).build()
+    bp = pr.boundary_points
+    u = pr.solve(bp[:, 0] ** 3 - 3 * bp[:, 0] * bp[:, 1] ** 2 + bp[:, 2] ** 2)
+    assert np.abs(u - (x ** 3 - 3 * x * y ** 2 + z ** 2)).max() < 1e-11
+
+
+def test_oct_merge_known_answer_variable_coefficients():
+    """(1 + x^2) u_xx + u_yy + u_zz + y u_z - u = f with u = x y + z^2 - y^3."""
+    L, p, q = 1, 6, 4
+    root = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    pts = O.leaf_points_3D(O.uniform_leaf_bounds_3D(root, L), p)
+    x, y, z = pts[..., 0], pts[..., 1], pts[..., 2]
+    u = x * y + z ** 2 - y ** 3
+    f = 0 + (-6 * y) + 2 + y * (2 * z) - u
+    ones = np.ones_like(x)
+    pr = O.Problem3D(root, L, p, q, {"D_xx": 1 + x ** 2, "D_yy": ones, "D_zz": ones, "D_z": y, "I": -ones}, f).build()
+    bp = pr.boundary_points
+    ub = pr.solve(bp[:, 0] * bp[:, 1] + bp[:, 2] ** 2 - bp[:, 1] ** 3)
+    assert np.abs(ub - u).max() < 1e-11
