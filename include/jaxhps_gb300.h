@@ -94,7 +94,8 @@ HPS_API size_t hps_inverse_workspace_size(int dtype, int n, int batch);
 
 /* X[b] = inv(A[b]) by Gauss-Jordan elimination with partial pivoting.
  * X may alias A.  info[b] (device, may be NULL) = 0 or k+1 for a zero pivot
- * at step k.  Replaces jnp.linalg.inv at local_solve/_uniform_2D_DtN.py:257
+ * at step k, or -1 when the multi-CTA panel used for few large matrices hit
+ * its barrier time limit (X[b] is then invalid).  Replaces jnp.linalg.inv at local_solve/_uniform_2D_DtN.py:257
  * and merge/_schur_complement.py:107,146. */
 HPS_API int hps_inverse_batched(int dtype, int n, const void* A, long long lda, long long strideA, void* X,
                         long long ldx, long long strideX, int batch, int* info, void* workspace,

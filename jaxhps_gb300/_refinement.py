@@ -217,7 +217,7 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
         T = _refine_leaf_operators(dom, coeffs, [OP_KIND_2D[n] for n in names], consts, Y, Aii,
                                    torch.as_tensor(np.ascontiguousarray(pde_problem.Q[:, n_cb:]), device=dev,
                                                    dtype=torch.float32))
-    S_lst, Dinv_lst, B_lst = [], [], []
+    S_lst, Dinv_lst, B_lst, infos = [], [], [], []
     Tc = T.to(merge_dtype)
     n_levels = max(dom.L, 1)
     for lvl in range(n_levels):
@@ -225,11 +225,13 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
         if lvl == dom.L - top_fp64_levels:
             Tc = Tc.double()
         need_T = lvl < n_levels - 1 or return_top_T
-        S, _, Tc, _, Dinv, _, B = st.merge_level_dtn(Tc, None, maps, keep_D_inv=True, keep_B=True, need_T=need_T)
+        S, _, Tc, _, Dinv, _, B = st.merge_level_dtn(Tc, None, maps, keep_D_inv=True, keep_B=True, need_T=need_T,
+                                                     infos=infos)
         S_lst.append(S.float())
         Dinv_lst.append(Dinv.float())
         B_lst.append(B.float())
     del T
+    st.raise_on_sync_timeout(infos)
 
     f, multi = st._src3(pde_problem.source, n_leaves, p * p, torch.float64, dev)
 

@@ -188,8 +188,15 @@ def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None,
 # ---------------------------------------------------------------------------
 
 
+def raise_on_sync_timeout(infos) -> None:
+    """The blocked inverse marks a matrix whose multi-CTA panel barrier timed
+    out with info = -1 (its result is invalid).  One device sync."""
+    if infos and int(torch.stack([i.min() for i in infos]).min()) < 0:
+        raise nat.NativeError("blocked inverse: a multi-CTA panel barrier timed out; results are invalid")
+
+
 def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False,
-                    keep_B=False, iti=False, need_T=True):
+                    keep_B=False, iti=False, need_T=True, infos=None):
     """One batched merge level.  T_children: (n_merges*nch, nb, nb);
     h_children: (n_merges*nch, nb, nsrc) or None.  Returns
     (S, g_tilde, T_out, h_out, D_inv, BD_inv) and B when ``keep_B``.
@@ -224,6 +231,8 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
         nat.check(L.hps_merge_level_iti(C.byref(a), nat.stream_ptr()), "hps_merge_level_iti")
     else:
         nat.check(L.hps_merge_level_dtn(C.byref(a), nat.stream_ptr()), "hps_merge_level_dtn")
+    if infos is not None:
+        infos.append(info)
     if keep_B:
         return S, g_t, T_out, h_out, D_inv, BD_inv, B
     return S, g_t, T_out, h_out, D_inv, BD_inv
@@ -269,14 +278,15 @@ def merge_stage_generic(T_arr, h_arr, n_levels: int, maps_fn, device=None, subtr
         if h.dim() == 2:
             h = h.unsqueeze(-1)
         h = h.reshape(T.shape[0], T.shape[1], -1).contiguous()
-    S_lst, g_lst, Dinv_lst = [], [], []
+    S_lst, g_lst, Dinv_lst, infos = [], [], [], []
     for lvl in range(n_levels):
         maps = maps_fn(T.shape[1])
         need_T = lvl < n_levels - 1 or return_T or subtree_recomp
-        S, g_t, T, h, D_inv, _ = merge_level_dtn(T, h, maps, keep_D_inv=keep_D_inv, need_T=need_T)
+        S, g_t, T, h, D_inv, _ = merge_level_dtn(T, h, maps, keep_D_inv=keep_D_inv, need_T=need_T, infos=infos)
         S_lst.append(S)
         g_lst.append(g_t if (g_t is None or multi) else g_t[..., 0])
         Dinv_lst.append(D_inv)
+    raise_on_sync_timeout(infos)
     if subtree_recomp:
         return T, (h if (h is None or multi) else h[..., 0])
     out = (S_lst, g_lst)

@@ -375,9 +375,13 @@ constexpr int BP = 32;       // panel width
 constexpr int PANEL_NT = 1024;
 
 struct GjeWs {
-  // per-matrix region sizes (elements / bytes), each 256-byte aligned
-  size_t mat, pan, u, g, h, e, piv, rinv, used, per;
+  // per-matrix region sizes (bytes), each 256-byte aligned; sync = the
+  // multi-CTA panel's barrier and proposal slots
+  size_t mat, pan, u, g, h, e, piv, rinv, used, sync, per;
 };
+
+// Upper bound on the CTAs that share one matrix's panel.
+static int coop_nct_cap(int n) { return n / 16 < 1 ? 1 : (n / 16 > 1024 ? 1024 : n / 16); }
 
 static size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -392,7 +396,12 @@ static GjeWs gje_layout(size_t es, int n) {
   w.piv = al256(4 * (size_t)n);
   w.rinv = al256(4 * (size_t)n);
   w.used = al256((size_t)n);
-  w.per = w.mat + w.pan + w.u + w.g + w.h + w.e + w.piv + w.rinv + w.used;
+  {
+    // as coop_layout() below with 8-byte magnitudes (an upper bound for every type)
+    const size_t cap = (size_t)coop_nct_cap(n);
+    w.sync = 256 + al256(2 * cap * 8) + al256(2 * cap * sizeof(int)) + al256(2 * cap * BP * es);
+  }
+  w.per = w.mat + w.pan + w.u + w.g + w.h + w.e + w.piv + w.rinv + w.used + w.sync;
   return w;
 }
 
@@ -531,6 +540,270 @@ gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G,
   }
   __syncthreads();
   for (int c = tid; c < bw; c += PANEL_NT) us[Rs[c]] = 1;
+}
+
+// --------------------------------------------------------------------------
+// Multi-CTA panel selection (few large matrices).
+//
+// Same result as gje_panel_kernel, but the panel's rows are split over
+// gridDim.x CTAs (a cooperative launch, so all of them are resident).  Per
+// panel column every CTA proposes its best unused row; the proposals (the
+// magnitude, the row index and the row's bw panel values) go to slots in
+// global memory, double-buffered by column parity, and one bounded grid
+// barrier per column makes them visible.  Every CTA then picks the same
+// pivot (largest magnitude, smallest index on ties) and updates its rows.
+// A barrier that does not complete within its spin limit sets the matrix's
+// error flag; the CTAs return and info[b] is set to -1.
+// --------------------------------------------------------------------------
+constexpr int CP_NT = 256;
+constexpr long long CP_SPIN_LIMIT = 1ll << 24;   // x >= 100 ns: a second or more
+
+struct CoopHdr {
+  unsigned count;
+  unsigned gen;
+  int err;
+  int pad;
+};
+
+__device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
+__device__ __forceinline__ c64 ld_cg(const c64* p) {
+  const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return c64{v.x, v.y};
+}
+__device__ __forceinline__ c128 ld_cg(const c128* p) {
+  const double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return c128{v.x, v.y};
+}
+
+// Barrier over the nct CTAs of one matrix; false on timeout or on an
+// earlier failure of this matrix.
+__device__ __forceinline__ bool coop_barrier(CoopHdr* hdr, unsigned nct) {
+  __shared__ int s_ok;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile CoopHdr* vh = hdr;
+    int ok = vh->err == 0;
+    if (ok) {
+      const unsigned g = vh->gen;
+      __threadfence();
+      const unsigned arrived = atomicAdd(&hdr->count, 1u) + 1u;
+      if (arrived == nct) {
+        atomicExch(&hdr->count, 0u);
+        __threadfence();
+        atomicAdd(&hdr->gen, 1u);
+      } else {
+        long long it = 0;
+        while (vh->gen == g) {
+          if (vh->err != 0 || ++it > CP_SPIN_LIMIT) {
+            ok = 0;
+            atomicExch(&hdr->err, 1);
+            break;
+          }
+          __nanosleep(100);
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Byte offsets inside one matrix's synchronisation block.
+struct CoopLayout {
+  size_t mag, idx, cand, per;
+};
+
+__host__ __device__ inline CoopLayout coop_layout(size_t es, size_t mag_size, int nct) {
+  auto a = [](size_t x) { return (x + 255) & ~size_t(255); };
+  CoopLayout c;
+  c.mag = 256;
+  c.idx = c.mag + a(2 * (size_t)nct * mag_size);
+  c.cand = c.idx + a(2 * (size_t)nct * sizeof(int));
+  c.per = c.cand + a(2 * (size_t)nct * BP * es);
+  return c;
+}
+
+template <class T>
+__global__ void __launch_bounds__(CP_NT)
+gje_panel_coop_kernel(int n, int k0, int bw, int rows_per, T* Mat, T* U, T* G, T* E, int* piv,
+                      unsigned char* used, int* info, unsigned char* sync, CoopLayout lay) {
+  using MagT = typename MagOf<T>::type;
+  const int b = blockIdx.y, cta = blockIdx.x, nct = gridDim.x;
+  const long long nn = (long long)n * n;
+  T* M = Mat + (long long)b * nn;
+  int* pv = piv + (long long)b * n;
+  unsigned char* us = used + (long long)b * n;
+  unsigned char* sb = sync + (size_t)b * lay.per;
+  CoopHdr* hdr = reinterpret_cast<CoopHdr*>(sb);
+  MagT* smag = reinterpret_cast<MagT*>(sb + lay.mag);
+  int* sidx = reinterpret_cast<int*>(sb + lay.idx);
+  T* scand = reinterpret_cast<T*>(sb + lay.cand);
+
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* P = reinterpret_cast<T*>(smraw);   // P[c * rows_per + i], i local row
+  T* fcol = P + (size_t)BP * rows_per;
+  unsigned char* ul = reinterpret_cast<unsigned char*>(fcol + rows_per);
+  __shared__ T rowr[BP];
+  __shared__ int Rs[BP];
+  __shared__ MagT wbest[CP_NT / 32];
+  __shared__ int widx[CP_NT / 32];
+  __shared__ int s_r, s_cta;
+  __shared__ MagT s_best;
+  __shared__ T s_pinv;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = cta * rows_per;
+  const int nr = max(0, min(n - r0, rows_per));
+
+  for (int e = tid; e < nr * bw; e += CP_NT) {
+    const int i = e / bw, c = e % bw;
+    P[c * rows_per + i] = M[(long long)(r0 + i) * n + k0 + c];
+  }
+  for (int i = tid; i < nr; i += CP_NT) ul[i] = us[r0 + i];
+  __syncthreads();
+
+  for (int c = 0; c < bw; ++c) {
+    const int buf = c & 1;
+    // this CTA's candidate
+    MagT best = -1;
+    int bi = n;
+    for (int i = tid; i < nr; i += CP_NT) {
+      if (!ul[i]) {
+        const MagT mg = nan_to_inf(pivmag(P[c * rows_per + i]));
+        if (mg > best) {
+          best = mg;
+          bi = r0 + i;
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      wbest[warp] = best;
+      widx[warp] = bi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      best = lane < CP_NT / 32 ? wbest[lane] : (MagT)-1;
+      bi = lane < CP_NT / 32 ? widx[lane] : n;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        smag[buf * nct + cta] = best;
+        sidx[buf * nct + cta] = bi;
+        s_r = bi;
+      }
+    }
+    __syncthreads();
+    {
+      const int lbi = s_r;
+      if (tid < BP)
+        scand[((size_t)buf * nct + cta) * BP + tid] =
+            (lbi < n && tid < bw) ? P[tid * rows_per + (lbi - r0)] : zero<T>();
+    }
+    if (!coop_barrier(hdr, (unsigned)nct)) {
+      if (cta == 0 && tid == 0 && info) info[b] = -1;
+      return;
+    }
+    // the pivot: same choice in every CTA
+    if (warp == 0) {
+      best = -1;
+      bi = n;
+      int bc = 0;
+      for (int k = lane; k < nct; k += 32) {
+        const MagT m = ld_cg(smag + buf * nct + k);
+        const int ix = ld_cg(sidx + buf * nct + k);
+        if (m > best || (m == best && ix < bi)) {
+          best = m;
+          bi = ix;
+          bc = k;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        const int oc = __shfl_xor_sync(0xffffffffu, bc, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+          bc = oc;
+        }
+      }
+      if (lane == 0) {
+        s_r = bi;
+        s_best = best;
+        s_cta = bc;
+        Rs[c] = bi;
+        if (cta == 0) {
+          pv[k0 + c] = bi;
+          if (!(best > 0) && info && info[b] == 0) info[b] = k0 + c + 1;
+        }
+      }
+    }
+    __syncthreads();
+    const int r = s_r;
+    if (tid == 0) {
+      const T pc = ld_cg(scand + ((size_t)buf * nct + s_cta) * BP + c);
+      s_pinv = (s_best > 0) ? rcp_(pc) : zero<T>();
+    }
+    __syncthreads();
+    const T pinv = s_pinv;
+    if (tid < bw) rowr[tid] = mul(ld_cg(scand + ((size_t)buf * nct + s_cta) * BP + tid), pinv);
+    for (int i = tid; i < nr; i += CP_NT) fcol[i] = P[c * rows_per + i];
+    if (tid == 0 && r >= r0 && r < r0 + nr) ul[r - r0] = 2;
+    __syncthreads();
+    for (int e = tid; e < nr * bw; e += CP_NT) {
+      const int i = e % nr, c2 = e / nr;
+      T& x = P[c2 * rows_per + i];
+      if (r0 + i == r) {
+        x = (c2 == c) ? pinv : rowr[c2];
+      } else {
+        const T f = fcol[i];
+        x = (c2 == c) ? neg(mul(f, pinv)) : fms_(f, rowr[c2], x);
+      }
+    }
+    __syncthreads();
+  }
+
+  // outputs, as gje_panel_kernel: panel back into M, U, E (pivot rows this CTA owns), G, used flags
+  T* Ub = U + (long long)b * n * BP;
+  T* Gb = G + (long long)b * BP * n;
+  T* Eb = E + (long long)b * BP * BP;
+  for (int e = tid; e < nr * bw; e += CP_NT) {
+    const int i = e / bw, c = e % bw;
+    const T v = P[c * rows_per + i];
+    M[(long long)(r0 + i) * n + k0 + c] = v;
+    Ub[(long long)(r0 + i) * BP + c] = (ul[i] == 2) ? zero<T>() : v;
+  }
+  for (int e = tid; e < bw * bw; e += CP_NT) {
+    const int c1 = e / bw, c2 = e % bw;
+    const int rr = Rs[c1];
+    if (rr >= r0 && rr < r0 + nr) Eb[c1 * BP + c2] = P[c2 * rows_per + (rr - r0)];
+  }
+  for (long long e = (long long)cta * CP_NT + tid; e < (long long)bw * n; e += (long long)nct * CP_NT) {
+    const int c1 = (int)(e / n), j = (int)(e % n);
+    Gb[(long long)c1 * n + j] = (j >= k0 && j < k0 + bw) ? zero<T>() : M[(long long)Rs[c1] * n + j];
+  }
+  for (int i = tid; i < nr; i += CP_NT) us[r0 + i] = (ul[i] == 2) ? 1 : ul[i];
 }
 
 template <class T>
@@ -701,6 +974,44 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
   int* rinv = reinterpret_cast<int*>(base);
   base += L.rinv * batch;
   unsigned char* used = base;
+  base += L.used * batch;
+  unsigned char* syncb = base;
+
+  // Few matrices: split each panel over several CTAs (cooperative launch).
+  int nct = 0, rows_per = 0;
+  size_t csmem = 0;
+  {
+    int dev = 0, sms = 0, coop_ok = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, dev);
+    if (coop_ok && sms > 0 && batch < sms && n > 64) {
+      nct = 2 * sms / batch;
+      if (nct > coop_nct_cap(n)) nct = coop_nct_cap(n);
+      bool fits = false;
+      for (int iter = 0; iter < 6 && nct >= 2; ++iter) {
+        rows_per = (n + nct - 1) / nct;
+        nct = (n + rows_per - 1) / rows_per;
+        csmem = es * ((size_t)BP * rows_per + rows_per) + (size_t)rows_per + 16;
+        if (csmem > 200 * 1024) break;
+        cudaFuncSetAttribute(gje_panel_coop_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_coop_kernel<T>, CP_NT, csmem);
+        if ((long long)per_sm * sms >= (long long)nct * batch) {
+          fits = true;
+          break;
+        }
+        nct = per_sm * sms / batch;
+      }
+      if (!fits || nct < 2) nct = 0;
+      cudaGetLastError();   // a refused attribute or occupancy query only disables this path
+    }
+  }
+  const CoopLayout clay = coop_layout(es, sizeof(typename MagOf<T>::type), nct > 0 ? nct : 1);
+  if (nct > 0) {
+    cudaError_t e = cudaMemsetAsync(syncb, 0, clay.per * (size_t)batch, st);
+    if (e != cudaSuccess) return e;
+  }
 
   const long long nn = (long long)n * n;
   for (int b0 = 0; b0 < batch; b0 += 65535) {
@@ -714,20 +1025,38 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
   // Panel width: the widest of 32/16/8/4 whose panel fits in shared memory;
   // wider panels mean fewer (rank-bw) trailing GEMM updates.
   int bwmax = BP;
-  while (bwmax > 4 && es * (size_t)n * bwmax > 200 * 1024) bwmax /= 2;
-  const size_t pan_smem = es * (size_t)n * bwmax;
-  const int use_smem = pan_smem <= 200 * 1024;
-  if (!use_smem) bwmax = BP;
-  if (use_smem)
-    cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pan_smem);
+  int use_smem = 0;
+  size_t pan_smem = 0;
+  if (nct == 0) {
+    while (bwmax > 4 && es * (size_t)n * bwmax > 200 * 1024) bwmax /= 2;
+    pan_smem = es * (size_t)n * bwmax;
+    use_smem = pan_smem <= 200 * 1024;
+    if (!use_smem) bwmax = BP;
+    if (use_smem)
+      cudaFuncSetAttribute(gje_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pan_smem);
+  }
   const T one_ = one<T>();
   for (int k0 = 0; k0 < n; k0 += bwmax) {
-    const int bw = (n - k0) < bwmax ? (n - k0) : bwmax;
+    int bw = (n - k0) < bwmax ? (n - k0) : bwmax;
     ProfScope ps(KC_INVERSE, st, 2.0 * (double)n * bw * bw * batch);
     note_launch();
-    gje_panel_kernel<T><<<batch, PANEL_NT, use_smem ? pan_smem : 0, st>>>(
-        n, k0, bw, Mat, Pw, use_smem, U, G, E, piv, used, info);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e;
+    if (nct > 0) {
+      int n_ = n, k0_ = k0, rp = rows_per;
+      T *Mat_ = Mat, *U_ = U, *G_ = G, *E_ = E;
+      int* piv_ = piv;
+      unsigned char* used_ = used;
+      int* info_ = info;
+      unsigned char* sync_ = syncb;
+      CoopLayout lay_ = clay;
+      void* args[] = {&n_, &k0_, &bw, &rp, &Mat_, &U_, &G_, &E_, &piv_, &used_, &info_, &sync_, &lay_};
+      e = cudaLaunchCooperativeKernel((void*)gje_panel_coop_kernel<T>, dim3(nct, batch), dim3(CP_NT), args, csmem,
+                                      st);
+    } else {
+      gje_panel_kernel<T><<<batch, PANEL_NT, use_smem ? pan_smem : 0, st>>>(
+          n, k0, bw, Mat, Pw, use_smem, U, G, E, piv, used, info);
+      e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return e;
     // H = E G
     e = gemm_batched<T>(bw, n, bw, one_, E, BP, BP * BP, G, n, (long long)BP * n, zero<T>(), nullptr, 0,

@@ -808,6 +808,8 @@ def merge_stage_3D(T, h, L: int):
         g_lst.append(np.stack([o[3] for o in outs]))
         T = np.stack([o[1] for o in outs])
         h = np.stack([o[2] for o in outs])
+    # the root entries are stored without a batch axis (merge/_uniform_3D_DtN.py:116)
+    S_lst[-1], g_lst[-1] = S_lst[-1][0], g_lst[-1][0]
     return S_lst, g_lst, T[0], h[0]
 
 
@@ -842,6 +844,9 @@ def _propagate_down_oct(S, g, gt):
 
 
 def down_pass_3D(bdry, S_lst, g_lst, Y, v):
+    """down_pass/_uniform_3D_DtN.py:8-113; the root entries are expanded (:86-87)."""
+    S_lst = list(S_lst[:-1]) + [S_lst[-1][None]]
+    g_lst = list(g_lst[:-1]) + [g_lst[-1][None]]
     g = bdry[None]
     for lvl in range(len(S_lst) - 1, -1, -1):
         S, gt = S_lst[lvl], g_lst[lvl]

@@ -71,6 +71,7 @@ def test_build_solve_3D_matches_oracle(cuda, L, p, q, nsrc, extra):
     assert len(pde.S_lst) == len(ref.S_lst)
     for a, b in zip(pde.S_lst, ref.S_lst):
         assert tuple(a.shape) == b.shape and _rel(a, b) < 1e-10
+    assert pde.S_lst[-1].dim() == 2   # root stored without a batch axis, like the reference
 
 
 def test_merge_stage_3D_without_top_T(cuda):
@@ -81,6 +82,7 @@ def test_merge_stage_3D_without_top_T(cuda):
     S2, g2, Ttop = st3.merge_stage_uniform_3D_DtN(T, h, l=2, device=cuda, return_T=True)
     for a, b in zip(S1 + g1, S2 + g2):
         assert torch.equal(a, b)
+    assert S1[-1].dim() == 2 and g1[-1].dim() == 2
     assert tuple(Ttop.shape) == (24 * 16 * 4, 24 * 16 * 4)
 
 

@@ -91,3 +91,20 @@ def test_inverse_large_blocked(cuda):
     A = rng.standard_normal((1, n, n)) + np.sqrt(n) * np.eye(n)
     X = nat.inverse(torch.as_tensor(A, device=cuda)).cpu().numpy()
     assert np.abs(X[0] @ A[0] - np.eye(n)).max() < 1e-10
+
+
+@pytest.mark.parametrize("n,dt", [(3000, "f32"), (2500, "f64"), (700, "c64")])
+def test_inverse_large_single_matrix_multi_cta_panel(cuda, n, dt):
+    """One large matrix: the panel is split over many CTAs (cooperative launch)."""
+    from jaxhps_gb300 import _native as nat
+
+    tdt, npdt, tol = DT[dt]
+    rng = np.random.default_rng(n)
+    A = _rand(rng, (1, n, n), npdt) + (2 * np.sqrt(n)) * np.eye(n, dtype=npdt)
+    A = np.ascontiguousarray(A[:, rng.permutation(n), :])
+    info = torch.zeros(1, dtype=torch.int32, device=cuda)
+    X = nat.inverse(torch.as_tensor(A, device=cuda), info=info).cpu().numpy()
+    assert int(info.item()) == 0
+    Xe = np.linalg.inv(A.astype(np.complex128 if np.iscomplexobj(A) else np.float64))
+    rel = np.abs(X - Xe).max() / np.abs(Xe).max()
+    assert rel < tol * 20, rel
