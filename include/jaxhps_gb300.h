@@ -318,6 +318,13 @@ HPS_API int hps_residual_update_2d(const hps_residual2d_args* a, const float* du
 HPS_API int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
                               const double* g, double* u_full, void* stream);
 
+/* out[l][i][j] = sum_o coeffs[o][l][row0+i] * ops[o][row0+i][j] for rows
+ * row0 .. row0+n_rows-1 of every leaf's operator A (FP64; row stride ld,
+ * leaf stride `stride`).  The assembly of assemble_diff_operator
+ * (local_solve/_uniform_2D_DtN.py:182-218), kept for FP64 residuals. */
+HPS_API int hps_assemble_rows(int n_leaves, int n_pts, int row0, int n_rows, int n_ops, const double* ops,
+                              const double* coeffs, double* out, long long ld, long long stride, void* stream);
+
 /* r32 = f[:, n_cb:, :] rounded to FP32 (the residual at zero). */
 HPS_API int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32,
                              void* stream);

@@ -148,3 +148,24 @@ def compute_boundary_Gauss_points_adaptive_3D(root: DiscretizationNode3D, q: int
 
 def get_all_uniform_leaves_3D(root: DiscretizationNode3D, L: int):
     return [DiscretizationNode3D(*b, depth=L) for b in uniform_leaf_bounds_3D(root.bounds, L)]
+
+
+def leaf_boundary_gauss_points_3D(bounds: np.ndarray, q: int) -> np.ndarray:
+    """(n_leaves, 6q^2, 3) Gauss nodes of every leaf boundary, in the leaf's
+    own face order (-x, +x, -y, +y, -z, +z; meshgrid 'ij' inside a face)."""
+    g = gauss_points(q)
+    b = np.atleast_2d(np.asarray(bounds, dtype=np.float64))
+    out = np.empty((len(b), 6 * q * q, 3))
+    tang = ((1, 2), (1, 2), (0, 2), (0, 2), (0, 1), (0, 1))
+    for f in range(6):
+        ax, side = f // 2, f % 2
+        ta, tb = tang[f]
+        U = 0.5 * (b[:, 2 * ta + 1:2 * ta + 2] - b[:, 2 * ta:2 * ta + 1]) * g[None] + \
+            0.5 * (b[:, 2 * ta:2 * ta + 1] + b[:, 2 * ta + 1:2 * ta + 2])
+        V = 0.5 * (b[:, 2 * tb + 1:2 * tb + 2] - b[:, 2 * tb:2 * tb + 1]) * g[None] + \
+            0.5 * (b[:, 2 * tb:2 * tb + 1] + b[:, 2 * tb + 1:2 * tb + 2])
+        sl = slice(f * q * q, (f + 1) * q * q)
+        out[:, sl, ax] = b[:, 2 * ax + side][:, None]
+        out[:, sl, ta] = np.repeat(U, q, axis=1)
+        out[:, sl, tb] = np.tile(V, (1, q))
+    return out

@@ -142,6 +142,8 @@ def _declare(lib):
     lib.hps_assemble_u_2d.restype = ci
     lib.hps_interior_f32.argtypes = [cll, ci, ci, ci, vp, vp, vp]
     lib.hps_interior_f32.restype = ci
+    lib.hps_assemble_rows.argtypes = [ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp]
+    lib.hps_assemble_rows.restype = ci
 
 
 EXPORTED_SYMBOLS = (
@@ -149,7 +151,7 @@ EXPORTED_SYMBOLS = (
     "hps_inverse_batched", "hps_convert", "hps_local_solve_dtn_workspace_size", "hps_local_solve_dtn",
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
     "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
-    "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32",
+    "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
 )
 
 

@@ -589,6 +589,18 @@ int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside,
   return HPS_OK;
 }
 
+int hps_assemble_rows(int n_leaves, int n_pts, int row0, int n_rows, int n_ops, const double* ops,
+                      const double* coeffs, double* out, long long ld, long long stride, void* stream) {
+  if (n_leaves <= 0 || n_pts <= 0 || row0 < 0 || n_rows <= 0 || row0 + n_rows > n_pts || n_ops <= 0 || !ops ||
+      !coeffs || !out || ld < n_pts || stride < (long long)n_rows * ld) {
+    set_error("hps_assemble_rows: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(leaf_assemble<double, double>(n_leaves, n_pts, row0, n_rows, n_pts, n_ops, ops, coeffs, out, ld, stride,
+                                          nullptr, 0, 0, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
 int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32, void* stream) {
   if (n_leaves <= 0 || n_pts <= n_cb || nsrc <= 0 || !f || !r32) {
     set_error("hps_interior_f32: invalid arguments");

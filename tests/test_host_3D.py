@@ -174,3 +174,60 @@ def test_oct_down_scatter_maps_reproduce_oracle(nf):
             cd = maps.code[c, k]
             out[c, k] = g[cd] if cd >= 0 else gi[-cd - 1]
     assert np.allclose(out, ref)
+
+
+def test_leaf_gauss_nodes_3D_and_pairing():
+    from jaxhps_gb300._refinement import node_maps
+
+    root = hps.DiscretizationNode3D(-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    q = 4
+    one = g3.leaf_boundary_gauss_points_3D(np.array([root.bounds]), q)[0]
+    assert np.allclose(one, g3.compute_boundary_Gauss_points_uniform_3D(root, 0, q))
+    dom = hps.Domain(p=6, q=q, root=root, L=2)
+    nodes = g3.leaf_boundary_gauss_points_3D(g3.uniform_leaf_bounds_3D(root.bounds, 2), q)
+    nbr, bnode = node_maps(nodes, dom.boundary_points, scale=2.0)
+    flat = nodes.reshape(-1, 3)
+    inner = nbr >= 0
+    assert np.allclose(flat[inner], flat[nbr[inner]]) and (nbr[nbr[inner]] == np.nonzero(inner)[0]).all()
+    assert (~inner).sum() == dom.boundary_points.shape[0]
+    assert np.allclose(flat[bnode], dom.boundary_points)
+
+
+def _oracle_leaf_boundary_data_3D(pr, bdry):
+    S_lst = list(pr.S_lst[:-1]) + [pr.S_lst[-1][None]]
+    g_lst = list(pr.g_lst[:-1]) + [pr.g_lst[-1][None]]
+    g = bdry[None]
+    for lvl in range(len(S_lst) - 1, -1, -1):
+        g = np.concatenate([O._propagate_down_oct(S_lst[lvl][m], g[m], g_lst[lvl][m])
+                            for m in range(S_lst[lvl].shape[0])])
+    return g
+
+
+def test_oracle_3D_solution_is_zero_of_dense_residual():
+    """The discrete system the 3D mixed solver iterates on (collocation rows,
+    flux continuity at paired Gauss nodes, Dirichlet data) is solved by the
+    oracle's FP64 direct solution."""
+    from jaxhps_gb300._refinement import node_maps
+
+    L, p, q = 2, 6, 4
+    rb = (-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
+    rng = np.random.default_rng(4)
+    pts = O.leaf_points_3D(O.uniform_leaf_bounds_3D(rb, L), p)
+    c = 1 + 0.3 * np.exp(-(pts ** 2).sum(-1))
+    ones = np.ones_like(c)
+    f = rng.standard_normal(c.shape + (2,))
+    pr = O.Problem3D(rb, L, p, q, {"D_xx": ones, "D_yy": ones, "D_zz": ones, "I": -c}, f).build()
+    bdry = np.stack([np.sin(pr.boundary_points[:, 0]), pr.boundary_points[:, 2]], -1)
+    u = pr.solve(bdry)
+    gl = _oracle_leaf_boundary_data_3D(pr, bdry)
+    A = O.assemble_operator(pr.coeffs, pr.ops, pts.shape[0], p ** 3)
+    n_cb = pr.P.shape[0]
+    u_full = np.concatenate([np.einsum("ab,lbs->las", pr.P, gl), u[:, n_cb:]], 1)
+    r = f[:, n_cb:] - np.einsum("lab,lbs->las", A[:, n_cb:], u_full)
+    assert np.abs(r).max() < 1e-9 * np.abs(f).max()
+    flux = np.einsum("ab,lbs->las", pr.Q, u_full).reshape(-1, 2)
+    nodes = g3.leaf_boundary_gauss_points_3D(g3.uniform_leaf_bounds_3D(rb, L), q)
+    nbr, bnode = node_maps(nodes, pr.boundary_points, scale=2.0)
+    inner = nbr >= 0
+    assert np.abs(flux[inner] + flux[nbr[inner]]).max() < 1e-8 * np.abs(flux).max()
+    assert np.allclose(gl.reshape(-1, 2)[bnode], bdry)
