@@ -325,6 +325,31 @@ HPS_API int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double
 HPS_API int hps_assemble_rows(int n_leaves, int n_pts, int row0, int n_rows, int n_ops, const double* ops,
                               const double* coeffs, double* out, long long ld, long long stride, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Adaptive octree refinement check.  Replaces the per-node check of
+ * generate_adaptive_mesh_level_restriction (_adaptive_discretization_3D.py
+ * :34-210, :424-503): evaluate f on a node's grid and its eight children's
+ * grids, interpolate node -> children (L_8f1) and compare.
+ * ------------------------------------------------------------------------- */
+
+/* pts (n_nodes, 9, p^3, 3): for every node (bounds (n_nodes, 6) = xmin, xmax,
+ * ymin, ymax, zmin, zmax) its own Chebyshev points then those of children
+ * a..h, each grid in exterior-first order (perm[k] = raster index
+ * ix p^2 + iy p + iz of position k; cheb = 1D points on [-1, 1]). */
+HPS_API int hps_refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
+                                 double* pts, void* stream);
+
+/* From f at those points (f_values (n_nodes, 9, p^3)): diff_max[n] =
+ * max |L_8f1 f_node - f_children|, ref_max[n] = max |f_children|, and
+ * (l2_err may be NULL) the Clenshaw-Curtis weighted squared L2 norm of the
+ * difference over the children.  interp_lo/hi (p x p): 1D interpolation
+ * from the node's points to a child's lower/upper half points; iperm =
+ * inverse of perm; cc_weights = Clenshaw-Curtis weights on [-1, 1]. */
+HPS_API int hps_refine_check_3d(int n_nodes, int p, const double* f_values, const int* perm, const int* iperm,
+                                const double* interp_lo, const double* interp_hi, const double* cc_weights,
+                                const double* bounds, double* diff_max, double* ref_max, double* l2_err,
+                                void* stream);
+
 /* r32 = f[:, n_cb:, :] rounded to FP32 (the residual at zero). */
 HPS_API int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32,
                              void* stream);

@@ -144,6 +144,10 @@ def _declare(lib):
     lib.hps_interior_f32.restype = ci
     lib.hps_assemble_rows.argtypes = [ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp]
     lib.hps_assemble_rows.restype = ci
+    lib.hps_refine_points_3d.argtypes = [ci, ci, vp, vp, vp, vp, vp]
+    lib.hps_refine_points_3d.restype = ci
+    lib.hps_refine_check_3d.argtypes = [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.hps_refine_check_3d.restype = ci
 
 
 EXPORTED_SYMBOLS = (
@@ -152,6 +156,7 @@ EXPORTED_SYMBOLS = (
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
     "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
+    "hps_refine_points_3d", "hps_refine_check_3d",
 )
 
 

@@ -24,6 +24,11 @@ cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col
 template <class T>
 cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds, T* dst, long long ldd,
                      long long sd, cudaStream_t st);
+cudaError_t refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
+                             double* pts, cudaStream_t st);
+cudaError_t refine_check_3d(int n_nodes, int p, const double* fv, const int* perm, const int* iperm,
+                            const double* Ilo, const double* Ihi, const double* wref, const double* bounds,
+                            double* diff, double* ref, double* l2, cudaStream_t st);
 template <class T>
 cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Tc, const T* hc,
                          const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
@@ -586,6 +591,31 @@ int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside,
     return HPS_ERR_ARG;
   }
   HPS_CHECK(assemble_u_2d(n_leaves, p, q, nsrc, Pside, u_int, g, u_full, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
+                         double* pts, void* stream) {
+  if (n_nodes < 0 || p < 2 || !bounds || !cheb || !perm || !pts) {
+    set_error("hps_refine_points_3d: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (n_nodes == 0) return HPS_OK;
+  HPS_CHECK(refine_points_3d(n_nodes, p, bounds, cheb, perm, pts, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_refine_check_3d(int n_nodes, int p, const double* f_values, const int* perm, const int* iperm,
+                        const double* interp_lo, const double* interp_hi, const double* cc_weights,
+                        const double* bounds, double* diff_max, double* ref_max, double* l2_err, void* stream) {
+  if (n_nodes < 0 || p < 2 || p > 16 || !f_values || !perm || !iperm || !interp_lo || !interp_hi || !cc_weights ||
+      !bounds || !diff_max || !ref_max) {
+    set_error("hps_refine_check_3d: invalid arguments (2 <= p <= 16)");
+    return HPS_ERR_ARG;
+  }
+  if (n_nodes == 0) return HPS_OK;
+  HPS_CHECK(refine_check_3d(n_nodes, p, f_values, perm, iperm, interp_lo, interp_hi, cc_weights, bounds, diff_max,
+                            ref_max, l2_err, (cudaStream_t)stream));
   return HPS_OK;
 }
 

@@ -890,3 +890,189 @@ class Problem3D:
         b2 = b if b.ndim == 2 else b[:, None]
         u = down_pass_3D(b2, self.S_lst, self.g_lst, self.Y, self.v)
         return u if self.multi else u[..., 0]
+
+
+# ---------------------------------------------------------------------------
+# Adaptive octree meshing  (src/jaxhps/_adaptive_discretization_3D.py:34-503,
+#                           _discretization_tree_operations_3D.py:26-98,
+#                           _precompute_operators_3D.py:412-500)
+# ---------------------------------------------------------------------------
+
+
+def chebyshev_weights(n: int, bounds) -> np.ndarray:
+    """Clenshaw-Curtis weights on [a, b] (quadrature/_discretization.py:40-86)."""
+    a, b = bounds
+    c = 2.0 / np.concatenate([[1.0], 1.0 - np.arange(2, n, 2) ** 2])
+    start = n // 2 if n % 2 else n // 2 + 1
+    c = np.concatenate([c, np.flip(c[1:start])])
+    w = np.fft.ifft(c).real
+    out = np.concatenate([w, [w[0] / 2]])
+    out[0] = w[0] / 2
+    return out * (b - a) / 2
+
+
+def L_8f1(p: int) -> np.ndarray:
+    """Dense node -> eight children interpolation, rows blocks a..h each in
+    exterior-first order, columns exterior-first (_precompute_operators_3D.py
+    :412-500)."""
+    c = chebyshev_points(p)
+    lo, hi = affine_transform(c, (-1.0, 0.0)), affine_transform(c, (0.0, 1.0))
+    Bl, Bh = barycentric_matrix_1D(c, lo), barycentric_matrix_1D(c, hi)
+    r = ext_first_order_3D(p)
+    bits = ((0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1), (0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0))
+    blocks = []
+    for bx, by, bz in bits:
+        M = np.kron(np.kron(Bh if bx else Bl, Bh if by else Bl), Bh if bz else Bl)
+        blocks.append(M[r][:, r])
+    return np.concatenate(blocks)
+
+
+class OctNode:
+    """Minimal octree node for the oracle (bounds, depth, children, face counts)."""
+
+    def __init__(self, bounds, depth=0):
+        self.b = tuple(float(x) for x in bounds)
+        self.depth = depth
+        self.children = []
+        self.n = [None] * 6
+
+    def leaves(self):
+        if not self.children:
+            return [self]
+        out = []
+        for ch in self.children:
+            out += ch.leaves()
+        return out
+
+
+def oracle_add_eight_children(node: OctNode, root: OctNode = None, q: int = None):
+    """_discretization_tree_operations_3D.py:26-98."""
+    if node.children:
+        return
+    node.children = [OctNode(b, node.depth + 1) for b in oct_children_bounds(node.b)]
+    if q is None:
+        return
+    q2 = q * q
+    for ch in node.children:
+        ch.n = [q2] * 6
+    node.n = [4 * q2] * 6
+    if root is None or node is root:
+        return
+    cur = root
+    while node not in cur.children:   # ancestors from the root to the parent
+        for k in range(6):
+            if cur.b[k] == node.b[k]:
+                cur.n[k] += 3 * q2
+        xm, ym, zm = (cur.b[0] + cur.b[1]) / 2, (cur.b[2] + cur.b[3]) / 2, (cur.b[4] + cur.b[5]) / 2
+        x0, y0, z0 = node.b[0], node.b[2], node.b[4]
+        if x0 < xm:
+            i = (4 if z0 < zm else 0) if y0 < ym else (7 if z0 < zm else 3)
+        else:
+            i = (5 if z0 < zm else 1) if y0 < ym else (6 if z0 < zm else 2)
+        cur = cur.children[i]
+    for k in range(6):
+        if cur.b[k] == node.b[k]:
+            cur.n[k] += 3 * q2
+
+
+def _oracle_volumes(n: OctNode, root: OctNode):
+    s = n.b[1] - n.b[0]
+    x0, x1, y0, y1, z0, z1 = n.b
+    v = []
+    if x0 - s >= root.b[0]:
+        v.append((x0 - s, x0, y0, y1, z0, z1))
+    if x1 + s <= root.b[1]:
+        v.append((x1, x1 + s, y0, y1, z0, z1))
+    if y0 - s >= root.b[2]:
+        v.append((x0, x1, y0 - s, y0, z0, z1))
+    if y1 + s <= root.b[3]:
+        v.append((x0, x1, y1, y1 + s, z0, z1))
+    if z0 - s >= root.b[4]:
+        v.append((x0, x1, y0, y1, z0 - s, z0))
+    if z1 + s <= root.b[5]:
+        v.append((x0, x1, y0, y1, z1, z1 + s))
+    return v
+
+
+def _oracle_find_or_add(node: OctNode, root: OctNode, q, vol):
+    """find_or_add_child (_adaptive_discretization_3D.py:317-420)."""
+    xmin, xmax, ymin, ymax, zmin, zmax = vol
+    side = node.b[1] - node.b[0]
+    req = xmax - xmin
+    if np.allclose(req * 2, side):
+        if not node.children:
+            oracle_add_eight_children(node, root, q)
+            return node
+        return None
+    xm, ym, zm = (node.b[0] + node.b[1]) / 2, (node.b[2] + node.b[3]) / 2, (node.b[4] + node.b[5]) / 2
+    if xmin < xm:
+        i = (4 if zmin < zm else 0) if ymin < ym else (7 if zmin < zm else 3)
+    else:
+        i = (5 if zmin < zm else 1) if ymin < ym else (6 if zmin < zm else 2)
+    child = node.children[i]
+    if np.allclose(side, 4 * req):
+        if not child.children:
+            oracle_add_eight_children(child, root, q)
+            return child
+        return None
+    if side < 2 * req:
+        raise ValueError("Requested volume is too large for the current node")
+    return _oracle_find_or_add(child, root, q, vol)
+
+
+def oracle_adaptive_mesh_3D(root: OctNode, f, tol: float, p: int, q: int, restrict: bool = True,
+                            l2: bool = False):
+    """generate_adaptive_mesh_level_restriction (_adaptive_discretization_3D.py:34-210)
+    with the dense L_8f1 check; ``f`` takes (..., 3) NumPy points.  Refines in
+    place; returns the number of rounds."""
+    Lop = L_8f1(p)
+    r = ext_first_order_3D(p)
+
+    def sq_l2(vals, b):
+        w = np.einsum("i,j,k->ijk", chebyshev_weights(p, b[0:2]), chebyshev_weights(p, b[2:4]),
+                      chebyshev_weights(p, b[4:6])).ravel()[r]
+        return float(np.sum(w * vals ** 2))
+
+    if l2:
+        oracle_add_eight_children(root, root, q)
+        gn = sum(sq_l2(f(leaf_points_3D(np.array([lf.b]), p)[0]), lf.b) for lf in root.leaves())
+        tol = tol ** 2
+    else:
+        gn = float(np.max(f(leaf_points_3D(oct_children_bounds(root.b), p).reshape(-1, 3))))
+    queue = root.leaves()
+    rounds = 0
+    while queue:
+        rounds += 1
+        ok, nrms = [], []
+        for node in queue:
+            f0 = f(leaf_points_3D(np.array([node.b]), p)[0])
+            f1 = f(leaf_points_3D(oct_children_bounds(node.b), p).reshape(-1, 3))
+            d = Lop @ f0 - f1
+            if l2:
+                kids = oct_children_bounds(node.b)
+                err = sum(sq_l2(d[k * p ** 3:(k + 1) * p ** 3], kids[k]) for k in range(8))
+                ok.append(err / gn < tol)
+                nrms.append(0.0)
+            else:
+                nrm = max(gn, float(np.max(np.abs(f1))))
+                ok.append(float(np.max(np.abs(d))) / nrm < tol)
+                nrms.append(nrm)
+        if not l2:
+            gn = max(nrms)
+        new_queue = []
+        for node, good in zip(queue, ok):
+            if good:
+                continue
+            oracle_add_eight_children(node, root, q)
+            new_queue += node.children
+            if restrict:
+                pending = [node]
+                while pending:
+                    fc = pending.pop()
+                    for vol in _oracle_volumes(fc, root):
+                        n = _oracle_find_or_add(root, root, q, vol)
+                        if n is not None:
+                            pending.append(n)
+                            new_queue += n.children
+        queue = new_queue
+    return rounds
