@@ -350,6 +350,33 @@ HPS_API int hps_refine_check_3d(int n_nodes, int p, const double* f_values, cons
                                 const double* bounds, double* diff_max, double* ref_max, double* l2_err,
                                 void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Learned refinement proposal: a 513 -> 64 -> 64 -> 1 MLP (ReLU) over 8^3
+ * uniform samples of f per octree node plus its depth.  No counterpart in
+ * the reference: it proposes refinements for the adaptive meshing above,
+ * whose plain criterion still judges every accepted leaf.  Parameters are
+ * one FP32 vector of hps_mlp_param_count() entries: W1 (64 x 513), b1, W2
+ * (64 x 64), b2, w3 (64), b3.
+ * ------------------------------------------------------------------------- */
+HPS_API int hps_mlp_param_count(void);
+/* pts (n, 512, 3): cell-centred 8x8x8 sample points of each node's bounds (n, 6). */
+HPS_API int hps_mlp_sample_points(int n, const double* bounds, double* pts, void* stream);
+/* X (n, 513) FP32 = [f_samples / scale, depth / 16]. */
+HPS_API int hps_mlp_features(int n, const double* f_samples, const int* depth, double scale, float* X, void* stream);
+/* logit (n); H1, H2 (n, 64) hidden activations (may be NULL for inference). */
+HPS_API int hps_mlp_forward(int n, const float* X, const float* params, float* H1, float* H2, float* logit,
+                            void* stream);
+/* Binary cross-entropy with logits (weight pos_weight on label 1): dlogit =
+ * d(mean loss)/dlogit; *loss_sum (may be NULL) += summed weighted loss. */
+HPS_API int hps_mlp_bce(int n, const float* logit, const float* labels, float pos_weight, float* dlogit,
+                        float* loss_sum, void* stream);
+/* grad += d(loss)/d(params) for the rows given dlogit (grad zeroed by the caller). */
+HPS_API int hps_mlp_backward(int n, const float* X, const float* params, const float* H1, const float* H2,
+                             const float* dlogit, float* grad, void* stream);
+/* One Adam step (step counts from 1). */
+HPS_API int hps_mlp_adam(float* params, const float* grad, float* m, float* v, float lr, float beta1, float beta2,
+                         float eps, int step, void* stream);
+
 /* r32 = f[:, n_cb:, :] rounded to FP32 (the residual at zero). */
 HPS_API int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32,
                              void* stream);

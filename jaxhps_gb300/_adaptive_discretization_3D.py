@@ -246,4 +246,4 @@ def generate_adaptive_mesh_level_restriction(root: DiscretizationNode3D, f_fn: C
         queue = new_queue
     if stats is not None:
         stats.update(rounds=n_rounds, checked=n_checked, proposed=n_proposed, seconds=time.perf_counter() - t0,
-                     leaves=len(get_all_leaves(root)))
+                     leaves=len(get_all_leaves(root)), global_norm=global_nrm, tol=tol)

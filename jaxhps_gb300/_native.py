@@ -148,6 +148,20 @@ def _declare(lib):
     lib.hps_refine_points_3d.restype = ci
     lib.hps_refine_check_3d.argtypes = [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.hps_refine_check_3d.restype = ci
+    lib.hps_mlp_param_count.argtypes = []
+    lib.hps_mlp_param_count.restype = ci
+    lib.hps_mlp_sample_points.argtypes = [ci, vp, vp, vp]
+    lib.hps_mlp_sample_points.restype = ci
+    lib.hps_mlp_features.argtypes = [ci, vp, vp, C.c_double, vp, vp]
+    lib.hps_mlp_features.restype = ci
+    lib.hps_mlp_forward.argtypes = [ci, vp, vp, vp, vp, vp, vp]
+    lib.hps_mlp_forward.restype = ci
+    lib.hps_mlp_bce.argtypes = [ci, vp, vp, C.c_float, vp, vp, vp]
+    lib.hps_mlp_bce.restype = ci
+    lib.hps_mlp_backward.argtypes = [ci, vp, vp, vp, vp, vp, vp, vp]
+    lib.hps_mlp_backward.restype = ci
+    lib.hps_mlp_adam.argtypes = [vp, vp, vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, ci, vp]
+    lib.hps_mlp_adam.restype = ci
 
 
 EXPORTED_SYMBOLS = (
@@ -156,7 +170,8 @@ EXPORTED_SYMBOLS = (
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
     "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
-    "hps_refine_points_3d", "hps_refine_check_3d",
+    "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
+    "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam",
 )
 
 

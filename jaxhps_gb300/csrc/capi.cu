@@ -26,6 +26,16 @@ cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds,
                      long long sd, cudaStream_t st);
 cudaError_t refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
                              double* pts, cudaStream_t st);
+int mlp_param_count();
+cudaError_t mlp_sample_points(int n, const double* bounds, double* pts, cudaStream_t st);
+cudaError_t mlp_features(int n, const double* fvals, const int* depth, double inv_scale, float* X, cudaStream_t st);
+cudaError_t mlp_forward(int n, const float* X, const float* P, float* H1, float* H2, float* logit, cudaStream_t st);
+cudaError_t mlp_bce(int n, const float* logit, const float* y, float wpos, float* dlogit, float* loss,
+                    cudaStream_t st);
+cudaError_t mlp_backward(int n, const float* X, const float* P, const float* H1, const float* H2,
+                         const float* dlogit, float* G, cudaStream_t st);
+cudaError_t mlp_adam(float* P, const float* G, float* M, float* V, float lr, float b1, float b2, float eps, int step,
+                     cudaStream_t st);
 cudaError_t refine_check_3d(int n_nodes, int p, const double* fv, const int* perm, const int* iperm,
                             const double* Ilo, const double* Ihi, const double* wref, const double* bounds,
                             double* diff, double* ref, double* l2, cudaStream_t st);
@@ -616,6 +626,65 @@ int hps_refine_check_3d(int n_nodes, int p, const double* f_values, const int* p
   if (n_nodes == 0) return HPS_OK;
   HPS_CHECK(refine_check_3d(n_nodes, p, f_values, perm, iperm, interp_lo, interp_hi, cc_weights, bounds, diff_max,
                             ref_max, l2_err, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_mlp_param_count(void) { return mlp_param_count(); }
+
+int hps_mlp_sample_points(int n, const double* bounds, double* pts, void* stream) {
+  if (n < 0 || (n > 0 && (!bounds || !pts))) {
+    set_error("hps_mlp_sample_points: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(mlp_sample_points(n, bounds, pts, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_mlp_features(int n, const double* f_samples, const int* depth, double scale, float* X, void* stream) {
+  if (n < 0 || !(scale != 0.0) || (n > 0 && (!f_samples || !depth || !X))) {
+    set_error("hps_mlp_features: invalid arguments (scale must be non-zero)");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(mlp_features(n, f_samples, depth, 1.0 / scale, X, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_mlp_forward(int n, const float* X, const float* params, float* H1, float* H2, float* logit, void* stream) {
+  if (n < 0 || (n > 0 && (!X || !params || !logit))) {
+    set_error("hps_mlp_forward: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(mlp_forward(n, X, params, H1, H2, logit, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_mlp_bce(int n, const float* logit, const float* labels, float pos_weight, float* dlogit, float* loss_sum,
+                void* stream) {
+  if (n < 0 || (n > 0 && (!logit || !labels || !dlogit))) {
+    set_error("hps_mlp_bce: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(mlp_bce(n, logit, labels, pos_weight, dlogit, loss_sum, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_mlp_backward(int n, const float* X, const float* params, const float* H1, const float* H2,
+                     const float* dlogit, float* grad, void* stream) {
+  if (n < 0 || (n > 0 && (!X || !params || !H1 || !H2 || !dlogit || !grad))) {
+    set_error("hps_mlp_backward: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(mlp_backward(n, X, params, H1, H2, dlogit, grad, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_mlp_adam(float* params, const float* grad, float* m, float* v, float lr, float beta1, float beta2, float eps,
+                 int step, void* stream) {
+  if (!params || !grad || !m || !v || step < 1) {
+    set_error("hps_mlp_adam: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(mlp_adam(params, grad, m, v, lr, beta1, beta2, eps, step, (cudaStream_t)stream));
   return HPS_OK;
 }
 

@@ -1076,3 +1076,58 @@ def oracle_adaptive_mesh_3D(root: OctNode, f, tol: float, p: int, q: int, restri
                             new_queue += n.children
         queue = new_queue
     return rounds
+
+
+# ---------------------------------------------------------------------------
+# Refinement-proposal MLP (no reference counterpart): 513 -> 64 -> 64 -> 1,
+# ReLU, weighted binary cross-entropy with logits, Adam.
+# ---------------------------------------------------------------------------
+
+
+def mlp_unpack(params: np.ndarray):
+    p = np.asarray(params, dtype=np.float64)
+    o = 0
+    out = []
+    for shape in ((64, 513), (64,), (64, 64), (64,), (64,), (1,)):
+        n = int(np.prod(shape))
+        out.append(p[o:o + n].reshape(shape))
+        o += n
+    return out
+
+
+def mlp_forward(params, X):
+    W1, b1, W2, b2, w3, b3 = mlp_unpack(params)
+    H1 = np.maximum(X @ W1.T + b1, 0.0)
+    H2 = np.maximum(H1 @ W2.T + b2, 0.0)
+    return H2 @ w3 + b3[0], H1, H2
+
+
+def mlp_loss(params, X, y, pos_weight=1.0):
+    z, _, _ = mlp_forward(params, X)
+    w = np.where(y > 0.5, pos_weight, 1.0)
+    return float(np.mean(w * (np.maximum(z, 0) - z * y + np.log1p(np.exp(-np.abs(z))))))
+
+
+def mlp_grad(params, X, y, pos_weight=1.0):
+    """Gradient of mlp_loss by back-propagation, packed like the parameters."""
+    W1, b1, W2, b2, w3, b3 = mlp_unpack(params)
+    z, H1, H2 = mlp_forward(params, X)
+    n = X.shape[0]
+    w = np.where(y > 0.5, pos_weight, 1.0)
+    dz = w * (1.0 / (1.0 + np.exp(-z)) - y) / n
+    gw3 = H2.T @ dz
+    gb3 = np.array([dz.sum()])
+    d2 = np.outer(dz, w3) * (H2 > 0)
+    gW2 = d2.T @ H1
+    gb2 = d2.sum(0)
+    d1 = (d2 @ W2) * (H1 > 0)
+    gW1 = d1.T @ X
+    gb1 = d1.sum(0)
+    return np.concatenate([gW1.ravel(), gb1, gW2.ravel(), gb2, gw3, gb3])
+
+
+def adam_step(params, grad, m, v, step, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+    m = b1 * m + (1 - b1) * grad
+    v = b2 * v + (1 - b2) * grad ** 2
+    p = params - lr * (m / (1 - b1 ** step)) / (np.sqrt(v / (1 - b2 ** step)) + eps)
+    return p, m, v

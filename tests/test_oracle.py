@@ -173,3 +173,17 @@ def test_oct_merge_known_answer_variable_coefficients():
     bp = pr.boundary_points
     ub = pr.solve(bp[:, 0] * bp[:, 1] + bp[:, 2] ** 2 - bp[:, 1] ** 3)
     assert np.abs(ub - u).max() < 1e-11
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    n_par = 64 * 513 + 64 + 64 * 64 + 64 + 64 + 1
+    params = rng.standard_normal(n_par) * 0.05
+    X = rng.standard_normal((7, 513))
+    y = (rng.random(7) > 0.5).astype(float)
+    g = O.mlp_grad(params, X, y, pos_weight=2.5)
+    for k in list(rng.choice(n_par, 40, replace=False)) + [n_par - 1, n_par - 2]:
+        e = np.zeros(n_par)
+        e[k] = 1e-6
+        fd = (O.mlp_loss(params + e, X, y, 2.5) - O.mlp_loss(params - e, X, y, 2.5)) / 2e-6
+        assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(g[k])) + 1e-8, k
