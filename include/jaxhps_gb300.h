@@ -326,6 +326,30 @@ HPS_API int hps_assemble_rows(int n_leaves, int n_pts, int row0, int n_rows, int
                               const double* coeffs, double* out, long long ld, long long stride, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Adaptive merges (merge/_adaptive_3D_DtN.py:30-565,
+ * merge/_utils_adaptive_3D_DtN.py:647-743, down_pass/_adaptive_3D_DtN.py).
+ * ------------------------------------------------------------------------- */
+
+/* Index-map code of a padding slot: a child with fewer boundary points than
+ * the merge's common child size leaves its tail slots unused. */
+#define HPS_CODE_PAD (-2147483647 - 1)
+
+/* Panel map along one axis of a batch of matrices.  mode 0 (rows):
+ * out[b][i][c] for i < n_out, c < n_other; mode 1 (columns): out[b][r][j] for
+ * r < n_other, j < n_out.  table (n_out x 4 int, 16-byte aligned) gives per
+ * output index {kind, in_start, local, n_k}: kind 0 copies input index
+ * in_start + local; kind 1 combines input indices in_start .. in_start+n_k-1
+ * with row `local` of M (mode 0: M is m_len x n_k) or column `local` of M
+ * (mode 1: M is n_k x m_len).  Compresses four fine interface panels into
+ * one (L_1f4 on rows, L_4f1 on columns) and expands them back (L_4f1). */
+HPS_API int hps_panel_map(int dtype, int mode, int batch, int n_out, int n_other, int m_len, const int* table,
+                          const void* M, const void* in, long long ld_in, long long stride_in, void* out,
+                          long long ld_out, long long stride_out, void* stream);
+
+/* x[b][:] *= scale[b] (scale FP64 on the device) for n_per elements per batch. */
+HPS_API int hps_scale_batched(int dtype, int batch, long long n_per, const double* scale, void* x, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Adaptive octree refinement check.  Replaces the per-node check of
  * generate_adaptive_mesh_level_restriction (_adaptive_discretization_3D.py
  * :34-210, :424-503): evaluate f on a node's grid and its eight children's

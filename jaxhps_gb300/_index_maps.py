@@ -19,6 +19,11 @@ import numpy as np
 import torch
 
 
+# Code of a padding slot (a child with fewer boundary points than the merge's
+# common child size); the C ABI's HPS_CODE_PAD.
+CODE_PAD = -(2 ** 31)
+
+
 @dataclass
 class MergeMaps:
     nch: int
@@ -53,6 +58,8 @@ def maps_from_code(code: np.ndarray, n_ext: int, n_int: int) -> MergeMaps:
     for c in range(nch):
         for k in range(nb):
             cd = code[c, k]
+            if cd == CODE_PAD:
+                continue
             if cd >= 0:
                 assert ext_c[cd] < 0, "exterior point mapped twice"
                 ext_c[cd], ext_l[cd] = c, k

@@ -19,6 +19,7 @@ _lock = threading.Lock()
 _lib = None
 
 HPS_F64, HPS_F32, HPS_C128, HPS_C64 = 0, 1, 2, 3
+HPS_CODE_PAD = -(2 ** 31)
 
 TORCH_TO_HPS = {
     torch.float64: HPS_F64,
@@ -148,6 +149,10 @@ def _declare(lib):
     lib.hps_refine_points_3d.restype = ci
     lib.hps_refine_check_3d.argtypes = [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.hps_refine_check_3d.restype = ci
+    lib.hps_panel_map.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp, cll, cll, vp]
+    lib.hps_panel_map.restype = ci
+    lib.hps_scale_batched.argtypes = [ci, ci, cll, vp, vp, vp]
+    lib.hps_scale_batched.restype = ci
     lib.hps_mlp_param_count.argtypes = []
     lib.hps_mlp_param_count.restype = ci
     lib.hps_mlp_sample_points.argtypes = [ci, vp, vp, vp]
@@ -171,7 +176,8 @@ EXPORTED_SYMBOLS = (
     "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
-    "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam",
+    "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
+    "hps_scale_batched",
 )
 
 

@@ -84,7 +84,10 @@ def local_solve_stage_uniform_2D_DtN(pde_problem, host_device=None, device=None,
     return _local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, device, dtype, keep_inverse)
 
 
-def _local_solve_dtn(pde_problem, P_np, Q_np, device, dtype, keep_inverse, source=None, want_source=True):
+def _local_solve_dtn(pde_problem, P_np, Q_np, device, dtype, keep_inverse, source=None, want_source=True,
+                     coefficients=None):
+    """``coefficients`` = (ops, coeffs, is_complex) overrides the problem's own
+    (adaptive leaves pass per-leaf rescaled coefficients)."""
     L = nat.lib()
     dev = _device(device)
     dom = pde_problem.domain
@@ -92,7 +95,7 @@ def _local_solve_dtn(pde_problem, P_np, Q_np, device, dtype, keep_inverse, sourc
     n_pts = dom.interior_points.shape[1]
     n_cb = P_np.shape[0]
     ng = P_np.shape[1]
-    ops_t, coeffs, cplx = _coefficients(pde_problem, dev)
+    ops_t, coeffs, cplx = _coefficients(pde_problem, dev) if coefficients is None else coefficients
     if cplx or _is_complex(pde_problem.source if source is None else source):
         dtype = REAL_TO_COMPLEX.get(dtype, dtype)
     P = _as_tensor(P_np, dtype, dev)

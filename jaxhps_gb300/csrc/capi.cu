@@ -26,6 +26,11 @@ cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds,
                      long long sd, cudaStream_t st);
 cudaError_t refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
                              double* pts, cudaStream_t st);
+template <class T>
+cudaError_t panel_map(int mode, int batch, int n_out, int n_other, int m_len, const int* tab, const T* M, const T* in,
+                      long long ld_in, long long s_in, T* out, long long ld_out, long long s_out, cudaStream_t st);
+template <class T>
+cudaError_t scale_batched(int batch, long long n_per, const double* scale, T* x, cudaStream_t st);
 int mlp_param_count();
 cudaError_t mlp_sample_points(int n, const double* bounds, double* pts, cudaStream_t st);
 cudaError_t mlp_features(int n, const double* fvals, const int* depth, double inv_scale, float* X, cudaStream_t st);
@@ -357,6 +362,21 @@ static int up_impl(const hps_up_args* a, cudaStream_t st) {
   return HPS_OK;
 }
 
+template <class T>
+static int panel_map_entry(int mode, int batch, int n_out, int n_other, int m_len, const int* tab, const void* M,
+                           const void* in, long long ld_in, long long s_in, void* out, long long ld_out,
+                           long long s_out, void* stream) {
+  HPS_CHECK(panel_map<T>(mode, batch, n_out, n_other, m_len, tab, (const T*)M, (const T*)in, ld_in, s_in, (T*)out,
+                         ld_out, s_out, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+template <class T>
+static int scale_entry(int batch, long long n_per, const double* scale, void* x, void* stream) {
+  HPS_CHECK(scale_batched<T>(batch, n_per, scale, (T*)x, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
 }  // namespace hps
 
 using namespace hps;
@@ -627,6 +647,34 @@ int hps_refine_check_3d(int n_nodes, int p, const double* f_values, const int* p
   HPS_CHECK(refine_check_3d(n_nodes, p, f_values, perm, iperm, interp_lo, interp_hi, cc_weights, bounds, diff_max,
                             ref_max, l2_err, (cudaStream_t)stream));
   return HPS_OK;
+}
+
+int hps_panel_map(int dtype, int mode, int batch, int n_out, int n_other, int m_len, const int* table,
+                  const void* M, const void* in, long long ld_in, long long stride_in, void* out, long long ld_out,
+                  long long stride_out, void* stream) {
+  if ((mode != 0 && mode != 1) || batch < 0 || n_out < 0 || n_other < 0 || (batch > 0 && (!table || !in || !out))) {
+    set_error("hps_panel_map: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  switch (dtype) {
+    case HPS_F64: return panel_map_entry<double>(mode, batch, n_out, n_other, m_len, table, M, in, ld_in, stride_in,
+                                                 out, ld_out, stride_out, stream);
+    case HPS_F32: return panel_map_entry<float>(mode, batch, n_out, n_other, m_len, table, M, in, ld_in, stride_in,
+                                                out, ld_out, stride_out, stream);
+    case HPS_C128: return panel_map_entry<c128>(mode, batch, n_out, n_other, m_len, table, M, in, ld_in, stride_in,
+                                                out, ld_out, stride_out, stream);
+    case HPS_C64: return panel_map_entry<c64>(mode, batch, n_out, n_other, m_len, table, M, in, ld_in, stride_in,
+                                              out, ld_out, stride_out, stream);
+    default: set_error("hps_panel_map: unknown dtype %d", dtype); return HPS_ERR_ARG;
+  }
+}
+
+int hps_scale_batched(int dtype, int batch, long long n_per, const double* scale, void* x, void* stream) {
+  if (batch < 0 || n_per < 0 || (batch > 0 && (!scale || !x))) {
+    set_error("hps_scale_batched: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  DISPATCH(dtype, scale_entry, batch, n_per, scale, x, stream)
 }
 
 int hps_mlp_param_count(void) { return mlp_param_count(); }

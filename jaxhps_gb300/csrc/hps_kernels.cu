@@ -5,6 +5,7 @@
 // kernel serves 2D quad merges and 3D oct merges alike.
 #include "hps_common.cuh"
 #include "hps_internal.h"
+#include "../../include/jaxhps_gb300.h"
 
 namespace hps {
 
@@ -337,7 +338,9 @@ __global__ void down_scatter_kernel(int nch, int nb, int n_ext, int n_int, int n
     const int s = (int)(e % ns);
     const int ck = (int)(e / ns);  // c*nb + k
     const int cd = code[ck];
-    const T v = (cd >= 0) ? gpar[(m * n_ext + cd) * ns + s] : gint[(m * n_int + (-cd - 1)) * ns + s];
+    // HPS_CODE_PAD marks padding slots of a child with fewer boundary points
+    const T v = (cd == HPS_CODE_PAD) ? zero<T>()
+                : (cd >= 0) ? gpar[(m * n_ext + cd) * ns + s] : gint[(m * n_int + (-cd - 1)) * ns + s];
     gch[m * cnt + e] = v;
   }
 }

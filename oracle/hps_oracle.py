@@ -1131,3 +1131,245 @@ def adam_step(params, grad, m, v, step, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
     v = b2 * v + (1 - b2) * grad ** 2
     p = params - lr * (m / (1 - b1 ** step)) / (np.sqrt(v / (1 - b2 ** step)) + eps)
     return p, m, v
+
+
+# ---------------------------------------------------------------------------
+# Adaptive 3D DtN build/solve  (local_solve/_adaptive_3D_DtN.py:13-175,
+#   merge/_adaptive_3D_DtN.py:30-565, merge/_utils_adaptive_3D_DtN.py:11-881,
+#   down_pass/_adaptive_3D_DtN.py:15-394) on OctNode trees whose face counts
+#   ``n`` were kept by oracle_add_eight_children.
+# ---------------------------------------------------------------------------
+
+_FACE_ORDERS = ((4, 7, 3, 0, 5, 6, 2, 1), (4, 5, 1, 0, 7, 6, 2, 3), (0, 1, 2, 3, 4, 5, 6, 7))
+
+
+def oracle_face_leaves(node: OctNode):
+    """get_ordered_lst_of_boundary_nodes (_grid_creation_3D.py:375-417)."""
+    def walk(n, order):
+        if not n.children:
+            return [n]
+        out = []
+        for i in order:
+            out += walk(n.children[i], order)
+        return out
+    return [[lf for lf in walk(node, _FACE_ORDERS[f // 2]) if lf.b[f] == node.b[f]] for f in range(6)]
+
+
+def oracle_projection_lst(l0, l1):
+    """merge/_utils_adaptive_3D_DtN.py:11-57."""
+    o0, o1 = [], []
+    i0 = i1 = 0
+    while i0 < len(l0) and i1 < len(l1):
+        s0, s1 = l0[i0].b[1] - l0[i0].b[0], l1[i1].b[1] - l1[i1].b[0]
+        if s0 == s1:
+            o0.append(False), o1.append(False)
+            i0 += 1
+            i1 += 1
+        elif s0 < s1:
+            o0 += [True] * 4
+            o1.append(False)
+            i0 += 4
+            i1 += 1
+        else:
+            o1 += [True] * 4
+            o0.append(False)
+            i1 += 4
+            i0 += 1
+    return o0, o1
+
+
+def _compress_rows(T, L, flags):
+    """_compress_rows_from_lst (:676-711): groups of 4 panels -> L @ rows."""
+    npp = L.shape[0]
+    out, i = [], 0
+    while i < len(flags):
+        if flags[i]:
+            out.append(L @ T[i * npp:(i + 4) * npp])
+            i += 4
+        else:
+            out.append(T[i * npp:(i + 1) * npp])
+            i += 1
+    return np.concatenate(out, axis=0)
+
+
+def _compress_cols(T, L, flags):
+    """_compress_cols_from_lst (:647-674): groups of 4 panels -> cols @ L."""
+    npp = L.shape[1]
+    out, i = [], 0
+    while i < len(flags):
+        if flags[i]:
+            out.append(T[:, i * npp:(i + 4) * npp] @ L)
+            i += 4
+        else:
+            out.append(T[:, i * npp:(i + 1) * npp])
+            i += 1
+    return np.concatenate(out, axis=1)
+
+
+def _deproject(g, L, flags, npp):
+    """Inverse direction of one interface side (_deproject_merge_interface_3D)."""
+    out, i, k = [], 0, 0
+    while i < len(flags):
+        seg = g[k:k + npp]
+        if flags[i]:
+            out.append(L @ seg)
+            i += 4
+        else:
+            out.append(seg)
+            i += 1
+        k += npp
+    return np.concatenate(out, axis=0), k
+
+
+def _label_pairs():
+    """label -> ((child, face), (child, face)) from the _OCT_CHILD table."""
+    pairs = {}
+    for c, (_, ints) in enumerate(_OCT_CHILD):
+        for lab, f in ints:
+            pairs.setdefault(lab, []).append((c, f))
+    return pairs
+
+
+def oracle_adaptive_oct_merge(node: OctNode, L_4f1, L_1f4):
+    kids = node.children
+    fl = [oracle_face_leaves(k) for k in kids]
+    pairs = _label_pairs()
+    flags = {}
+    for lab in range(9, 21):
+        (c0, f0), (c1, f1) = pairs[lab]
+        a, b = oracle_projection_lst(fl[c0][f0], fl[c1][f1])
+        flags[(c0, lab)], flags[(c1, lab)] = a, b
+    ns = kids[0].h.shape[1]
+    subs = []
+    for c, (ext_faces, ints) in enumerate(_OCT_CHILD):
+        n = kids[c].n
+        off = np.concatenate([[0], np.cumsum(n)])
+        sets = [np.concatenate([np.arange(off[f], off[f + 1]) for f in ext_faces])] + \
+               [np.arange(off[f], off[f + 1]) for _, f in ints]
+        labs = [None] + [lab for lab, _ in ints]
+        blk = {}
+        for i, (ri, rl) in enumerate(zip(sets, labs)):
+            for j, (ci, cl) in enumerate(zip(sets, labs)):
+                M = kids[c].T[np.ix_(ri, ci)]
+                if rl is not None and any(flags[(c, rl)]):
+                    M = _compress_rows(M, L_1f4, flags[(c, rl)])
+                if cl is not None and any(flags[(c, cl)]):
+                    M = _compress_cols(M, L_4f1, flags[(c, cl)])
+                blk[(rl, cl)] = M
+            v = kids[c].h[ri]
+            if rl is not None and any(flags[(c, rl)]):
+                v = _compress_rows(v, L_1f4, flags[(c, rl)])
+            blk[("h", rl)] = v
+        subs.append(blk)
+    msz = {lab: subs[pairs[lab][0][0]][(lab, lab)].shape[0] for lab in range(9, 21)}
+    ioff = dict(zip(range(9, 21), np.concatenate([[0], np.cumsum([msz[l] for l in range(9, 21)])])))
+    esz = [subs[c][(None, None)].shape[0] for c in range(8)]
+    eoff = np.concatenate([[0], np.cumsum(esz)])
+    n_ext, n_int = int(eoff[-1]), int(sum(msz.values()))
+    B = np.zeros((n_ext, n_int))
+    Cm = np.zeros((n_int, n_ext))
+    D = np.zeros((n_int, n_int))
+    dh = np.zeros((n_int, ns))
+    hx = np.zeros((n_ext, ns))
+    A = np.zeros((n_ext, n_ext))
+    for c, (_, ints) in enumerate(_OCT_CHILD):
+        es = slice(eoff[c], eoff[c + 1])
+        A[es, es] = subs[c][(None, None)]
+        hx[es] = subs[c][("h", None)]
+        for lab, _ in ints:
+            ls = slice(ioff[lab], ioff[lab] + msz[lab])
+            B[es, ls] = subs[c][(None, lab)]
+            Cm[ls, es] = subs[c][(lab, None)]
+            dh[ls] += subs[c][("h", lab)]
+            for lab2, _ in ints:
+                D[ls, slice(ioff[lab2], ioff[lab2] + msz[lab2])] += subs[c][(lab, lab2)]
+    Dinv = np.linalg.inv(D)
+    S = -Dinv @ Cm
+    T = A + B @ S
+    gt = -Dinv @ dh
+    h_out = hx + B @ gt
+    # re-order the regions [x-face, y-face, z-face] of a..h into faces 0..5 (:745-881)
+    r = []
+    for F, order in enumerate(_OCT_FACE_CHILDREN):
+        for c in order:
+            faces = _OCT_CHILD[c][0]
+            k = faces.index(F)
+            start = eoff[c] + sum(kids[c].n[f] for f in faces[:k])
+            r.append(np.arange(start, start + kids[c].n[F]))
+    r = np.concatenate(r)
+    return S[:, r], T[np.ix_(r, r)], h_out[r], gt, flags, msz
+
+
+def oracle_adaptive_build_3D(root: OctNode, p: int, q: int, coeffs: dict, source):
+    """Leaf stage with per-leaf rescaled operators and Q / h, then merges
+    from the deepest level up (merge_stage_adaptive_3D_DtN, :30-149)."""
+    leaves = root.leaves()
+    dx, dy, dz, dxx, dyy, dzz, dxy, dxz, dyz = diff_operators_3D(p, 1.0)
+    ops = {"D_xx": dxx, "D_xy": dxy, "D_yy": dyy, "D_xz": dxz, "D_yz": dyz, "D_zz": dzz, "D_x": dx, "D_y": dy,
+           "D_z": dz, "I": np.eye(p ** 3)}
+    order = {"D_xx": 2, "D_xy": 2, "D_yy": 2, "D_xz": 2, "D_yz": 2, "D_zz": 2, "D_x": 1, "D_y": 1, "D_z": 1, "I": 0}
+    P = P_3D_DtN(p, q)
+    Q = Q_3D_DtN(p, q, dx, dy, dz)
+    src = np.asarray(source)
+    src = src if src.ndim == 3 else src[..., None]
+    for i, lf in enumerate(leaves):
+        h = (lf.b[1] - lf.b[0]) / 2
+        A = sum(np.asarray(coeffs[k])[i][:, None] * ops[k] / h ** order[k] for k in coeffs if coeffs[k] is not None)
+        Y, T, v, hv = leaf_dtn(A[None], src[i:i + 1], P, Q / h)
+        lf.Y, lf.T, lf.v, lf.h = Y[0], T[0], v[0], hv[0]
+    g = q * q
+    gq = gauss_points(q)
+    lo, hi = affine_transform(gq, (-1.0, 0.0)), affine_transform(gq, (0.0, 1.0))
+    quarters = ((lo, lo), (hi, lo), (hi, hi), (lo, hi))
+    L_4f1 = np.concatenate([_bary2D(gq, gq, u, v) for u, v in quarters])
+    L_1f4 = np.zeros((g, 4 * g))
+    for k, (u, v) in enumerate(quarters):
+        rows = (((gq < 0) if u is lo else (gq >= 0))[:, None] & ((gq < 0) if v is lo else (gq >= 0))[None, :]).ravel()
+        L_1f4[rows, k * g:(k + 1) * g] = _bary2D(u, v, gq, gq)[rows]
+
+    def merge(node):
+        for ch in node.children:
+            if ch.children:
+                merge(ch)
+        node.S, node.T, node.h, node.gt, node.flags, node.msz = oracle_adaptive_oct_merge(node, L_4f1, L_1f4)
+
+    merge(root)
+    root.L_4f1 = L_4f1
+    return root
+
+
+def oracle_adaptive_solve_3D(root: OctNode, bdry):
+    """down_pass_adaptive_3D_DtN (:15-142, _propagate_down_oct :176-394)."""
+    L_4f1 = root.L_4f1
+    g_all = np.asarray(bdry)
+    root.g = g_all if g_all.ndim == 2 else g_all[:, None]
+    pairs = _label_pairs()
+
+    def down(node):
+        if not node.children:
+            return
+        kids = node.children
+        gi = node.S @ node.g + node.gt
+        foff = np.concatenate([[0], np.cumsum(node.n)])
+        faces = [node.g[foff[f]:foff[f + 1]] for f in range(6)]
+        ioff = np.concatenate([[0], np.cumsum([node.msz[l] for l in range(9, 21)])])
+        iface = {}
+        npp = L_4f1.shape[1]
+        for k, lab in enumerate(range(9, 21)):
+            seg = gi[ioff[k]:ioff[k + 1]]
+            for c, f in pairs[lab]:
+                iface[(c, f)] = _deproject(seg, L_4f1, node.flags[(c, lab)], npp)[0]
+        for c, ch in enumerate(kids):
+            parts = []
+            for f in range(6):
+                if (c, f) in iface:
+                    parts.append(iface[(c, f)])
+                else:
+                    order = _OCT_FACE_CHILDREN[f]
+                    start = sum(kids[o].n[f] for o in order[:order.index(c)])
+                    parts.append(faces[f][start:start + ch.n[f]])
+            ch.g = np.concatenate(parts)
+            down(ch)
+
+    down(root)
+    return np.stack([lf.Y @ lf.g + lf.v for lf in root.leaves()])

@@ -187,3 +187,46 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         e[k] = 1e-6
         fd = (O.mlp_loss(params + e, X, y, 2.5) - O.mlp_loss(params - e, X, y, 2.5)) / 2e-6
         assert abs(fd - g[k]) <= 1e-6 * max(1.0, abs(g[k])) + 1e-8, k
+
+
+def _adaptive_oracle_tree(q):
+    root = O.OctNode((0, 1, 0, 1, 0, 1))
+    O.oracle_add_eight_children(root, root, q)
+    for ch in root.children:
+        O.oracle_add_eight_children(ch, root, q)
+    O.oracle_add_eight_children(root.children[0].children[1], root, q)
+    O.oracle_add_eight_children(root.children[6].children[0], root, q)
+    return root
+
+
+def _oracle_root_boundary_points(root, q):
+    fl = O.oracle_face_leaves(root)
+    g = O.gauss_points(q)
+    tang = ((1, 2), (1, 2), (0, 2), (0, 2), (0, 1), (0, 1))
+    out = []
+    for f in range(6):
+        a, b = tang[f]
+        for lf in fl[f]:
+            U, V = np.meshgrid(O.affine_transform(g, lf.b[2 * a:2 * a + 2]), O.affine_transform(g, lf.b[2 * b:2 * b + 2]),
+                               indexing="ij")
+            P3 = np.empty((q * q, 3))
+            P3[:, f // 2] = root.b[f]
+            P3[:, a], P3[:, b] = U.ravel(), V.ravel()
+            out.append(P3)
+    return np.concatenate(out)
+
+
+def test_adaptive_oracle_polynomial_known_answer():
+    """A degree-3 solution is reproduced through compressed interfaces
+    (L_1f4 / L_4f1 are exact on degree < q polynomials)."""
+    p, q = 6, 4
+    root = _adaptive_oracle_tree(q)
+    leaves = root.leaves()
+    pts = O.leaf_points_3D(np.array([lf.b for lf in leaves]), p)
+    x, y, z = pts[..., 0], pts[..., 1], pts[..., 2]
+    ones = np.ones_like(x)
+    O.oracle_adaptive_build_3D(root, p, q, {"D_xx": ones, "D_yy": ones, "D_zz": ones, "D_x": y}, 2 * ones + y * (3 * x ** 2 - 3 * y ** 2))
+    bp = _oracle_root_boundary_points(root, q)
+    u = O.oracle_adaptive_solve_3D(root, bp[:, 0] ** 3 - 3 * bp[:, 0] * bp[:, 1] ** 2 + bp[:, 2] ** 2)
+    assert np.abs(u[..., 0] - (x ** 3 - 3 * x * y ** 2 + z ** 2)).max() < 1e-11
+    assert any(any(v) for v in root.flags.values())     # the tree exercises compression
