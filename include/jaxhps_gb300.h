@@ -257,10 +257,15 @@ HPS_API int hps_down_level(const hps_down_args* a, void* stream);
 /* ---------------------------------------------------------------------------
  * One up-pass level for new leaf data without rebuilding (the reference's
  * up_pass_uniform_2D_DtN / _ItI, up_pass/_uniform_2D_DtN.py:8-173):
- *   dh = h_a + h_b on every interface,  g~ = -D_inv dh,
- *   h_out = h_ext + B g~.
- * Uses the D_inv and B kept from the merge stage.
+ *   dh = h_a + h_b on every interface (ItI: the partner side's h),
+ *   g~ = -D_inv dh,
+ *   h_out = h_ext + B g~            (B the merge's B), or
+ *   h_out = h_ext - B dh            (flags & HPS_UP_B_IS_BD_INV: B holds B D_inv,
+ *                                    as stored by the no-source build).
+ * Uses the D_inv and B (or B D_inv) kept from the merge stage.
  * ------------------------------------------------------------------------- */
+#define HPS_UP_B_IS_BD_INV 1
+#define HPS_UP_ITI 2
 typedef struct {
   int dtype;
   int n_merges, nch, nb, n_int, n_ext, nsrc;
@@ -271,6 +276,7 @@ typedef struct {
   void* dh;               /* scratch (n_merges, n_int, nsrc) */
   void* g_tilde;          /* out (n_merges, n_int, nsrc) */
   void* h_out;            /* out (n_merges, n_ext, nsrc) */
+  int flags;              /* HPS_UP_B_IS_BD_INV | HPS_UP_ITI */
 } hps_up_args;
 
 HPS_API int hps_up_level(const hps_up_args* a, void* stream);

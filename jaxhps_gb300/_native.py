@@ -20,6 +20,7 @@ _lib = None
 
 HPS_F64, HPS_F32, HPS_C128, HPS_C64 = 0, 1, 2, 3
 HPS_CODE_PAD = -(2 ** 31)
+HPS_UP_B_IS_BD_INV, HPS_UP_ITI = 1, 2
 
 TORCH_TO_HPS = {
     torch.float64: HPS_F64,
@@ -74,7 +75,7 @@ class UpArgs(C.Structure):
     _fields_ = [
         ("dtype", ci), ("n_merges", ci), ("nch", ci), ("nb", ci), ("n_int", ci), ("n_ext", ci), ("nsrc", ci),
         ("h_children", vp), ("int_c", vp), ("int_l", vp), ("ext_c", vp), ("ext_l", vp),
-        ("D_inv", vp), ("B", vp), ("dh", vp), ("g_tilde", vp), ("h_out", vp),
+        ("D_inv", vp), ("B", vp), ("dh", vp), ("g_tilde", vp), ("h_out", vp), ("flags", ci),
     ]
 
 

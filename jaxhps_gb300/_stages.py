@@ -241,9 +241,10 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
     return S, g_t, T_out, h_out, D_inv, BD_inv
 
 
-def up_level(h_children, D_inv, B, maps):
-    """One up-pass level with stored D_inv and B (reference up_pass/_uniform_2D_DtN.py:8-173):
-    returns (g_tilde, h_out)."""
+def up_level(h_children, D_inv, B, maps, b_is_bd_inv: bool = False, iti: bool = False):
+    """One up-pass level with stored D_inv and B, or B D_inv with
+    ``b_is_bd_inv`` (reference up_pass/_uniform_2D_DtN.py:8-173,
+    up_pass/_uniform_2D_ItI.py:8-214): returns (g_tilde, h_out)."""
     L = nat.lib()
     n_m, n_int, _ = D_inv.shape
     n_ext = B.shape[1]
@@ -257,7 +258,8 @@ def up_level(h_children, D_inv, B, maps):
                    nsrc=ns, h_children=h_children.data_ptr(), int_c=md["int_c"].data_ptr(),
                    int_l=md["int_l"].data_ptr(), ext_c=md["ext_c"].data_ptr(), ext_l=md["ext_l"].data_ptr(),
                    D_inv=D_inv.data_ptr(), B=B.data_ptr(), dh=dh.data_ptr(), g_tilde=g_t.data_ptr(),
-                   h_out=h_out.data_ptr())
+                   h_out=h_out.data_ptr(),
+                   flags=(nat.HPS_UP_B_IS_BD_INV if b_is_bd_inv else 0) | (nat.HPS_UP_ITI if iti else 0))
     nat.check(L.hps_up_level(C.byref(a), nat.stream_ptr()), "hps_up_level")
     return g_t, h_out
 

@@ -350,15 +350,25 @@ template <class T>
 static int up_impl(const hps_up_args* a, cudaStream_t st) {
   const int nm = a->n_merges, ni = a->n_int, ne = a->n_ext, ns = a->nsrc;
   const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
-  HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, ns, nullptr, (const T*)a->h_children, a->int_c, a->int_l,
-                            a->ext_c, a->ext_l, nullptr, nullptr, nullptr, nullptr, nullptr, (T*)a->dh,
-                            (T*)a->h_out, st));
+  if (a->flags & HPS_UP_ITI)
+    HPS_CHECK(merge_gather_iti<T>(nm, a->nch, a->nb, ni, ne, ns, nullptr, (const T*)a->h_children, a->int_c,
+                                  a->int_l, a->ext_c, a->ext_l, nullptr, nullptr, nullptr, nullptr, (T*)a->dh,
+                                  (T*)a->h_out, st));
+  else
+    HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, ns, nullptr, (const T*)a->h_children, a->int_c, a->int_l,
+                              a->ext_c, a->ext_l, nullptr, nullptr, nullptr, nullptr, nullptr, (T*)a->dh,
+                              (T*)a->h_out, st));
   HPS_CHECK(gemm_batched<T>(ni, ns, ni, mone, (const T*)a->D_inv, ni, (long long)ni * ni, (const T*)a->dh, ns,
                             (long long)ni * ns, zero_, nullptr, 0, 0, (T*)a->g_tilde, ns, (long long)ni * ns, nm,
                             st));
-  HPS_CHECK(gemm_batched<T>(ne, ns, ni, one_, (const T*)a->B, ni, (long long)ne * ni, (const T*)a->g_tilde, ns,
-                            (long long)ni * ns, one_, (T*)a->h_out, ns, (long long)ne * ns, (T*)a->h_out, ns,
-                            (long long)ne * ns, nm, st));
+  if (a->flags & HPS_UP_B_IS_BD_INV)
+    HPS_CHECK(gemm_batched<T>(ne, ns, ni, mone, (const T*)a->B, ni, (long long)ne * ni, (const T*)a->dh, ns,
+                              (long long)ni * ns, one_, (T*)a->h_out, ns, (long long)ne * ns, (T*)a->h_out, ns,
+                              (long long)ne * ns, nm, st));
+  else
+    HPS_CHECK(gemm_batched<T>(ne, ns, ni, one_, (const T*)a->B, ni, (long long)ne * ni, (const T*)a->g_tilde, ns,
+                              (long long)ni * ns, one_, (T*)a->h_out, ns, (long long)ne * ns, (T*)a->h_out, ns,
+                              (long long)ne * ns, nm, st));
   return HPS_OK;
 }
 

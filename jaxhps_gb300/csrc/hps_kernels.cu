@@ -244,14 +244,14 @@ __global__ void merge_gather_iti_kernel(int nch, int nb, int n_int, int n_ext, i
   const long long m = blockIdx.y + m_base;
   const int seg = blockIdx.z;
   const long long nbb = (long long)nb * nb;
-  const T* Rm = Rc + m * nch * nbb;
+  const T* Rm = Rc ? Rc + m * nch * nbb : nullptr;
   const T* hm = hc ? hc + m * nch * (long long)nb * ns : nullptr;
   long long cnt;
   switch (seg) {
-    case 0: cnt = (long long)n_int * n_int; break;
-    case 1: cnt = (long long)n_int * n_ext; break;
-    case 2: cnt = (long long)n_ext * n_int; break;
-    case 3: cnt = Tout ? (long long)n_ext * n_ext : 0; break;
+    case 0: cnt = Rm ? (long long)n_int * n_int : 0; break;
+    case 1: cnt = Rm ? (long long)n_int * n_ext : 0; break;
+    case 2: cnt = Rm ? (long long)n_ext * n_int : 0; break;
+    case 3: cnt = (Rm && Tout) ? (long long)n_ext * n_ext : 0; break;
     case 4: cnt = hm ? (long long)n_int * ns : 0; break;
     default: cnt = hm ? (long long)n_ext * ns : 0; break;
   }
@@ -300,8 +300,8 @@ cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext
   if (gx > 512) gx = 512;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
-    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * ((double)n_int * n_int + 2.0 * n_int * n_ext +
-                                                       (Tout ? (double)n_ext * n_ext : 0.0) +
+    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * ((Rc ? (double)n_int * n_int + 2.0 * n_int * n_ext : 0.0) +
+                                                       ((Rc && Tout) ? (double)n_ext * n_ext : 0.0) +
                                                        (double)(n_int + n_ext) * ns));
     note_launch();
     merge_gather_iti_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Rc, hc, int_c, int_l, ext_c,
