@@ -2,7 +2,8 @@
 direct solver with the public API of meliao/jaxhps:
 
     Domain, DiscretizationNode2D, DiscretizationNode3D, get_all_leaves,
-    PDEProblem, build_solver, solve
+    PDEProblem, build_solver, solve, solve_subtree, upward_pass_subtree,
+    downward_pass_subtree
 
 The leaf solves, merges and down pass run as hand-written sm_103a CUDA
 kernels behind a C ABI (include/jaxhps_gb300.h); host code here only builds
@@ -21,6 +22,7 @@ from ._domain import Domain
 from ._pdeproblem import PDEProblem
 from ._build_solver import build_solver
 from ._solve import solve
+from ._subtree import downward_pass_subtree, solve_subtree, upward_pass_subtree
 
 
 def local_solve_chunksize_2D(p: int, dtype=None) -> int:
@@ -45,6 +47,9 @@ __all__ = [
     "PDEProblem",
     "build_solver",
     "solve",
+    "solve_subtree",
+    "upward_pass_subtree",
+    "downward_pass_subtree",
     "local_solve_chunksize_2D",
     "local_solve_chunksize_3D",
 ]
