@@ -26,6 +26,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 from pathlib import Path
@@ -93,7 +94,7 @@ CLOCK_Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active
 class ClockSampler:
     def __init__(self):
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"jaxhps_gb300_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:

@@ -384,7 +384,7 @@ HPS_API int hps_refine_check_3d(int n_nodes, int p, const double* f_values, cons
  * Learned refinement proposal: a 513 -> 64 -> 64 -> 1 MLP (ReLU) over 8^3
  * uniform samples of f per octree node plus its depth.  No counterpart in
  * the reference: it proposes refinements for the adaptive meshing above,
- * whose plain criterion still judges every accepted leaf.  Parameters are
+ * whose plain criterion still decides every accepted leaf.  Parameters are
  * one FP32 vector of hps_mlp_param_count() entries: W1 (64 x 513), b1, W2
  * (64 x 64), b2, w3 (64), b3.
  * ------------------------------------------------------------------------- */

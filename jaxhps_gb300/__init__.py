@@ -27,8 +27,8 @@ from ._subtree import downward_pass_subtree, solve_subtree, upward_pass_subtree
 
 def local_solve_chunksize_2D(p: int, dtype=None) -> int:
     """Leaf-stage chunk size.  The reference sizes chunks for an 80 GB GPU
-    (_device_config.py:37-62); all leaves of the BASELINE problems fit a
-    GB300's HBM at once, so the whole level is one chunk."""
+    (_device_config.py:37-62); on a GB300 the leaves of trees up to 4^10
+    (2D) / 8^6 (3D) leaves fit HBM at once, so the whole level is one chunk."""
     return 4 ** 10
 
 

@@ -2,9 +2,9 @@
 // (ReLU hidden layers, one logit out) that predicts, from 8^3 uniform
 // samples of f over an octree node plus the node's depth, whether the
 // adaptive meshing criterion will refine the node.  This component has no
-// counterpart in the reference; it proposes refinements that the plain
+// counterpart in the reference; it proposes refinements, and the plain
 // interpolation criterion (_adaptive_discretization_3D.py:475-503) still
-// judges.
+// decides every accepted leaf.
 //
 // Parameters are one FP32 vector: W1 (64 x 513, row = hidden unit), b1 (64),
 // W2 (64 x 64, row = output unit), b2 (64), w3 (64), b3 (1).

@@ -86,7 +86,7 @@ def _front(c, R, k):
     return f
 
 
-def _judge(root, f, tol, p, gn, cuda):
+def _all_leaves_pass(root, f, tol, p, gn, cuda):
     """Every leaf passes the plain L-infinity criterion at norm gn."""
     leaves = get_all_leaves(root)
     consts = ad._CheckConstants(p, cuda)
@@ -119,7 +119,7 @@ def test_trained_proposer_saves_checks(cuda):
     assert mlp["proposed"] > 0
     assert mlp["checked"] < plain["checked"]
     assert mlp["leaves"] <= 1.25 * plain["leaves"]
-    # the plain criterion, at the plain run's final global norm, judges every accepted leaf of both trees
+    # the plain criterion, at the plain run's final global norm, decides every accepted leaf of both trees
     gn = plain["global_norm"]
     for root, _ in runs.values():
-        assert _judge(root, target, tol, p, gn, cuda)
+        assert _all_leaves_pass(root, target, tol, p, gn, cuda)
