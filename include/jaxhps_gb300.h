@@ -60,6 +60,10 @@ HPS_API const char* hps_version(void);
 /* Number of CUDA kernels this library has enqueued since it was loaded. */
 HPS_API long long hps_launch_count(void);
 
+/* Non-zero if a tensor-core GEMM launch of this process ever hit its bounded
+ * wait (its output is then invalid).  Synchronises with the device. */
+HPS_API int hps_gemm_tc_status(void);
+
 /* Live profiler.  hps_profile_begin(mask) arms CUDA-event timing of every
  * later launch whose kernel class c has bit (1 << c) set in mask (classes:
  * 1 GEMM, 2 inverse, 3 gather/scatter/assembly, 4 refinement residual),

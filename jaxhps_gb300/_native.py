@@ -154,6 +154,8 @@ def _declare(lib):
     lib.hps_panel_map.restype = ci
     lib.hps_scale_batched.argtypes = [ci, ci, cll, vp, vp, vp]
     lib.hps_scale_batched.restype = ci
+    lib.hps_gemm_tc_status.argtypes = []
+    lib.hps_gemm_tc_status.restype = ci
     lib.hps_mlp_param_count.argtypes = []
     lib.hps_mlp_param_count.restype = ci
     lib.hps_mlp_sample_points.argtypes = [ci, vp, vp, vp]
@@ -178,7 +180,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched",
+    "hps_scale_batched", "hps_gemm_tc_status",
 )
 
 

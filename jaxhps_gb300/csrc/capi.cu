@@ -406,6 +406,8 @@ const char* hps_version(void) { return "jaxhps_gb300 0.1.0 (sm_103a)"; }
 
 long long hps_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+int hps_gemm_tc_status(void) { return gemm_tc_error(); }
+
 int hps_profile_begin(int class_mask) {
   g_prof.mask = (unsigned)class_mask;
   g_prof.used = 0;

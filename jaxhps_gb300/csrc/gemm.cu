@@ -8,6 +8,10 @@
 // u = Y g + v).  Register-tiled, double-buffered through shared memory,
 // templated over the element type so the same code serves f64 / f32 /
 // complex128 / complex64.
+#include <stdlib.h>
+
+#include <type_traits>
+
 #include "hps_common.cuh"
 #include "hps_internal.h"
 
@@ -143,11 +147,26 @@ static cudaError_t launch_gemm_cfg(int M, int N, int K, T alpha, const T* A, lon
   return cudaGetLastError();
 }
 
+// FP32 products on the tensor cores (gemm_tc.cu) unless HPS_GEMM_TC=0.
+static bool tc_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("HPS_GEMM_TC");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <class T>
 cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda, long long sA,
                          const T* B, long long ldb, long long sB, T beta, const T* C, long long ldc,
                          long long sC, T* D, long long ldd, long long sD, int batch, cudaStream_t st) {
   if (M <= 0 || N <= 0 || batch <= 0) return cudaSuccess;
+  if constexpr (std::is_same<T, float>::value) {
+    // measured: the tensor-core kernel wins once a tile has enough K-steps to
+    // amortise its pipeline prologue and epilogue
+    if (tc_enabled() && M >= 128 && N >= 32 && K >= 128)
+      return gemm_tf32x3(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+  }
   if (sizeof(T) == 4) {
     const long long tiles128 = (long long)((M + 127) / 128) * ((N + 127) / 128) * batch;
     if (M >= 96 && N >= 96 && tiles128 >= 120)

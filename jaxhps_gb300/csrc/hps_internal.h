@@ -24,6 +24,13 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
                             long long sX, int batch, int* info, void* ws, size_t ws_bytes,
                             cudaStream_t st);
 
+// FP32 GEMM on the tensor cores (TF32 split into hi + lo, three products);
+// gemm_tc_error() reports whether a CTA's bounded wait ever ran out.
+cudaError_t gemm_tf32x3(int M, int N, int K, float alpha, const float* A, long long lda, long long sA,
+                        const float* B, long long ldb, long long sB, float beta, const float* C, long long ldc,
+                        long long sC, float* D, long long ldd, long long sD, int batch, cudaStream_t st);
+int gemm_tc_error();
+
 // Largest n served by the register-resident single-CTA kernel.
 int inverse_small_nmax(int dtype);
 
