@@ -108,3 +108,24 @@ def test_inverse_large_single_matrix_multi_cta_panel(cuda, n, dt):
     Xe = np.linalg.inv(A.astype(np.complex128 if np.iscomplexobj(A) else np.float64))
     rel = np.abs(X - Xe).max() / np.abs(Xe).max()
     assert rel < tol * 20, rel
+
+
+@pytest.mark.parametrize("m,n,k,batch,odd", [(196, 64, 196, 3, False), (300, 200, 150, 2, False), (257, 33, 131, 2, True),
+                                             (1100, 300, 257, 1, False)])
+def test_gemm_tensor_core_path(cuda, m, n, k, batch, odd):
+    """FP32 shapes the dispatcher sends to the tcgen05 kernel (3xTF32): FP32-level
+    accuracy, ragged tiles, unaligned leading dimensions, C aliasing D."""
+    from jaxhps_gb300 import _native as nat
+
+    rng = np.random.default_rng(m + n + k)
+    pad = 1 if odd else 0
+    Ab = rng.standard_normal((batch, m, k + pad)).astype(np.float32)
+    B = rng.standard_normal((batch, k, n)).astype(np.float32)
+    Cm = rng.standard_normal((batch, m, n)).astype(np.float32)
+    tA = torch.as_tensor(Ab, device=cuda)[:, :, :k]          # lda = k + 1 when odd: unaligned rows
+    tB, tC = torch.as_tensor(B, device=cuda), torch.as_tensor(Cm, device=cuda)
+    nat.gemm(tA, tB, tC, alpha=0.75, beta=-1.25, Cmat=tC)    # in place
+    ref = 0.75 * (Ab[:, :, :k].astype(np.float64) @ B) - 1.25 * Cm
+    err = np.abs(tC.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err < 2e-6 * max(1.0, np.sqrt(k / 64)), err
+    assert nat.load_library().hps_gemm_tc_status() == 0
