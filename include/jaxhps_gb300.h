@@ -411,6 +411,20 @@ HPS_API int hps_mlp_backward(int n, const float* X, const float* params, const f
 HPS_API int hps_mlp_adam(float* params, const float* grad, float* m, float* v, float lr, float beta1, float beta2,
                          float eps, int step, void* stream);
 
+/* As hps_assemble_rows with complex128 coefficients and output. */
+HPS_API int hps_assemble_rows_complex(int n_leaves, int n_pts, int row0, int n_rows, int n_ops, const double* ops,
+                                      const void* coeffs, void* out, long long ld, long long stride, void* stream);
+
+/* ItI refinement interface terms (complex128 in, complex64 out; node = leaf*4q + k):
+ *   hcorr[node] = t_out[node] + t_in[nbr[node]]  (0 where nbr < 0),
+ *   r_bdry[b]   = t_given[b] - t_in[bdry_node[b]]  (t_given NULL: zero data).
+ * t_out = outgoing impedance QH u, t_in = incoming impedance state; hcorr is
+ * minus the residual of the partner's interface equation t_in(a) + t_out(b) = 0
+ * (the coupling of the ItI merges, merge/_uniform_2D_ItI.py:182-375). */
+HPS_API int hps_iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in,
+                            void* hcorr, int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry,
+                            void* stream);
+
 /* r32 = f[:, n_cb:, :] rounded to FP32 (the residual at zero). */
 HPS_API int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32,
                              void* stream);

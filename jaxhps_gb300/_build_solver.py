@@ -26,6 +26,9 @@ def build_solver(pde_problem, return_top_T: bool = False, compute_device=None, h
         raise ValueError(f"precision must be one of {sorted(_PREC)}")
     dom = pde_problem.domain
     if precision == "mixed":
+        if pde_problem.use_ItI:
+            from ._refinement_iti import build_mixed_iti
+            return build_mixed_iti(pde_problem, return_top_T=return_top_T, device=compute_device, **refine_kw)
         if dom.bool_uniform and not dom.bool_2D and not pde_problem.use_ItI:
             from ._refinement_dense import build_mixed_dense
             return build_mixed_dense(pde_problem, return_top_T=return_top_T, device=compute_device, **refine_kw)

@@ -154,6 +154,10 @@ def _declare(lib):
     lib.hps_panel_map.restype = ci
     lib.hps_scale_batched.argtypes = [ci, ci, cll, vp, vp, vp]
     lib.hps_scale_batched.restype = ci
+    lib.hps_iti_combine.argtypes = [cll, ci, vp, vp, vp, vp, ci, vp, vp, vp, vp]
+    lib.hps_iti_combine.restype = ci
+    lib.hps_assemble_rows_complex.argtypes = [ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp]
+    lib.hps_assemble_rows_complex.restype = ci
     lib.hps_gemm_tc_status.argtypes = []
     lib.hps_gemm_tc_status.restype = ci
     lib.hps_mlp_param_count.argtypes = []
@@ -180,7 +184,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_assemble_rows_complex",
 )
 
 

@@ -1,0 +1,192 @@
+"""Mixed-precision ItI (Helmholtz-type) build and refined solve, uniform 2D.
+
+Build (complex64): the leaf inverses inv(B), B = [G; A_int] (the reference's
+get_ItI, local_solve/_uniform_2D_ItI.py:120-186), the leaf maps Y, and per
+merge level S, D^-1 and B D^-1 (merge/_uniform_2D_ItI.py with the no-source
+bookkeeping of merge/_nosource_uniform_2D_ItI.py) — a complex64 HPS solver
+used as the approximate inverse M.  Each leaf's interior rows A_int are
+assembled once in complex128 for the residuals.
+
+Solve: unknowns u (every leaf point) and t (incoming impedance at every leaf
+Gauss node), complex128, from zero.  The discrete system J is
+    leaf rows       B u = [P t ; f_int]
+    interface rows  t(a) + t_out(b) = 0  at paired nodes a, b  (t_out = QH u)
+    boundary rows   t = given incoming impedance data
+and each iteration computes its residual in complex128 and applies M:
+    v  = inv(B) r_leaf,  h = QH v + hcorr  (hcorr: the interface residuals),
+    up pass with D^-1, B D^-1; down pass from the boundary residual -> dt,
+    du = Y dt + v;  u += du, t += dt
+until max|du| <= tol max|u|.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from . import _stages as st
+from ._index_maps import quad_merge_maps_iti
+from ._nosource import _nosource_merge
+from ._refinement_dense import _node_pairing
+
+
+@dataclass
+class ItiMixedState:
+    mixed: bool
+    iti: bool
+    n_leaves: int
+    n_pts: int
+    n_cb: int
+    Aint: torch.Tensor          # (n_leaves, n_i, n_pts) complex128
+    G64: torch.Tensor           # (n_cb, n_pts) complex128
+    P64: torch.Tensor           # (n_cb, n_g) complex128
+    QH64: torch.Tensor          # (n_g, n_pts) complex128
+    Binv: torch.Tensor          # (n_leaves, n_pts, n_pts) complex64
+    Y: torch.Tensor             # (n_leaves, n_pts, n_g) complex64
+    QH32: torch.Tensor          # (n_g, n_pts) complex64
+    S_lst: List[torch.Tensor]
+    Dinv_lst: List[torch.Tensor]
+    BDinv_lst: List[torch.Tensor]
+    f: torch.Tensor             # (n_leaves, n_pts, nsrc) complex128
+    multi: bool
+    nbr: torch.Tensor
+    bnode: torch.Tensor
+    tol: float = 1e-12
+    max_iters: int = 30
+    history: list = field(default_factory=list)
+
+
+def build_mixed_iti(pde_problem, return_top_T=False, device=None, tol: float = 1e-12, max_iters: int = 30):
+    dom = pde_problem.domain
+    if not pde_problem.use_ItI or not dom.bool_2D or not dom.bool_uniform:
+        raise NotImplementedError("this mixed-precision path serves uniform 2D ItI problems")
+    if pde_problem.source is None:
+        raise ValueError("mixed precision needs the source at build time")
+    L = nat.lib()
+    dev = st._device(device)
+    src = pde_problem.source
+    pde_problem.source = None
+    try:
+        Y, T, _, _, Binv = st.local_solve_stage_uniform_2D_ItI(pde_problem, device=dev, dtype=torch.complex64,
+                                                               keep_inverse=True)
+    finally:
+        pde_problem.source = src
+    P_np, G_np, QH_np = pde_problem.P, pde_problem.G, pde_problem.QH
+    n_cb, n_pts = G_np.shape
+    n_i, nl = n_pts - n_cb, dom.n_leaves
+    ops_t, coeffs, cplx = st._coefficients(pde_problem, dev)
+    coeffs = coeffs.to(torch.complex128).contiguous()
+    Aint = torch.empty((nl, n_i, n_pts), dtype=torch.complex128, device=dev)
+    nat.check(L.hps_assemble_rows_complex(nl, n_pts, n_cb, n_i, ops_t.shape[0], ops_t.data_ptr(), coeffs.data_ptr(),
+                                          Aint.data_ptr(), n_pts, n_i * n_pts, nat.stream_ptr()),
+              "hps_assemble_rows_complex")
+    out = _nosource_merge(T, dom.L, True, dev, return_top_T)
+    del T
+    f, multi = st._src3(src, nl, n_pts, torch.complex128, dev)
+    nbr, bnode = _node_pairing(dom, dev)
+
+    def c(x, dt):
+        return torch.as_tensor(np.ascontiguousarray(x), device=dev).to(dt)
+
+    state = ItiMixedState(
+        mixed=True, iti=True, n_leaves=nl, n_pts=n_pts, n_cb=n_cb, Aint=Aint, G64=c(G_np, torch.complex128),
+        P64=c(P_np, torch.complex128), QH64=c(QH_np, torch.complex128), Binv=Binv, Y=Y,
+        QH32=c(QH_np, torch.complex64), S_lst=out[0], Dinv_lst=out[1], BDinv_lst=out[2], f=f, multi=multi, nbr=nbr,
+        bnode=bnode, tol=tol, max_iters=max_iters)
+    pde_problem._state = state
+    pde_problem._precision = "mixed"
+    pde_problem.Y = Y
+    pde_problem.S_lst, pde_problem.D_inv_lst, pde_problem.BD_inv_lst = out[0], out[1], out[2]
+    pde_problem.g_tilde_lst = []
+    if return_top_T:
+        return out[3]
+    return None
+
+
+def _residual(state: ItiMixedState, u, t, r64, r32, t_out):
+    """r64 = [P t - G u ; f_int - A_int u] per leaf, r32 its complex64 copy,
+    t_out = QH u (complex128)."""
+    n_cb = state.n_cb
+    nat.gemm(state.P64, t, r64[:, :n_cb])
+    nat.gemm(state.G64, u, r64[:, :n_cb], alpha=-1.0, beta=1.0, Cmat=r64[:, :n_cb])
+    nat.gemm(state.Aint, u, r64[:, n_cb:], alpha=-1.0, beta=1.0, Cmat=state.f[:, n_cb:])
+    nat.gemm(state.QH64, u, t_out)
+    nat.check(nat.lib().hps_convert(nat.HPS_C128, nat.HPS_C64, r64.numel(), r64.data_ptr(), r32.data_ptr(),
+                                    nat.stream_ptr()), "hps_convert")
+
+
+def correction(state: ItiMixedState, r32, hcorr, rb32):
+    """(du, dt) = M r with the complex64 operators."""
+    v = torch.empty_like(r32)
+    nat.gemm(state.Binv, r32, v)
+    h = torch.empty_like(hcorr)
+    nat.gemm(state.QH32, v, h, 1.0, 1.0, Cmat=hcorr)
+    g_t_lst = []
+    for Dinv, BDinv in zip(state.Dinv_lst, state.BDinv_lst):
+        g_t, h = st.up_level(h, Dinv, BDinv, quad_merge_maps_iti(BDinv.shape[1] // 8), b_is_bd_inv=True, iti=True)
+        g_t_lst.append(g_t)
+    gch = rb32.unsqueeze(0)
+    for lvl in range(len(state.S_lst) - 1, -1, -1):
+        S = state.S_lst[lvl]
+        gch = st.down_level(S, g_t_lst[lvl], gch, quad_merge_maps_iti(S.shape[2] // 8))
+    nat.gemm(state.Y, gch, v, 1.0, 1.0, Cmat=v)     # du = Y dt + v
+    return v, gch
+
+
+def _accumulate(x32: torch.Tensor, y64: torch.Tensor) -> None:
+    """y64 += x32 for complex tensors (as interleaved real pairs)."""
+    nat.check(nat.lib().hps_accumulate(2 * x32.numel(), x32.data_ptr(), y64.data_ptr(), nat.stream_ptr()),
+              "hps_accumulate")
+
+
+def solve_mixed_iti(pde_problem, boundary_data, source=None, host_device="cpu", tol=None, max_iters=None):
+    state: ItiMixedState = pde_problem._state
+    if source is not None:
+        raise ValueError("the mixed-precision solver takes the source at build time")
+    L = nat.lib()
+    dev = state.Binv.device
+    tol = state.tol if tol is None else tol
+    max_iters = state.max_iters if max_iters is None else max_iters
+    ns = state.f.shape[-1]
+    tg = boundary_data if isinstance(boundary_data, torch.Tensor) else torch.as_tensor(np.asarray(boundary_data))
+    tg = tg.to(device=dev, dtype=torch.complex128)
+    if tg.dim() == 1:
+        tg = tg.unsqueeze(-1)
+    if tg.shape[-1] != ns:
+        if tg.shape[-1] == 1:
+            tg = tg.expand(-1, ns)
+        else:
+            raise ValueError("boundary data and source have different numbers of right-hand sides")
+    tg = tg.contiguous()
+    nl, n_pts = state.n_leaves, state.n_pts
+    ng = state.P64.shape[1]
+    u = torch.zeros((nl, n_pts, ns), dtype=torch.complex128, device=dev)
+    t = torch.zeros((nl, ng, ns), dtype=torch.complex128, device=dev)
+    t_out = torch.zeros((nl, ng, ns), dtype=torch.complex128, device=dev)
+    r64 = torch.empty((nl, n_pts, ns), dtype=torch.complex128, device=dev)
+    r32 = torch.empty((nl, n_pts, ns), dtype=torch.complex64, device=dev)
+    hcorr = torch.empty((nl, ng, ns), dtype=torch.complex64, device=dev)
+    rb32 = torch.empty((tg.shape[0], ns), dtype=torch.complex64, device=dev)
+    sp = nat.stream_ptr()
+    _residual(state, u, t, r64, r32, t_out)
+    state.history = []
+    for _ in range(max_iters):
+        nat.check(L.hps_iti_combine(nl * ng, ns, state.nbr.data_ptr(), t_out.data_ptr(), t.data_ptr(), hcorr.data_ptr(),
+                                    tg.shape[0], state.bnode.data_ptr(), tg.data_ptr(), rb32.data_ptr(), sp),
+                  "hps_iti_combine")
+        du, dt = correction(state, r32, hcorr, rb32)
+        _accumulate(du, u)
+        _accumulate(dt, t)
+        step = float(du.abs().max().item())
+        size = float(u.abs().max().item())
+        state.history.append(step / max(size, 1e-300))
+        if step <= tol * size:
+            break
+        _residual(state, u, t, r64, r32, t_out)
+    if not state.multi:
+        u = u[..., 0]
+    return st._to_host(u, host_device)

@@ -17,6 +17,9 @@ from . import _stages as st
 def solve(pde_problem, boundary_data, source=None, compute_device=None, host_device="cpu", **refine_kw):
     dom = pde_problem.domain
     state = getattr(pde_problem, "_state", None)
+    if state is not None and getattr(state, "iti", False):
+        from ._refinement_iti import solve_mixed_iti
+        return solve_mixed_iti(pde_problem, boundary_data, source=source, host_device=host_device, **refine_kw)
     if state is not None and getattr(state, "dense", False):
         from ._refinement_dense import solve_mixed_dense
         return solve_mixed_dense(pde_problem, boundary_data, source=source, host_device=host_device, **refine_kw)

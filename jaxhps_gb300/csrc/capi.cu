@@ -66,6 +66,8 @@ cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const doub
                          const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
                          cudaStream_t st);
 cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st);
+cudaError_t iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in, void* hcorr,
+                        int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry, cudaStream_t st);
 cudaError_t jx_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
                          const double* coeffs, const double* inv_half, const double* D1, const double* D2,
                          const double* Pside, const double* Qside, const int* perm, const float* du, const float* dg,
@@ -745,6 +747,30 @@ int hps_mlp_adam(float* params, const float* grad, float* m, float* v, float lr,
     return HPS_ERR_ARG;
   }
   HPS_CHECK(mlp_adam(params, grad, m, v, lr, beta1, beta2, eps, step, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in, void* hcorr,
+                    int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry, void* stream) {
+  if (n_nodes <= 0 || nsrc <= 0 || !nbr || !t_out || !t_in || !hcorr || n_bdry < 0 ||
+      (n_bdry > 0 && (!bdry_node || !r_bdry))) {
+    set_error("hps_iti_combine: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(iti_combine(n_nodes, nsrc, nbr, t_out, t_in, hcorr, n_bdry, bdry_node, t_given, r_bdry,
+                        (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_assemble_rows_complex(int n_leaves, int n_pts, int row0, int n_rows, int n_ops, const double* ops,
+                              const void* coeffs, void* out, long long ld, long long stride, void* stream) {
+  if (n_leaves <= 0 || n_pts <= 0 || row0 < 0 || n_rows <= 0 || row0 + n_rows > n_pts || n_ops <= 0 || !ops ||
+      !coeffs || !out || ld < n_pts || stride < (long long)n_rows * ld) {
+    set_error("hps_assemble_rows_complex: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(leaf_assemble<c128, c128>(n_leaves, n_pts, row0, n_rows, n_pts, n_ops, ops, (const c128*)coeffs,
+                                      (c128*)out, ld, stride, nullptr, 0, 0, (cudaStream_t)stream));
   return HPS_OK;
 }
 

@@ -258,6 +258,52 @@ cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const doub
   return cudaGetLastError();
 }
 
+// ItI interface terms (complex, interleaved re/im):
+//   hcorr[node] = t_out[node] + t_in[nbr[node]]   (0 where nbr < 0), complex64
+//   r_bdry[b]   = t_given[b] - t_in[bdry_node[b]],                     complex64
+// hcorr is minus the residual of the partner node's interface equation
+// t_in(a) + t_out(b) = 0, folded into b's outgoing data for the up pass.
+__global__ void iti_combine_kernel(long long n_nodes, int nsrc, const int* __restrict__ nbr,
+                                   const double2* __restrict__ t_out, const double2* __restrict__ t_in,
+                                   float2* __restrict__ hcorr, int n_bdry, const int* __restrict__ bdry_node,
+                                   const double2* __restrict__ t_given, float2* __restrict__ r_bdry) {
+  const long long total = n_nodes * nsrc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long node = e / nsrc;
+    const int s = (int)(e % nsrc);
+    const int nb = nbr[node];
+    float2 h = make_float2(0.f, 0.f);
+    if (nb >= 0) {
+      const double2 a = t_out[e], b = t_in[(long long)nb * nsrc + s];
+      h = make_float2((float)(a.x + b.x), (float)(a.y + b.y));
+    }
+    hcorr[e] = h;
+  }
+  const long long tb = (long long)n_bdry * nsrc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tb;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / nsrc;
+    const int s = (int)(e % nsrc);
+    const double2 g = t_given ? t_given[e] : make_double2(0.0, 0.0);
+    const double2 t = t_in[(long long)bdry_node[b] * nsrc + s];
+    r_bdry[e] = make_float2((float)(g.x - t.x), (float)(g.y - t.y));
+  }
+}
+
+cudaError_t iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in, void* hcorr,
+                        int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry, cudaStream_t st) {
+  long long g = (n_nodes * nsrc + 255) / 256;
+  if (g > 8192) g = 8192;
+  if (g < 1) g = 1;
+  ProfScope ps(KC_MOVE, st, (double)n_nodes * nsrc * 40.0 + (double)n_bdry * nsrc * 40.0);
+  note_launch();
+  iti_combine_kernel<<<(int)g, 256, 0, st>>>(n_nodes, nsrc, nbr, (const double2*)t_out, (const double2*)t_in,
+                                             (float2*)hcorr, n_bdry, bdry_node, (const double2*)t_given,
+                                             (float2*)r_bdry);
+  return cudaGetLastError();
+}
+
 // y[i] += x[i] (x FP32, y FP64), for n elements; returns nothing.
 __global__ void accumulate_kernel(long long n, const float* __restrict__ x, double* y) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
