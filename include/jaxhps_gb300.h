@@ -421,6 +421,36 @@ HPS_API int hps_assemble_rows_complex(int n_leaves, int n_pts, int row0, int n_r
  * t_out = outgoing impedance QH u, t_in = incoming impedance state; hcorr is
  * minus the residual of the partner's interface equation t_in(a) + t_out(b) = 0
  * (the coupling of the ItI merges, merge/_uniform_2D_ItI.py:182-375). */
+/* Residual of the ItI leaf and interface system (complex128; no counterpart
+ * in the reference, which solves in complex128 directly).  Per leaf, with u
+ * the values at all p^2 points (exterior-first) and t_in the incoming
+ * impedance at the 4q Gauss nodes (get_ItI's system,
+ * local_solve/_uniform_2D_ItI.py:120-186):
+ *   r[:n_cb]  = P t_in - G u        (G = N~ + i eta I, the incoming impedance)
+ *   r[n_cb:]  = f_int - A_int u     (tensor-product derivatives)
+ *   t_out     = QH u                (outgoing impedance at the Gauss nodes)
+ * r is written as complex64, t_out as complex128. */
+typedef struct {
+  int n_leaves, p, q, nsrc, n_ops;
+  int op_kind[10];         /* as in hps_residual2d_args */
+  int coef_complex;        /* 1: coeffs are complex128, 0: float64 */
+  double eta;
+  const void* coeffs;      /* (n_ops, n_leaves, p*p) */
+  const double* inv_half;  /* (n_leaves) 2 / leaf side length */
+  const double* D1;        /* (p, p) */
+  const double* D2;        /* (p, p) */
+  const double* Pside;     /* (p, q) */
+  const double* Qside;     /* (q, p) */
+  const int* perm;         /* (p*p) */
+  const void* u;           /* (n_leaves, p*p, nsrc) complex128 */
+  const void* t_in;        /* (n_leaves, 4q, nsrc) complex128 */
+  const void* f;           /* (n_leaves, p*p, nsrc) complex128, or NULL for a zero source */
+  void* r;                 /* out (n_leaves, p*p, nsrc) complex64 */
+  void* t_out;             /* out (n_leaves, 4q, nsrc) complex128 */
+} hps_residual_iti2d_args;
+
+HPS_API int hps_residual_iti_2d(const hps_residual_iti2d_args* a, void* stream);
+
 HPS_API int hps_iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in,
                             void* hcorr, int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry,
                             void* stream);

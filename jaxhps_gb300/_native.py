@@ -87,6 +87,15 @@ class Residual2DArgs(C.Structure):
     ]
 
 
+class ResidualIti2DArgs(C.Structure):
+    _fields_ = [
+        ("n_leaves", ci), ("p", ci), ("q", ci), ("nsrc", ci), ("n_ops", ci), ("op_kind", ci * 10),
+        ("coef_complex", ci), ("eta", C.c_double),
+        ("coeffs", vp), ("inv_half", vp), ("D1", vp), ("D2", vp), ("Pside", vp), ("Qside", vp), ("perm", vp),
+        ("u", vp), ("t_in", vp), ("f", vp), ("r", vp), ("t_out", vp),
+    ]
+
+
 class DownArgs(C.Structure):
     _fields_ = [
         ("dtype", ci), ("n_merges", ci), ("nch", ci), ("nb", ci), ("n_int", ci), ("n_ext", ci),
@@ -156,6 +165,8 @@ def _declare(lib):
     lib.hps_scale_batched.restype = ci
     lib.hps_iti_combine.argtypes = [cll, ci, vp, vp, vp, vp, ci, vp, vp, vp, vp]
     lib.hps_iti_combine.restype = ci
+    lib.hps_residual_iti_2d.argtypes = [P(ResidualIti2DArgs), vp]
+    lib.hps_residual_iti_2d.restype = ci
     lib.hps_assemble_rows_complex.argtypes = [ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp]
     lib.hps_assemble_rows_complex.restype = ci
     lib.hps_gemm_tc_status.argtypes = []
@@ -184,7 +195,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_assemble_rows_complex",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_assemble_rows_complex",
 )
 
 

@@ -12,7 +12,8 @@ Gauss node), complex128, from zero.  The discrete system J is
     leaf rows       B u = [P t ; f_int]
     interface rows  t(a) + t_out(b) = 0  at paired nodes a, b  (t_out = QH u)
     boundary rows   t = given incoming impedance data
-and each iteration computes its residual in complex128 and applies M:
+and each iteration computes its residual in complex128 (hps_residual_iti_2d:
+tensor-product derivatives, no stored per-leaf rows) and applies M:
     v  = inv(B) r_leaf,  h = QH v + hcorr  (hcorr: the interface residuals),
     up pass with D^-1, B D^-1; down pass from the boundary residual -> dt,
     du = Y dt + v;  u += du, t += dt
@@ -24,6 +25,8 @@ from __future__ import annotations
 from dataclasses import dataclass, field
 from typing import List
 
+import ctypes as C
+
 import numpy as np
 import torch
 
@@ -31,6 +34,8 @@ from . import _native as nat
 from . import _stages as st
 from ._index_maps import quad_merge_maps_iti
 from ._nosource import _nosource_merge
+from ._pdeproblem import COEFF_NAMES_2D
+from ._refinement import OP_KIND_2D, _domain_constants
 from ._refinement_dense import _node_pairing
 
 
@@ -41,10 +46,12 @@ class ItiMixedState:
     n_leaves: int
     n_pts: int
     n_cb: int
-    Aint: torch.Tensor          # (n_leaves, n_i, n_pts) complex128
-    G64: torch.Tensor           # (n_cb, n_pts) complex128
-    P64: torch.Tensor           # (n_cb, n_g) complex128
-    QH64: torch.Tensor          # (n_g, n_pts) complex128
+    p: int
+    q: int
+    eta: float
+    coeffs: torch.Tensor        # (n_ops, n_leaves, p^2) float64 or complex128
+    op_kind: List[int]
+    consts: dict
     Binv: torch.Tensor          # (n_leaves, n_pts, n_pts) complex64
     Y: torch.Tensor             # (n_leaves, n_pts, n_g) complex64
     QH32: torch.Tensor          # (n_g, n_pts) complex64
@@ -60,13 +67,29 @@ class ItiMixedState:
     history: list = field(default_factory=list)
 
 
+def _coefficients(pde_problem, dev):
+    """Active coefficients stacked (n_ops, n_leaves, p^2) and their op kinds;
+    complex128 when any coefficient is complex."""
+    arrs, names = [], []
+    for name in COEFF_NAMES_2D:
+        c = getattr(pde_problem, f"{name}_coefficients")
+        if c is not None:
+            arrs.append(c)
+            names.append(name)
+    cplx = any(st._is_complex(c) for c in arrs)
+    dt = torch.complex128 if cplx else torch.float64
+    return torch.stack([st._as_tensor(c, dt, dev) for c in arrs]).contiguous(), [OP_KIND_2D[n] for n in names]
+
+
 def build_mixed_iti(pde_problem, return_top_T=False, device=None, tol: float = 1e-12, max_iters: int = 30):
     dom = pde_problem.domain
     if not pde_problem.use_ItI or not dom.bool_2D or not dom.bool_uniform:
         raise NotImplementedError("this mixed-precision path serves uniform 2D ItI problems")
     if pde_problem.source is None:
         raise ValueError("mixed precision needs the source at build time")
-    L = nat.lib()
+    r = dom.root
+    if not np.isclose(r.xmax - r.xmin, r.ymax - r.ymin):
+        raise NotImplementedError("the mixed-precision residual assumes square leaves")
     dev = st._device(device)
     src = pde_problem.source
     pde_problem.source = None
@@ -75,28 +98,19 @@ def build_mixed_iti(pde_problem, return_top_T=False, device=None, tol: float = 1
                                                                keep_inverse=True)
     finally:
         pde_problem.source = src
-    P_np, G_np, QH_np = pde_problem.P, pde_problem.G, pde_problem.QH
-    n_cb, n_pts = G_np.shape
-    n_i, nl = n_pts - n_cb, dom.n_leaves
-    ops_t, coeffs, cplx = st._coefficients(pde_problem, dev)
-    coeffs = coeffs.to(torch.complex128).contiguous()
-    Aint = torch.empty((nl, n_i, n_pts), dtype=torch.complex128, device=dev)
-    nat.check(L.hps_assemble_rows_complex(nl, n_pts, n_cb, n_i, ops_t.shape[0], ops_t.data_ptr(), coeffs.data_ptr(),
-                                          Aint.data_ptr(), n_pts, n_i * n_pts, nat.stream_ptr()),
-              "hps_assemble_rows_complex")
+    n_cb, n_pts = pde_problem.G.shape
+    nl = dom.n_leaves
+    coeffs, op_kind = _coefficients(pde_problem, dev)
     out = _nosource_merge(T, dom.L, True, dev, return_top_T)
     del T
     f, multi = st._src3(src, nl, n_pts, torch.complex128, dev)
     nbr, bnode = _node_pairing(dom, dev)
-
-    def c(x, dt):
-        return torch.as_tensor(np.ascontiguousarray(x), device=dev).to(dt)
-
+    QH32 = torch.as_tensor(np.ascontiguousarray(pde_problem.QH), device=dev).to(torch.complex64)
     state = ItiMixedState(
-        mixed=True, iti=True, n_leaves=nl, n_pts=n_pts, n_cb=n_cb, Aint=Aint, G64=c(G_np, torch.complex128),
-        P64=c(P_np, torch.complex128), QH64=c(QH_np, torch.complex128), Binv=Binv, Y=Y,
-        QH32=c(QH_np, torch.complex64), S_lst=out[0], Dinv_lst=out[1], BDinv_lst=out[2], f=f, multi=multi, nbr=nbr,
-        bnode=bnode, tol=tol, max_iters=max_iters)
+        mixed=True, iti=True, n_leaves=nl, n_pts=n_pts, n_cb=n_cb, p=dom.p, q=dom.q, eta=float(pde_problem.eta),
+        coeffs=coeffs, op_kind=op_kind, consts=_domain_constants(dom, dev), Binv=Binv, Y=Y, QH32=QH32,
+        S_lst=out[0], Dinv_lst=out[1], BDinv_lst=out[2], f=f, multi=multi, nbr=nbr, bnode=bnode, tol=tol,
+        max_iters=max_iters)
     pde_problem._state = state
     pde_problem._precision = "mixed"
     pde_problem.Y = Y
@@ -107,16 +121,19 @@ def build_mixed_iti(pde_problem, return_top_T=False, device=None, tol: float = 1
     return None
 
 
-def _residual(state: ItiMixedState, u, t, r64, r32, t_out):
-    """r64 = [P t - G u ; f_int - A_int u] per leaf, r32 its complex64 copy,
-    t_out = QH u (complex128)."""
-    n_cb = state.n_cb
-    nat.gemm(state.P64, t, r64[:, :n_cb])
-    nat.gemm(state.G64, u, r64[:, :n_cb], alpha=-1.0, beta=1.0, Cmat=r64[:, :n_cb])
-    nat.gemm(state.Aint, u, r64[:, n_cb:], alpha=-1.0, beta=1.0, Cmat=state.f[:, n_cb:])
-    nat.gemm(state.QH64, u, t_out)
-    nat.check(nat.lib().hps_convert(nat.HPS_C128, nat.HPS_C64, r64.numel(), r64.data_ptr(), r32.data_ptr(),
-                                    nat.stream_ptr()), "hps_convert")
+def _residual(state: ItiMixedState, u, t, r32, t_out):
+    """r32 = [P t - G u ; f_int - A_int u] per leaf (complex64), t_out = QH u
+    (complex128), both from complex128 arithmetic."""
+    cs = state.consts
+    a = nat.ResidualIti2DArgs(
+        n_leaves=state.n_leaves, p=state.p, q=state.q, nsrc=u.shape[-1], n_ops=len(state.op_kind),
+        coef_complex=int(state.coeffs.is_complex()), eta=state.eta, coeffs=state.coeffs.data_ptr(),
+        inv_half=cs["inv_half"].data_ptr(), D1=cs["D1"].data_ptr(), D2=cs["D2"].data_ptr(),
+        Pside=cs["Pside"].data_ptr(), Qside=cs["Qside"].data_ptr(), perm=cs["perm"].data_ptr(), u=u.data_ptr(),
+        t_in=t.data_ptr(), f=state.f.data_ptr(), r=r32.data_ptr(), t_out=t_out.data_ptr())
+    for i, k in enumerate(state.op_kind):
+        a.op_kind[i] = k
+    nat.check(nat.lib().hps_residual_iti_2d(C.byref(a), nat.stream_ptr()), "hps_residual_iti_2d")
 
 
 def correction(state: ItiMixedState, r32, hcorr, rb32):
@@ -163,16 +180,15 @@ def solve_mixed_iti(pde_problem, boundary_data, source=None, host_device="cpu", 
             raise ValueError("boundary data and source have different numbers of right-hand sides")
     tg = tg.contiguous()
     nl, n_pts = state.n_leaves, state.n_pts
-    ng = state.P64.shape[1]
+    ng = state.Y.shape[2]
     u = torch.zeros((nl, n_pts, ns), dtype=torch.complex128, device=dev)
     t = torch.zeros((nl, ng, ns), dtype=torch.complex128, device=dev)
     t_out = torch.zeros((nl, ng, ns), dtype=torch.complex128, device=dev)
-    r64 = torch.empty((nl, n_pts, ns), dtype=torch.complex128, device=dev)
     r32 = torch.empty((nl, n_pts, ns), dtype=torch.complex64, device=dev)
     hcorr = torch.empty((nl, ng, ns), dtype=torch.complex64, device=dev)
     rb32 = torch.empty((tg.shape[0], ns), dtype=torch.complex64, device=dev)
     sp = nat.stream_ptr()
-    _residual(state, u, t, r64, r32, t_out)
+    _residual(state, u, t, r32, t_out)
     state.history = []
     for _ in range(max_iters):
         nat.check(L.hps_iti_combine(nl * ng, ns, state.nbr.data_ptr(), t_out.data_ptr(), t.data_ptr(), hcorr.data_ptr(),
@@ -186,7 +202,7 @@ def solve_mixed_iti(pde_problem, boundary_data, source=None, host_device="cpu", 
         state.history.append(step / max(size, 1e-300))
         if step <= tol * size:
             break
-        _residual(state, u, t, r64, r32, t_out)
+        _residual(state, u, t, r32, t_out)
     if not state.multi:
         u = u[..., 0]
     return st._to_host(u, host_device)

@@ -24,6 +24,10 @@ cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col
 template <class T>
 cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds, T* dst, long long ldd,
                      long long sd, cudaStream_t st);
+template <class T>
+cudaError_t row_equilibrate(int batch, int n, T* A, long long lda, long long sA, double* s, cudaStream_t st);
+template <class T>
+cudaError_t col_scale(int batch, int n, T* X, long long ldx, long long sX, const double* s, cudaStream_t st);
 cudaError_t refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
                              double* pts, cudaStream_t st);
 template <class T>
@@ -66,6 +70,11 @@ cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const doub
                          const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
                          cudaStream_t st);
 cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st);
+cudaError_t residual_iti_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds, int cplx,
+                            double eta, const void* coeffs, const double* inv_half, const double* D1,
+                            const double* D2, const double* Pside, const double* Qside, const int* perm,
+                            const void* u, const void* t_in, const void* f, void* r, void* t_out, int need_uy,
+                            cudaStream_t st);
 cudaError_t iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in, void* hcorr,
                         int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry, cudaStream_t st);
 cudaError_t jx_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
@@ -215,6 +224,7 @@ static int leaf_dtn_impl(const hps_leaf_dtn_args* a, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 static size_t leaf_iti_ws(const hps_leaf_iti_args* a, Carver* cv) {
   cv->take(inverse_workspace_bytes(a->dtype, a->n_pts, a->n_leaves));
+  cv->take(sizeof(double) * (size_t)a->n_leaves * a->n_pts);
   return cv->used + 256;
 }
 
@@ -227,6 +237,7 @@ static int leaf_iti_impl(const hps_leaf_iti_args* a, cudaStream_t st) {
   Carver cv(wsb);
   const size_t invb = inverse_workspace_bytes(a->dtype, np, nl);
   void* invws = cv.take(invb);
+  double* rscale = (double*)cv.take(sizeof(double) * (size_t)nl * np);
   T* Bm = (T*)a->B_inv;
   const long long sB = (long long)np * np;
   HPS_CHECK(set_rows<T>(nl, ncb, np, (const T*)a->G, np, Bm, np, sB, st));
@@ -238,7 +249,11 @@ static int leaf_iti_impl(const hps_leaf_iti_args* a, cudaStream_t st) {
     e = leaf_assemble<T, double>(nl, np, ncb, ni, 0, a->n_ops, a->ops, (const double*)a->coeffs, nullptr, 0, 0,
                                  Bm + (size_t)ncb * np, np, sB, st);
   HPS_CHECK(e);
+  // inv(B) = inv(diag(s) B) diag(s): the impedance rows (~p^2/h) and the PDE
+  // rows (~p^4/h^2) are brought to one scale before elimination
+  HPS_CHECK(row_equilibrate<T>(nl, np, Bm, np, sB, rscale, st));
   HPS_CHECK(inverse_batched<T>(np, Bm, np, sB, Bm, np, sB, nl, a->info, invws, invb, st));
+  HPS_CHECK(col_scale<T>(nl, np, Bm, np, sB, rscale, st));
   const T one_ = one<T>(), zero_ = zero<T>();
   HPS_CHECK(gemm_batched<T>(np, ng, ncb, one_, Bm, np, sB, (const T*)a->P, ng, 0, zero_, nullptr, 0, 0,
                             (T*)a->Y, ng, (long long)np * ng, nl, st));
@@ -589,22 +604,51 @@ int hps_up_level(const hps_up_args* a, void* stream) {
   DISPATCH(a->dtype, up_impl, a, (cudaStream_t)stream)
 }
 
-static int pack_op_kinds(const hps_residual2d_args* a, unsigned long long* kinds, int* need_uy) {
+static int pack_kinds(int n_ops, const int* op_kind, unsigned long long* kinds, int* need_uy) {
   // op kinds packed 4 bits each; D_xy needs the u_y field on the whole grid
-  if (a->n_ops > 10) {
+  if (n_ops > 10) {
     set_error("residual: at most 10 operators");
     return HPS_ERR_ARG;
   }
   *kinds = 0;
   *need_uy = 0;
-  for (int o = 0; o < a->n_ops; ++o) {
-    if (a->op_kind[o] < 0 || a->op_kind[o] > 5) {
-      set_error("residual: bad op kind %d", a->op_kind[o]);
+  for (int o = 0; o < n_ops; ++o) {
+    if (op_kind[o] < 0 || op_kind[o] > 5) {
+      set_error("residual: bad op kind %d", op_kind[o]);
       return HPS_ERR_ARG;
     }
-    *kinds |= (unsigned long long)a->op_kind[o] << (4 * o);
-    if (a->op_kind[o] == 1) *need_uy = 1;
+    *kinds |= (unsigned long long)op_kind[o] << (4 * o);
+    if (op_kind[o] == 1) *need_uy = 1;
   }
+  return HPS_OK;
+}
+
+static int pack_op_kinds(const hps_residual2d_args* a, unsigned long long* kinds, int* need_uy) {
+  return pack_kinds(a->n_ops, a->op_kind, kinds, need_uy);
+}
+
+int hps_residual_iti_2d(const hps_residual_iti2d_args* a, void* stream) {
+  if (!a || a->n_leaves <= 0 || a->p < 3 || a->q <= 0 || a->nsrc <= 0 || a->n_ops <= 0 || !a->coeffs ||
+      !a->inv_half || !a->D1 || !a->D2 || !a->Pside || !a->Qside || !a->perm || !a->u || !a->t_in || !a->r ||
+      !a->t_out) {
+    set_error("hps_residual_iti_2d: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (a->n_leaves > 2147483647 || (a->nsrc + 15) / 16 > 65535) {
+    set_error("hps_residual_iti_2d: too many right-hand sides");
+    return HPS_ERR_ARG;
+  }
+  unsigned long long kinds = 0;
+  int need_uy = 0;
+  if (pack_kinds(a->n_ops, a->op_kind, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
+  cudaError_t e = residual_iti_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, a->coef_complex, a->eta,
+                                  a->coeffs, a->inv_half, a->D1, a->D2, a->Pside, a->Qside, a->perm, a->u, a->t_in,
+                                  a->f, a->r, a->t_out, need_uy, (cudaStream_t)stream);
+  if (e == cudaErrorInvalidValue) {
+    set_error("hps_residual_iti_2d: p, q too large for the shared-memory layout");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(e);
   return HPS_OK;
 }
 

@@ -147,6 +147,79 @@ static cudaError_t launch_gemm_cfg(int M, int N, int K, T alpha, const T* A, lon
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Skinny products (N <= 8 columns: one or a few right-hand sides).  A tiled
+// kernel would spend most of a 64-wide N tile on padding; here one warp owns
+// one row of A, its lanes stride over K (coalesced reads of A, the dominant
+// traffic) and the N partial sums are reduced with shuffles.  The kernel is
+// bound by reading A once.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float shfl_xor_(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double shfl_xor_(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ c64 shfl_xor_(c64 v, int m) {
+  return c64{__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
+}
+__device__ __forceinline__ c128 shfl_xor_(c128 v, int m) {
+  return c128{__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m)};
+}
+
+constexpr int SK_WARPS = 8;
+
+template <class T, int NB>
+__global__ void __launch_bounds__(SK_WARPS * 32)
+gemm_skinny_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, long long lda, long long sA,
+                   const T* __restrict__ B, long long ldb, long long sB, T beta, const T* C, long long ldc,
+                   long long sC, T* D, long long ldd, long long sD, int use_c) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * SK_WARPS + (threadIdx.x >> 5);
+  if (row >= M) return;  // uniform across the warp
+  const long long bz = blockIdx.y;
+  const T* a = A + bz * sA + (long long)row * lda;
+  const T* b = B + bz * sB;
+  T acc[NB];
+#pragma unroll
+  for (int n = 0; n < NB; ++n) acc[n] = zero<T>();
+#pragma unroll 4
+  for (int k = lane; k < K; k += 32) {
+    const T av = a[k];
+    const T* br = b + (long long)k * ldb;
+#pragma unroll
+    for (int n = 0; n < NB; ++n)
+      if (n < N) acc[n] = fma_(av, br[n], acc[n]);
+  }
+#pragma unroll
+  for (int n = 0; n < NB; ++n)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[n] = add(acc[n], shfl_xor_(acc[n], o));
+  if (lane < N) {
+    T v = acc[0];
+#pragma unroll
+    for (int n = 1; n < NB; ++n)
+      if (lane == n) v = acc[n];
+    T out = mul(alpha, v);
+    if (use_c) out = fma_(beta, C[bz * sC + (long long)row * ldc + lane], out);
+    D[bz * sD + (long long)row * ldd + lane] = out;
+  }
+}
+
+template <class T, int NB>
+static cudaError_t launch_skinny(int M, int N, int K, T alpha, const T* A, long long lda, long long sA, const T* B,
+                                 long long ldb, long long sB, T beta, const T* C, long long ldc, long long sC, T* D,
+                                 long long ldd, long long sD, int batch, cudaStream_t st) {
+  const int use_c = (C != nullptr);
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    dim3 grid((M + SK_WARPS - 1) / SK_WARPS, nb);
+    const double cplx = (sizeof(T) == 16 || (sizeof(T) == 8 && DTypeOf<T>::value == C64)) ? 4.0 : 1.0;
+    ProfScope ps(KC_GEMM, st, 2.0 * cplx * M * (double)N * K * nb);
+    note_launch();
+    gemm_skinny_kernel<T, NB><<<grid, SK_WARPS * 32, 0, st>>>(
+        M, N, K, alpha, A + b0 * sA, lda, sA, B + b0 * sB, ldb, sB, beta, use_c ? C + b0 * sC : nullptr, ldc, sC,
+        D + b0 * sD, ldd, sD, use_c);
+  }
+  return cudaGetLastError();
+}
+
 // FP32 products on the tensor cores (gemm_tc.cu) unless HPS_GEMM_TC=0.
 static bool tc_enabled() {
   static const bool on = [] {
@@ -161,6 +234,15 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
                          const T* B, long long ldb, long long sB, T beta, const T* C, long long ldc,
                          long long sC, T* D, long long ldd, long long sD, int batch, cudaStream_t st) {
   if (M <= 0 || N <= 0 || batch <= 0) return cudaSuccess;
+  if (N <= 8 && K >= 32) {
+    if (N == 1)
+      return launch_skinny<T, 1>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+    if (N <= 2)
+      return launch_skinny<T, 2>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+    if (N <= 4)
+      return launch_skinny<T, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+    return launch_skinny<T, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+  }
   if constexpr (std::is_same<T, float>::value) {
     // measured: the tensor-core kernel wins once a tile has enough K-steps to
     // amortise its pipeline prologue and epilogue

@@ -122,6 +122,78 @@ cudaError_t set_rows(int batch, int rows, int cols, const T* src, long long lds,
 }
 
 // ---------------------------------------------------------------------------
+// Row equilibration of a batch of square matrices by powers of two.
+//   s[b][r] = 2^-e with max_c |A[b][r][c]| = f 2^e, f in [0.5, 1);  A[b][r][:] *= s[b][r]
+// and the matching column scaling of the inverse, X[b][:][c] *= s[b][c],
+// which turns inv(diag(s) A) into inv(A).  Scaling by powers of two is exact,
+// so only the pivot order of the elimination changes: rows whose magnitudes
+// differ by orders (the ItI leaf matrix stacks impedance rows ~p^2/h over
+// PDE rows ~p^4/h^2) no longer lose the small rows' digits to the large.
+// One warp per row.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float scale_by(float v, double s) { return v * (float)s; }
+__device__ __forceinline__ double scale_by(double v, double s) { return v * s; }
+__device__ __forceinline__ c64 scale_by(c64 v, double s) { return c64{v.x * (float)s, v.y * (float)s}; }
+__device__ __forceinline__ c128 scale_by(c128 v, double s) { return c128{v.x * s, v.y * s}; }
+__device__ __forceinline__ double absmag(float v) { return fabs((double)v); }
+__device__ __forceinline__ double absmag(double v) { return fabs(v); }
+__device__ __forceinline__ double absmag(c64 v) { return fmax(fabs((double)v.x), fabs((double)v.y)); }
+__device__ __forceinline__ double absmag(c128 v) { return fmax(fabs(v.x), fabs(v.y)); }
+
+template <class T>
+__global__ void row_equilibrate_kernel(long long rows_total, int n, T* A, long long lda, long long sA, double* s) {
+  const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= rows_total) return;
+  const long long b = row / n;
+  const int r = (int)(row % n);
+  T* a = A + b * sA + (long long)r * lda;
+  double m = 0.0;
+  for (int c = lane; c < n; c += 32) m = fmax(m, absmag(a[c]));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  int e = 0;
+  if (m > 0.0 && m <= 1.7e308) frexp(m, &e);
+  const double sc = ldexp(1.0, -e);
+  for (int c = lane; c < n; c += 32) a[c] = scale_by(a[c], sc);
+  if (lane == 0) s[row] = sc;
+}
+
+template <class T>
+__global__ void col_scale_kernel(int batch, int n, T* X, long long ldx, long long sX, const double* __restrict__ s) {
+  const long long total = (long long)batch * n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / ((long long)n * n);
+    const int rc = (int)(e % ((long long)n * n));
+    const int r = rc / n, c = rc % n;
+    T* x = X + b * sX + (long long)r * ldx + c;
+    *x = scale_by(*x, s[b * n + c]);
+  }
+}
+
+template <class T>
+cudaError_t row_equilibrate(int batch, int n, T* A, long long lda, long long sA, double* s, cudaStream_t st) {
+  if (batch <= 0 || n <= 0) return cudaSuccess;
+  const long long rows = (long long)batch * n;
+  const long long g = (rows + 7) / 8;
+  ProfScope ps(KC_MOVE, st, 2.0 * (double)rows * n * sizeof(T));
+  note_launch();
+  row_equilibrate_kernel<T><<<(unsigned)g, 256, 0, st>>>(rows, n, A, lda, sA, s);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t col_scale(int batch, int n, T* X, long long ldx, long long sX, const double* s, cudaStream_t st) {
+  if (batch <= 0 || n <= 0) return cudaSuccess;
+  long long g = ((long long)batch * n * n + 255) / 256;
+  if (g > 16384) g = 16384;
+  ProfScope ps(KC_MOVE, st, 2.0 * (double)batch * n * n * sizeof(T));
+  note_launch();
+  col_scale_kernel<T><<<(int)g, 256, 0, st>>>(batch, n, X, ldx, sX, s);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Merge gather  (reference: merge/_uniform_2D_DtN.py:206-475,
 // merge/_schur_complement.py:182-237, 3D: merge/_schur_complement.py:293-774)
 //
@@ -390,6 +462,8 @@ cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st) {
   template cudaError_t leaf_assemble<T, c128>(int, int, int, int, int, int, const double*, const c128*, T*,     \
                                               long long, long long, T*, long long, long long, cudaStream_t);    \
   template cudaError_t set_rows<T>(int, int, int, const T*, long long, T*, long long, long long, cudaStream_t); \
+  template cudaError_t row_equilibrate<T>(int, int, T*, long long, long long, double*, cudaStream_t);              \
+  template cudaError_t col_scale<T>(int, int, T*, long long, long long, const double*, cudaStream_t);           \
   template cudaError_t merge_gather<T>(int, int, int, int, int, int, const T*, const T*, const int*, const int*, \
                                        const int*, const int*, const int*, T*, T*, T*, T*, T*, T*, cudaStream_t); \
   template cudaError_t down_scatter<T>(int, int, int, int, int, int, const int*, const T*, const T*, T*,        \

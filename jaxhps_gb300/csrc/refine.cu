@@ -217,6 +217,225 @@ cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigne
 }
 
 // ---------------------------------------------------------------------------
+// ItI residual (complex128).  Unknowns per leaf: u at all p^2 points
+// (exterior-first order) and the incoming impedance t_in at the 4q Gauss
+// nodes.  The leaf system of get_ItI (local_solve/_uniform_2D_ItI.py:120-186)
+// is B u = [P t_in ; f_int] with B = [G ; A_int], G = N~ + i eta I the
+// incoming impedance at the Chebyshev boundary points
+// (_precompute_operators_2D.py:243-265).  Written here:
+//   r[k]      = (P t_in)[k] - (u_n + i eta u)(k)        k < 4(p-1)
+//   r[ncb+i]  = f_int[i] - sum_o c_o (D_o u)(i)
+//   t_out[j]  = Q (u_n - i eta u)   at the Gauss nodes (QH u,
+//               _precompute_operators_2D.py:195-240)
+// r is rounded to complex64 (the input of the complex64 correction); t_out
+// stays complex128 for the interface equations.  Same tensor-product
+// evaluation as residual_2d: derivatives act along one grid axis.
+// ---------------------------------------------------------------------------
+template <bool CPLX>
+__global__ void __launch_bounds__(RES_NT)
+residual_iti_2d_kernel(int n_leaves, int p, int q, int nsrc, int SC, int n_ops, unsigned long long kinds,
+                       double eta, const void* __restrict__ coeffs_v, const double* __restrict__ inv_half,
+                       const double* __restrict__ D1g, const double* __restrict__ D2g,
+                       const double* __restrict__ Pside_g, const double* __restrict__ Qside_g,
+                       const int* __restrict__ perm_g, const double2* __restrict__ u_g,
+                       const double2* __restrict__ tin_g, const double2* __restrict__ f, float2* __restrict__ r,
+                       double2* __restrict__ t_out, int need_uy) {
+  extern __shared__ double sm[];
+  const int pp = p * p;
+  const int m = p - 1;
+  const int ncb = 4 * m;
+  const int ni = pp - ncb;
+  const int nq = 4 * q;
+  double2* u = reinterpret_cast<double2*>(sm);          // pp * SC (meshgrid layout)
+  double2* uy = u + pp * SC;                            // pp * SC when D_xy is active
+  double2* ts = uy + (need_uy ? pp * SC : 0);           // nq * SC
+  double2* nd = ts + nq * SC;                           // 4p * SC
+  double* D1 = reinterpret_cast<double*>(nd + 4 * p * SC);
+  double* D2 = D1 + pp;
+  double* Ps = D2 + pp;
+  double* Qs = Ps + p * q;
+  int* perm = reinterpret_cast<int*>(Qs + q * p);
+
+  const long long l = blockIdx.x;
+  const int s0 = blockIdx.y * SC;
+  const int sc = min(SC, nsrc - s0);
+  const int tid = threadIdx.x;
+  const double ih = inv_half[l];
+  const double ih2 = ih * ih;
+  for (int e = tid; e < pp; e += RES_NT) {
+    D1[e] = D1g[e];
+    D2[e] = D2g[e];
+    perm[e] = perm_g[e];
+  }
+  for (int e = tid; e < p * q; e += RES_NT) {
+    Ps[e] = Pside_g[e];
+    Qs[e] = Qside_g[e];
+  }
+  for (int e = tid; e < nq * SC; e += RES_NT) {
+    const int k = e / SC, s = e % SC;
+    ts[e] = (s < sc) ? tin_g[(l * nq + k) * nsrc + s0 + s] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int e = tid; e < pp * SC; e += RES_NT) {
+    const int k = e / SC, s = e % SC;
+    u[perm[k] * SC + s] = (s < sc) ? u_g[(l * pp + k) * nsrc + s0 + s] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  if (need_uy) {
+    for (int e = tid; e < pp * SC; e += RES_NT) {
+      const int idx = e / SC, s = e % SC;
+      const int ix = idx / p, iy = idx % p;
+      double2 v = make_double2(0.0, 0.0);
+      for (int k = 0; k < p; ++k) {
+        const double d = D1[iy * p + k];
+        const double2 w = u[(ix * p + k) * SC + s];
+        v.x = fma(d, w.x, v.x);
+        v.y = fma(d, w.y, v.y);
+      }
+      uy[e] = make_double2(-ih * v.x, -ih * v.y);
+    }
+    __syncthreads();
+  }
+  // PDE rows
+  for (int e = tid; e < ni * SC; e += RES_NT) {
+    const int i = e / SC, s = e % SC;
+    if (s >= sc) continue;
+    const int idx = perm[ncb + i];
+    const int ix = idx / p, iy = idx % p;
+    const long long pt = (long long)l * pp + ncb + i;
+    double2 acc = f ? f[pt * nsrc + s0 + s] : make_double2(0.0, 0.0);
+    for (int o = 0; o < n_ops; ++o) {
+      double2 fld = make_double2(0.0, 0.0);
+      const double2* src = u;
+      int base = 0, stride = 0;
+      const double* Dm = D1;
+      double fac = 1.0;
+      bool ident = false;
+      switch ((int)((kinds >> (4 * o)) & 15ull)) {
+        case OP_XX: Dm = D2 + ix * p; base = iy; stride = p; fac = ih2; break;
+        case OP_YY: Dm = D2 + iy * p; base = ix * p; stride = 1; fac = ih2; break;
+        case OP_X:  Dm = D1 + ix * p; base = iy; stride = p; fac = ih; break;
+        case OP_Y:  Dm = D1 + iy * p; base = ix * p; stride = 1; fac = -ih; break;
+        case OP_XY: Dm = D1 + ix * p; base = iy; stride = p; fac = ih; src = uy; break;
+        default: ident = true;
+      }
+      if (ident) {
+        fld = u[idx * SC + s];
+      } else {
+        for (int j = 0; j < p; ++j) {
+          const double2 w = src[(base + j * stride) * SC + s];
+          fld.x = fma(Dm[j], w.x, fld.x);
+          fld.y = fma(Dm[j], w.y, fld.y);
+        }
+        fld.x *= fac;
+        fld.y *= fac;
+      }
+      double cr, ci = 0.0;
+      if (CPLX) {
+        const double2 c = reinterpret_cast<const double2*>(coeffs_v)[(long long)o * n_leaves * pp + pt];
+        cr = c.x;
+        ci = c.y;
+      } else {
+        cr = reinterpret_cast<const double*>(coeffs_v)[(long long)o * n_leaves * pp + pt];
+      }
+      acc.x -= cr * fld.x - ci * fld.y;
+      acc.y -= cr * fld.y + ci * fld.x;
+    }
+    r[((long long)l * pp + ncb + i) * nsrc + s0 + s] = make_float2((float)acc.x, (float)acc.y);
+  }
+  // outward normal derivative at the p points of each side:
+  //  S: -u_y on iy=p-1 (W->E)   E: u_x on ix=p-1 (S->N)
+  //  N:  u_y on iy=0   (E->W)   W: -u_x on ix=0  (N->S)
+  for (int e = tid; e < 4 * p * SC; e += RES_NT) {
+    const int st = e / SC, s = e % SC;
+    const int side = st / p, t = st % p;
+    const double* Dm;
+    int base, stride;
+    double fac;
+    if (side == 0) { Dm = D1 + (p - 1) * p; base = t * p; stride = 1; fac = ih; }
+    else if (side == 1) { Dm = D1 + (p - 1) * p; base = p - 1 - t; stride = p; fac = ih; }
+    else if (side == 2) { Dm = D1; base = (p - 1 - t) * p; stride = 1; fac = -ih; }
+    else { Dm = D1; base = t; stride = p; fac = -ih; }
+    double2 v = make_double2(0.0, 0.0);
+    for (int j = 0; j < p; ++j) {
+      const double2 w = u[(base + j * stride) * SC + s];
+      v.x = fma(Dm[j], w.x, v.x);
+      v.y = fma(Dm[j], w.y, v.y);
+    }
+    nd[e] = make_double2(fac * v.x, fac * v.y);
+  }
+  __syncthreads();
+  // impedance rows at the Chebyshev boundary points (side's t-th point, t < p-1)
+  for (int e = tid; e < ncb * SC; e += RES_NT) {
+    const int k = e / SC, s = e % SC;
+    if (s >= sc) continue;
+    const int side = k / m, t = k % m;
+    double2 pt = make_double2(0.0, 0.0);
+    for (int j = 0; j < q; ++j) {
+      const double w = Ps[t * q + j];
+      const double2 g = ts[(side * q + j) * SC + s];
+      pt.x = fma(w, g.x, pt.x);
+      pt.y = fma(w, g.y, pt.y);
+    }
+    const double2 un = nd[(side * p + t) * SC + s];
+    const double2 uv = u[perm[k] * SC + s];
+    // (u_n + i eta u) = (un.x - eta uv.y) + i (un.y + eta uv.x)
+    const double gx = un.x - eta * uv.y, gy = un.y + eta * uv.x;
+    r[((long long)l * pp + k) * nsrc + s0 + s] = make_float2((float)(pt.x - gx), (float)(pt.y - gy));
+  }
+  // outgoing impedance at the Gauss nodes
+  for (int e = tid; e < nq * SC; e += RES_NT) {
+    const int k = e / SC, s = e % SC;
+    if (s >= sc) continue;
+    const int side = k / q, j = k % q;
+    double2 v = make_double2(0.0, 0.0);
+    for (int t = 0; t < p; ++t) {
+      const double2 un = nd[(side * p + t) * SC + s];
+      const double2 uv = u[perm[(side * m + t) % ncb] * SC + s];
+      // (u_n - i eta u) = (un.x + eta uv.y) + i (un.y - eta uv.x)
+      const double w = Qs[j * p + t];
+      v.x = fma(w, un.x + eta * uv.y, v.x);
+      v.y = fma(w, un.y - eta * uv.x, v.y);
+    }
+    t_out[((long long)l * nq + k) * nsrc + s0 + s] = v;
+  }
+}
+
+size_t residual_iti_2d_smem(int p, int q, int SC, int need_uy) {
+  const int pp = p * p;
+  size_t z = (size_t)pp * SC * (need_uy ? 2 : 1) + (size_t)4 * q * SC + (size_t)4 * p * SC;
+  size_t d = 2 * (size_t)pp + 2 * (size_t)p * q;
+  return z * sizeof(double2) + d * sizeof(double) + (size_t)pp * sizeof(int);
+}
+
+cudaError_t residual_iti_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds, int cplx,
+                            double eta, const void* coeffs, const double* inv_half, const double* D1,
+                            const double* D2, const double* Pside, const double* Qside, const int* perm,
+                            const void* u, const void* t_in, const void* f, void* r, void* t_out, int need_uy,
+                            cudaStream_t st) {
+  const int SC = nsrc < RES_SC ? nsrc : RES_SC;
+  const size_t smem = residual_iti_2d_smem(p, q, SC, need_uy);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(residual_iti_2d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(residual_iti_2d_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  dim3 grid(n_leaves, (nsrc + SC - 1) / SC);
+  const double work = 8.0 * n_leaves * (double)nsrc * (p * p * (double)p * (n_ops + 2) + 8.0 * p * q);
+  ProfScope ps(KC_RESIDUAL, st, work);
+  note_launch();
+  if (cplx)
+    residual_iti_2d_kernel<true><<<grid, RES_NT, smem, st>>>(
+        n_leaves, p, q, nsrc, SC, n_ops, kinds, eta, coeffs, inv_half, D1, D2, Pside, Qside, perm,
+        (const double2*)u, (const double2*)t_in, (const double2*)f, (float2*)r, (double2*)t_out, need_uy);
+  else
+    residual_iti_2d_kernel<false><<<grid, RES_NT, smem, st>>>(
+        n_leaves, p, q, nsrc, SC, n_ops, kinds, eta, coeffs, inv_half, D1, D2, Pside, Qside, perm,
+        (const double2*)u, (const double2*)t_in, (const double2*)f, (float2*)r, (double2*)t_out, need_uy);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Interface flux mismatch and boundary-data residual.
 //   hcorr[l][k] = (F[l][k] + F[nbr(l,k)]) / 2   for interior interface nodes,
 //               0                               on the domain boundary;
