@@ -1,13 +1,21 @@
 #!/usr/bin/env python
 """HPS build+solve benchmark on one GB300.
 
-Workload (default): 2D variable-coefficient problem on [-1,1]^2,
-L = d_xx + d_yy + c(x,y), c = 1 + 0.5 * sum of 4 Gaussian bumps (seeded
-centres in [-0.8,0.8]^2, width 0.2); uniform quadtree L=7 (16384 leaves),
-p=16, q=14, DtN; 64 right-hand sides, each a seeded sum of 8 Gaussian
-sources (width 0.1) with Dirichlet data b_j (x^2 - y^2).
+Workload ``poisson`` (default): 2D variable-coefficient problem on
+[-1,1]^2, L = d_xx + d_yy + c(x,y), c = 1 + 0.5 * sum of 4 Gaussian bumps
+(seeded centres in [-0.8,0.8]^2, width 0.2); uniform quadtree L=7 (16384
+leaves), p=16, q=14, DtN; 64 right-hand sides, each a seeded sum of 8
+Gaussian sources (width 0.1) with Dirichlet data b_j (x^2 - y^2).  FP32
+build + FP64 refinement against the plain FP64 path.
 
-One step = build_solver + solve of all 64 right-hand sides.
+Workload ``helmholtz`` (--workload helmholtz): 2D Helmholtz scattering with
+ItI maps, Delta u + k^2 (1 + q) u = f, k = 40, q = 0.5 * sum of 20 seeded
+Gaussian bumps (width 0.05), scattered-field source f = -k^2 q u_in for a
+plane wave u_in at a seeded angle, zero incoming impedance data, eta = k;
+uniform quadtree L=8 (65536 leaves), p=16, q=14, one right-hand side.
+complex64 build + complex128 refinement against the plain complex128 path.
+
+One step = build_solver + solve of all right-hand sides.
 Metric: leaves/s = n_leaves / (t_build + t_solve).
 
   value : inputs already resident in HBM, result left in HBM.
@@ -36,7 +44,11 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-WORKLOAD = dict(name="2D var-coeff DtN, uniform quadtree", L=7, p=16, q=14, nsrc=64)
+WORKLOADS = {
+    "poisson": dict(name="2D var-coeff DtN, uniform quadtree", L=7, p=16, q=14, nsrc=64),
+    "helmholtz": dict(name="2D Helmholtz scattering ItI k=40, uniform quadtree", L=8, p=16, q=14, nsrc=1, k=40.0),
+}
+WORKLOAD = WORKLOADS["poisson"]
 
 
 # ---------------------------------------------------------------------------
@@ -80,6 +92,39 @@ def make_inputs(L, p, q, nsrc, device):
     g = (bp[:, 0] ** 2 - bp[:, 1] ** 2)[:, None] * b[None, :]
     ones = torch.ones_like(c)
     return dom, dict(D_xx_coefficients=ones, D_yy_coefficients=ones, I_coefficients=c), f, g
+
+
+def helmholtz_fields(x, k, seed=40):
+    """(q, u_in) of the scattering workload at points x (..., 2), numpy."""
+    rng = np.random.default_rng(seed)
+    z = rng.uniform(-0.8, 0.8, (20, 2))
+    qv = 0.5 * np.exp(-((x[..., None, :] - z) ** 2).sum(-1) / (2 * 0.05 ** 2)).sum(-1)
+    th = rng.uniform(0, 2 * np.pi)
+    uin = np.exp(1j * k * (x @ np.array([np.cos(th), np.sin(th)])))
+    return qv, uin
+
+
+def make_inputs_helmholtz(L, p, q, k, device):
+    """Domain, coefficients (I = k^2 (1 + q)), source -k^2 q u_in and zero
+    incoming impedance data, generated on `device`."""
+    import torch
+
+    import jaxhps_gb300 as hps
+
+    root = hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0)
+    dom = hps.Domain(p=p, q=q, root=root, L=L)
+    x = torch.as_tensor(dom.interior_points, device=device)
+    rng = np.random.default_rng(40)
+    z = torch.as_tensor(rng.uniform(-0.8, 0.8, (20, 2)), device=device)
+    th = rng.uniform(0, 2 * np.pi)
+    qv = 0.5 * torch.exp(-((x[..., None, :] - z) ** 2).sum(-1) / (2 * 0.05 ** 2)).sum(-1)
+    d = torch.tensor([np.cos(th), np.sin(th)], dtype=torch.float64, device=device)
+    uin = torch.exp(1j * k * (x @ d))
+    f = (-k ** 2 * qv * uin).unsqueeze(-1).contiguous()
+    g = torch.zeros((dom.boundary_points.shape[0], 1), dtype=torch.complex128, device=device)
+    ones = torch.ones_like(qv)
+    return dom, dict(D_xx_coefficients=ones, D_yy_coefficients=ones, I_coefficients=k ** 2 * (1 + qv),
+                     use_ItI=True, eta=k), f, g
 
 
 # ---------------------------------------------------------------------------
@@ -138,6 +183,22 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 
+def cpu_oracle_sample_helmholtz(L_sample=4, p=16, q=14, k=40.0):
+    from oracle import hps_oracle as O
+
+    root = (-1.0, 1.0, -1.0, 1.0)
+    pts = O.leaf_points_2D(O.uniform_leaf_bounds_2D(root, L_sample), p)
+    qv, uin = helmholtz_fields(pts, k)
+    ones = np.ones_like(qv)
+    t0 = time.perf_counter()
+    pr = O.Problem2D(root, L_sample, p, q, {"D_xx": ones, "D_yy": ones, "I": k ** 2 * (1 + qv)}, -k ** 2 * qv * uin,
+                     iti=True, eta=k).build()
+    pr.solve(np.zeros(pr.boundary_points.shape[0], dtype=np.complex128))
+    dt = time.perf_counter() - t0
+    n = 4 ** L_sample
+    return n / dt, dt, n
+
+
 def cpu_oracle_sample(L_sample=5, p=16, q=14, nsrc=64):
     from oracle import hps_oracle as O
 
@@ -170,23 +231,34 @@ def cpu_threads():
 # ---------------------------------------------------------------------------
 
 
+def _cpu_sample(args):
+    if args.workload == "helmholtz":
+        L_s = min(args.ref_L, 4)
+        v, dt, n = cpu_oracle_sample_helmholtz(L_s)
+        what = f"complex128 NumPy/SciPy oracle (ItI), build+solve of the same problem at L={L_s} ({n} leaves, p=16, q=14, 1 RHS)"
+    else:
+        v, dt, n = cpu_oracle_sample(args.ref_L)
+        what = (f"FP64 NumPy/SciPy oracle (CPU restatement of the reference algorithm), build+solve of the same "
+                f"problem at L={args.ref_L} ({n} leaves, p=16, q=14, 64 RHS)")
+    return v, dt, n, what
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    wl = WORKLOADS[args.workload]
     vals = []
     for i in range(args.warmup + args.steps):
-        v, dt, n = cpu_oracle_sample(args.ref_L)
+        v, dt, n, sample = _cpu_sample(args)
         if i >= args.warmup:
             vals.append(v)
     value = float(np.median(vals))
-    sample = (f"FP64 NumPy/SciPy oracle (CPU restatement of the reference algorithm), build+solve of the same "
-              f"problem at L={args.ref_L} ({4 ** args.ref_L} leaves, p=16, q=14, 64 RHS)")
     line = {
         "impl": "reference", "metric": "build+solve leaves/s", "value": value, "unit": "leaves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD["name"], **{k: WORKLOAD[k] for k in
-                                                                                    ("L", "p", "q", "nsrc")}},
+        "dtype": "c128" if args.workload == "helmholtz" else "f64", "data": "synthetic",
+        "config": {"workload": wl["name"], **{k: wl[k] for k in ("L", "p", "q", "nsrc")}},
         "cpu_baseline": {"value": value, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "leaves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -205,12 +277,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["float64", "float32", "mixed"])
     ap.add_argument("--fp64-steps", dest="fp64_steps", type=int, default=1)
-    ap.add_argument("--L", type=int, default=WORKLOAD["L"])
+    ap.add_argument("--L", type=int, default=None)
     ap.add_argument("--ref-L", dest="ref_L", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--breakdown", action="store_true")
+    ap.add_argument("--workload", default="poisson", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.L is None:
+        args.L = wl["L"]
     if args.impl == "reference":
         return run_reference(args)
 
@@ -228,8 +304,13 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    L, p, q, ns = args.L, WORKLOAD["p"], WORKLOAD["q"], WORKLOAD["nsrc"]
-    dom, coeffs, f, g = make_inputs(L, p, q, ns, dev)
+    L, p, q, ns = args.L, wl["p"], wl["q"], wl["nsrc"]
+    if args.workload == "helmholtz":
+        dom, coeffs, f, g = make_inputs_helmholtz(L, p, q, wl["k"], dev)
+    else:
+        dom, coeffs, f, g = make_inputs(L, p, q, ns, dev)
+    arrays = {k: v for k, v in coeffs.items() if isinstance(v, torch.Tensor)}
+    flags = {k: v for k, v in coeffs.items() if not isinstance(v, torch.Tensor)}
     n_leaves = dom.n_leaves
     pde = hps.PDEProblem(dom, source=f, **coeffs)
 
@@ -253,10 +334,12 @@ def main():
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")   # lets a profiler select the timed steps
     e0.record()
     for _ in range(args.steps):
         u = step()
     e1.record()
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     barrier()
     ms = e0.elapsed_time(e1)
@@ -270,16 +353,28 @@ def main():
     ms_per_step = ms / args.steps
     value = world * n_leaves / (ms_per_step / 1e3)
     iters = len(pde._state.history) if getattr(pde, "_state", None) is not None else None
+    pde.reset()                      # the comparison run below needs the memory
+    nat.release_workspace()
+    torch.cuda.empty_cache()
 
     # the plain FP64 GPU path on the same problem: its rate, and the error of
     # this run's solution against it
     err, fp64 = None, None
     if args.precision != "float64":
         pde64 = hps.PDEProblem(dom, source=f, **coeffs)
+        torch.cuda.synchronize()
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record()
         hps.build_solver(pde64, precision="float64")
         u64 = hps.solve(pde64, g, host_device=None)
+        b1.record()
+        torch.cuda.synchronize()
         err = float(((u - u64).abs().max() / u64.abs().max()).item())
-        if args.fp64_steps > 0:
+        if args.fp64_steps <= 0:
+            ms64 = b0.elapsed_time(b1)
+            fp64 = {"value": n_leaves / (ms64 / 1e3), "unit": "leaves/s", "ms_per_step": ms64,
+                    "speedup_of_this_path": ms64 / ms_per_step, "note": "one run, the first of this path"}
+        else:
             torch.cuda.synchronize()
             a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a0.record()
@@ -301,10 +396,11 @@ def main():
     if not args.no_e2e:
         hf = f.cpu().pin_memory()
         hg = g.cpu().pin_memory()
-        hco = {k: v.cpu().pin_memory() for k, v in coeffs.items()}
-        h2d = hf.numel() * 8 + hg.numel() * 8 + sum(v.numel() * 8 for v in hco.values())
-        d2h = n_leaves * p * p * ns * 8
-        pde_h = hps.PDEProblem(dom, source=hf, **hco)
+        hco = {k: v.cpu().pin_memory() for k, v in arrays.items()}
+        h2d = (hf.numel() * hf.element_size() + hg.numel() * hg.element_size() +
+               sum(v.numel() * v.element_size() for v in hco.values()))
+        d2h = n_leaves * p * p * ns * u.element_size()
+        pde_h = hps.PDEProblem(dom, source=hf, **hco, **flags)
 
         def estep():
             pde_h.reset()
@@ -351,25 +447,33 @@ def main():
     else:
         peak = peaks.get("bf16_tflops", 1900.0)
         achieved = k_work / (k_ms / 1e3) / 1e12
+        # the class runs FP32 / complex64 arithmetic on the SIMT pipe (and the
+        # 3xTF32 tensor-core kernel): its own ceiling is the FP32 FMA rate,
+        # 152 SMs x 128 lanes x 2 flop x the sampled SM clock
+        mhz = (clk or {}).get("sm_mhz") or 2070.0
+        fp32_peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                     "frac": achieved / peak, "traffic": None, "kernel": names[dom_cls],
                     "flops_per_launch": k_work / max(k_n, 1),
-                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured" if peaks else "fallback"}
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured" if peaks else "fallback",
+                    "fp32_simt_peak_tflops": fp32_peak, "frac_of_fp32_simt": achieved / fp32_peak}
     roofline["avg_launch_ms"] = avg_ms
     roofline["share_of_step"] = k_ms / ms
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, dt, n = cpu_oracle_sample(args.ref_L)
-        cpu = {"value": v, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
-               "sample": f"FP64 oracle build+solve at L={args.ref_L} ({n} leaves, p=16, q=14, 64 RHS), {dt:.1f} s"}
+        v, dt, n, what = _cpu_sample(args)
+        cpu = {"value": v, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port", "sample": f"{what}, {dt:.1f} s"}
 
-    dtype = {"float64": "f64", "float32": "f32", "mixed": "f32+f64-refinement"}[args.precision]
+    if args.workload == "helmholtz":
+        dtype = {"float64": "c128", "float32": "c64", "mixed": "c64+c128-refinement"}[args.precision]
+    else:
+        dtype = {"float64": "f64", "float32": "f32", "mixed": "f32+f64-refinement"}[args.precision]
     line = {
         "metric": "build+solve leaves/s", "value": value, "unit": "leaves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-        "config": {"workload": WORKLOAD["name"], "L": L, "n_leaves": n_leaves, "p": p, "q": q, "nsrc": ns,
+        "config": {"workload": wl["name"], "L": L, "n_leaves": n_leaves, "p": p, "q": q, "nsrc": ns,
                    "precision": args.precision, "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (operator set is several GB)"},
         "rel_err_vs_fp64": err, "refinement_iterations": iters, "fp64_path": fp64,

@@ -64,6 +64,14 @@ HPS_API long long hps_launch_count(void);
  * wait (its output is then invalid).  Synchronises with the device. */
 HPS_API int hps_gemm_tc_status(void);
 
+/* Which batched products run on the tcgen05 kernel: 0 none (SIMT kernels
+ * only), 1 the shapes where it was measured faster (default; HPS_GEMM_TC=0 in
+ * the environment starts a process at 0), 2 every FP32 and complex64 product
+ * (for tests and measurements).  Returns the previous policy, or -1 for an
+ * invalid one.  Process-wide; not meant to change while work is in flight.
+ * No counterpart in the reference. */
+HPS_API int hps_gemm_policy(int policy);
+
 /* Live profiler.  hps_profile_begin(mask) arms CUDA-event timing of every
  * later launch whose kernel class c has bit (1 << c) set in mask (classes:
  * 1 GEMM, 2 inverse, 3 gather/scatter/assembly, 4 refinement residual),
@@ -224,6 +232,18 @@ typedef struct {
   int* info;          /* (n_merges) or NULL */
   void* workspace;
   size_t workspace_bytes;
+  /* Optional block structure (host arrays; counts 0 = dense products).  C is
+   * zero outside c_rects, rows (i0, n_i) x columns (e0, n_e); B is zero
+   * outside b_rects, rows (e0, n_e) x columns (i0, n_i).  `first` marks the
+   * first rectangle over its column range (C) or row range (B); together the
+   * rectangles must cover every exterior index.  The products S = -D^-1 C,
+   * T_out += B S, h_out += B g~ and B D^-1 then run on the rectangles only
+   * (a row of C touches only the exterior of the children sharing that
+   * interface point: 1/4 of it in the ItI and 3D merges, 1/2 in 2D DtN). */
+  int n_c_rects;
+  const int* c_rects; /* (n_c_rects, 5): i0, n_i, e0, n_e, first */
+  int n_b_rects;
+  const int* b_rects; /* (n_b_rects, 5): e0, n_e, i0, n_i, first */
 } hps_merge_args;
 
 HPS_API size_t hps_merge_level_dtn_workspace_size(const hps_merge_args* a);

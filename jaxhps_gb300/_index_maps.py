@@ -74,6 +74,62 @@ def maps_from_code(code: np.ndarray, n_ext: int, n_int: int) -> MergeMaps:
     return MergeMaps(nch, nb, n_int, n_ext, code, int_c, int_l, ext_c, ext_l, loc)
 
 
+def _runs(keys):
+    """Maximal runs [start, start+len) of equal consecutive keys."""
+    out, i, n = [], 0, len(keys)
+    while i < n:
+        j = i + 1
+        while j < n and keys[j] == keys[i]:
+            j += 1
+        out.append((i, j - i, keys[i]))
+        i = j
+    return out
+
+
+def merge_rects(maps, iti: bool):
+    """Block structure of a merge's C (n_int x n_ext) and B (n_ext x n_int).
+
+    Row i of C holds the partner child's (ItI) or both children's (DtN)
+    exterior entries, column j of B its owner's (ItI) or both children's; all
+    else is zero.  Returns int32 arrays (n, 5) of rectangles
+    (i0, n_i, e0, n_e, first) for C and (e0, n_e, i0, n_i, first) for B, as
+    hps_merge_args takes them, or None when they would not save a fifth of
+    the dense products.  Cached on the maps object."""
+    cache = maps.__dict__.setdefault("_rects", {})
+    if iti in cache:
+        return cache[iti]
+    int_c = np.asarray(maps.int_c)
+    if iti:
+        cset = [frozenset((int(c),)) for c in int_c[:, 1]]
+        bset = [frozenset((int(c),)) for c in int_c[:, 0]]
+    else:
+        cset = bset = [frozenset((int(a), int(b))) for a, b in int_c]
+    ext_runs = _runs([int(c) for c in maps.ext_c])
+    c_rects, b_rects = [], []
+    seen = set()
+    for e0, le, ch in ext_runs:
+        for i0, li, cs in _runs(cset):
+            if ch in cs:
+                c_rects.append((i0, li, e0, le, 0 if e0 in seen else 1))
+                seen.add(e0)
+    seen = set()
+    for e0, le, ch in ext_runs:
+        for i0, li, bs in _runs(bset):
+            if ch in bs:
+                b_rects.append((e0, le, i0, li, 0 if e0 in seen else 1))
+                seen.add(e0)
+    covered_c = {r[2] for r in c_rects}
+    covered_b = {r[0] for r in b_rects}
+    all_e = {e0 for e0, _, _ in ext_runs}
+    out = None
+    work = sum(r[1] * r[3] for r in c_rects) + sum(r[1] * r[3] for r in b_rects)
+    if covered_c == all_e and covered_b == all_e and work <= 0.8 * 2 * maps.n_int * maps.n_ext:
+        out = (np.ascontiguousarray(np.array(c_rects, dtype=np.int32)),
+               np.ascontiguousarray(np.array(b_rects, dtype=np.int32)))
+    cache[iti] = out
+    return out
+
+
 @lru_cache(maxsize=None)
 def quad_merge_maps_dtn(nc: int) -> MergeMaps:
     """2D quad merge of children a,b,c,d (SW,SE,NE,NW) with nc Gauss points

@@ -68,6 +68,7 @@ class MergeArgs(C.Structure):
         ("int_c", vp), ("int_l", vp), ("ext_c", vp), ("ext_l", vp), ("loc", vp),
         ("S", vp), ("g_tilde", vp), ("T_out", vp), ("h_out", vp), ("D_inv", vp), ("BD_inv", vp),
         ("B_out", vp), ("info", vp), ("workspace", vp), ("workspace_bytes", csz),
+        ("n_c_rects", ci), ("c_rects", vp), ("n_b_rects", ci), ("b_rects", vp),
     ]
 
 
@@ -167,6 +168,8 @@ def _declare(lib):
     lib.hps_iti_combine.restype = ci
     lib.hps_residual_iti_2d.argtypes = [P(ResidualIti2DArgs), vp]
     lib.hps_residual_iti_2d.restype = ci
+    lib.hps_gemm_policy.argtypes = [ci]
+    lib.hps_gemm_policy.restype = ci
     lib.hps_assemble_rows_complex.argtypes = [ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp]
     lib.hps_assemble_rows_complex.restype = ci
     lib.hps_gemm_tc_status.argtypes = []
@@ -195,7 +198,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_assemble_rows_complex",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_assemble_rows_complex",
 )
 
 

@@ -11,13 +11,18 @@ moved to ``host_device`` when one is given.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import List, Sequence, Tuple
 
 import numpy as np
 import torch
 
 from . import _native as nat
-from ._index_maps import quad_merge_maps_dtn
+from ._index_maps import merge_rects, quad_merge_maps_dtn
+
+# Block-structured merge products (merge_rects); HPS_MERGE_RECTS=0 selects the
+# dense products.
+_RECTS = os.environ.get("HPS_MERGE_RECTS", "1") != "0"
 
 REAL_TO_COMPLEX = {torch.float64: torch.complex128, torch.float32: torch.complex64}
 
@@ -227,6 +232,10 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
         loc=md["loc"].data_ptr(), S=S.data_ptr(), g_tilde=nat.ptr(g_t), T_out=nat.ptr(T_out),
         h_out=nat.ptr(h_out), D_inv=nat.ptr(D_inv), BD_inv=nat.ptr(BD_inv), B_out=nat.ptr(B),
         info=info.data_ptr(), workspace=None, workspace_bytes=0)
+    rects = merge_rects(maps, iti) if _RECTS else None
+    if rects is not None:
+        a.n_c_rects, a.c_rects = rects[0].shape[0], rects[0].ctypes.data
+        a.n_b_rects, a.b_rects = rects[1].shape[0], rects[1].ctypes.data
     wsb = L.hps_merge_level_dtn_workspace_size(C.byref(a))
     ws = nat.workspace(wsb, dev)
     a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()

@@ -311,21 +311,63 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st, bool iti) {
                                st));
   const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
   T* S = (T*)a->S;
-  HPS_CHECK(gemm_batched<T>(ni, ne, ni, mone, D, ni, (long long)ni * ni, C, ne, (long long)ni * ne, zero_, nullptr,
-                            0, 0, S, ne, (long long)ni * ne, nm, st));
-  if (a->T_out)
-    HPS_CHECK(gemm_batched<T>(ne, ne, ni, one_, B, ni, (long long)ne * ni, S, ne, (long long)ni * ne, one_,
-                              (T*)a->T_out, ne, (long long)ne * ne, (T*)a->T_out, ne, (long long)ne * ne, nm, st));
-  if (with_h) {
-    HPS_CHECK(gemm_batched<T>(ni, ns, ni, mone, D, ni, (long long)ni * ni, dh, ns, (long long)ni * ns, zero_,
-                              nullptr, 0, 0, (T*)a->g_tilde, ns, (long long)ni * ns, nm, st));
-    HPS_CHECK(gemm_batched<T>(ne, ns, ni, one_, B, ni, (long long)ne * ni, (const T*)a->g_tilde, ns,
-                              (long long)ni * ns, one_, (T*)a->h_out, ns, (long long)ne * ns, (T*)a->h_out, ns,
-                              (long long)ne * ns, nm, st));
+  const long long sDD = (long long)ni * ni, sC = (long long)ni * ne, sB = (long long)ne * ni, sT = (long long)ne * ne;
+  const bool rects = a->n_c_rects > 0 && a->n_b_rects > 0;
+  // S = -D^-1 C
+  if (rects) {
+    for (int r = 0; r < a->n_c_rects; ++r) {
+      const int* q = a->c_rects + 5 * r;   // i0, n_i, e0, n_e, first
+      HPS_CHECK(gemm_batched<T>(ni, q[3], q[1], mone, D + q[0], ni, sDD, C + (long long)q[0] * ne + q[2], ne, sC,
+                                q[4] ? zero_ : one_, q[4] ? nullptr : S + q[2], ne, sC, S + q[2], ne, sC, nm, st));
+    }
+  } else {
+    HPS_CHECK(gemm_batched<T>(ni, ne, ni, mone, D, ni, sDD, C, ne, sC, zero_, nullptr, 0, 0, S, ne, sC, nm, st));
   }
-  if (a->BD_inv)
-    HPS_CHECK(gemm_batched<T>(ne, ni, ni, one_, B, ni, (long long)ne * ni, D, ni, (long long)ni * ni, zero_,
-                              nullptr, 0, 0, (T*)a->BD_inv, ni, (long long)ne * ni, nm, st));
+  // T_out = A + B S
+  if (a->T_out) {
+    T* To = (T*)a->T_out;
+    if (rects) {
+      for (int r = 0; r < a->n_b_rects; ++r) {
+        const int* q = a->b_rects + 5 * r;   // e0, n_e, i0, n_i, first
+        HPS_CHECK(gemm_batched<T>(q[1], ne, q[3], one_, B + (long long)q[0] * ni + q[2], ni, sB,
+                                  S + (long long)q[2] * ne, ne, sC, one_, To + (long long)q[0] * ne, ne, sT,
+                                  To + (long long)q[0] * ne, ne, sT, nm, st));
+      }
+    } else {
+      HPS_CHECK(gemm_batched<T>(ne, ne, ni, one_, B, ni, sB, S, ne, sC, one_, To, ne, sT, To, ne, sT, nm, st));
+    }
+  }
+  if (with_h) {
+    T* gt = (T*)a->g_tilde;
+    T* ho = (T*)a->h_out;
+    const long long sg = (long long)ni * ns, sh = (long long)ne * ns;
+    HPS_CHECK(gemm_batched<T>(ni, ns, ni, mone, D, ni, sDD, dh, ns, sg, zero_, nullptr, 0, 0, gt, ns, sg, nm, st));
+    if (rects) {
+      for (int r = 0; r < a->n_b_rects; ++r) {
+        const int* q = a->b_rects + 5 * r;
+        HPS_CHECK(gemm_batched<T>(q[1], ns, q[3], one_, B + (long long)q[0] * ni + q[2], ni, sB,
+                                  gt + (long long)q[2] * ns, ns, sg, one_, ho + (long long)q[0] * ns, ns, sh,
+                                  ho + (long long)q[0] * ns, ns, sh, nm, st));
+      }
+    } else {
+      HPS_CHECK(gemm_batched<T>(ne, ns, ni, one_, B, ni, sB, gt, ns, sg, one_, ho, ns, sh, ho, ns, sh, nm, st));
+    }
+  }
+  // B D^-1
+  if (a->BD_inv) {
+    T* BD = (T*)a->BD_inv;
+    if (rects) {
+      for (int r = 0; r < a->n_b_rects; ++r) {
+        const int* q = a->b_rects + 5 * r;
+        T* o = BD + (long long)q[0] * ni;
+        HPS_CHECK(gemm_batched<T>(q[1], ni, q[3], one_, B + (long long)q[0] * ni + q[2], ni, sB,
+                                  D + (long long)q[2] * ni, ni, sDD, q[4] ? zero_ : one_, q[4] ? nullptr : o, ni, sB,
+                                  o, ni, sB, nm, st));
+      }
+    } else {
+      HPS_CHECK(gemm_batched<T>(ne, ni, ni, one_, B, ni, sB, D, ni, sDD, zero_, nullptr, 0, 0, BD, ni, sB, nm, st));
+    }
+  }
   return HPS_OK;
 }
 
@@ -422,6 +464,8 @@ extern "C" {
 const char* hps_version(void) { return "jaxhps_gb300 0.1.0 (sm_103a)"; }
 
 long long hps_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int hps_gemm_policy(int policy) { return set_gemm_policy(policy); }
 
 int hps_gemm_tc_status(void) { return gemm_tc_error(); }
 
@@ -567,6 +611,38 @@ size_t hps_merge_level_dtn_workspace_size(const hps_merge_args* a) {
   return merge_ws(a, &cv);
 }
 
+// Rectangles of the block-structured merge products: in bounds, and over the
+// exterior index each range is written first by the rectangle marked `first`
+// and only accumulated afterwards, with every exterior index covered.
+static bool rects_ok(int n, const int* r, int n_int, int n_ext, bool c_form) {
+  std::vector<char> done(n_ext, 0);
+  for (int k = 0; k < n; ++k) {
+    const int* q = r + 5 * k;
+    const int i0 = c_form ? q[0] : q[2], li = c_form ? q[1] : q[3];
+    const int e0 = c_form ? q[2] : q[0], le = c_form ? q[3] : q[1];
+    if (i0 < 0 || li <= 0 || i0 + li > n_int || e0 < 0 || le <= 0 || e0 + le > n_ext || (q[4] != 0 && q[4] != 1))
+      return false;
+    for (int e = e0; e < e0 + le; ++e) {
+      if ((bool)done[e] == (bool)q[4]) return false;
+      done[e] = 1;
+    }
+  }
+  for (int e = 0; e < n_ext; ++e)
+    if (!done[e]) return false;
+  return true;
+}
+
+static int check_merge_rects(const hps_merge_args* a, const char* who) {
+  if (a->n_c_rects == 0 && a->n_b_rects == 0) return HPS_OK;
+  if (a->n_c_rects <= 0 || a->n_b_rects <= 0 || !a->c_rects || !a->b_rects ||
+      !rects_ok(a->n_c_rects, a->c_rects, a->n_int, a->n_ext, true) ||
+      !rects_ok(a->n_b_rects, a->b_rects, a->n_int, a->n_ext, false)) {
+    set_error("%s: invalid block rectangles", who);
+    return HPS_ERR_ARG;
+  }
+  return HPS_OK;
+}
+
 int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
   if (!a || a->n_merges <= 0 || a->nch <= 0 || a->nb <= 0 || a->n_int <= 0 || a->n_ext <= 0 || !a->T_children ||
       !a->int_c || !a->int_l || !a->ext_c || !a->ext_l || !a->loc || !a->S) {
@@ -578,6 +654,7 @@ int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
               hps_merge_level_dtn_workspace_size(a));
     return HPS_ERR_WORKSPACE;
   }
+  if (check_merge_rects(a, "hps_merge_level_dtn") != HPS_OK) return HPS_ERR_ARG;
   DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream, false)
 }
 
@@ -592,6 +669,7 @@ int hps_merge_level_iti(const hps_merge_args* a, void* stream) {
               hps_merge_level_dtn_workspace_size(a));
     return HPS_ERR_WORKSPACE;
   }
+  if (check_merge_rects(a, "hps_merge_level_iti") != HPS_OK) return HPS_ERR_ARG;
   DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream, true)
 }
 

@@ -10,9 +10,11 @@
 // complex128 / complex64.
 #include <stdlib.h>
 
+#include <atomic>
 #include <type_traits>
 
 #include "hps_common.cuh"
+
 #include "hps_internal.h"
 
 namespace hps {
@@ -220,13 +222,27 @@ static cudaError_t launch_skinny(int M, int N, int K, T alpha, const T* A, long 
   return cudaGetLastError();
 }
 
-// FP32 products on the tensor cores (gemm_tc.cu) unless HPS_GEMM_TC=0.
-static bool tc_enabled() {
-  static const bool on = [] {
+// Which products run on the tensor cores (gemm_tc.cu): 0 none, 1 the shapes
+// where they were measured faster (default), 2 every FP32 / complex64 product.
+// HPS_GEMM_TC=0 in the environment starts the process at 0; hps_gemm_policy()
+// changes it.
+static std::atomic<int> g_policy{-1};
+
+static int gemm_policy() {
+  int p = g_policy.load(std::memory_order_relaxed);
+  if (p < 0) {
     const char* e = getenv("HPS_GEMM_TC");
-    return !(e && e[0] == '0');
-  }();
-  return on;
+    p = (e && e[0] == '0') ? 0 : 1;
+    g_policy.store(p, std::memory_order_relaxed);
+  }
+  return p;
+}
+
+int set_gemm_policy(int p) {
+  if (p < 0 || p > 2) return -1;
+  const int old = gemm_policy();
+  g_policy.store(p, std::memory_order_relaxed);
+  return old;
 }
 
 template <class T>
@@ -243,11 +259,17 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
       return launch_skinny<T, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
     return launch_skinny<T, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
   }
+  const int pol = gemm_policy();
   if constexpr (std::is_same<T, float>::value) {
     // measured: the tensor-core kernel wins once a tile has enough K-steps to
     // amortise its pipeline prologue and epilogue
-    if (tc_enabled() && M >= 128 && N >= 32 && K >= 128)
+    if (pol == 2 || (pol == 1 && M >= 128 && N >= 32 && K >= 128))
       return gemm_tf32x3(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+  }
+  if constexpr (std::is_same<T, c64>::value) {
+    // complex64 as one real product of size (M, 2N, 2K) on the tensor cores
+    if (alpha.y == 0.f && beta.y == 0.f && (pol == 2 || (pol == 1 && M >= 128 && N >= 16 && K >= 64)))
+      return gemm_tf32x3_c64(M, N, K, alpha.x, A, lda, sA, B, ldb, sB, beta.x, C, ldc, sC, D, ldd, sD, batch, st);
   }
   if (sizeof(T) == 4) {
     const long long tiles128 = (long long)((M + 127) / 128) * ((N + 127) / 128) * batch;

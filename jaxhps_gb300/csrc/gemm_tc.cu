@@ -146,7 +146,16 @@ struct TcCfg {
 
 // Persistent: each CTA loops over (batch, m-tile, n-tile) work items; TMEM
 // and the barriers are set up once per CTA and the barrier phases carry over.
-template <int BN>
+//
+// CPLX: complex64 operands as one real product.  With A (M x K complex,
+// interleaved re/im) read as a real M x 2K matrix and B (K x N complex)
+// expanded to the real 2K x 2N matrix with 2x2 blocks [[Br, Bi], [-Bi, Br]],
+// the real product is C (M x N complex, interleaved) itself:
+//   C[m][2n]   = sum_k Ar Br - Ai Bi,   C[m][2n+1] = sum_k Ar Bi + Ai Br.
+// The kernel then runs on the real dimensions (M, 2N, 2K); only the B
+// staging differs: a K-tile of 32 real rows is 16 complex rows, copied raw
+// and expanded while it is split into TF32 hi / lo.
+template <int BN, bool CPLX>
 __global__ void __launch_bounds__(TC_NT)
 gemm_tf32x3_kernel(int M, int N, int K, float alpha, const float* __restrict__ A, long long lda, long long sA,
                    const float* __restrict__ B, long long ldb, long long sB, float beta, const float* C,
@@ -159,6 +168,9 @@ gemm_tf32x3_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
   constexpr int NS = Cfg::NS;
   constexpr int A_F4 = TC_BM * TC_BK / 4 / TC_NT;   // 16-byte chunks per thread, A tile (4)
   constexpr int B_F4 = TC_BK * BN / 4 / TC_NT;      // 16-byte chunks per thread, B tile (2 or 4)
+  constexpr int B_ROWS = CPLX ? TC_BK / 2 : TC_BK;  // rows of B copied per K-tile
+  constexpr int B_F4L = B_ROWS * BN / 4 / TC_NT;    // 16-byte copies per thread, B tile
+  const int KB = CPLX ? K / 2 : K;                  // rows of B in global memory
   constexpr int OUT_LD = BN + 1;                     // epilogue staging stride (odd: conflict-free)
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char* smem =
@@ -223,13 +235,13 @@ gemm_tf32x3_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
         }
       }
 #pragma unroll
-      for (int i = 0; i < B_F4; ++i) {
+      for (int i = 0; i < B_F4L; ++i) {
         const int f = tid + TC_NT * i;
         const int kr = f / (BN / 4), nn = (f % (BN / 4)) * 4;
-        const int gk = k0 + kr, gn = n0 + nn;
+        const int gk = (CPLX ? k0 / 2 : k0) + kr, gn = n0 + nn;
         unsigned char* dst = sb + Cfg::OFF_BRAW + kr * (BN * 4) + nn * 4;
-        const float* src = Bb + (long long)(gk < K ? gk : 0) * ldb + (gn < N ? gn : 0);
-        const int avail = (gk < K) ? max(0, min(4, N - gn)) : 0;
+        const float* src = Bb + (long long)(gk < KB ? gk : 0) * ldb + (gn < N ? gn : 0);
+        const int avail = (gk < KB) ? max(0, min(4, N - gn)) : 0;
         if (vecB) {
           cp_async16(dst, src, avail * 4);
         } else {
@@ -262,8 +274,17 @@ gemm_tf32x3_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
       for (int i = 0; i < B_F4; ++i) {
         const int f = tid + TC_NT * i;
         const int nn = f % BN, kq = (f / BN) * 4;
-        const float4 x = make_float4(rb[(kq + 0) * BN + nn], rb[(kq + 1) * BN + nn], rb[(kq + 2) * BN + nn],
-                                     rb[(kq + 3) * BN + nn]);
+        float4 x;
+        if (CPLX) {
+          // real rows kq..kq+3 are complex rows kq/2, kq/2+1; an odd real row
+          // holds (-Bi, Br) where an even one holds (Br, Bi)
+          const int r0 = (kq >> 1) * BN, r1 = r0 + BN, nx = nn ^ 1;
+          const float sg = (nn & 1) ? 1.0f : -1.0f;
+          x = make_float4(rb[r0 + nn], sg * rb[r0 + nx], rb[r1 + nn], sg * rb[r1 + nx]);
+        } else {
+          x = make_float4(rb[(kq + 0) * BN + nn], rb[(kq + 1) * BN + nn], rb[(kq + 2) * BN + nn],
+                          rb[(kq + 3) * BN + nn]);
+        }
         store_split4(st_base + Cfg::OFF_BHI, st_base + Cfg::OFF_BLO, nn, kq, x);
       }
       // make the generic-proxy stores visible to the tensor core (async proxy)
@@ -370,12 +391,12 @@ int gemm_tc_error() {
   return h;
 }
 
-template <int BN>
+template <int BN, bool CPLX>
 static cudaError_t launch_tc(int M, int N, int K, float alpha, const float* A, long long lda, long long sA,
                              const float* B, long long ldb, long long sB, float beta, const float* C, long long ldc,
                              long long sC, float* D, long long ldd, long long sD, int batch, cudaStream_t st) {
   const size_t smem = tc_smem_bytes<BN>();
-  cudaFuncSetAttribute(gemm_tf32x3_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(gemm_tf32x3_kernel<BN, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   static int sms = 0;
   if (!sms) {
     int dev = 0;
@@ -384,7 +405,7 @@ static cudaError_t launch_tc(int M, int N, int K, float alpha, const float* A, l
     if (sms <= 0) sms = 148;
   }
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gemm_tf32x3_kernel<BN>, TC_NT, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gemm_tf32x3_kernel<BN, CPLX>, TC_NT, smem);
   if (per_sm < 1) per_sm = 1;
   const long long n_tiles = (long long)batch * ((M + TC_BM - 1) / TC_BM) * ((N + BN - 1) / BN);
   const long long grid = n_tiles < (long long)sms * per_sm ? n_tiles : (long long)sms * per_sm;
@@ -393,8 +414,8 @@ static cudaError_t launch_tc(int M, int N, int K, float alpha, const float* A, l
   const int vecB = (ldb % 4 == 0) && (sB % 4 == 0) && ((reinterpret_cast<uintptr_t>(B) & 15) == 0);
   ProfScope ps(KC_GEMM, st, 2.0 * (double)M * N * K * batch);
   note_launch();
-  gemm_tf32x3_kernel<BN><<<(unsigned)grid, TC_NT, smem, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
-                                                              sC, D, ldd, sD, batch, vecA, vecB);
+  gemm_tf32x3_kernel<BN, CPLX><<<(unsigned)grid, TC_NT, smem, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
+                                                                    ldc, sC, D, ldd, sD, batch, vecA, vecB);
   return cudaGetLastError();
 }
 
@@ -404,8 +425,26 @@ cudaError_t gemm_tf32x3(int M, int N, int K, float alpha, const float* A, long l
   if (M <= 0 || N <= 0 || batch <= 0) return cudaSuccess;
   if (K <= 0) return cudaErrorInvalidValue;   // callers keep K = 0 on the SIMT path
   if (N >= 128)
-    return launch_tc<128>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
-  return launch_tc<64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+    return launch_tc<128, false>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+  return launch_tc<64, false>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+}
+
+// complex64 with real alpha, beta: the real product of the interleaved views
+// on dimensions (M, 2N, 2K), strides in floats.
+cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long long lda, long long sA,
+                            const c64* B, long long ldb, long long sB, float beta, const c64* C, long long ldc,
+                            long long sC, c64* D, long long ldd, long long sD, int batch, cudaStream_t st) {
+  if (M <= 0 || N <= 0 || batch <= 0) return cudaSuccess;
+  if (K <= 0) return cudaErrorInvalidValue;
+  const float* Af = reinterpret_cast<const float*>(A);
+  const float* Bf = reinterpret_cast<const float*>(B);
+  const float* Cf = reinterpret_cast<const float*>(C);
+  float* Df = reinterpret_cast<float*>(D);
+  if (2 * N >= 128)
+    return launch_tc<128, true>(M, 2 * N, 2 * K, alpha, Af, 2 * lda, 2 * sA, Bf, 2 * ldb, 2 * sB, beta, Cf, 2 * ldc,
+                                2 * sC, Df, 2 * ldd, 2 * sD, batch, st);
+  return launch_tc<64, true>(M, 2 * N, 2 * K, alpha, Af, 2 * lda, 2 * sA, Bf, 2 * ldb, 2 * sB, beta, Cf, 2 * ldc,
+                             2 * sC, Df, 2 * ldd, 2 * sD, batch, st);
 }
 
 }  // namespace hps

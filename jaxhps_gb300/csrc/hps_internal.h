@@ -29,7 +29,12 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
 cudaError_t gemm_tf32x3(int M, int N, int K, float alpha, const float* A, long long lda, long long sA,
                         const float* B, long long ldb, long long sB, float beta, const float* C, long long ldc,
                         long long sC, float* D, long long ldd, long long sD, int batch, cudaStream_t st);
+cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long long lda, long long sA,
+                            const c64* B, long long ldb, long long sB, float beta, const c64* C, long long ldc,
+                            long long sC, c64* D, long long ldd, long long sD, int batch, cudaStream_t st);
 int gemm_tc_error();
+// Sets the tensor-core policy of gemm_batched (0, 1, 2); returns the old one.
+int set_gemm_policy(int p);
 
 // Largest n served by the register-resident single-CTA kernel.
 int inverse_small_nmax(int dtype);

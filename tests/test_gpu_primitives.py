@@ -129,3 +129,59 @@ def test_gemm_tensor_core_path(cuda, m, n, k, batch, odd):
     err = np.abs(tC.cpu().numpy() - ref).max() / np.abs(ref).max()
     assert err < 2e-6 * max(1.0, np.sqrt(k / 64)), err
     assert nat.load_library().hps_gemm_tc_status() == 0
+
+
+@pytest.mark.parametrize("m,n,k,batch,odd", [(196, 64, 196, 3, False), (300, 20, 150, 2, False), (257, 33, 131, 2, True),
+                                             (1100, 300, 257, 1, False)])
+def test_gemm_tensor_core_complex64(cuda, m, n, k, batch, odd):
+    """complex64 products on the tcgen05 kernel (one real product of the
+    interleaved A with the 2x2-block expansion of B): complex64-level
+    accuracy, ragged tiles, unaligned leading dimensions, C aliasing D."""
+    from jaxhps_gb300 import _native as nat
+
+    rng = np.random.default_rng(m + n + k + 1)
+    pad = 1 if odd else 0
+
+    def cr(*shape):
+        return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+    Ab, B, Cm = cr(batch, m, k + pad), cr(batch, k, n), cr(batch, m, n)
+    tA = torch.as_tensor(Ab, device=cuda)[:, :, :k]
+    tB, tC = torch.as_tensor(B, device=cuda), torch.as_tensor(Cm, device=cuda)
+    nat.gemm(tA, tB, tC, alpha=0.75, beta=-1.25, Cmat=tC)
+    ref = 0.75 * (Ab[:, :, :k].astype(np.complex128) @ B) - 1.25 * Cm
+    err = np.abs(tC.cpu().numpy() - ref).max() / np.abs(ref).max()
+    # FP32 accumulation over the 2k real terms of each complex dot product
+    assert err < 2e-6 * max(1.0, np.sqrt(2 * k / 64)), err
+    assert nat.load_library().hps_gemm_tc_status() == 0
+
+
+@pytest.mark.parametrize("dt,m,n,k,batch", [("c64", 56, 14, 14, 3), ("f32", 5, 3, 7, 2), ("f32", 56, 64, 256, 2),
+                                            ("c64", 130, 33, 17, 2), ("c64", 256, 56, 60, 4), ("f32", 64, 1, 40, 3)])
+def test_gemm_policy_every_product_on_tensor_cores(cuda, dt, m, n, k, batch):
+    """hps_gemm_policy(2) sends every FP32 / complex64 product to the tcgen05
+    kernel, including tiles far below its 128-row tile and K below one
+    K-step: results stay at FP32 accuracy; the policy is restored."""
+    from jaxhps_gb300 import _native as nat
+
+    L = nat.load_library()
+    rng = np.random.default_rng(m * n + k)
+    if dt == "c64":
+        def r(*s):
+            return (rng.standard_normal(s) + 1j * rng.standard_normal(s)).astype(np.complex64)
+    else:
+        def r(*s):
+            return rng.standard_normal(s).astype(np.float32)
+    A, B, Cm = r(batch, m, k), r(batch, k, n), r(batch, m, n)
+    tA, tB, tC = (torch.as_tensor(x, device=cuda) for x in (A, B, Cm))
+    old = L.hps_gemm_policy(2)
+    try:
+        nat.gemm(tA, tB, tC, alpha=1.5, beta=0.5, Cmat=tC)
+        torch.cuda.synchronize()
+    finally:
+        L.hps_gemm_policy(old)
+    assert old == 1
+    ref = 1.5 * (A.astype(np.complex128) @ B) + 0.5 * Cm
+    err = np.abs(tC.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err < 3e-6 * max(1.0, np.sqrt(2 * k / 64)), err
+    assert L.hps_gemm_tc_status() == 0
