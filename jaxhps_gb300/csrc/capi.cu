@@ -102,7 +102,12 @@ struct Profiler {
 };
 static Profiler g_prof;
 
+// Scopes nest (an inversion's panel kernels and GEMM updates): only the
+// outermost records, so no launch is counted twice.
+static thread_local int g_prof_depth = 0;
+
 ProfScope::ProfScope(int cls, cudaStream_t s, double w) : on(false), st(s), slot(-1) {
+  if (++g_prof_depth > 1) return;
   if (cls <= 0 || cls >= N_KC || !(g_prof.mask & (1u << cls))) return;
   if (g_prof.used * 2 + 2 > (int)g_prof.ev.size()) {
     for (int i = 0; i < 256; ++i) {
@@ -122,6 +127,7 @@ ProfScope::ProfScope(int cls, cudaStream_t s, double w) : on(false), st(s), slot
 
 ProfScope::~ProfScope() {
   if (on) cudaEventRecord(g_prof.ev[2 * slot + 1], st);
+  --g_prof_depth;
 }
 
 void set_error(const char* fmt, ...) {

@@ -46,9 +46,10 @@ void note_launch();
 // Kernel classes for the live profiler (hps_profile_begin/end).
 enum KernelClass : int { KC_GEMM = 1, KC_INVERSE = 2, KC_MOVE = 3, KC_RESIDUAL = 4 };
 
-// RAII scope placed around one kernel launch: when the profiler is armed for
-// `cls`, records a CUDA event pair on `st` around the launch and adds the
-// launch's algorithmic flop (or byte) count.
+// RAII scope placed around one kernel launch (or a sequence of them): when
+// the profiler is armed for `cls`, records a CUDA event pair on `st` around
+// it and adds its algorithmic flop (or byte) count.  Scopes opened inside
+// another scope record nothing; the outermost one owns the time.
 struct ProfScope {
   bool on;
   cudaStream_t st;

@@ -188,7 +188,9 @@ constexpr int SB_TY = 16, SB_TX = 32;
 template <class T>
 size_t inv_sblock_smem(int n, int KB) {
   const int ldm = n + 1;
-  return sizeof(T) * ((size_t)n * ldm + (size_t)KB * n) + sizeof(int) * 2 * (size_t)n + (size_t)n + 16;
+  // M | G (KB x n, the sweep) sharing storage with the panel's two row
+  // buffers (2 x n x KB) | piv | colof | used
+  return sizeof(T) * ((size_t)n * ldm + 2 * (size_t)KB * n) + sizeof(int) * 2 * (size_t)n + (size_t)n + 16;
 }
 
 template <class T, int KB, int RN>
@@ -197,25 +199,25 @@ inv_sblock_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T
                   int* info) {
   using MagT = typename MagOf<T>::type;
   constexpr int RA = 4;
+  constexpr int NW = SB_NT / 32;
   extern __shared__ __align__(16) unsigned char sbraw[];
   const int ldm = n + 1;
   T* M = reinterpret_cast<T*>(sbraw);
-  T* G = M + (size_t)n * ldm;
-  int* piv = reinterpret_cast<int*>(G + (size_t)KB * n);
+  T* G = M + (size_t)n * ldm;        // sweep: pivot rows (KB x n)
+  T* PB = G;                         // panel: 2 buffers of every row's panel segment, [c2][row] (KB x n each)
+  int* piv = reinterpret_cast<int*>(G + 2 * (size_t)KB * n);
   int* colof = piv + n;
   unsigned char* used = reinterpret_cast<unsigned char*>(colof + n);
-  __shared__ T rowr[KB];
   __shared__ int Rs[KB];
-  __shared__ MagT wbest[SB_NT / 32];
-  __shared__ int widx[SB_NT / 32];
-  __shared__ int s_r;
-  __shared__ T s_pinv;
+  __shared__ MagT cand_m[2][NW];
+  __shared__ int cand_i[2][NW];
   __shared__ int s_info;
 
   const long long bb = blockIdx.x;
   const T* Ab = A + bb * sA;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ty = tid / SB_TX, tx = tid % SB_TX;
+  const bool has_row = tid < n;   // thread tid owns row tid during the panels (n <= SB_NT)
 
   for (int e = tid; e < n * n; e += SB_NT) {
     const int i = e / n, j = e % n;
@@ -225,90 +227,112 @@ inv_sblock_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T
   if (tid == 0) s_info = 0;
   __syncthreads();
 
+  // warp-level arg-max of (magnitude, row), ties to the smaller row; lane 0
+  // publishes the warp's candidate
+  auto publish_candidate = [&](int buf, MagT mg, int bi) {
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const MagT ob = __shfl_xor_sync(0xffffffffu, mg, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ob > mg || (ob == mg && oi < bi)) {
+        mg = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      cand_m[buf][warp] = mg;
+      cand_i[buf][warp] = bi;
+    }
+  };
+
   for (int k0 = 0; k0 < n; k0 += KB) {
     const int bw = min(KB, n - k0);
-    // ---- panel: Gauss-Jordan restricted to columns k0 .. k0+bw-1
-    for (int c = 0; c < bw; ++c) {
-      const int col = k0 + c;
+    // ---- panel: Gauss-Jordan restricted to columns k0 .. k0+bw-1, one
+    // barrier per column.  Each thread keeps its row's panel segment in
+    // registers and publishes it (double-buffered) so that every thread can
+    // form the scaled pivot row itself after the barrier.
+    T rv[KB];
+    int ust = has_row ? used[tid] : 1;   // 0 free, 1 pivot of an earlier block, 2 of this block
+#pragma unroll
+    for (int c2 = 0; c2 < KB; ++c2) rv[c2] = (has_row && c2 < bw) ? M[tid * ldm + k0 + c2] : zero<T>();
+    if (has_row) {
+#pragma unroll
+      for (int c2 = 0; c2 < KB; ++c2) PB[c2 * n + tid] = rv[c2];   // consecutive rows: conflict-free
+    }
+    publish_candidate(0, (has_row && !ust) ? nan_to_inf(pivmag(rv[0])) : (MagT)-1, (has_row && !ust) ? tid : n);
+    __syncthreads();
+    // unrolled over the block: c is a constant in each copy, so rv[c] and the
+    // (c2 == c) choices below are plain register accesses
+#pragma unroll
+    for (int c = 0; c < KB; ++c) {
+      if (c >= bw) break;
+      const int pb = c & 1;
       MagT best = -1;
-      int bi = n;
-      for (int i = tid; i < n; i += SB_NT) {
-        if (!used[i]) {
-          const MagT mg = nan_to_inf(pivmag(M[i * ldm + col]));
-          if (mg > best) {
-            best = mg;
-            bi = i;
-          }
-        }
-      }
+      int r = n;
 #pragma unroll
-      for (int off = 16; off; off >>= 1) {
-        const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) {
+      for (int w = 0; w < NW; ++w) {
+        const MagT ob = cand_m[pb][w];
+        const int oi = cand_i[pb][w];
+        if (ob > best || (ob == best && oi < r)) {
           best = ob;
-          bi = oi;
+          r = oi;
         }
       }
-      if (lane == 0) {
-        wbest[warp] = best;
-        widx[warp] = bi;
-      }
-      __syncthreads();
-      if (warp == 0) {
-        best = lane < SB_NT / 32 ? wbest[lane] : (MagT)-1;
-        bi = lane < SB_NT / 32 ? widx[lane] : n;
-#pragma unroll
-        for (int off = 16; off; off >>= 1) {
-          const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
-          const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) {
-            best = ob;
-            bi = oi;
-          }
-        }
-        const T pv = (best > 0) ? rcp_(M[bi * ldm + col]) : zero<T>();
-        if (lane < bw) rowr[lane] = mul(M[bi * ldm + k0 + lane], pv);
-        if (lane == 0) {
-          s_r = bi;
-          s_pinv = pv;
-          used[bi] = 2;
-          Rs[c] = bi;
-          piv[col] = bi;
-          colof[bi] = col;
-          if (!(best > 0) && s_info == 0) s_info = col + 1;
-        }
-      }
-      __syncthreads();
-      const int r = s_r;
-      const T pinv = s_pinv;  // read from shared: row r is rewritten below
-      // one thread per row: no two threads touch the same row of the panel;
-      // the row is staged in registers so its loads are issued together
+      // r < n: rows not yet pivots remain (n - k0 - c of them), each a candidate
+      if (r >= n) r = 0;
+      const T* prow = PB + (size_t)pb * n * KB + r;
       T rr[KB];
 #pragma unroll
-      for (int c2 = 0; c2 < KB; ++c2) rr[c2] = (c2 < bw) ? rowr[c2] : zero<T>();
-      for (int i = tid; i < n; i += SB_NT) {
-        T* Mi = M + i * ldm + k0;
-        T rv[KB];
+      for (int c2 = 0; c2 < KB; ++c2) rr[c2] = prow[c2 * n];   // one address per load: broadcast
+      T pinv = zero<T>();
 #pragma unroll
-        for (int c2 = 0; c2 < KB; ++c2) rv[c2] = (c2 < bw) ? Mi[c2] : zero<T>();
-        T f = zero<T>();
+      for (int c2 = 0; c2 < KB; ++c2)
+        if (c2 == c) pinv = (best > 0) ? rcp_(rr[c2]) : zero<T>();
 #pragma unroll
-        for (int c2 = 0; c2 < KB; ++c2)
-          if (c2 == c) f = rv[c2];
-        if (i == r) {
+      for (int c2 = 0; c2 < KB; ++c2) rr[c2] = mul(rr[c2], pinv);
+      if (tid == 0) {
+        Rs[c] = r;
+        piv[k0 + c] = r;
+        colof[r] = k0 + c;
+        if (!(best > 0) && s_info == 0) s_info = k0 + c + 1;
+      }
+      if (has_row) {
+        if (tid == r) {
 #pragma unroll
           for (int c2 = 0; c2 < KB; ++c2) rv[c2] = (c2 == c) ? pinv : rr[c2];
+          ust = 2;
         } else {
+          T f = zero<T>();
+#pragma unroll
+          for (int c2 = 0; c2 < KB; ++c2)
+            if (c2 == c) f = rv[c2];
 #pragma unroll
           for (int c2 = 0; c2 < KB; ++c2) rv[c2] = (c2 == c) ? neg(mul(f, pinv)) : fms_(f, rr[c2], rv[c2]);
         }
+      }
+      if (c + 1 < bw) {
+        if (has_row) {
+          T* dst = PB + (size_t)(pb ^ 1) * n * KB + tid;
+#pragma unroll
+          for (int c2 = 0; c2 < KB; ++c2) dst[c2 * n] = rv[c2];
+        }
+        T nxt = zero<T>();
 #pragma unroll
         for (int c2 = 0; c2 < KB; ++c2)
-          if (c2 < bw) Mi[c2] = rv[c2];
+          if (c2 == c + 1) nxt = rv[c2];
+        publish_candidate(pb ^ 1, (has_row && !ust) ? nan_to_inf(pivmag(nxt)) : (MagT)-1,
+                          (has_row && !ust) ? tid : n);
+        __syncthreads();
       }
-      __syncthreads();
     }
+    __syncthreads();   // every thread has read the last pivot row before G overwrites the buffers
+    if (has_row) {
+#pragma unroll
+      for (int c2 = 0; c2 < KB; ++c2)
+        if (c2 < bw) M[tid * ldm + k0 + c2] = rv[c2];
+      used[tid] = (unsigned char)ust;
+    }
+    __syncthreads();
     // ---- pivot rows outside the panel, before the sweep
     for (int e = tid; e < bw * n; e += SB_NT) {
       const int k = e / n, j = e % n;
@@ -329,6 +353,7 @@ inv_sblock_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T
           acc[a][b] = (i < n && j < n && !isR[a]) ? M[i * ldm + j] : zero<T>();
         }
       }
+#pragma unroll 4
       for (int k = 0; k < bw; ++k) {
         T z[RA], gk[RN];
 #pragma unroll
@@ -845,20 +870,27 @@ __global__ void gje_permute_out_kernel(int n, const T* Mat, const int* piv, cons
 // launches when the tableau fits in shared memory.
 constexpr size_t SB_SMEM_MAX = 220 * 1024;
 
+// Panel width: 16 columns of 4-byte elements, 8 of 8-byte ones (the panel
+// keeps two rows of it in registers, fully unrolled).
+template <class T>
+constexpr int sb_kb() {
+  return sizeof(T) <= 4 ? 16 : 8;
+}
+
 template <class T>
 static bool sblock_fits(int n) {
-  return n > 64 && n <= 256 && inv_sblock_smem<T>(n, 16) <= SB_SMEM_MAX;
+  return n > 64 && n <= 256 && inv_sblock_smem<T>(n, sb_kb<T>()) <= SB_SMEM_MAX;
 }
 
 template <class T, int RN>
 static cudaError_t launch_sblock_rn(int n, const T* A, long long lda, long long sA, T* X, long long ldx, long long sX,
                                     int batch, int* info, cudaStream_t st) {
-  const size_t smem = inv_sblock_smem<T>(n, 16);
-  cudaFuncSetAttribute(inv_sblock_kernel<T, 16, RN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t smem = inv_sblock_smem<T>(n, sb_kb<T>());
+  cudaFuncSetAttribute(inv_sblock_kernel<T, sb_kb<T>(), RN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const double cplx = (DTypeOf<T>::value == C64 || DTypeOf<T>::value == C128) ? 4.0 : 1.0;
   ProfScope ps(KC_INVERSE, st, 2.0 * cplx * (double)n * n * n * batch);
   note_launch();
-  inv_sblock_kernel<T, 16, RN><<<batch, SB_NT, smem, st>>>(n, A, lda, sA, X, ldx, sX, info);
+  inv_sblock_kernel<T, sb_kb<T>(), RN><<<batch, SB_NT, smem, st>>>(n, A, lda, sA, X, ldx, sX, info);
   return cudaGetLastError();
 }
 
@@ -942,6 +974,10 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
                             long long sX, int batch, int* info, void* ws, size_t ws_bytes,
                             cudaStream_t st) {
   if (n <= 0 || batch <= 0) return cudaSuccess;
+  // one profiler record for the whole inversion (its panel kernels and the
+  // GEMM updates nested below): 2 n^3 flops per matrix, x4 for complex
+  const double cplx = (sizeof(T) == 16 || DTypeOf<T>::value == C64) ? 4.0 : 1.0;
+  ProfScope whole(KC_INVERSE, st, 2.0 * cplx * (double)n * n * n * batch);
   if (info) cudaMemsetAsync(info, 0, sizeof(int) * (size_t)batch, st);
   const int dtype = DTypeOf<T>::value;
   if constexpr (sizeof(T) <= 8) {

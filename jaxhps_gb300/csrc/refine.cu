@@ -561,6 +561,21 @@ __device__ __forceinline__ df32 df_split(double x) {
 }
 __device__ __forceinline__ double df_join(float s, float e) { return (double)s + (double)e; }
 
+// (s, e) with |e| <= |s| ulp-wise; FastTwoSum on the FP32 pipe
+__device__ __forceinline__ df32 df_norm(float s, float e) {
+  const float h = s + e;
+  return df32{h, e - (h - s)};
+}
+
+// a * b for pairs, renormalised (FP32 pipe only)
+__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_norm(p, e);
+}
+
 // (s, e) += a * b ; s carries the running sum, e the low-order terms
 __device__ __forceinline__ void df_mac(float& s, float& e, df32 a, df32 b) {
   const float p = a.hi * b.hi;
@@ -588,8 +603,10 @@ jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lo
   const int nq = 4 * q;
   df32* u = reinterpret_cast<df32*>(smf);          // pp * SC
   df32* uy = u + pp * RES_SC;                       // pp * SC when D_xy is active
-  df32* nd = uy + (need_uy ? pp * RES_SC : 0);      // 4p * SC
-  df32* D1 = nd + 4 * p * RES_SC;
+  df32* nd = uy + (need_uy ? pp * RES_SC : 0);      // 4p * SC; before that, the coefficient pairs
+  df32* cf = nd;                                    // n_ops * ni: c * scale of every interior point
+  const int ndr = max(4 * p * RES_SC, n_ops * ni);
+  df32* D1 = nd + ndr;
   df32* D2 = D1 + pp;
   df32* Ps = D2 + pp;
   df32* Qs = Ps + p * q;
@@ -602,11 +619,27 @@ jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lo
   const int tid = threadIdx.x;
   const double ih = inv_half[l];
   const double ih2 = ih * ih;
+  const df32 ihd = df_split(ih), mihd = df32{-ihd.hi, -ihd.lo};
 
   for (int e = tid; e < pp; e += RES_NT) {
     D1[e] = df_split(D1g[e]);
     D2[e] = df_split(D2g[e]);
     perm[e] = perm_g[e];
+  }
+  // the FP64 coefficient times the operator's 1/h scaling, split once per
+  // point (not per right-hand side): the only FP64 arithmetic of the PDE rows
+  for (int e = tid; e < n_ops * ni; e += RES_NT) {
+    const int o = e / ni, i = e % ni;
+    double sc;
+    switch ((int)((kinds >> (4 * o)) & 15ull)) {
+      case OP_XX:
+      case OP_YY: sc = ih2; break;
+      case OP_X:
+      case OP_XY: sc = ih; break;
+      case OP_Y: sc = -ih; break;
+      default: sc = 1.0;
+    }
+    cf[e] = df_split(sc * coeffs[(long long)o * n_leaves * pp + (long long)l * pp + ncb + i]);
   }
   for (int e = tid; e < p * q; e += RES_NT) {
     Ps[e] = df_split(Pside_g[e]);
@@ -638,8 +671,7 @@ jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lo
       hs *= 0.5f;
       he *= 0.5f;
     }
-    const double v = df_join(hs, he);
-    u[perm[k] * RES_SC + s] = df_split(v);
+    u[perm[k] * RES_SC + s] = df_norm(hs, he);
   }
   __syncthreads();
   if (need_uy) {
@@ -648,7 +680,7 @@ jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lo
       const int ix = idx / p, iy = idx % p;
       float hs = 0.f, he = 0.f;
       for (int k = 0; k < p; ++k) df_mac(hs, he, D1[iy * p + k], u[(ix * p + k) * RES_SC + s]);
-      uy[e] = df_split(-ih * df_join(hs, he));
+      uy[e] = df_mul(mihd, df_norm(hs, he));
     }
     __syncthreads();
   }
@@ -657,65 +689,58 @@ jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lo
     if (s >= sc) continue;
     const int idx = perm[ncb + i];
     const int ix = idx / p, iy = idx % p;
-    const long long pt = (long long)l * pp + ncb + i;
-    double acc = 0.0;
+    float as = 0.f, ae = 0.f;   // sum over the operators, as a pair
     for (int o = 0; o < n_ops; ++o) {
-      const double c = coeffs[(long long)o * n_leaves * pp + pt];
       float hs = 0.f, he = 0.f;
-      double scale = 1.0;
       switch ((int)((kinds >> (4 * o)) & 15ull)) {
         case OP_XX:
           for (int j = 0; j < p; ++j) df_mac(hs, he, D2[ix * p + j], u[(j * p + iy) * RES_SC + s]);
-          scale = ih2;
           break;
         case OP_YY:
           for (int j = 0; j < p; ++j) df_mac(hs, he, D2[iy * p + j], u[(ix * p + j) * RES_SC + s]);
-          scale = ih2;
           break;
         case OP_X:
           for (int j = 0; j < p; ++j) df_mac(hs, he, D1[ix * p + j], u[(j * p + iy) * RES_SC + s]);
-          scale = ih;
           break;
         case OP_Y:
           for (int j = 0; j < p; ++j) df_mac(hs, he, D1[iy * p + j], u[(ix * p + j) * RES_SC + s]);
-          scale = -ih;
           break;
         case OP_XY:
           for (int j = 0; j < p; ++j) df_mac(hs, he, D1[ix * p + j], uy[(j * p + iy) * RES_SC + s]);
-          scale = ih;
           break;
         default:
           hs = u[idx * RES_SC + s].hi;
           he = u[idx * RES_SC + s].lo;
       }
-      acc = fma(c * scale, df_join(hs, he), acc);
+      df_mac(as, ae, cf[o * ni + i], df32{hs, he});
     }
     const long long o = ((long long)l * ni + i) * nsrc + s0 + s;
-    const double r = r_int[o] - acc;
+    const double r = r_int[o] - df_join(as, ae);
     r_int[o] = r;
     r32[o] = (float)r;
   }
+  __syncthreads();   // nd below reuses the coefficient pairs' storage
   for (int e = tid; e < 4 * p * RES_SC; e += RES_NT) {
     const int st = e / RES_SC, s = e % RES_SC;
     const int side = st / p, t = st % p;
     float hs = 0.f, he = 0.f;
-    double sg;
+    df32 sg;
     if (side == 0) {
       for (int k = 0; k < p; ++k) df_mac(hs, he, D1[(p - 1) * p + k], u[(t * p + k) * RES_SC + s]);
-      sg = ih;
+      sg = ihd;
     } else if (side == 1) {
       const int iy = p - 1 - t;
       for (int j = 0; j < p; ++j) df_mac(hs, he, D1[(p - 1) * p + j], u[(j * p + iy) * RES_SC + s]);
-      sg = ih;
+      sg = ihd;
     } else if (side == 2) {
       const int ix = p - 1 - t;
       for (int k = 0; k < p; ++k) df_mac(hs, he, D1[k], u[(ix * p + k) * RES_SC + s]);
-      sg = -ih;
+      sg = mihd;
     } else {
       for (int j = 0; j < p; ++j) df_mac(hs, he, D1[j], u[(j * p + t) * RES_SC + s]);
-      sg = -ih;
+      sg = mihd;
     }
-    nd[e] = df_split(sg * df_join(hs, he));
+    nd[e] = df_mul(sg, df_norm(hs, he));
   }
   __syncthreads();
   for (int e = tid; e < nq * RES_SC; e += RES_NT) {
@@ -728,10 +753,11 @@ jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lo
   }
 }
 
-size_t jx_update_2d_smem(int p, int q, int need_uy) {
+size_t jx_update_2d_smem(int p, int q, int need_uy, int n_ops) {
   const int pp = p * p;
-  size_t pairs = (size_t)pp * RES_SC * (need_uy ? 2 : 1) + (size_t)4 * p * RES_SC + 2 * (size_t)pp +
-                 2 * (size_t)p * q;
+  const size_t ni = (size_t)pp - 4 * (size_t)(p - 1);
+  const size_t ndr = (size_t)4 * p * RES_SC > n_ops * ni ? (size_t)4 * p * RES_SC : n_ops * ni;
+  size_t pairs = (size_t)pp * RES_SC * (need_uy ? 2 : 1) + ndr + 2 * (size_t)pp + 2 * (size_t)p * q;
   return pairs * sizeof(df32) + (size_t)4 * q * RES_SC * sizeof(float) + (size_t)pp * sizeof(int);
 }
 
@@ -739,7 +765,7 @@ cudaError_t jx_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsign
                          const double* coeffs, const double* inv_half, const double* D1, const double* D2,
                          const double* Pside, const double* Qside, const int* perm, const float* du, const float* dg,
                          double* r_int, float* r32, double* flux, int need_uy, cudaStream_t st) {
-  const size_t smem = jx_update_2d_smem(p, q, need_uy);
+  const size_t smem = jx_update_2d_smem(p, q, need_uy, n_ops);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(jx_update_2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid(n_leaves, (nsrc + RES_SC - 1) / RES_SC);
