@@ -244,6 +244,15 @@ typedef struct {
   const int* c_rects; /* (n_c_rects, 5): i0, n_i, e0, n_e, first */
   int n_b_rects;
   const int* b_rects; /* (n_b_rects, 5): e0, n_e, i0, n_i, first */
+  /* Optional two-colour structure of D (ItI merges; n_x = 0: none).  With
+   * the unknowns permuted by colour_perm (device, n_int: original index of
+   * each permuted position, the first n_x of colour X), D = [[I, D12],
+   * [D21, I]]; D^-1 is then formed from the inverse of the n_x x n_x matrix
+   * W = I - D12 D21 (the reference's _invert_D_ItI,
+   * merge/_schur_complement.py:78-114) instead of inverting D itself.
+   * Requires n_int - n_x == n_x. */
+  int n_x;
+  const int* colour_perm;
 } hps_merge_args;
 
 HPS_API size_t hps_merge_level_dtn_workspace_size(const hps_merge_args* a);

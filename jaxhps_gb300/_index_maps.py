@@ -130,6 +130,49 @@ def merge_rects(maps, iti: bool):
     return out
 
 
+def colour_perm(maps):
+    """Two-colouring of an ItI merge's interface unknowns, or None.
+
+    Unknown u (owned by child own(u), its equation coupling to the partner
+    child par(u)) gets the colour of its owner.  When the children split in
+    two classes with every owner/partner pair across them and the classes
+    hold n_int/2 unknowns each, D = [[I, D12], [D21, I]] in the order
+    returned (colour X first) and its inverse needs only the n_int/2 inverse
+    of I - D12 D21 (hps_merge_args.n_x, colour_perm).  Cached on the maps."""
+    cache = maps.__dict__.setdefault("_colour", {})
+    if "perm" in cache:
+        return cache["perm"]
+    own = np.asarray(maps.int_c)[:, 0]
+    par = np.asarray(maps.int_c)[:, 1]
+    col = {}
+    edges = {}
+    for a, b in zip(own.tolist(), par.tolist()):
+        edges.setdefault(a, set()).add(b)
+        edges.setdefault(b, set()).add(a)
+    ok = True
+    for start in sorted(edges):
+        if start in col:
+            continue
+        col[start] = 0
+        stack = [start]
+        while stack and ok:
+            c = stack.pop()
+            for d in edges[c]:
+                if d not in col:
+                    col[d] = 1 - col[c]
+                    stack.append(d)
+                elif col[d] == col[c]:
+                    ok = False
+    out = None
+    if ok:
+        cu = np.array([col[int(c)] for c in own])
+        x, y = np.nonzero(cu == 0)[0], np.nonzero(cu == 1)[0]
+        if len(x) == len(y) == maps.n_int // 2 and 2 * len(x) == maps.n_int:
+            out = np.ascontiguousarray(np.concatenate([x, y]).astype(np.int32))
+    cache["perm"] = out
+    return out
+
+
 @lru_cache(maxsize=None)
 def quad_merge_maps_dtn(nc: int) -> MergeMaps:
     """2D quad merge of children a,b,c,d (SW,SE,NE,NW) with nc Gauss points

@@ -69,6 +69,7 @@ class MergeArgs(C.Structure):
         ("S", vp), ("g_tilde", vp), ("T_out", vp), ("h_out", vp), ("D_inv", vp), ("BD_inv", vp),
         ("B_out", vp), ("info", vp), ("workspace", vp), ("workspace_bytes", csz),
         ("n_c_rects", ci), ("c_rects", vp), ("n_b_rects", ci), ("b_rects", vp),
+        ("n_x", ci), ("colour_perm", vp),
     ]
 
 

@@ -18,11 +18,24 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from ._index_maps import merge_rects, quad_merge_maps_dtn
+from ._index_maps import colour_perm, merge_rects, quad_merge_maps_dtn
 
 # Block-structured merge products (merge_rects); HPS_MERGE_RECTS=0 selects the
-# dense products.
+# dense products.  ItI merges invert D through its two-colour structure
+# (colour_perm); HPS_MERGE_TWO_COLOUR=0 inverts D directly.
 _RECTS = os.environ.get("HPS_MERGE_RECTS", "1") != "0"
+_TWO_COLOUR = os.environ.get("HPS_MERGE_TWO_COLOUR", "1") != "0"
+
+
+def colour_perm_device(maps, dev):
+    perm = colour_perm(maps)
+    if perm is None:
+        return None
+    cache = maps.__dict__.setdefault("_colour_dev", {})
+    key = str(dev)
+    if key not in cache:
+        cache[key] = torch.as_tensor(perm, device=dev)
+    return cache[key]
 
 REAL_TO_COMPLEX = {torch.float64: torch.complex128, torch.float32: torch.complex64}
 
@@ -236,6 +249,10 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
     if rects is not None:
         a.n_c_rects, a.c_rects = rects[0].shape[0], rects[0].ctypes.data
         a.n_b_rects, a.b_rects = rects[1].shape[0], rects[1].ctypes.data
+    if iti and _TWO_COLOUR:
+        cp = colour_perm_device(maps, dev)
+        if cp is not None:
+            a.n_x, a.colour_perm = n_int // 2, cp.data_ptr()
     wsb = L.hps_merge_level_dtn_workspace_size(C.byref(a))
     ws = nat.workspace(wsb, dev)
     a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()

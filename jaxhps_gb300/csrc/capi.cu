@@ -28,6 +28,14 @@ template <class T>
 cudaError_t row_equilibrate(int batch, int n, T* A, long long lda, long long sA, double* s, cudaStream_t st);
 template <class T>
 cudaError_t col_scale(int batch, int n, T* X, long long ldx, long long sX, const double* s, cudaStream_t st);
+template <class T>
+cudaError_t perm_gather(int batch, int n, int nr, int nc, const T* M, long long sM, const int* perm, int r0, int c0,
+                        T* out, long long sO, cudaStream_t st);
+template <class T>
+cudaError_t perm_scatter(int batch, int n, int nr, int nc, T* M, long long sM, const int* perm, int r0, int c0,
+                         const T* in, long long sI, int add_identity, cudaStream_t st);
+template <class T>
+cudaError_t add_identity(int batch, int n, T* X, long long sX, cudaStream_t st);
 cudaError_t refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
                              double* pts, cudaStream_t st);
 template <class T>
@@ -287,7 +295,13 @@ static size_t merge_ws(const hps_merge_args* a, Carver* cv) {
   cv->take(es * nm * a->n_int * a->n_ext);                       // C
   cv->take(es * nm * a->n_ext * a->n_int);                       // B
   cv->take(es * nm * a->n_int * (a->nsrc > 0 ? a->nsrc : 1));    // dh
-  cv->take(inverse_workspace_bytes(a->dtype, a->n_int, a->n_merges));
+  if (a->n_x > 0) {
+    // two-colour inverse: D12, D21, W, P (n_x^2 each) and W's inverse scratch
+    for (int k = 0; k < 4; ++k) cv->take(es * nm * a->n_x * a->n_x);
+    cv->take(inverse_workspace_bytes(a->dtype, a->n_x, a->n_merges));
+  } else {
+    cv->take(inverse_workspace_bytes(a->dtype, a->n_int, a->n_merges));
+  }
   return cv->used + 256;
 }
 
@@ -302,7 +316,15 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st, bool iti) {
   T* B = (T*)cv.take(sizeof(T) * (size_t)nm * ne * ni);
   if (a->B_out) B = (T*)a->B_out;
   T* dh = (T*)cv.take(sizeof(T) * (size_t)nm * ni * (ns > 0 ? ns : 1));
-  const size_t invb = inverse_workspace_bytes(a->dtype, ni, nm);
+  const int nx = a->n_x;
+  T *X12 = nullptr, *X21 = nullptr, *Wm = nullptr, *Pm = nullptr;
+  if (nx > 0) {
+    X12 = (T*)cv.take(sizeof(T) * (size_t)nm * nx * nx);
+    X21 = (T*)cv.take(sizeof(T) * (size_t)nm * nx * nx);
+    Wm = (T*)cv.take(sizeof(T) * (size_t)nm * nx * nx);
+    Pm = (T*)cv.take(sizeof(T) * (size_t)nm * nx * nx);
+  }
+  const size_t invb = inverse_workspace_bytes(a->dtype, nx > 0 ? nx : ni, nm);
   void* invws = cv.take(invb);
   const bool with_h = ns > 0 && a->h_children && a->h_out && a->g_tilde;
   if (iti)
@@ -313,9 +335,28 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st, bool iti) {
     HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, with_h ? ns : 0, (const T*)a->T_children,
                               with_h ? (const T*)a->h_children : nullptr, a->int_c, a->int_l, a->ext_c, a->ext_l,
                               a->loc, D, C, B, (T*)a->T_out, dh, (T*)a->h_out, st));
-  HPS_CHECK(inverse_batched<T>(ni, D, ni, (long long)ni * ni, D, ni, (long long)ni * ni, nm, a->info, invws, invb,
-                               st));
   const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
+  if (nx > 0) {
+    // D = [[I, D12], [D21, I]] in colour order; W = I - D12 D21,
+    // D^-1 = [[W^-1, -W^-1 D12], [-D21 W^-1, I + D21 W^-1 D12]]
+    const long long sD = (long long)ni * ni, sx = (long long)nx * nx;
+    const int* cp = a->colour_perm;
+    HPS_CHECK(perm_gather<T>(nm, ni, nx, nx, D, sD, cp, 0, nx, X12, sx, st));
+    HPS_CHECK(perm_gather<T>(nm, ni, nx, nx, D, sD, cp, nx, 0, X21, sx, st));
+    HPS_CHECK(gemm_batched<T>(nx, nx, nx, mone, X12, nx, sx, X21, nx, sx, zero_, nullptr, 0, 0, Wm, nx, sx, nm, st));
+    HPS_CHECK(add_identity<T>(nm, nx, Wm, sx, st));
+    HPS_CHECK(inverse_batched<T>(nx, Wm, nx, sx, Wm, nx, sx, nm, a->info, invws, invb, st));
+    HPS_CHECK(gemm_batched<T>(nx, nx, nx, mone, Wm, nx, sx, X12, nx, sx, zero_, nullptr, 0, 0, Pm, nx, sx, nm, st));
+    HPS_CHECK(perm_scatter<T>(nm, ni, nx, nx, D, sD, cp, 0, 0, Wm, sx, 0, st));
+    HPS_CHECK(perm_scatter<T>(nm, ni, nx, nx, D, sD, cp, 0, nx, Pm, sx, 0, st));
+    HPS_CHECK(gemm_batched<T>(nx, nx, nx, mone, X21, nx, sx, Wm, nx, sx, zero_, nullptr, 0, 0, X12, nx, sx, nm, st));
+    HPS_CHECK(perm_scatter<T>(nm, ni, nx, nx, D, sD, cp, nx, 0, X12, sx, 0, st));
+    HPS_CHECK(gemm_batched<T>(nx, nx, nx, mone, X21, nx, sx, Pm, nx, sx, zero_, nullptr, 0, 0, Wm, nx, sx, nm, st));
+    HPS_CHECK(perm_scatter<T>(nm, ni, nx, nx, D, sD, cp, nx, nx, Wm, sx, 1, st));
+  } else {
+    HPS_CHECK(inverse_batched<T>(ni, D, ni, (long long)ni * ni, D, ni, (long long)ni * ni, nm, a->info, invws, invb,
+                                 st));
+  }
   T* S = (T*)a->S;
   const long long sDD = (long long)ni * ni, sC = (long long)ni * ne, sB = (long long)ne * ni, sT = (long long)ne * ne;
   const bool rects = a->n_c_rects > 0 && a->n_b_rects > 0;
@@ -661,6 +702,10 @@ int hps_merge_level_dtn(const hps_merge_args* a, void* stream) {
     return HPS_ERR_WORKSPACE;
   }
   if (check_merge_rects(a, "hps_merge_level_dtn") != HPS_OK) return HPS_ERR_ARG;
+  if (a->n_x != 0) {
+    set_error("hps_merge_level_dtn: the two-colour inverse applies to ItI merges only");
+    return HPS_ERR_ARG;
+  }
   DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream, false)
 }
 
@@ -676,6 +721,10 @@ int hps_merge_level_iti(const hps_merge_args* a, void* stream) {
     return HPS_ERR_WORKSPACE;
   }
   if (check_merge_rects(a, "hps_merge_level_iti") != HPS_OK) return HPS_ERR_ARG;
+  if (a->n_x < 0 || (a->n_x > 0 && (2 * a->n_x != a->n_int || !a->colour_perm))) {
+    set_error("hps_merge_level_iti: two-colour structure needs n_x = n_int / 2 and colour_perm");
+    return HPS_ERR_ARG;
+  }
   DISPATCH(a->dtype, merge_impl, a, (cudaStream_t)stream, true)
 }
 

@@ -194,6 +194,86 @@ cudaError_t col_scale(int batch, int n, T* X, long long ldx, long long sX, const
 }
 
 // ---------------------------------------------------------------------------
+// Permuted block copies for the two-colour inverse of the ItI merge matrix:
+//   gather:  out[b][i][j] = M[b][perm[r0+i]][perm[c0+j]]
+//   scatter: M[b][perm[r0+i]][perm[c0+j]] = in[b][i][j] (+1 on i == j)
+//   add_identity: X[b][i][i] += 1
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void perm_gather_kernel(int n, int nr, int nc, const T* __restrict__ M, long long sM,
+                                   const int* __restrict__ perm, int r0, int c0, T* out, long long sO) {
+  const long long b = blockIdx.y;
+  const long long tot = (long long)nr * nc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / nc), j = (int)(e % nc);
+    out[b * sO + e] = M[b * sM + (long long)perm[r0 + i] * n + perm[c0 + j]];
+  }
+}
+
+template <class T>
+__global__ void perm_scatter_kernel(int n, int nr, int nc, T* M, long long sM, const int* __restrict__ perm, int r0,
+                                    int c0, const T* __restrict__ in, long long sI, int add_identity) {
+  const long long b = blockIdx.y;
+  const long long tot = (long long)nr * nc;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / nc), j = (int)(e % nc);
+    T v = in[b * sI + e];
+    if (add_identity && i == j) v = add(v, one<T>());
+    M[b * sM + (long long)perm[r0 + i] * n + perm[c0 + j]] = v;
+  }
+}
+
+template <class T>
+__global__ void add_identity_kernel(int n, T* X, long long sX) {
+  const long long b = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    X[b * sX + (long long)i * n + i] = add(X[b * sX + (long long)i * n + i], one<T>());
+}
+
+static inline int blocks_for(long long work) {
+  long long g = (work + 255) / 256;
+  return (int)(g < 1 ? 1 : (g > 1024 ? 1024 : g));
+}
+
+template <class T>
+cudaError_t perm_gather(int batch, int n, int nr, int nc, const T* M, long long sM, const int* perm, int r0, int c0,
+                        T* out, long long sO, cudaStream_t st) {
+  const int gx = blocks_for((long long)nr * nc);
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * (double)nr * nc * nb);
+    note_launch();
+    perm_gather_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(n, nr, nc, M + b0 * sM, sM, perm, r0, c0, out + b0 * sO, sO);
+  }
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t perm_scatter(int batch, int n, int nr, int nc, T* M, long long sM, const int* perm, int r0, int c0,
+                         const T* in, long long sI, int add_identity, cudaStream_t st) {
+  const int gx = blocks_for((long long)nr * nc);
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * (double)nr * nc * nb);
+    note_launch();
+    perm_scatter_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(n, nr, nc, M + b0 * sM, sM, perm, r0, c0, in + b0 * sI, sI,
+                                                         add_identity);
+  }
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t add_identity(int batch, int n, T* X, long long sX, cudaStream_t st) {
+  const int gx = blocks_for(n);
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    note_launch();
+    add_identity_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(n, X + b0 * sX, sX);
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Merge gather  (reference: merge/_uniform_2D_DtN.py:206-475,
 // merge/_schur_complement.py:182-237, 3D: merge/_schur_complement.py:293-774)
 //
@@ -464,6 +544,11 @@ cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st) {
   template cudaError_t set_rows<T>(int, int, int, const T*, long long, T*, long long, long long, cudaStream_t); \
   template cudaError_t row_equilibrate<T>(int, int, T*, long long, long long, double*, cudaStream_t);              \
   template cudaError_t col_scale<T>(int, int, T*, long long, long long, const double*, cudaStream_t);           \
+  template cudaError_t perm_gather<T>(int, int, int, int, const T*, long long, const int*, int, int, T*,       \
+                                      long long, cudaStream_t);                                                  \
+  template cudaError_t perm_scatter<T>(int, int, int, int, T*, long long, const int*, int, int, const T*,       \
+                                       long long, int, cudaStream_t);                                            \
+  template cudaError_t add_identity<T>(int, int, T*, long long, cudaStream_t);                                 \
   template cudaError_t merge_gather<T>(int, int, int, int, int, int, const T*, const T*, const int*, const int*, \
                                        const int*, const int*, const int*, T*, T*, T*, T*, T*, T*, cudaStream_t); \
   template cudaError_t down_scatter<T>(int, int, int, int, int, int, const int*, const T*, const T*, T*,        \
