@@ -480,6 +480,39 @@ typedef struct {
 
 HPS_API int hps_residual_iti_2d(const hps_residual_iti2d_args* a, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Interpolation between the HPS grid and rectangular grids (replaces the
+ * reference's _interpolation_methods.py:23-340 behind Domain.interp_*).
+ * Barycentric Lagrange interpolation with the reference's coincident-point
+ * rule: a target equal to a source node is moved off it by DBL_EPSILON.
+ * ------------------------------------------------------------------------ */
+
+/* out[r][k] = 1 / (d_k w_k nf_r), d_k = to_pts[r] - src_pts[k], nf_r =
+ * sum_k 1 / (w_k d_k): row r of the 1D interpolation matrix from src_pts
+ * (weights src_weights) to to_pts[r].  transposed != 0 writes each group of
+ * rows_per_group rows as columns: out[g][k][r % rows_per_group]. */
+HPS_API int hps_interp_rows(long long n_rows, int n_src, const double* to_pts, const double* src_pts,
+                            const double* src_weights, double* out, int rows_per_group, int transposed, void* stream);
+
+/* out[g][c] = in[g][idx[c]] for c < n_out (in: n_groups x n_in). */
+HPS_API int hps_gather_cols(long long n_groups, int n_in, int n_out, const int* idx, const double* in, double* out,
+                            void* stream);
+
+/* Values at n_targets points (targets: (n_targets, dim)) of the piecewise
+ * polynomial given by f (n_leaves, p^dim, nsrc) on the leaves' Chebyshev
+ * grids (exterior-first order, rearrange: meshgrid index of each point).
+ * Each target takes the first leaf in leaf order whose closed box
+ * (leaf_bounds (n_leaves, 2 dim): min, max per axis) contains it, or leaf 0;
+ * cells (n_cells[0] x .. x n_cells[dim-1], device) maps the finest cells of
+ * the box at cell_origin with sizes cell_size (host arrays) to a leaf.
+ * leaf_nodes / leaf_weights (n_leaves, dim, p): each axis' interpolation
+ * nodes and barycentric weights.  out (n_targets, nsrc).  p <= 32. */
+HPS_API int hps_interp_from_leaves(int dim, long long n_targets, int nsrc, const double* targets, int p,
+                                   const double* leaf_bounds, const double* leaf_nodes, const double* leaf_weights,
+                                   const int* rearrange, const int* cells, const int* n_cells,
+                                   const double* cell_origin, const double* cell_size, const double* f, double* out,
+                                   void* stream);
+
 HPS_API int hps_iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in,
                             void* hcorr, int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry,
                             void* stream);

@@ -46,6 +46,62 @@ class Domain:
                 self.interior_points = g3.compute_interior_Chebyshev_points_adaptive_3D(root, self.p)
                 self.boundary_points = g3.compute_boundary_Gauss_points_adaptive_3D(root, self.q)
 
+    def leaf_bounds(self) -> np.ndarray:
+        """(n_leaves, 2d) leaf boxes (min, max per axis) in leaf order."""
+        if self.bool_uniform:
+            if self.bool_2D:
+                return g2.uniform_leaf_bounds_2D(self.root.bounds, self.L)
+            from . import _grid_creation_3D as g3
+            return g3.uniform_leaf_bounds_3D(self.root.bounds, self.L)
+        from ._interpolation import _leaf_bounds
+        return _leaf_bounds(get_all_leaves(self.root))
+
+    def interp_to_interior_points(self, values, sample_points_x, sample_points_y, sample_points_z=None,
+                                  host_device="cpu"):
+        """Values on the HPS grid (n_leaves, p^d) of the interpolant of
+        ``values`` (n_x, n_y) or (n_x, n_y, n_z) given on
+        meshgrid(sample_points_x, sample_points_y[, sample_points_z],
+        indexing='ij') (src/jaxhps/_domain.py:99-206)."""
+        from . import _interpolation as ip
+        n = [np.shape(sample_points_x)[0], np.shape(sample_points_y)[0]]
+        if self.bool_2D:
+            if sample_points_z is not None:
+                raise ValueError("sample_points_z is only for 3D domains")
+        else:
+            if sample_points_z is None:
+                raise ValueError("3D domains need sample_points_z")
+            n.append(np.shape(sample_points_z)[0])
+        if tuple(values.shape) != tuple(n):
+            raise ValueError(f"values have shape {tuple(values.shape)}, expected {tuple(n)}")
+        if self.bool_2D:
+            return ip.interp_to_hps_2D(self.leaf_bounds(), values, self.p, sample_points_x, sample_points_y,
+                                       host_device=host_device)
+        return ip.interp_to_hps_3D(self.leaf_bounds(), values, self.p, sample_points_x, sample_points_y,
+                                   sample_points_z, host_device=host_device)
+
+    def interp_to_boundary_points(self, sample_points, sample_values, sample_f):
+        """Not implemented in the reference either (src/jaxhps/_domain.py:208-216)."""
+        raise NotImplementedError("interp_to_boundary_points is not implemented yet.")
+
+    def interp_from_interior_points(self, samples, eval_points_x, eval_points_y, eval_points_z=None,
+                                    host_device="cpu"):
+        """(values on the rectangular grid, target points) of the HPS
+        function ``samples`` (n_leaves, p^d[, n_src]) (src/jaxhps/_domain.py
+        :218-294)."""
+        from . import _interpolation as ip
+        if self.bool_2D and eval_points_z is not None:
+            raise ValueError("eval_points_z is only for 3D domains")
+        if not self.bool_2D and eval_points_z is None:
+            raise ValueError("3D domains need eval_points_z")
+        n_leaves, n_per_leaf = self.interior_points.shape[:2]
+        if tuple(samples.shape[:2]) != (n_leaves, n_per_leaf):
+            raise ValueError(f"samples have shape {tuple(samples.shape)}, expected ({n_leaves}, {n_per_leaf}, ...)")
+        if self.bool_2D:
+            return ip.interp_from_hps_2D(self.leaf_bounds(), self.p, samples, eval_points_x, eval_points_y,
+                                         host_device=host_device)
+        return ip.interp_from_hps_3D(self.leaf_bounds(), self.p, samples, eval_points_x, eval_points_y,
+                                     eval_points_z, host_device=host_device)
+
     def get_adaptive_boundary_data_lst(self, f: Callable) -> List[np.ndarray]:
         """Boundary data split per side (2D: S, E, N, W) or face (3D: -x, +x,
         -y, +y, -z, +z) as in src/jaxhps/_domain.py:296-365."""

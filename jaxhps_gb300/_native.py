@@ -171,6 +171,13 @@ def _declare(lib):
     lib.hps_residual_iti_2d.restype = ci
     lib.hps_gemm_policy.argtypes = [ci]
     lib.hps_gemm_policy.restype = ci
+    lib.hps_interp_rows.argtypes = [cll, ci, vp, vp, vp, vp, ci, ci, vp]
+    lib.hps_interp_rows.restype = ci
+    lib.hps_gather_cols.argtypes = [cll, ci, ci, vp, vp, vp, vp]
+    lib.hps_gather_cols.restype = ci
+    lib.hps_interp_from_leaves.argtypes = [ci, cll, ci, vp, ci, vp, vp, vp, vp, vp, P(ci), P(C.c_double),
+                                           P(C.c_double), vp, vp, vp]
+    lib.hps_interp_from_leaves.restype = ci
     lib.hps_assemble_rows_complex.argtypes = [ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp]
     lib.hps_assemble_rows_complex.restype = ci
     lib.hps_gemm_tc_status.argtypes = []
@@ -199,7 +206,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_assemble_rows_complex",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
 )
 
 

@@ -78,6 +78,14 @@ cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const doub
                          const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
                          cudaStream_t st);
 cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st);
+cudaError_t interp_rows(long long n_rows, int n_src, const double* to, const double* src, const double* w,
+                        double* out, int rpg, int transposed, cudaStream_t st);
+cudaError_t gather_cols(long long n_groups, int n_in, int n_out, const int* idx, const double* in, double* out,
+                        cudaStream_t st);
+cudaError_t interp_from_leaves(int dim, long long n_t, int nsrc, const double* tpts, int p, const double* bounds,
+                               const double* nodes, const double* wts, const int* rearr, const int* cells,
+                               const int* nc, const double* lo, const double* h, const double* f, double* out,
+                               cudaStream_t st);
 cudaError_t residual_iti_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds, int cplx,
                             double eta, const void* coeffs, const double* inv_half, const double* D1,
                             const double* D2, const double* Pside, const double* Qside, const int* perm,
@@ -513,6 +521,47 @@ const char* hps_version(void) { return "jaxhps_gb300 0.1.0 (sm_103a)"; }
 long long hps_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int hps_gemm_policy(int policy) { return set_gemm_policy(policy); }
+
+int hps_interp_rows(long long n_rows, int n_src, const double* to_pts, const double* src_pts,
+                    const double* src_weights, double* out, int rows_per_group, int transposed, void* stream) {
+  if (n_rows < 0 || n_src <= 0 || !to_pts || !src_pts || !src_weights || !out || rows_per_group <= 0 ||
+      (transposed && n_rows % rows_per_group != 0)) {
+    set_error("hps_interp_rows: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(interp_rows(n_rows, n_src, to_pts, src_pts, src_weights, out, rows_per_group, transposed,
+                        (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_gather_cols(long long n_groups, int n_in, int n_out, const int* idx, const double* in, double* out,
+                    void* stream) {
+  if (n_groups < 0 || n_in <= 0 || n_out <= 0 || !idx || !in || !out) {
+    set_error("hps_gather_cols: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(gather_cols(n_groups, n_in, n_out, idx, in, out, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_interp_from_leaves(int dim, long long n_targets, int nsrc, const double* targets, int p,
+                           const double* leaf_bounds, const double* leaf_nodes, const double* leaf_weights,
+                           const int* rearrange, const int* cells, const int* n_cells, const double* cell_origin,
+                           const double* cell_size, const double* f, double* out, void* stream) {
+  if ((dim != 2 && dim != 3) || n_targets < 0 || nsrc <= 0 || p < 2 || p > 32 || !targets || !leaf_bounds ||
+      !leaf_nodes || !leaf_weights || !rearrange || !cells || !n_cells || !cell_origin || !cell_size || !f || !out) {
+    set_error("hps_interp_from_leaves: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  for (int a = 0; a < dim; ++a)
+    if (n_cells[a] <= 0 || !(cell_size[a] > 0.0)) {
+      set_error("hps_interp_from_leaves: invalid cell table");
+      return HPS_ERR_ARG;
+    }
+  HPS_CHECK(interp_from_leaves(dim, n_targets, nsrc, targets, p, leaf_bounds, leaf_nodes, leaf_weights, rearrange,
+                               cells, n_cells, cell_origin, cell_size, f, out, (cudaStream_t)stream));
+  return HPS_OK;
+}
 
 int hps_gemm_tc_status(void) { return gemm_tc_error(); }
 

@@ -1373,3 +1373,94 @@ def oracle_adaptive_solve_3D(root: OctNode, bdry):
 
     down(root)
     return np.stack([lf.Y @ lf.g + lf.v for lf in root.leaves()])
+
+
+# ---------------------------------------------------------------------------
+# Interpolation between the HPS grid and rectangular grids
+# (src/jaxhps/_interpolation_methods.py:23-340,
+#  quadrature/_interpolation.py:117-320)
+# ---------------------------------------------------------------------------
+
+_EPS = np.finfo(np.float64).eps
+
+
+def barycentric_matrix_nd(from_axes, to_axes) -> np.ndarray:
+    """Tensor-product barycentric matrix on meshgrid(..., indexing='ij')
+    grids, rows = targets, columns = sources, with exact zero distances
+    replaced by EPS, evaluated as the reference does: one reciprocal of the
+    product of all distance, weight and normalisation factors
+    (quadrature/_interpolation.py:158-213 for 2D, :255-320 for 3D)."""
+    dist, w, nf = [], [], []
+    for f, t in zip(from_axes, to_axes):
+        f = np.asarray(f, dtype=np.float64)
+        t = np.asarray(t, dtype=np.float64)
+        diff = f[:, None] - f[None, :]
+        np.fill_diagonal(diff, 1.0)
+        wa = np.prod(diff, axis=0)
+        d = t[None, :] - f[:, None]
+        d = np.where(d == 0, _EPS, d)
+        dist.append(d)
+        w.append(wa)
+        nf.append(np.sum(1.0 / (wa[:, None] * d), axis=0))
+    if len(from_axes) == 2:
+        M = 1.0 / (dist[0].T[:, None, :, None] * dist[1].T[None, :, None, :] * w[0][None, None, :, None]
+                   * w[1][None, None, None, :] * nf[0][:, None, None, None] * nf[1][None, :, None, None])
+        return M.reshape(len(to_axes[0]) * len(to_axes[1]), -1)
+    M = 1.0 / (dist[0].T[:, None, None, :, None, None] * dist[1].T[None, :, None, None, :, None]
+               * dist[2].T[None, None, :, None, None, :] * w[0][None, None, None, :, None, None]
+               * w[1][None, None, None, None, :, None] * w[2][None, None, None, None, None, :]
+               * nf[0][:, None, None, None, None, None] * nf[1][None, :, None, None, None, None]
+               * nf[2][None, None, :, None, None, None])
+    return M.reshape(len(to_axes[0]) * len(to_axes[1]) * len(to_axes[2]), -1)
+
+
+def _first_containing_leaf(pts: np.ndarray, bounds: np.ndarray) -> np.ndarray:
+    """Index of the first leaf whose closed box contains each point, 0 when
+    none does (argmax of the containment table, _interpolation_methods.py
+    :63-76, :180-195)."""
+    d = pts.shape[1]
+    inside = np.ones((pts.shape[0], bounds.shape[0]), dtype=bool)
+    for a in range(d):
+        inside &= (pts[:, a, None] >= bounds[None, :, 2 * a]) & (pts[:, a, None] <= bounds[None, :, 2 * a + 1])
+    return np.argmax(inside, axis=1)
+
+
+def oracle_interp_from_hps(bounds: np.ndarray, p: int, f_evals: np.ndarray, axes):
+    """interp_from_hps_2D / _3D (_interpolation_methods.py:23-141, :144-266):
+    targets from meshgrid(*axes) (default 'xy' indexing), values reshaped to
+    (n_x, n_y[, n_z])[+ (n_src,)].  Returns (values, target_pts)."""
+    d = len(axes)
+    c = chebyshev_points(p)
+    grids = np.meshgrid(*axes)
+    target = np.stack(grids, axis=d)
+    pts = target.reshape(-1, d)
+    leaf = _first_containing_leaf(pts, bounds)
+    order = ext_first_order_2D(p) if d == 2 else ext_first_order_3D(p)
+    f = np.asarray(f_evals)
+    multi = f.ndim == 3
+    out = np.zeros((pts.shape[0],) + ((f.shape[2],) if multi else ()), dtype=f.dtype)
+    for k in range(pts.shape[0]):
+        b = bounds[leaf[k]]
+        from_axes = [affine_transform(c, (b[2 * a], b[2 * a + 1])) for a in range(d)]
+        if d == 2:
+            from_axes[1] = np.flip(from_axes[1])
+        I = barycentric_matrix_nd(from_axes, [[pts[k, a]] for a in range(d)])[:, order]
+        out[k] = (I @ f[leaf[k]])[0]
+    shape = tuple(len(a) for a in axes) + ((f.shape[2],) if multi else ())
+    return out.reshape(shape), target
+
+
+def oracle_interp_to_hps(bounds: np.ndarray, samples: np.ndarray, p: int, axes) -> np.ndarray:
+    """interp_to_single_Chebyshev_panel_2D / _3D vmapped over the leaves
+    (_interpolation_methods.py:269-340): (n_leaves, p^d)."""
+    d = len(axes)
+    c = chebyshev_points(p)
+    order = ext_first_order_2D(p) if d == 2 else ext_first_order_3D(p)
+    out = []
+    for b in bounds:
+        to_axes = [affine_transform(c, (b[2 * a], b[2 * a + 1])) for a in range(d)]
+        if d == 2:
+            to_axes[1] = np.flip(to_axes[1])
+        I = barycentric_matrix_nd(axes, to_axes)[order, :]
+        out.append(I @ np.asarray(samples).reshape(-1))
+    return np.stack(out)
