@@ -413,6 +413,16 @@ HPS_API int hps_refine_check_3d(int n_nodes, int p, const double* f_values, cons
                                 const double* bounds, double* diff_max, double* ref_max, double* l2_err,
                                 void* stream);
 
+/* 2D analogues (reference _adaptive_discretization_2D.py:34-197): per node 5
+ * blocks of p^2 points (the node, then children a..d = SW, SE, NE, NW), pts
+ * (n_nodes, 5, p^2, 2); bounds (n_nodes, 4); the check compares the node's
+ * values interpolated to the four children with f there. */
+HPS_API int hps_refine_points_2d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
+                                 double* pts, void* stream);
+HPS_API int hps_refine_check_2d(int n_nodes, int p, const double* f_values, const int* perm, const int* iperm,
+                                const double* I_lo, const double* I_hi, const double* w_ref, const double* bounds,
+                                double* diff_max, double* ref_max, double* l2, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Learned refinement proposal: a 513 -> 64 -> 64 -> 1 MLP (ReLU) over 8^3
  * uniform samples of f per octree node plus its depth.  No counterpart in

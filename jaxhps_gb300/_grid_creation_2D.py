@@ -87,6 +87,25 @@ def compute_boundary_Gauss_points_uniform_2D(root: DiscretizationNode2D, L: int,
     ])
 
 
+def compute_boundary_Gauss_points_adaptive_2D(root: DiscretizationNode2D, q: int) -> np.ndarray:
+    """Root boundary Gauss points of an adaptive quadtree: q per boundary
+    leaf, S (W->E), E (S->N), N (E->W), W (N->S) (:142-203)."""
+    from ._discretization_tree_operations_2D import get_ordered_lst_of_boundary_nodes
+
+    g = gauss_points(q)
+    s, e, n, w = get_ordered_lst_of_boundary_nodes(root)
+    xs = np.concatenate([affine_transform(g, (lf.xmin, lf.xmax)) for lf in s])
+    ye = np.concatenate([affine_transform(g, (lf.ymin, lf.ymax)) for lf in e])
+    xn = np.concatenate([affine_transform(g, (lf.xmax, lf.xmin)) for lf in n])
+    yw = np.concatenate([affine_transform(g, (lf.ymax, lf.ymin)) for lf in w])
+    return np.concatenate([
+        np.stack([xs, np.full_like(xs, root.ymin)], -1),
+        np.stack([np.full_like(ye, root.xmax), ye], -1),
+        np.stack([xn, np.full_like(xn, root.ymax)], -1),
+        np.stack([np.full_like(yw, root.xmin), yw], -1),
+    ])
+
+
 def get_all_uniform_leaves_2D(root: DiscretizationNode2D, L: int):
     b = uniform_leaf_bounds_2D(root.bounds, L)
     return [DiscretizationNode2D(*x, depth=L) for x in b]

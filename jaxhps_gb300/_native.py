@@ -159,8 +159,12 @@ def _declare(lib):
     lib.hps_assemble_rows.restype = ci
     lib.hps_refine_points_3d.argtypes = [ci, ci, vp, vp, vp, vp, vp]
     lib.hps_refine_points_3d.restype = ci
+    lib.hps_refine_points_2d.argtypes = [ci, ci, vp, vp, vp, vp, vp]
+    lib.hps_refine_points_2d.restype = ci
     lib.hps_refine_check_3d.argtypes = [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.hps_refine_check_3d.restype = ci
+    lib.hps_refine_check_2d.argtypes = [ci, ci, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.hps_refine_check_2d.restype = ci
     lib.hps_panel_map.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, cll, cll, vp, cll, cll, vp]
     lib.hps_panel_map.restype = ci
     lib.hps_scale_batched.argtypes = [ci, ci, cll, vp, vp, vp]
@@ -206,7 +210,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
 )
 
 

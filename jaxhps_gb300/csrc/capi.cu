@@ -38,6 +38,11 @@ template <class T>
 cudaError_t add_identity(int batch, int n, T* X, long long sX, cudaStream_t st);
 cudaError_t refine_points_3d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
                              double* pts, cudaStream_t st);
+cudaError_t refine_points_2d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
+                             double* pts, cudaStream_t st);
+cudaError_t refine_check_2d(int n_nodes, int p, const double* fv, const int* perm, const int* iperm,
+                            const double* Ilo, const double* Ihi, const double* wref, const double* bounds,
+                            double* diff, double* ref, double* l2, cudaStream_t st);
 template <class T>
 cudaError_t panel_map(int mode, int batch, int n_out, int n_other, int m_len, const int* tab, const T* M, const T* in,
                       long long ld_in, long long s_in, T* out, long long ld_out, long long s_out, cudaStream_t st);
@@ -885,6 +890,31 @@ int hps_refine_check_3d(int n_nodes, int p, const double* f_values, const int* p
   }
   if (n_nodes == 0) return HPS_OK;
   HPS_CHECK(refine_check_3d(n_nodes, p, f_values, perm, iperm, interp_lo, interp_hi, cc_weights, bounds, diff_max,
+                            ref_max, l2_err, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_refine_points_2d(int n_nodes, int p, const double* bounds, const double* cheb, const int* perm,
+                         double* pts, void* stream) {
+  if (n_nodes < 0 || p < 2 || !bounds || !cheb || !perm || !pts) {
+    set_error("hps_refine_points_2d: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (n_nodes == 0) return HPS_OK;
+  HPS_CHECK(refine_points_2d(n_nodes, p, bounds, cheb, perm, pts, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_refine_check_2d(int n_nodes, int p, const double* f_values, const int* perm, const int* iperm,
+                        const double* interp_lo, const double* interp_hi, const double* cc_weights,
+                        const double* bounds, double* diff_max, double* ref_max, double* l2_err, void* stream) {
+  if (n_nodes < 0 || p < 2 || p > 64 || !f_values || !perm || !iperm || !interp_lo || !interp_hi || !cc_weights ||
+      !bounds || !diff_max || !ref_max) {
+    set_error("hps_refine_check_2d: invalid arguments (2 <= p <= 64)");
+    return HPS_ERR_ARG;
+  }
+  if (n_nodes == 0) return HPS_OK;
+  HPS_CHECK(refine_check_2d(n_nodes, p, f_values, perm, iperm, interp_lo, interp_hi, cc_weights, bounds, diff_max,
                             ref_max, l2_err, (cudaStream_t)stream));
   return HPS_OK;
 }

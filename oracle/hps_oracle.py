@@ -1464,3 +1464,355 @@ def oracle_interp_to_hps(bounds: np.ndarray, samples: np.ndarray, p: int, axes) 
         I = barycentric_matrix_nd(axes, to_axes)[order, :]
         out.append(I @ np.asarray(samples).reshape(-1))
     return np.stack(out)
+
+
+# ---------------------------------------------------------------------------
+# Adaptive 2D (quadtree) DtN build and solve
+# (local_solve/_adaptive_2D_DtN.py, merge/_adaptive_2D_DtN.py:24-433 with
+#  merge/_utils_adaptive_2D_DtN.py:11-584, down_pass/_adaptive_2D_DtN.py)
+# ---------------------------------------------------------------------------
+
+
+class QuadNode:
+    """Quadtree node of the oracle: bounds b = (xmin, xmax, ymin, ymax),
+    children SW, SE, NE, NW."""
+
+    def __init__(self, b, depth=0):
+        self.b = tuple(float(x) for x in b)
+        self.depth = depth
+        self.children = []
+
+    def split(self):
+        x0, x1, y0, y1 = self.b
+        xm, ym = (x0 + x1) / 2, (y0 + y1) / 2
+        self.children = [QuadNode(bb, self.depth + 1) for bb in
+                         ((x0, xm, y0, ym), (xm, x1, y0, ym), (xm, x1, ym, y1), (x0, xm, ym, y1))]
+        return self.children
+
+    def leaves(self):
+        if not self.children:
+            return [self]
+        return [lf for ch in self.children for lf in ch.leaves()]
+
+
+def oracle_side_leaves_2D(node: QuadNode):
+    """Leaves along S (W->E), E (S->N), N (E->W), W (N->S) of the subtree."""
+    lv = node.leaves()
+    x0, x1, y0, y1 = node.b
+    s = sorted([l for l in lv if l.b[2] == y0], key=lambda l: l.b[0])
+    e = sorted([l for l in lv if l.b[1] == x1], key=lambda l: l.b[2])
+    n = sorted([l for l in lv if l.b[3] == y1], key=lambda l: -l.b[0])
+    w = sorted([l for l in lv if l.b[0] == x0], key=lambda l: -l.b[2])
+    return s, e, n, w
+
+
+def _compress_list_2D(l0, l1):
+    """Two facing leaf lists, both ordered outside inward: which panels are
+    compressed two to one (_find_compression_list_5..8, :11-197)."""
+    o0, o1 = [], []
+    i0 = i1 = 0
+    while i0 < len(l0) and i1 < len(l1):
+        s0, s1 = l0[i0].b[1] - l0[i0].b[0], l1[i1].b[1] - l1[i1].b[0]
+        if s0 == s1:
+            o0.append(False), o1.append(False)
+            i0 += 1
+            i1 += 1
+        elif s0 < s1:
+            o0 += [True, True]
+            o1.append(False)
+            i0 += 2
+            i1 += 1
+        else:
+            o1 += [True, True]
+            o0.append(False)
+            i1 += 2
+            i0 += 1
+    return o0, o1
+
+
+def _compress2(T, L, flags, axis):
+    """_compress_rows_from_lst / _compress_cols_from_lst (:520-584)."""
+    q = L.shape[0] if axis == 0 else L.shape[1]
+    out, i = [], 0
+    while i < len(flags):
+        if flags[i] and flags[i + 1]:
+            out.append(L @ T[q * i:q * (i + 2)] if axis == 0 else T[:, q * i:q * (i + 2)] @ L)
+            i += 2
+        else:
+            out.append(T[q * i:q * (i + 1)] if axis == 0 else T[:, q * i:q * (i + 1)])
+            i += 1
+    return np.concatenate(out, axis=axis)
+
+
+def oracle_adaptive_quad_merge(node: QuadNode, q: int, L_2f1, L_1f2):
+    """_adaptive_quad_merge_2D_DtN (merge/_adaptive_2D_DtN.py:198-433)."""
+    a, b, c, d = node.children
+    sl = [oracle_side_leaves_2D(k) for k in node.children]
+    # compression lists, outside inward: a5, b5, b6, c6, c7, d7, d8, a8
+    a5, b5 = _compress_list_2D(sl[0][1], sl[1][3][::-1])
+    b6, c6 = _compress_list_2D(sl[1][2], sl[2][0][::-1])
+    c7, d7 = _compress_list_2D(sl[2][3], sl[3][1][::-1])
+    d8, a8 = _compress_list_2D(sl[3][0], sl[0][2][::-1])
+
+    def blocks(k, sets, flags):
+        T, h = k.T, k.h
+        out = {}
+        for i, (ri, fi) in enumerate(zip(sets, flags)):
+            for j, (ci, fj) in enumerate(zip(sets, flags)):
+                M = T[np.ix_(ri, ci)]
+                M = _compress2(M, L_1f2, fi, 0)
+                M = _compress2(M, L_2f1, fj, 1)
+                out[(i, j)] = M
+            out[("h", i)] = _compress2(h[ri], L_1f2, fi, 0)
+        return out
+
+    def idx(k):
+        n = k.n
+        return np.arange(sum(n)), n
+
+    ia, na = idx(a)
+    ib, nb = idx(b)
+    ic, nc = idx(c)
+    id_, nd = idx(d)
+    A_ = blocks(a, [np.concatenate([ia[-na[3]:], ia[:na[0]]]), ia[na[0]:na[0] + na[1]],
+                    np.flipud(ia[na[0] + na[1]:na[0] + na[1] + na[2]])],
+                [[False] * ((na[3] + na[0]) // q), a5, a8])
+    B_ = blocks(b, [ib[:nb[0] + nb[1]], ib[nb[0] + nb[1]:nb[0] + nb[1] + nb[2]], np.flipud(ib[-nb[3]:])],
+                [[False] * ((nb[0] + nb[1]) // q), b6, b5])
+    C_ = blocks(c, [np.flipud(ic[:nc[0]]), ic[nc[0]:nc[0] + nc[1] + nc[2]], ic[-nc[3]:]],
+                [c6, [False] * ((nc[1] + nc[2]) // q), c7])
+    D_ = blocks(d, [id_[:nd[0]], np.flipud(id_[nd[0]:nd[0] + nd[1]]), id_[nd[0] + nd[1]:]],
+                [d8, d7, [False] * ((nd[2] + nd[3]) // q)])
+    # a: (1, 5, 8) = (0, 1, 2); b: (2, 6, 5); c: (6, 3, 7); d: (8, 7, 4)
+    n1, n5, n8 = A_[(0, 0)].shape[0], A_[(1, 1)].shape[0], A_[(2, 2)].shape[0]
+    n2, n6 = B_[(0, 0)].shape[0], B_[(1, 1)].shape[0]
+    n3, n7 = C_[(1, 1)].shape[0], C_[(2, 2)].shape[0]
+    n4 = D_[(2, 2)].shape[0]
+    Z = np.zeros
+    Bm = np.block([[A_[(0, 1)], Z((n1, n6)), Z((n1, n7)), A_[(0, 2)]],
+                   [B_[(0, 2)], B_[(0, 1)], Z((n2, n7)), Z((n2, n8))],
+                   [Z((n3, n5)), C_[(1, 0)], C_[(1, 2)], Z((n3, n8))],
+                   [Z((n4, n5)), Z((n4, n6)), D_[(2, 1)], D_[(2, 0)]]])
+    Cm = np.block([[A_[(1, 0)], B_[(2, 0)], Z((n5, n3)), Z((n5, n4))],
+                   [Z((n6, n1)), B_[(1, 0)], C_[(0, 1)], Z((n6, n4))],
+                   [Z((n7, n1)), Z((n7, n2)), C_[(2, 1)], D_[(1, 2)]],
+                   [A_[(2, 0)], Z((n8, n2)), Z((n8, n3)), D_[(0, 2)]]])
+    Dm = np.block([[A_[(1, 1)] + B_[(2, 2)], B_[(2, 1)], Z((n5, n7)), A_[(1, 2)]],
+                   [B_[(1, 2)], B_[(1, 1)] + C_[(0, 0)], C_[(0, 2)], Z((n6, n8))],
+                   [Z((n7, n5)), C_[(2, 0)], C_[(2, 2)] + D_[(1, 1)], D_[(1, 0)]],
+                   [A_[(2, 1)], Z((n8, n6)), D_[(0, 1)], D_[(0, 0)] + A_[(2, 2)]]])
+    A = np.zeros((n1 + n2 + n3 + n4,) * 2)
+    o = np.cumsum([0, n1, n2, n3, n4])
+    for k, blk in enumerate([A_[(0, 0)], B_[(0, 0)], C_[(1, 1)], D_[(2, 2)]]):
+        A[o[k]:o[k + 1], o[k]:o[k + 1]] = blk
+    dh = np.concatenate([A_[("h", 1)] + B_[("h", 2)], B_[("h", 1)] + C_[("h", 0)], C_[("h", 2)] + D_[("h", 1)],
+                         D_[("h", 0)] + A_[("h", 2)]])
+    hx = np.concatenate([A_[("h", 0)], B_[("h", 0)], C_[("h", 1)], D_[("h", 2)]])
+    Dinv = np.linalg.inv(Dm)
+    S = -Dinv @ Cm
+    T = A + Bm @ S
+    gt = -Dinv @ dh
+    h_out = hx + Bm @ gt
+    r = na[3]
+    S = np.roll(S, -r, axis=1)
+    T = np.roll(np.roll(T, -r, axis=0), -r, axis=1)
+    h_out = np.roll(h_out, -r, axis=0)
+    flags = dict(a5=a5, b5=b5, b6=b6, c6=c6, c7=c7, d7=d7, d8=d8, a8=a8)
+    return S, T, h_out, gt, flags, (n5, n6, n7, n8)
+
+
+def oracle_adaptive_build_2D(root: QuadNode, p: int, q: int, coeffs: dict, source):
+    """Leaf stage with per-leaf rescaled operators, Q / h and h / h, then
+    merges from the deepest level up (merge_stage_adaptive_2D_DtN)."""
+    leaves = root.leaves()
+    dx, dy, dxx, dyy, dxy = diff_operators_2D(p, 1.0)
+    ops = {"D_xx": dxx, "D_xy": dxy, "D_yy": dyy, "D_x": dx, "D_y": dy, "I": np.eye(p * p)}
+    order = {"D_xx": 2, "D_xy": 2, "D_yy": 2, "D_x": 1, "D_y": 1, "I": 0}
+    P = P_2D_DtN(p, q)
+    Q = Q_2D_DtN(p, q, dx, dy)
+    src = np.asarray(source)
+    src = src if src.ndim == 3 else src[..., None]
+    for i, lf in enumerate(leaves):
+        h = (lf.b[1] - lf.b[0]) / 2
+        A = sum(np.asarray(coeffs[k])[i][:, None] * ops[k] / h ** order[k] for k in coeffs if coeffs[k] is not None)
+        Y, T, v, hv = leaf_dtn(A[None], src[i:i + 1], P, Q / h)
+        lf.Y, lf.T, lf.v, lf.h = Y[0], T[0], v[0], hv[0]
+        lf.n = [q, q, q, q]
+    gq = gauss_points(q)
+    L_2f1 = barycentric_matrix_1D(gq, np.concatenate([affine_transform(gq, (-1.0, 0.0)),
+                                                      affine_transform(gq, (0.0, 1.0))]))
+    L_1f2 = barycentric_matrix_1D(np.concatenate([affine_transform(gq, (-1.0, 0.0)),
+                                                  affine_transform(gq, (0.0, 1.0))]), gq)
+
+    def merge(node):
+        for ch in node.children:
+            if ch.children:
+                merge(ch)
+        node.S, node.T, node.h, node.gt, node.flags, node.isz = oracle_adaptive_quad_merge(node, q, L_2f1, L_1f2)
+        sl = oracle_side_leaves_2D(node)
+        node.n = [q * len(x) for x in sl]
+
+    merge(root)
+    root.L_2f1 = L_2f1
+    return root
+
+
+def _expand2(g, L, flags, q):
+    out, i, k = [], 0, 0
+    while i < len(flags):
+        seg = g[k:k + q]
+        if flags[i]:
+            out.append(L @ seg)
+            i += 2
+        else:
+            out.append(seg)
+            i += 1
+        k += q
+    return np.concatenate(out, axis=0)
+
+
+def oracle_adaptive_solve_2D(root: QuadNode, bdry, q: int):
+    """Down pass (down_pass/_adaptive_2D_DtN.py): every node's interface
+    values from S g + g~, decompressed with L_2f1 where the merge compressed,
+    then each child's boundary in its own S, E, N, W order; leaves u = Y g + v."""
+    L = root.L_2f1
+    g0 = np.asarray(bdry)
+    g0 = g0 if g0.ndim == 2 else g0[:, None]
+
+    def down(node, g):
+        if not node.children:
+            node.u = node.Y @ g + node.v
+            return
+        gi = node.S @ g + node.gt
+        n5, n6, n7, n8 = node.isz
+        o = np.cumsum([0, n5, n6, n7, n8])
+        f = node.flags
+        i5, i6, i7, i8 = (gi[o[k]:o[k + 1]] for k in range(4))
+        # outside-inward interface values per child side, expanded
+        a5, b5 = _expand2(i5, L, f["a5"], q), _expand2(i5, L, f["b5"], q)
+        b6, c6 = _expand2(i6, L, f["b6"], q), _expand2(i6, L, f["c6"], q)
+        c7, d7 = _expand2(i7, L, f["c7"], q), _expand2(i7, L, f["d7"], q)
+        d8, a8 = _expand2(i8, L, f["d8"], q), _expand2(i8, L, f["a8"], q)
+        a, b, c, d = node.children
+        # merged exterior [a_S, b_S, b_E, c_E, c_N, d_N, d_W, a_W]
+        sizes = [a.n[0], b.n[0], b.n[1], c.n[1], c.n[2], d.n[2], d.n[3], a.n[3]]
+        e = np.split(g, np.cumsum(sizes)[:-1])
+        down(a, np.concatenate([e[0], a5, a8[::-1], e[7]]))
+        down(b, np.concatenate([e[1], e[2], b6, b5[::-1]]))
+        down(c, np.concatenate([c6[::-1], e[3], e[4], c7]))
+        down(d, np.concatenate([d8, d7[::-1], e[5], e[6]]))
+
+    down(root, g0)
+    return np.stack([lf.u for lf in root.leaves()])
+
+
+def L_4f1_2D(p: int) -> np.ndarray:
+    """Dense node -> four children interpolation, row blocks a..d each in
+    exterior-first order, columns exterior-first (_precompute_operators_2D.py
+    :303-328); y runs north to south on the leaf grids."""
+    c = chebyshev_points(p)
+    lo, hi = affine_transform(c, (-1.0, 0.0)), affine_transform(c, (0.0, 1.0))
+    Bl, Bh = barycentric_matrix_1D(c, lo), barycentric_matrix_1D(c, hi)
+    r = ext_first_order_2D(p)
+    blocks = []
+    for bx, by in ((0, 0), (1, 0), (1, 1), (0, 1)):
+        Bx = Bh if bx else Bl
+        By = (Bh if by else Bl)[::-1, ::-1]
+        M = np.kron(Bx, By)
+        blocks.append(M[r][:, r])
+    return np.concatenate(blocks)
+
+
+def oracle_adaptive_mesh_2D(root: QuadNode, f, tol: float, p: int, restrict: bool = True, l2: bool = False):
+    """generate_adaptive_mesh_level_restriction_2D (_adaptive_discretization_2D.py
+    :34-197) with the dense L_4f1 check; ``f`` takes (..., 2) NumPy points.
+    Refines in place; returns the number of rounds."""
+    Lop = L_4f1_2D(p)
+    r = ext_first_order_2D(p)
+
+    def sq_l2(vals, b):
+        w = np.outer(chebyshev_weights(p, b[0:2]), chebyshev_weights(p, b[2:4])).ravel()[r]
+        return float(np.sum(w * vals ** 2))
+
+    def kids(b):
+        return np.array(quad_children_bounds(b))
+
+    if l2:
+        root.split()
+        gn = sum(sq_l2(f(leaf_points_2D(np.array([lf.b]), p)[0]), lf.b) for lf in root.leaves())
+        tol = tol ** 2
+    else:
+        gn = float(np.max(f(leaf_points_2D(kids(root.b), p).reshape(-1, 2))))
+
+    def find_or_add(node, vol):
+        xmin, xmax, ymin, ymax = vol
+        side = node.b[1] - node.b[0]
+        req = xmax - xmin
+        if np.allclose(req * 2, side):
+            if not node.children:
+                node.split()
+                return node
+            return None
+        xm, ym = (node.b[0] + node.b[1]) / 2, (node.b[2] + node.b[3]) / 2
+        i = (0 if ymin < ym else 3) if xmin < xm else (1 if ymin < ym else 2)
+        child = node.children[i]
+        if np.allclose(side, 4 * req):
+            if not child.children:
+                child.split()
+                return child
+            return None
+        if side < 2 * req:
+            raise ValueError("Requested volume is too large for the current node")
+        return find_or_add(child, vol)
+
+    def neighbours(n):
+        s = n.b[1] - n.b[0]
+        x0, x1, y0, y1 = n.b
+        v = []
+        if x0 - s >= root.b[0]:
+            v.append((x0 - s, x0, y0, y1))
+        if x1 + s <= root.b[1]:
+            v.append((x1, x1 + s, y0, y1))
+        if y0 - s >= root.b[2]:
+            v.append((x0, x1, y0 - s, y0))
+        if y1 + s <= root.b[3]:
+            v.append((x0, x1, y1, y1 + s))
+        return v
+
+    queue = root.leaves()
+    rounds = 0
+    while queue:
+        rounds += 1
+        ok, nrms = [], []
+        for node in queue:
+            f0 = f(leaf_points_2D(np.array([node.b]), p)[0])
+            kb = kids(node.b)
+            f1 = f(leaf_points_2D(kb, p).reshape(-1, 2))
+            d = Lop @ f0 - f1
+            if l2:
+                err = sum(sq_l2(d[k * p * p:(k + 1) * p * p], kb[k]) for k in range(4))
+                ok.append(err / gn < tol)
+                nrms.append(0.0)
+            else:
+                nrm = max(gn, float(np.max(np.abs(f1))))
+                ok.append(float(np.max(np.abs(d))) / nrm < tol)
+                nrms.append(nrm)
+        if not l2:
+            gn = max(nrms)
+        new_queue = []
+        for node, good in zip(queue, ok):
+            if good:
+                continue
+            node.split()
+            new_queue += node.children
+            if restrict:
+                pending = [node]
+                while pending:
+                    fc = pending.pop()
+                    for vol in neighbours(fc):
+                        n = find_or_add(root, vol)
+                        if n is not None:
+                            pending.append(n)
+                            new_queue += n.children
+        queue = new_queue
+    return rounds
