@@ -24,6 +24,8 @@
 //    zeroed), E = inv(A[R,C]) (the panel's pivot rows after elimination).
 #include <stdio.h>
 
+#include <stdlib.h>
+
 #include "hps_common.cuh"
 #include "hps_internal.h"
 
@@ -405,6 +407,15 @@ struct GjeWs {
   size_t mat, pan, u, g, h, e, piv, rinv, used, sync, per;
 };
 
+// Multi-CTA panels run as thread-block clusters unless HPS_CLUSTER_PANELS=0.
+static bool cluster_panels_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("HPS_CLUSTER_PANELS");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 // Upper bound on the CTAs that share one matrix's panel.
 static int coop_nct_cap(int n) { return n / 16 < 1 ? 1 : (n / 16 > 1024 ? 1024 : n / 16); }
 
@@ -422,8 +433,9 @@ static GjeWs gje_layout(size_t es, int n) {
   w.rinv = al256(4 * (size_t)n);
   w.used = al256((size_t)n);
   {
-    // as coop_layout() below with 8-byte magnitudes (an upper bound for every type)
-    const size_t cap = (size_t)coop_nct_cap(n);
+    // as coop_layout() below with 8-byte magnitudes (an upper bound for every
+    // type), for the larger of the cooperative cap and a 16-CTA cluster
+    const size_t cap = (size_t)(coop_nct_cap(n) > 16 ? coop_nct_cap(n) : 16);
     w.sync = 256 + al256(2 * cap * 8) + al256(2 * cap * sizeof(int)) + al256(2 * cap * BP * es);
   }
   w.per = w.mat + w.pan + w.u + w.g + w.h + w.e + w.piv + w.rinv + w.used + w.sync;
@@ -653,7 +665,18 @@ __host__ __device__ inline CoopLayout coop_layout(size_t es, size_t mag_size, in
   return c;
 }
 
-template <class T>
+// Hardware barrier over the CTAs of a thread-block cluster, with
+// release / acquire ordering at cluster scope for the global-memory exchange
+// of pivot candidates.  A cluster is co-scheduled by construction and every
+// CTA reaches every barrier, so it needs no timeout.
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// CLUSTER: the nct CTAs of a matrix form one thread-block cluster (nct <= 16)
+// and synchronise with the cluster barrier; otherwise they are part of a
+// cooperative launch and use the bounded software barrier above.
+template <class T, bool CLUSTER>
 __global__ void __launch_bounds__(CP_NT)
 gje_panel_coop_kernel(int n, int k0, int bw, int rows_per, T* Mat, T* U, T* G, T* E, int* piv,
                       unsigned char* used, int* info, unsigned char* sync, CoopLayout lay) {
@@ -744,7 +767,9 @@ gje_panel_coop_kernel(int n, int k0, int bw, int rows_per, T* Mat, T* U, T* G, T
         scand[((size_t)buf * nct + cta) * BP + tid] =
             (lbi < n && tid < bw) ? P[tid * rows_per + (lbi - r0)] : zero<T>();
     }
-    if (!coop_barrier(hdr, (unsigned)nct)) {
+    if (CLUSTER) {
+      cluster_sync_all();
+    } else if (!coop_barrier(hdr, (unsigned)nct)) {
       if (cta == 0 && tid == 0 && info) info[b] = -1;
       return;
     }
@@ -1030,9 +1055,10 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
         nct = (n + rows_per - 1) / rows_per;
         csmem = es * ((size_t)BP * rows_per + rows_per) + (size_t)rows_per + 16;
         if (csmem > 200 * 1024) break;
-        cudaFuncSetAttribute(gje_panel_coop_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
+        cudaFuncSetAttribute(gje_panel_coop_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)csmem);
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_coop_kernel<T>, CP_NT, csmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_coop_kernel<T, false>, CP_NT, csmem);
         if ((long long)per_sm * sms >= (long long)nct * batch) {
           fits = true;
           break;
@@ -1042,6 +1068,46 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
       if (!fits || nct < 2) nct = 0;
       cudaGetLastError();   // a refused attribute or occupancy query only disables this path
     }
+  }
+  // Prefer one thread-block cluster per matrix (hardware barrier): up to 16
+  // CTAs, each holding rows_per rows of the panel in shared memory.
+  int ncl = 0, rows_cl = 0;
+  size_t clsmem = 0;
+  if (nct > 0 && cluster_panels_enabled()) {
+    for (int want : {16, 8}) {
+      if (want > (coop_nct_cap(n) > 16 ? coop_nct_cap(n) : 16)) continue;
+      const int rp = (n + want - 1) / want;
+      const int nc = (n + rp - 1) / rp;
+      const size_t sm = es * ((size_t)BP * rp + rp) + (size_t)rp + 16;
+      if (sm > 200 * 1024 || nc < 2) continue;
+      auto kern = gje_panel_coop_kernel<T, true>;
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (nc > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(nc, batch);
+      cfg.blockDim = dim3(CP_NT);
+      cfg.dynamicSmemBytes = sm;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = nc;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      int max_cl = 0;
+      if (cudaOccupancyMaxActiveClusters(&max_cl, kern, &cfg) == cudaSuccess && max_cl >= 1) {
+        ncl = nc;
+        rows_cl = rp;
+        clsmem = sm;
+        break;
+      }
+    }
+    cudaGetLastError();   // a refused attribute or occupancy query only disables this path
+  }
+  if (ncl > 0) {
+    nct = ncl;
+    rows_per = rows_cl;
+    csmem = clsmem;
   }
   const CoopLayout clay = coop_layout(es, sizeof(typename MagOf<T>::type), nct > 0 ? nct : 1);
   if (nct > 0) {
@@ -1085,9 +1151,26 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
       int* info_ = info;
       unsigned char* sync_ = syncb;
       CoopLayout lay_ = clay;
-      void* args[] = {&n_, &k0_, &bw, &rp, &Mat_, &U_, &G_, &E_, &piv_, &used_, &info_, &sync_, &lay_};
-      e = cudaLaunchCooperativeKernel((void*)gje_panel_coop_kernel<T>, dim3(nct, batch), dim3(CP_NT), args, csmem,
-                                      st);
+      if (ncl > 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(nct, batch);
+        cfg.blockDim = dim3(CP_NT);
+        cfg.dynamicSmemBytes = csmem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = nct;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, gje_panel_coop_kernel<T, true>, n_, k0_, bw, rp, Mat_, U_, G_, E_, piv_,
+                               used_, info_, sync_, lay_);
+      } else {
+        void* args[] = {&n_, &k0_, &bw, &rp, &Mat_, &U_, &G_, &E_, &piv_, &used_, &info_, &sync_, &lay_};
+        e = cudaLaunchCooperativeKernel((void*)gje_panel_coop_kernel<T, false>, dim3(nct, batch), dim3(CP_NT), args,
+                                        csmem, st);
+      }
     } else {
       gje_panel_kernel<T><<<batch, PANEL_NT, use_smem ? pan_smem : 0, st>>>(
           n, k0, bw, Mat, Pw, use_smem, U, G, E, piv, used, info);
