@@ -26,6 +26,8 @@
 
 #include <stdlib.h>
 
+#include <cooperative_groups.h>
+
 #include "hps_common.cuh"
 #include "hps_internal.h"
 
@@ -614,6 +616,15 @@ __device__ __forceinline__ c128 ld_cg(const c128* p) {
   return c128{v.x, v.y};
 }
 
+__device__ __forceinline__ float shfl_T(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl_T(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ c64 shfl_T(c64 v, int src) {
+  return c64{__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src)};
+}
+__device__ __forceinline__ c128 shfl_T(c128 v, int src) {
+  return c128{__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src)};
+}
+
 // Barrier over the nct CTAs of one matrix; false on timeout or on an
 // earlier failure of this matrix.
 __device__ __forceinline__ bool coop_barrier(CoopHdr* hdr, unsigned nct) {
@@ -673,10 +684,7 @@ __device__ __forceinline__ void cluster_sync_all() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// CLUSTER: the nct CTAs of a matrix form one thread-block cluster (nct <= 16)
-// and synchronise with the cluster barrier; otherwise they are part of a
-// cooperative launch and use the bounded software barrier above.
-template <class T, bool CLUSTER>
+template <class T>
 __global__ void __launch_bounds__(CP_NT)
 gje_panel_coop_kernel(int n, int k0, int bw, int rows_per, T* Mat, T* U, T* G, T* E, int* piv,
                       unsigned char* used, int* info, unsigned char* sync, CoopLayout lay) {
@@ -767,9 +775,7 @@ gje_panel_coop_kernel(int n, int k0, int bw, int rows_per, T* Mat, T* U, T* G, T
         scand[((size_t)buf * nct + cta) * BP + tid] =
             (lbi < n && tid < bw) ? P[tid * rows_per + (lbi - r0)] : zero<T>();
     }
-    if (CLUSTER) {
-      cluster_sync_all();
-    } else if (!coop_barrier(hdr, (unsigned)nct)) {
+    if (!coop_barrier(hdr, (unsigned)nct)) {
       if (cta == 0 && tid == 0 && info) info[b] = -1;
       return;
     }
@@ -835,6 +841,191 @@ gje_panel_coop_kernel(int n, int k0, int bw, int rows_per, T* Mat, T* U, T* G, T
   }
 
   // outputs, as gje_panel_kernel: panel back into M, U, E (pivot rows this CTA owns), G, used flags
+  T* Ub = U + (long long)b * n * BP;
+  T* Gb = G + (long long)b * BP * n;
+  T* Eb = E + (long long)b * BP * BP;
+  for (int e = tid; e < nr * bw; e += CP_NT) {
+    const int i = e / bw, c = e % bw;
+    const T v = P[c * rows_per + i];
+    M[(long long)(r0 + i) * n + k0 + c] = v;
+    Ub[(long long)(r0 + i) * BP + c] = (ul[i] == 2) ? zero<T>() : v;
+  }
+  for (int e = tid; e < bw * bw; e += CP_NT) {
+    const int c1 = e / bw, c2 = e % bw;
+    const int rr = Rs[c1];
+    if (rr >= r0 && rr < r0 + nr) Eb[c1 * BP + c2] = P[c2 * rows_per + (rr - r0)];
+  }
+  for (long long e = (long long)cta * CP_NT + tid; e < (long long)bw * n; e += (long long)nct * CP_NT) {
+    const int c1 = (int)(e / n), j = (int)(e % n);
+    Gb[(long long)c1 * n + j] = (j >= k0 && j < k0 + bw) ? zero<T>() : M[(long long)Rs[c1] * n + j];
+  }
+  for (int i = tid; i < nr; i += CP_NT) us[r0 + i] = (ul[i] == 2) ? 1 : ul[i];
+}
+
+// Panel of one matrix on the nct CTAs of a thread-block cluster, pivot
+// candidates exchanged through distributed shared memory.  Per column: each
+// CTA publishes (magnitude, row, the row's panel values) in its own shared
+// memory (double-buffered); after the cluster barrier warp 0 of every CTA
+// reads the nct candidates in one round of remote loads, picks the pivot and
+// reads the pivot row in a second round; every thread then updates whole rows
+// of its CTA's slice (no read/write hazard inside a row) and computes the
+// next column's candidate on the way.  Two CTA barriers and one cluster
+// barrier per column.  Outputs as gje_panel_coop_kernel.
+template <class T>
+struct PanelPub {
+  typename MagOf<T>::type mag;
+  int idx;
+  T row[BP];
+};
+
+template <class T>
+__global__ void __launch_bounds__(CP_NT)
+gje_panel_cluster_kernel(int n, int k0, int bw, int rows_per, T* Mat, T* U, T* G, T* E, int* piv,
+                         unsigned char* used, int* info) {
+  namespace cg = cooperative_groups;
+  using MagT = typename MagOf<T>::type;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int b = blockIdx.y, cta = (int)cluster.block_rank(), nct = (int)cluster.num_blocks();
+  const long long nn = (long long)n * n;
+  T* M = Mat + (long long)b * nn;
+  int* pv = piv + (long long)b * n;
+  unsigned char* us = used + (long long)b * n;
+
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* P = reinterpret_cast<T*>(smraw);   // P[c * rows_per + i], i local row
+  unsigned char* ul = reinterpret_cast<unsigned char*>(P + (size_t)BP * rows_per);
+  __shared__ PanelPub<T> pub[2];
+  __shared__ T rowr[BP];
+  __shared__ int Rs[BP];
+  __shared__ MagT wbest[CP_NT / 32];
+  __shared__ int widx[CP_NT / 32];
+  __shared__ int s_r;
+  __shared__ T s_pinv;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int r0 = cta * rows_per;
+  const int nr = max(0, min(n - r0, rows_per));
+
+  for (int e = tid; e < nr * bw; e += CP_NT) {
+    const int i = e / bw, c = e % bw;
+    P[c * rows_per + i] = M[(long long)(r0 + i) * n + k0 + c];
+  }
+  for (int i = tid; i < nr; i += CP_NT) ul[i] = us[r0 + i];
+  __syncthreads();
+
+  auto better = [](MagT m, int i, MagT bm, int bi) { return m > bm || (m == bm && i < bi); };
+  // candidate of column 0 over this thread's rows
+  MagT best = -1;
+  int bi = n;
+  for (int i = tid; i < nr; i += CP_NT)
+    if (!ul[i]) {
+      const MagT mg = nan_to_inf(pivmag(P[i]));
+      if (better(mg, r0 + i, best, bi)) {
+        best = mg;
+        bi = r0 + i;
+      }
+    }
+
+  for (int c = 0; c < bw; ++c) {
+    const int buf = c & 1;
+    // CTA candidate -> pub[buf]
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (better(ob, oi, best, bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      wbest[warp] = best;
+      widx[warp] = bi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      MagT m = lane < CP_NT / 32 ? wbest[lane] : (MagT)-1;
+      int ix = lane < CP_NT / 32 ? widx[lane] : n;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const MagT ob = __shfl_xor_sync(0xffffffffu, m, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, ix, off);
+        if (better(ob, oi, m, ix)) {
+          m = ob;
+          ix = oi;
+        }
+      }
+      if (lane == 0) {
+        pub[buf].mag = m;
+        pub[buf].idx = ix;
+      }
+      if (lane < BP) pub[buf].row[lane] = (ix < n && lane < bw) ? P[lane * rows_per + (ix - r0)] : zero<T>();
+    }
+    cluster_sync_all();
+    // the pivot: the same choice in every CTA
+    if (warp == 0) {
+      MagT m = -1;
+      int ix = n, wc = 0;
+      if (lane < nct) {
+        const PanelPub<T>* rp = cluster.map_shared_rank(&pub[buf], lane);
+        m = rp->mag;
+        ix = rp->idx;
+        wc = lane;
+      }
+#pragma unroll
+      for (int off = 16; off; off >>= 1) {
+        const MagT ob = __shfl_xor_sync(0xffffffffu, m, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, ix, off);
+        const int oc = __shfl_xor_sync(0xffffffffu, wc, off);
+        if (better(ob, oi, m, ix)) {
+          m = ob;
+          ix = oi;
+          wc = oc;
+        }
+      }
+      const PanelPub<T>* wp = cluster.map_shared_rank(&pub[buf], wc);
+      const T rv = lane < BP ? wp->row[lane] : zero<T>();
+      const T pc = shfl_T(rv, c);   // lane c holds the pivot element
+      const T pinv = (m > 0) ? rcp_(pc) : zero<T>();
+      if (lane < BP) rowr[lane] = mul(rv, pinv);
+      if (lane == 0) {
+        s_r = ix;
+        s_pinv = pinv;
+        Rs[c] = ix;
+        if (cta == 0) {
+          pv[k0 + c] = ix;
+          if (!(m > 0) && info && info[b] == 0) info[b] = k0 + c + 1;
+        }
+      }
+    }
+    __syncthreads();
+    const int r = s_r;
+    const T pinv = s_pinv;
+    // whole-row updates; the next column's candidate on the way
+    best = -1;
+    bi = n;
+    for (int i = tid; i < nr; i += CP_NT) {
+      if (r0 + i == r) {
+        for (int c2 = 0; c2 < bw; ++c2) P[c2 * rows_per + i] = (c2 == c) ? pinv : rowr[c2];
+        ul[i] = 2;
+      } else {
+        const T f = P[c * rows_per + i];
+        for (int c2 = 0; c2 < bw; ++c2) {
+          T& x = P[c2 * rows_per + i];
+          x = (c2 == c) ? neg(mul(f, pinv)) : fms_(f, rowr[c2], x);
+        }
+        if (c + 1 < bw && !ul[i]) {
+          const MagT mg = nan_to_inf(pivmag(P[(c + 1) * rows_per + i]));
+          if (better(mg, r0 + i, best, bi)) {
+            best = mg;
+            bi = r0 + i;
+          }
+        }
+      }
+    }
+  }
+  // no CTA leaves while another may still read its published candidates
+  cluster_sync_all();
+
   T* Ub = U + (long long)b * n * BP;
   T* Gb = G + (long long)b * BP * n;
   T* Eb = E + (long long)b * BP * BP;
@@ -1055,10 +1246,10 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
         nct = (n + rows_per - 1) / rows_per;
         csmem = es * ((size_t)BP * rows_per + rows_per) + (size_t)rows_per + 16;
         if (csmem > 200 * 1024) break;
-        cudaFuncSetAttribute(gje_panel_coop_kernel<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(gje_panel_coop_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)csmem);
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_coop_kernel<T, false>, CP_NT, csmem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gje_panel_coop_kernel<T>, CP_NT, csmem);
         if ((long long)per_sm * sms >= (long long)nct * batch) {
           fits = true;
           break;
@@ -1078,9 +1269,9 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
       if (want > (coop_nct_cap(n) > 16 ? coop_nct_cap(n) : 16)) continue;
       const int rp = (n + want - 1) / want;
       const int nc = (n + rp - 1) / rp;
-      const size_t sm = es * ((size_t)BP * rp + rp) + (size_t)rp + 16;
+      const size_t sm = es * (size_t)BP * rp + (size_t)rp + 16;
       if (sm > 200 * 1024 || nc < 2) continue;
-      auto kern = gje_panel_coop_kernel<T, true>;
+      auto kern = gje_panel_cluster_kernel<T>;
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       if (nc > 8) cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
       cudaLaunchConfig_t cfg = {};
@@ -1164,11 +1355,11 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        e = cudaLaunchKernelEx(&cfg, gje_panel_coop_kernel<T, true>, n_, k0_, bw, rp, Mat_, U_, G_, E_, piv_,
-                               used_, info_, sync_, lay_);
+        e = cudaLaunchKernelEx(&cfg, gje_panel_cluster_kernel<T>, n_, k0_, bw, rp, Mat_, U_, G_, E_, piv_, used_,
+                               info_);
       } else {
         void* args[] = {&n_, &k0_, &bw, &rp, &Mat_, &U_, &G_, &E_, &piv_, &used_, &info_, &sync_, &lay_};
-        e = cudaLaunchCooperativeKernel((void*)gje_panel_coop_kernel<T, false>, dim3(nct, batch), dim3(CP_NT), args,
+        e = cudaLaunchCooperativeKernel((void*)gje_panel_coop_kernel<T>, dim3(nct, batch), dim3(CP_NT), args,
                                         csmem, st);
       }
     } else {
