@@ -261,14 +261,15 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
   }
   const int pol = gemm_policy();
   if constexpr (std::is_same<T, float>::value) {
-    // measured: the tensor-core kernel wins once a tile has enough K-steps to
-    // amortise its pipeline prologue and epilogue
-    if (pol == 2 || (pol == 1 && M >= 128 && N >= 32 && K >= 128))
+    // measured: the tensor-core kernel wins once tiles are wide (N >= 128)
+    // and have enough K-steps to amortise its pipeline prologue and epilogue;
+    // below that the 8x8-register SIMT tiles are as fast or faster
+    if (pol == 2 || (pol == 1 && M >= 128 && N >= 128 && K >= 128))
       return gemm_tf32x3(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
   }
   if constexpr (std::is_same<T, c64>::value) {
     // complex64 as one real product of size (M, 2N, 2K) on the tensor cores
-    if (alpha.y == 0.f && beta.y == 0.f && (pol == 2 || (pol == 1 && M >= 128 && N >= 16 && K >= 64)))
+    if (alpha.y == 0.f && beta.y == 0.f && (pol == 2 || (pol == 1 && M >= 128 && N >= 128 && K >= 128)))
       return gemm_tf32x3_c64(M, N, K, alpha.x, A, lda, sA, B, ldb, sB, beta.x, C, ldc, sC, D, ldd, sD, batch, st);
   }
   if (sizeof(T) == 4) {
@@ -276,6 +277,16 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
     if (M >= 96 && N >= 96 && tiles128 >= 120)
       return launch_gemm_cfg<T, 128, 128, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
                                                    ldc, sC, D, ldd, sD, batch, st);
+    // N <= 64 (many right-hand sides, leaf and merge blocks): 8x8 register
+    // tiles (16 shared loads per 64 FMAs instead of 8 per 16)
+    const long long tiles_m128 = (long long)((M + 127) / 128) * batch;
+    if (N > 32 && N <= 64 && M >= 96 && tiles_m128 >= 152)
+      return launch_gemm_cfg<T, 128, 64, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
+                                                  ldc, sC, D, ldd, sD, batch, st);
+    const long long tiles_m64 = (long long)((M + 63) / 64) * batch;
+    if (N > 32 && N <= 64 && M >= 32 && tiles_m64 >= 304)
+      return launch_gemm_cfg<T, 64, 64, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
+                                                 ldc, sC, D, ldd, sD, batch, st);
     return launch_gemm_cfg<T, 64, 64, 8, 4, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
                                                sC, D, ldd, sD, batch, st);
   }

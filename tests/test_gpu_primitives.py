@@ -113,9 +113,13 @@ def test_inverse_large_single_matrix_multi_cta_panel(cuda, n, dt):
 @pytest.mark.parametrize("m,n,k,batch,odd", [(196, 64, 196, 3, False), (300, 200, 150, 2, False), (257, 33, 131, 2, True),
                                              (1100, 300, 257, 1, False)])
 def test_gemm_tensor_core_path(cuda, m, n, k, batch, odd):
-    """FP32 shapes the dispatcher sends to the tcgen05 kernel (3xTF32): FP32-level
-    accuracy, ragged tiles, unaligned leading dimensions, C aliasing D."""
+    """FP32 products on the tcgen05 kernel (3xTF32; forced with
+    hps_gemm_policy(2)): FP32-level accuracy, ragged tiles, unaligned leading
+    dimensions, C aliasing D."""
     from jaxhps_gb300 import _native as nat
+
+    L = nat.load_library()
+    old_policy = L.hps_gemm_policy(2)
 
     rng = np.random.default_rng(m + n + k)
     pad = 1 if odd else 0
@@ -124,7 +128,11 @@ def test_gemm_tensor_core_path(cuda, m, n, k, batch, odd):
     Cm = rng.standard_normal((batch, m, n)).astype(np.float32)
     tA = torch.as_tensor(Ab, device=cuda)[:, :, :k]          # lda = k + 1 when odd: unaligned rows
     tB, tC = torch.as_tensor(B, device=cuda), torch.as_tensor(Cm, device=cuda)
-    nat.gemm(tA, tB, tC, alpha=0.75, beta=-1.25, Cmat=tC)    # in place
+    try:
+        nat.gemm(tA, tB, tC, alpha=0.75, beta=-1.25, Cmat=tC)    # in place
+        torch.cuda.synchronize()
+    finally:
+        L.hps_gemm_policy(old_policy)
     ref = 0.75 * (Ab[:, :, :k].astype(np.float64) @ B) - 1.25 * Cm
     err = np.abs(tC.cpu().numpy() - ref).max() / np.abs(ref).max()
     assert err < 2e-6 * max(1.0, np.sqrt(k / 64)), err
@@ -135,9 +143,13 @@ def test_gemm_tensor_core_path(cuda, m, n, k, batch, odd):
                                              (1100, 300, 257, 1, False)])
 def test_gemm_tensor_core_complex64(cuda, m, n, k, batch, odd):
     """complex64 products on the tcgen05 kernel (one real product of the
-    interleaved A with the 2x2-block expansion of B): complex64-level
-    accuracy, ragged tiles, unaligned leading dimensions, C aliasing D."""
+    interleaved A with the 2x2-block expansion of B; forced with
+    hps_gemm_policy(2)): complex64-level accuracy, ragged tiles, unaligned
+    leading dimensions, C aliasing D."""
     from jaxhps_gb300 import _native as nat
+
+    L = nat.load_library()
+    old_policy = L.hps_gemm_policy(2)
 
     rng = np.random.default_rng(m + n + k + 1)
     pad = 1 if odd else 0
@@ -148,7 +160,11 @@ def test_gemm_tensor_core_complex64(cuda, m, n, k, batch, odd):
     Ab, B, Cm = cr(batch, m, k + pad), cr(batch, k, n), cr(batch, m, n)
     tA = torch.as_tensor(Ab, device=cuda)[:, :, :k]
     tB, tC = torch.as_tensor(B, device=cuda), torch.as_tensor(Cm, device=cuda)
-    nat.gemm(tA, tB, tC, alpha=0.75, beta=-1.25, Cmat=tC)
+    try:
+        nat.gemm(tA, tB, tC, alpha=0.75, beta=-1.25, Cmat=tC)
+        torch.cuda.synchronize()
+    finally:
+        L.hps_gemm_policy(old_policy)
     ref = 0.75 * (Ab[:, :, :k].astype(np.complex128) @ B) - 1.25 * Cm
     err = np.abs(tC.cpu().numpy() - ref).max() / np.abs(ref).max()
     # FP32 accumulation over the 2k real terms of each complex dot product
