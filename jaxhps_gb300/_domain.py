@@ -13,7 +13,7 @@ from typing import Callable, List
 
 import numpy as np
 
-from ._discretization_tree import DiscretizationNode2D, DiscretizationNode3D, get_all_leaves
+from ._discretization_tree import DiscretizationNode2D, get_all_leaves
 from . import _grid_creation_2D as g2
 
 

@@ -27,7 +27,7 @@ import torch
 
 from . import _native as nat
 from . import _stages as st
-from ._quadrature import affine_transform, chebyshev_points
+from ._quadrature import chebyshev_points
 
 
 def _bary_weights(x: np.ndarray) -> np.ndarray:
@@ -64,8 +64,8 @@ def _leaf_nodes(bounds: np.ndarray, p: int, dim: int) -> Tuple[np.ndarray, np.nd
     nl = bounds.shape[0]
     nodes = np.empty((nl, dim, p))
     for a in range(dim):
-        lo, hi = bounds[:, 2 * a], bounds[:, 2 * a + 1]
-        nodes[:, a, :] = np.stack([affine_transform(c, (l, h)) for l, h in zip(lo, hi)]) if nl else nodes[:, a, :]
+        lo, hi = bounds[:, 2 * a:2 * a + 1], bounds[:, 2 * a + 1:2 * a + 2]
+        nodes[:, a, :] = 0.5 * (hi - lo) * c[None, :] + 0.5 * (lo + hi)   # affine_transform, per leaf
     if dim == 2:
         nodes[:, 1, :] = nodes[:, 1, ::-1]
     diff = nodes[:, :, :, None] - nodes[:, :, None, :]
@@ -187,7 +187,8 @@ def _to_hps(bounds: np.ndarray, samples, p: int, axes: Sequence[np.ndarray], dev
         raise ValueError(f"values have shape {tuple(V.shape)}, expected {tuple(n)}")
     nl = bounds.shape[0]
     c = chebyshev_points(p)
-    to = [np.stack([affine_transform(c, (b[2 * a], b[2 * a + 1])) for b in bounds]) for a in range(dim)]
+    to = [0.5 * (bounds[:, 2 * a + 1:2 * a + 2] - bounds[:, 2 * a:2 * a + 1]) * c[None, :]
+          + 0.5 * (bounds[:, 2 * a:2 * a + 1] + bounds[:, 2 * a + 1:2 * a + 2]) for a in range(dim)]
     if dim == 2:
         to[1] = np.ascontiguousarray(to[1][:, ::-1])
     Mx = _rows(to[0], axes[0], p, False, dev)                        # (nl p, n_x)

@@ -12,7 +12,6 @@ from __future__ import annotations
 
 import ctypes as C
 import os
-from typing import List, Sequence, Tuple
 
 import numpy as np
 import torch
