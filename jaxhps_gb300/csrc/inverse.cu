@@ -402,6 +402,7 @@ inv_sblock_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T
 // --------------------------------------------------------------------------
 constexpr int BP = 32;       // panel width
 constexpr int PANEL_NT = 1024;
+constexpr int PANEL_SMEM_ROWS = 4096;   // used flags kept in shared memory up to this n
 
 struct GjeWs {
   // per-matrix region sizes (bytes), each 256-byte aligned; sync = the
@@ -470,6 +471,10 @@ template <class T>
 __global__ void __launch_bounds__(PANEL_NT)
 gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G, T* E, int* piv,
                  unsigned char* used, int* info) {
+  // blockDim.x threads (a multiple of 32, <= PANEL_NT); thread t owns rows
+  // t, t + blockDim.x, ...  Two CTA barriers per column: B1 after every row
+  // update (which also forms the next column's pivot candidates), B2 after
+  // threads 0..bw-1 have formed the scaled pivot row while P is unchanged.
   using MagT = typename MagOf<T>::type;
   const long long b = blockIdx.x;
   const long long nn = (long long)n * n;
@@ -478,107 +483,133 @@ gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G,
   unsigned char* us = used + b * n;
   extern __shared__ unsigned char smraw[];
   const int ldp = n;
+  const int NT = blockDim.x;
   T* P = use_smem ? reinterpret_cast<T*>(smraw) : Pw + b * (long long)n * BP;
   __shared__ T rowr[BP];
   __shared__ int Rs[BP];
-  __shared__ MagT wbest[PANEL_NT / 32];
-  __shared__ int widx[PANEL_NT / 32];
-  __shared__ int s_r;
-  __shared__ MagT s_best;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  __shared__ MagT wbest[2][PANEL_NT / 32];
+  __shared__ int widx[2][PANEL_NT / 32];
+  __shared__ unsigned char ul_s[PANEL_SMEM_ROWS];
+  __shared__ T s_pinv_p;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = NT >> 5;
+  // used flags: shared when they fit, else the global array itself
+  unsigned char* ul = n <= PANEL_SMEM_ROWS ? ul_s : us;
 
-  for (int e = tid; e < n * bw; e += PANEL_NT) {
+  for (int e = tid; e < n * bw; e += NT) {
     const int i = e / bw, c = e % bw;
     P[c * ldp + i] = M[(long long)i * n + k0 + c];
   }
+  if (n <= PANEL_SMEM_ROWS)
+    for (int i = tid; i < n; i += NT) ul_s[i] = us[i];
   __syncthreads();
 
-  for (int c = 0; c < bw; ++c) {
-    const T* col = P + c * ldp;
-    MagT best = -1;
-    int bi = n;
-    for (int i = tid; i < n; i += PANEL_NT) {
-      if (!us[i]) {
-        const MagT mg = nan_to_inf(pivmag(col[i]));
-        if (mg > best) {
-          best = mg;
-          bi = i;
-        }
-      }
-    }
+  auto better = [](MagT m, int i, MagT bm, int bi) { return m > bm || (m == bm && i < bi); };
+  auto publish = [&](int buf, MagT best, int bi) {
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
       const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-      if (ob > best || (ob == best && oi < bi)) {
+      if (better(ob, oi, best, bi)) {
         best = ob;
         bi = oi;
       }
     }
     if (lane == 0) {
-      wbest[warp] = best;
-      widx[warp] = bi;
+      wbest[buf][warp] = best;
+      widx[buf][warp] = bi;
     }
-    __syncthreads();
-    if (warp == 0) {
-      best = lane < PANEL_NT / 32 ? wbest[lane] : (MagT)-1;
-      bi = lane < PANEL_NT / 32 ? widx[lane] : n;
-#pragma unroll
-      for (int off = 16; off; off >>= 1) {
-        const MagT ob = __shfl_xor_sync(0xffffffffu, best, off);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ob > best || (ob == best && oi < bi)) {
-          best = ob;
-          bi = oi;
+  };
+  {
+    MagT best = -1;
+    int bi = n;
+    for (int i = tid; i < n; i += NT)
+      if (!ul[i]) {
+        const MagT mg = nan_to_inf(pivmag(P[i]));
+        if (better(mg, i, best, bi)) {
+          best = mg;
+          bi = i;
         }
       }
-      if (lane == 0) {
-        s_r = bi;
-        s_best = best;
-        us[bi] = 2;  // pivot of the current panel
-        pv[k0 + c] = bi;
-        Rs[c] = bi;
-        if (!(best > 0) && info && info[b] == 0) info[b] = k0 + c + 1;
+    publish(0, best, bi);
+  }
+  __syncthreads();   // B1 of column 0
+
+  for (int c = 0; c < bw; ++c) {
+    const int buf = c & 1;
+    // every thread picks the same pivot from the warp candidates
+    MagT best = -1;
+    int r = n;
+    for (int w = 0; w < nw; ++w) {
+      const MagT m = wbest[buf][w];
+      const int ix = widx[buf][w];
+      if (better(m, ix, best, r)) {
+        best = m;
+        r = ix;
       }
     }
-    __syncthreads();
-    const int r = s_r;
-    const T pinv = (s_best > 0) ? rcp_(col[r]) : zero<T>();
-    if (tid < bw) rowr[tid] = mul(P[tid * ldp + r], pinv);
-    __syncthreads();
-    for (int i = tid; i < n; i += PANEL_NT) {
-      if (i == r) {
-        for (int c2 = 0; c2 < bw; ++c2) P[c2 * ldp + i] = rowr[c2];
-        P[c * ldp + i] = pinv;
-      } else {
-        const T f = P[c * ldp + i];
-        for (int c2 = 0; c2 < bw; ++c2) P[c2 * ldp + i] = fms_(f, rowr[c2], P[c2 * ldp + i]);
-        P[c * ldp + i] = neg(mul(f, pinv));
+    if (r >= n) r = 0;   // unreachable: n - k0 - c rows are still free
+    if (tid < bw) {
+      const T pinv = (best > 0) ? rcp_(P[c * ldp + r]) : zero<T>();
+      rowr[tid] = mul(P[tid * ldp + r], pinv);
+      if (tid == 0) s_pinv_p = pinv;
+    }
+    if (tid == 0) {
+      pv[k0 + c] = r;
+      Rs[c] = r;
+      if (!(best > 0) && info && info[b] == 0) info[b] = k0 + c + 1;
+    }
+    __syncthreads();   // B2: rowr and the pivot's reciprocal ready, every thread has read the candidates
+    // (row r is rewritten by its owner below: nobody reads it after B2)
+    const T pinv = s_pinv_p;
+    MagT nb = -1;
+    int ni = n;
+    for (int i = tid; i < n; i += NT) {
+      if (i == r) continue;
+      const T f = P[c * ldp + i];
+      for (int c2 = 0; c2 < bw; ++c2) {
+        T& x = P[c2 * ldp + i];
+        x = (c2 == c) ? neg(mul(f, pinv)) : fms_(f, rowr[c2], x);
+      }
+      if (c + 1 < bw && !ul[i]) {
+        const MagT mg = nan_to_inf(pivmag(P[(c + 1) * ldp + i]));
+        if (better(mg, i, nb, ni)) {
+          nb = mg;
+          ni = i;
+        }
       }
     }
-    __syncthreads();
+    // the pivot row last: its column c value was the pivot every thread read
+    if (r % NT == tid) {
+      for (int c2 = 0; c2 < bw; ++c2) P[c2 * ldp + r] = (c2 == c) ? pinv : rowr[c2];
+      ul[r] = 2;
+    }
+    if (c + 1 < bw) publish(buf ^ 1, nb, ni);
+    __syncthreads();   // B1 of column c + 1
   }
 
   // outputs: new panel back into M, U (pivot rows zeroed), E, G
   T* Ub = U + b * (long long)n * BP;
   T* Gb = G + b * (long long)BP * n;
   T* Eb = E + b * (long long)BP * BP;
-  for (int e = tid; e < n * bw; e += PANEL_NT) {
+  for (int e = tid; e < n * bw; e += NT) {
     const int i = e / bw, c = e % bw;
     const T v = P[c * ldp + i];
     M[(long long)i * n + k0 + c] = v;
-    Ub[(long long)i * BP + c] = (us[i] == 2) ? zero<T>() : v;
+    Ub[(long long)i * BP + c] = (ul[i] == 2) ? zero<T>() : v;
   }
-  for (int e = tid; e < bw * bw; e += PANEL_NT) {
+  for (int e = tid; e < bw * bw; e += NT) {
     const int c1 = e / bw, c2 = e % bw;
     Eb[c1 * BP + c2] = P[c2 * ldp + Rs[c1]];
   }
-  for (long long e = tid; e < (long long)bw * n; e += PANEL_NT) {
+  for (long long e = tid; e < (long long)bw * n; e += NT) {
     const int c1 = (int)(e / n), j = (int)(e % n);
     Gb[(long long)c1 * n + j] = (j >= k0 && j < k0 + bw) ? zero<T>() : M[(long long)Rs[c1] * n + j];
   }
   __syncthreads();
-  for (int c = tid; c < bw; c += PANEL_NT) us[Rs[c]] = 1;
+  if (n <= PANEL_SMEM_ROWS)
+    for (int i = tid; i < n; i += NT) us[i] = ul_s[i] == 2 ? 1 : ul_s[i];
+  else
+    for (int c = tid; c < bw; c += NT) us[Rs[c]] = 1;
 }
 
 // --------------------------------------------------------------------------
@@ -1363,8 +1394,9 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
                                         csmem, st);
       }
     } else {
-      gje_panel_kernel<T><<<batch, PANEL_NT, use_smem ? pan_smem : 0, st>>>(
-          n, k0, bw, Mat, Pw, use_smem, U, G, E, piv, used, info);
+      const int pnt = n >= PANEL_NT ? PANEL_NT : ((n + 31) / 32) * 32;
+      gje_panel_kernel<T><<<batch, pnt, use_smem ? pan_smem : 0, st>>>(n, k0, bw, Mat, Pw, use_smem, U, G, E, piv,
+                                                                       used, info);
       e = cudaGetLastError();
     }
     if (e != cudaSuccess) return e;
