@@ -407,13 +407,18 @@ def main():
             hps.build_solver(pde_h, precision=args.precision)
             return hps.solve(pde_h, hg, host_device="cpu")
 
-        estep()
+        # two warm-up calls: a caller that keeps one result while computing
+        # the next cycles between two page-locked result blocks, which the
+        # host allocator caches after the second call
+        uh = estep()
+        uh = estep()
         torch.cuda.synchronize()
+        n_e2e = max(2, args.steps // 2)
         t0 = time.perf_counter()
-        for _ in range(max(1, args.steps // 2)):
+        for _ in range(n_e2e):
             uh = estep()
         torch.cuda.synchronize()
-        te = (time.perf_counter() - t0) / max(1, args.steps // 2)
+        te = (time.perf_counter() - t0) / n_e2e
         e2e = {"value": world * n_leaves / te, "unit": "leaves/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": te * 1e3}
         del pde_h, uh

@@ -541,6 +541,12 @@ HPS_API int hps_flux_combine(long long n_nodes, int nsrc, const int* nbr, const 
 /* y += x elementwise (x FP32, y FP64). */
 HPS_API int hps_accumulate(long long n, const float* x, double* y, void* stream);
 
+/* y += x as hps_accumulate, and out[0] = max |x|, out[1] = max |y| after the
+ * update (per element, or per complex (re, im) pair when pairs != 0; n counts
+ * FP32 values): the refinement loop's convergence test in the same pass.
+ * out (2 doubles, device) is overwritten.  No counterpart in the reference. */
+HPS_API int hps_accumulate_max(long long n, int pairs, const float* x, double* y, double* out, void* stream);
+
 
 #ifdef __cplusplus
 }

@@ -173,6 +173,8 @@ def _declare(lib):
     lib.hps_iti_combine.restype = ci
     lib.hps_residual_iti_2d.argtypes = [P(ResidualIti2DArgs), vp]
     lib.hps_residual_iti_2d.restype = ci
+    lib.hps_accumulate_max.argtypes = [cll, ci, vp, vp, vp, vp]
+    lib.hps_accumulate_max.restype = ci
     lib.hps_gemm_policy.argtypes = [ci]
     lib.hps_gemm_policy.restype = ci
     lib.hps_interp_rows.argtypes = [cll, ci, vp, vp, vp, vp, ci, ci, vp]
@@ -210,7 +212,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
 )
 
 
@@ -349,3 +351,14 @@ def inverse(A, out=None, info=None):
     check(L.hps_inverse_batched(dt, n, A.data_ptr(), A.stride(1), A.stride(0), out.data_ptr(), out.stride(1),
                                 out.stride(0), b, ptr(info), ptr(ws), wsb, stream_ptr()), "hps_inverse_batched")
     return out
+
+
+def accumulate_max(x: torch.Tensor, y: torch.Tensor, out: torch.Tensor, pairs: bool = False):
+    """y += x (FP32 into FP64, or complex64 into complex128 with pairs) and
+    (max |x|, max |y|) as two Python floats (one device sync)."""
+    xf = torch.view_as_real(x) if x.is_complex() else x
+    check(lib().hps_accumulate_max(xf.numel(), int(pairs), x.data_ptr(), y.data_ptr(), out.data_ptr(), stream_ptr()),
+          "hps_accumulate_max")
+    mx, my = out.tolist()
+    return mx, my
+

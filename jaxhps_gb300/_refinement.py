@@ -330,16 +330,15 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
     # residual at x = 0 is b itself
     nat.check(L.hps_interior_f32(nl, p * p, 4 * (p - 1), ns, state.f.data_ptr(), r32.data_ptr(), sp),
               "hps_interior_f32")
+    maxima = torch.empty(2, dtype=torch.float64, device=dev)
     state.history = []
     for it in range(max_iters):
         nat.check(L.hps_flux_combine(nl * 4 * q, ns, state.nbr.data_ptr(), flux.data_ptr(), hcorr.data_ptr(),
                                      g_given.shape[0], state.bnode.data_ptr(), g_given.data_ptr(), g.data_ptr(),
                                      rb32.data_ptr(), sp), "hps_flux_combine")
         du, dg = correction(state, r32, hcorr, rb32)
-        nat.check(L.hps_accumulate(du.numel(), du.data_ptr(), u_int.data_ptr(), sp), "hps_accumulate")
         nat.check(L.hps_accumulate(dg.numel(), dg.data_ptr(), g.data_ptr(), sp), "hps_accumulate")
-        step = float(du.abs().max().item())
-        size = float(u_int.abs().max().item())
+        step, size = nat.accumulate_max(du, u_int, maxima)
         state.history.append(step / max(size, 1e-300))
         if step <= tol * size:
             break

@@ -189,16 +189,15 @@ def solve_mixed_iti(pde_problem, boundary_data, source=None, host_device="cpu", 
     rb32 = torch.empty((tg.shape[0], ns), dtype=torch.complex64, device=dev)
     sp = nat.stream_ptr()
     _residual(state, u, t, r32, t_out)
+    maxima = torch.empty(2, dtype=torch.float64, device=dev)
     state.history = []
     for _ in range(max_iters):
         nat.check(L.hps_iti_combine(nl * ng, ns, state.nbr.data_ptr(), t_out.data_ptr(), t.data_ptr(), hcorr.data_ptr(),
                                     tg.shape[0], state.bnode.data_ptr(), tg.data_ptr(), rb32.data_ptr(), sp),
                   "hps_iti_combine")
         du, dt = correction(state, r32, hcorr, rb32)
-        _accumulate(du, u)
         _accumulate(dt, t)
-        step = float(du.abs().max().item())
-        size = float(u.abs().max().item())
+        step, size = nat.accumulate_max(du, u, maxima, pairs=True)
         state.history.append(step / max(size, 1e-300))
         if step <= tol * size:
             break

@@ -61,9 +61,18 @@ def _is_complex(a) -> bool:
 
 
 def _to_host(t: torch.Tensor, host_device):
+    """``t`` on ``host_device`` (None: left where it is).  Device -> CPU
+    copies land in page-locked memory (torch caches those blocks), which
+    the copy engines fill at full link speed; a pageable destination is
+    staged through a bounce buffer at a fraction of it."""
     if host_device is None:
         return t
-    return t.to(torch.device(host_device))
+    dev = torch.device(host_device)
+    if dev.type == "cpu" and t.is_cuda:
+        out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        out.copy_(t)
+        return out
+    return t.to(dev)
 
 
 def _src3(src, n_leaves, n_pts, dtype, dev):

@@ -64,11 +64,12 @@ cudaError_t refine_check_3d(int n_nodes, int p, const double* fv, const int* per
 template <class T>
 cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Tc, const T* hc,
                          const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
-                         const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, cudaStream_t st);
+                         const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, int skip_zero,
+                         cudaStream_t st);
 template <class T>
 cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Rc, const T* hc,
                              const int* int_c, const int* int_l, const int* ext_c, const int* ext_l, T* D, T* C, T* B,
-                             T* Tout, T* dh, T* hext, cudaStream_t st);
+                             T* Tout, T* dh, T* hext, int skip_zero, cudaStream_t st);
 template <class T>
 cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, int ns, const int* code,
                          const T* gpar, const T* gint, T* gch, cudaStream_t st);
@@ -83,6 +84,7 @@ cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const doub
                          const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
                          cudaStream_t st);
 cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st);
+cudaError_t accumulate_max(long long n, int pairs, const float* x, double* y, double* out, cudaStream_t st);
 cudaError_t interp_rows(long long n_rows, int n_src, const double* to, const double* src, const double* w,
                         double* out, int rpg, int transposed, cudaStream_t st);
 cudaError_t gather_cols(long long n_groups, int n_in, int n_out, const int* idx, const double* in, double* out,
@@ -340,14 +342,18 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st, bool iti) {
   const size_t invb = inverse_workspace_bytes(a->dtype, nx > 0 ? nx : ni, nm);
   void* invws = cv.take(invb);
   const bool with_h = ns > 0 && a->h_children && a->h_out && a->g_tilde;
+  // with the block rectangles, the zero blocks of C (and of B unless B is
+  // returned) are never read: the gather leaves them unwritten
+  const bool rects_on = a->n_c_rects > 0 && a->n_b_rects > 0;
+  const int skip_zero = rects_on ? (1 | (a->B_out ? 0 : 2)) : 0;
   if (iti)
     HPS_CHECK(merge_gather_iti<T>(nm, a->nch, a->nb, ni, ne, with_h ? ns : 0, (const T*)a->T_children,
                                   with_h ? (const T*)a->h_children : nullptr, a->int_c, a->int_l, a->ext_c, a->ext_l,
-                                  D, C, B, (T*)a->T_out, dh, (T*)a->h_out, st));
+                                  D, C, B, (T*)a->T_out, dh, (T*)a->h_out, skip_zero, st));
   else
     HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, with_h ? ns : 0, (const T*)a->T_children,
                               with_h ? (const T*)a->h_children : nullptr, a->int_c, a->int_l, a->ext_c, a->ext_l,
-                              a->loc, D, C, B, (T*)a->T_out, dh, (T*)a->h_out, st));
+                              a->loc, D, C, B, (T*)a->T_out, dh, (T*)a->h_out, skip_zero, st));
   const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
   if (nx > 0) {
     // D = [[I, D12], [D21, I]] in colour order; W = I - D12 D21,
@@ -472,11 +478,11 @@ static int up_impl(const hps_up_args* a, cudaStream_t st) {
   if (a->flags & HPS_UP_ITI)
     HPS_CHECK(merge_gather_iti<T>(nm, a->nch, a->nb, ni, ne, ns, nullptr, (const T*)a->h_children, a->int_c,
                                   a->int_l, a->ext_c, a->ext_l, nullptr, nullptr, nullptr, nullptr, (T*)a->dh,
-                                  (T*)a->h_out, st));
+                                  (T*)a->h_out, 0, st));
   else
     HPS_CHECK(merge_gather<T>(nm, a->nch, a->nb, ni, ne, ns, nullptr, (const T*)a->h_children, a->int_c, a->int_l,
                               a->ext_c, a->ext_l, nullptr, nullptr, nullptr, nullptr, nullptr, (T*)a->dh,
-                              (T*)a->h_out, st));
+                              (T*)a->h_out, 0, st));
   HPS_CHECK(gemm_batched<T>(ni, ns, ni, mone, (const T*)a->D_inv, ni, (long long)ni * ni, (const T*)a->dh, ns,
                             (long long)ni * ns, zero_, nullptr, 0, 0, (T*)a->g_tilde, ns, (long long)ni * ns, nm,
                             st));
@@ -1080,6 +1086,15 @@ int hps_flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* 
   }
   HPS_CHECK(flux_combine(n_nodes, nsrc, nbr, flux, hcorr, n_bdry, bdry_node, g_given, g_state, r_bdry,
                          (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_accumulate_max(long long n, int pairs, const float* x, double* y, double* out, void* stream) {
+  if (n < 0 || !x || !y || !out || (pairs && n % 2)) {
+    set_error("hps_accumulate_max: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(accumulate_max(n, pairs, x, y, out, (cudaStream_t)stream));
   return HPS_OK;
 }
 

@@ -293,7 +293,7 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
                                     const T* __restrict__ hc, const int* __restrict__ int_c,
                                     const int* __restrict__ int_l, const int* __restrict__ ext_c,
                                     const int* __restrict__ ext_l, const int* __restrict__ loc, T* D, T* C,
-                                    T* B, T* Tout, T* dh, T* hext, long long m_base) {
+                                    T* B, T* Tout, T* dh, T* hext, int skip_zero, long long m_base) {
   const long long m = blockIdx.y + m_base;
   const int seg = blockIdx.z;
   const long long nbb = (long long)nb * nb;
@@ -326,13 +326,13 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
       const int c = ext_c[x];
       const int li = loc[c * n_int + i];
       if (li >= 0) v = Tm[c * nbb + (long long)li * nb + ext_l[x]];
-      C[m * n_int * (long long)n_ext + e] = v;
+      if (li >= 0 || !(skip_zero & 1)) C[m * n_int * (long long)n_ext + e] = v;
     } else if (seg == 2) {
       const int x = (int)(e / n_int), j = (int)(e % n_int);
       const int c = ext_c[x];
       const int lj = loc[c * n_int + j];
       if (lj >= 0) v = Tm[c * nbb + (long long)ext_l[x] * nb + lj];
-      B[m * n_ext * (long long)n_int + e] = v;
+      if (lj >= 0 || !(skip_zero & 2)) B[m * n_ext * (long long)n_int + e] = v;
     } else if (seg == 3) {
       const int x = (int)(e / n_ext), y = (int)(e % n_ext);
       const int c = ext_c[x];
@@ -358,7 +358,8 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
 template <class T>
 cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Tc, const T* hc,
                          const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
-                         const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, cudaStream_t st) {
+                         const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, int skip_zero,
+                         cudaStream_t st) {
   long long big = Tc ? (long long)n_ext * n_ext : (long long)n_ext * ns;
   int gx = (int)((big + 255) / 256);
   if (gx > 512) gx = 512;
@@ -369,7 +370,8 @@ cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, in
     ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (outs + (double)(n_int + n_ext) * ns));
     note_launch();
     merge_gather_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Tc, hc, int_c, int_l,
-                                                            ext_c, ext_l, loc, D, C, B, Tout, dh, hext, m0);
+                                                            ext_c, ext_l, loc, D, C, B, Tout, dh, hext, skip_zero,
+                                                            m0);
   }
   return cudaGetLastError();
 }
@@ -392,7 +394,7 @@ __global__ void merge_gather_iti_kernel(int nch, int nb, int n_int, int n_ext, i
                                         const T* __restrict__ hc, const int* __restrict__ int_c,
                                         const int* __restrict__ int_l, const int* __restrict__ ext_c,
                                         const int* __restrict__ ext_l, T* D, T* C, T* B, T* Tout, T* dh, T* hext,
-                                        long long m_base) {
+                                        int skip_zero, long long m_base) {
   const long long m = blockIdx.y + m_base;
   const int seg = blockIdx.z;
   const long long nbb = (long long)nb * nb;
@@ -419,13 +421,15 @@ __global__ void merge_gather_iti_kernel(int nch, int nb, int n_int, int n_ext, i
     } else if (seg == 1) {
       const int u = (int)(e / n_ext), x = (int)(e % n_ext);
       const int pc = int_c[2 * u + 1];
-      if (ext_c[x] == pc) v = Rm[pc * nbb + (long long)int_l[2 * u + 1] * nb + ext_l[x]];
-      C[m * n_int * (long long)n_ext + e] = v;
+      const bool nz = ext_c[x] == pc;
+      if (nz) v = Rm[pc * nbb + (long long)int_l[2 * u + 1] * nb + ext_l[x]];
+      if (nz || !(skip_zero & 1)) C[m * n_int * (long long)n_ext + e] = v;
     } else if (seg == 2) {
       const int x = (int)(e / n_int), w = (int)(e % n_int);
       const int c = ext_c[x];
-      if (int_c[2 * w] == c) v = Rm[c * nbb + (long long)ext_l[x] * nb + int_l[2 * w]];
-      B[m * n_ext * (long long)n_int + e] = v;
+      const bool nz = int_c[2 * w] == c;
+      if (nz) v = Rm[c * nbb + (long long)ext_l[x] * nb + int_l[2 * w]];
+      if (nz || !(skip_zero & 2)) B[m * n_ext * (long long)n_int + e] = v;
     } else if (seg == 3) {
       const int x = (int)(e / n_ext), y = (int)(e % n_ext);
       const int c = ext_c[x];
@@ -446,7 +450,7 @@ __global__ void merge_gather_iti_kernel(int nch, int nb, int n_int, int n_ext, i
 template <class T>
 cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Rc, const T* hc,
                              const int* int_c, const int* int_l, const int* ext_c, const int* ext_l, T* D, T* C, T* B,
-                             T* Tout, T* dh, T* hext, cudaStream_t st) {
+                             T* Tout, T* dh, T* hext, int skip_zero, cudaStream_t st) {
   long long big = (long long)(n_ext > n_int ? n_ext : n_int) * (n_ext > n_int ? n_ext : n_int);
   int gx = (int)((big + 255) / 256);
   if (gx > 512) gx = 512;
@@ -457,22 +461,22 @@ cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext
                                                        (double)(n_int + n_ext) * ns));
     note_launch();
     merge_gather_iti_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Rc, hc, int_c, int_l, ext_c,
-                                                                ext_l, D, C, B, Tout, dh, hext, m0);
+                                                                ext_l, D, C, B, Tout, dh, hext, skip_zero, m0);
   }
   return cudaGetLastError();
 }
 template cudaError_t merge_gather_iti<c64>(int, int, int, int, int, int, const c64*, const c64*, const int*,
                                            const int*, const int*, const int*, c64*, c64*, c64*, c64*, c64*, c64*,
-                                           cudaStream_t);
+                                           int, cudaStream_t);
 template cudaError_t merge_gather_iti<c128>(int, int, int, int, int, int, const c128*, const c128*, const int*,
                                             const int*, const int*, const int*, c128*, c128*, c128*, c128*, c128*,
-                                            c128*, cudaStream_t);
+                                            c128*, int, cudaStream_t);
 template cudaError_t merge_gather_iti<float>(int, int, int, int, int, int, const float*, const float*, const int*,
                                              const int*, const int*, const int*, float*, float*, float*, float*,
-                                             float*, float*, cudaStream_t);
+                                             float*, float*, int, cudaStream_t);
 template cudaError_t merge_gather_iti<double>(int, int, int, int, int, int, const double*, const double*, const int*,
                                               const int*, const int*, const int*, double*, double*, double*, double*,
-                                              double*, double*, cudaStream_t);
+                                              double*, double*, int, cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Down-pass scatter  (reference: down_pass/_uniform_2D_DtN.py:125-189)
@@ -550,7 +554,8 @@ cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st) {
                                        long long, int, cudaStream_t);                                            \
   template cudaError_t add_identity<T>(int, int, T*, long long, cudaStream_t);                                 \
   template cudaError_t merge_gather<T>(int, int, int, int, int, int, const T*, const T*, const int*, const int*, \
-                                       const int*, const int*, const int*, T*, T*, T*, T*, T*, T*, cudaStream_t); \
+                                       const int*, const int*, const int*, T*, T*, T*, T*, T*, T*, int,           \
+                                       cudaStream_t);                                                           \
   template cudaError_t down_scatter<T>(int, int, int, int, int, int, const int*, const T*, const T*, T*,        \
                                        cudaStream_t);
 HPS_INST_K(float)

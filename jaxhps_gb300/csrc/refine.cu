@@ -529,6 +529,87 @@ __global__ void accumulate_kernel(long long n, const float* __restrict__ x, doub
     y[e] += (double)x[e];
 }
 
+// y += x (n FP32 values into FP64), with the largest |x| and the largest
+// updated |y| (per element, or per (re, im) pair when pairs != 0) written to
+// out[0], out[1]: the refinement's convergence test in the same pass.
+// Non-negative doubles compare like their bit patterns, so the block maxima
+// combine through atomicMax on the 64-bit words.
+// max that keeps a NaN once seen (fmax would drop it and a NaN correction
+// could pass the convergence test)
+__device__ __forceinline__ double nanmax(double a, double b) {
+  return (a != a) ? a : ((b != b || b > a) ? b : a);
+}
+
+__global__ void accumulate_max_kernel(long long n, int pairs, const float* __restrict__ x, double* y,
+                                      unsigned long long* out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ unsigned long long sx[32], sy[32];
+  if (pairs) {
+    // complex magnitudes in FP64 (the complex refinement's vectors are short)
+    double mx = 0.0, my = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n / 2; e += stride) {
+      const float xr = x[2 * e], xi = x[2 * e + 1];
+      const double yr = y[2 * e] + (double)xr, yi = y[2 * e + 1] + (double)xi;
+      y[2 * e] = yr;
+      y[2 * e + 1] = yi;
+      mx = nanmax(mx, sqrt((double)xr * xr + (double)xi * xi));
+      my = nanmax(my, sqrt(yr * yr + yi * yi));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = nanmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      my = nanmax(my, __shfl_xor_sync(0xffffffffu, my, o));
+    }
+    if (lane == 0) {
+      sx[warp] = (unsigned long long)__double_as_longlong(mx);
+      sy[warp] = (unsigned long long)__double_as_longlong(my);
+    }
+  } else {
+    // magnitudes compared as integer bit patterns (sign cleared): no FP64
+    // compares on the FP64 pipe; a NaN sorts above every number and stays
+    unsigned int bx = 0;
+    unsigned long long by = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += stride) {
+      const float xv = x[e];
+      const double v = y[e] + (double)xv;
+      y[e] = v;
+      bx = max(bx, __float_as_uint(xv) & 0x7fffffffu);
+      by = max(by, (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      bx = max(bx, __shfl_xor_sync(0xffffffffu, bx, o));
+      by = max(by, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)by, o));
+    }
+    if (lane == 0) {
+      const float fx = __uint_as_float(bx);
+      sx[warp] = (unsigned long long)__double_as_longlong((double)fx);
+      sy[warp] = by;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long ax = sx[0], ay = sy[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      ax = max(ax, sx[w]);
+      ay = max(ay, sy[w]);
+    }
+    atomicMax(out, ax);
+    atomicMax(out + 1, ay);
+  }
+}
+
+cudaError_t accumulate_max(long long n, int pairs, const float* x, double* y, double* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  long long g = (n + 255) / 256;
+  if (g > 8192) g = 8192;
+  if (g < 1) g = 1;
+  ProfScope ps(KC_MOVE, st, 20.0 * (double)n);
+  note_launch();
+  accumulate_max_kernel<<<(int)g, 256, 0, st>>>(n, pairs, x, y, reinterpret_cast<unsigned long long*>(out));
+  return cudaGetLastError();
+}
+
 cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st) {
   long long g = (n + 255) / 256;
   if (g > 8192) g = 8192;
