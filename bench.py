@@ -413,7 +413,7 @@ def main():
         uh = estep()
         uh = estep()
         torch.cuda.synchronize()
-        n_e2e = max(2, args.steps // 2)
+        n_e2e = max(3, args.steps)
         t0 = time.perf_counter()
         for _ in range(n_e2e):
             uh = estep()
