@@ -67,7 +67,9 @@ HPS_API int hps_gemm_tc_status(void);
 /* Which batched products run on the tcgen05 kernel: 0 none (SIMT kernels
  * only), 1 the shapes where it was measured faster (default; HPS_GEMM_TC=0 in
  * the environment starts a process at 0), 2 every FP32 and complex64 product
- * (for tests and measurements).  Returns the previous policy, or -1 for an
+ * (for tests and measurements), 3 none and the FP32 8x8 SIMT tiles with 4-byte
+ * shared-memory loads instead of the 16-byte-load tiles (for comparisons;
+ * identical results).  Returns the previous policy, or -1 for an
  * invalid one.  Process-wide; not meant to change while work is in flight.
  * No counterpart in the reference. */
 HPS_API int hps_gemm_policy(int policy);

@@ -208,6 +208,7 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     dev = st._device(device)
     p, q, n_leaves = dom.p, dom.q, dom.n_leaves
     n_cb = 4 * (p - 1)
+    upload = st._SourceUpload(pde_problem.source, n_leaves, p * p, torch.float64, dev)
     Y, T, _, _, Aii = st._local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, dev, leaf_dtype,
                                           keep_inverse=True, want_source=False)
     Y, Aii = Y.float(), Aii.float()
@@ -233,7 +234,7 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     del T
     st.raise_on_sync_timeout(infos)
 
-    f, multi = st._src3(pde_problem.source, n_leaves, p * p, torch.float64, dev)
+    f, multi = upload.result()
 
     Q32 = torch.as_tensor(np.ascontiguousarray(pde_problem.Q[:, n_cb:]), device=dev, dtype=torch.float32)
     state = MixedState(

@@ -139,6 +139,7 @@ def build_mixed_dense(pde_problem, return_top_T=False, device=None, tol: float =
     n_pts = Q_np.shape[1]
     n_i = n_pts - n_cb
     nl = dom.n_leaves
+    upload = st._SourceUpload(pde_problem.source, nl, n_pts, torch.float64, dev)
     ops_t, coeffs, cplx = st._coefficients(pde_problem, dev)
     if cplx:
         raise NotImplementedError("mixed precision with complex coefficients is not implemented")
@@ -169,7 +170,7 @@ def build_mixed_dense(pde_problem, return_top_T=False, device=None, tol: float =
         B_lst.append(B.float())
     del T
     st.raise_on_sync_timeout(infos)
-    f, multi = st._src3(pde_problem.source, nl, n_pts, torch.float64, dev)
+    f, multi = upload.result()
     nbr, bnode = _node_pairing(dom, dev)
     state = DenseMixedState(
         mixed=True, dense=True, dim=dim, n_leaves=nl, n_pts=n_pts, n_cb=n_cb, Aint=Aint, P64=P64, Q64=Q64,

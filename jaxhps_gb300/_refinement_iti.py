@@ -92,6 +92,7 @@ def build_mixed_iti(pde_problem, return_top_T=False, device=None, tol: float = 1
         raise NotImplementedError("the mixed-precision residual assumes square leaves")
     dev = st._device(device)
     src = pde_problem.source
+    upload = st._SourceUpload(src, dom.n_leaves, pde_problem.G.shape[1], torch.complex128, dev)
     pde_problem.source = None
     try:
         Y, T, _, _, Binv = st.local_solve_stage_uniform_2D_ItI(pde_problem, device=dev, dtype=torch.complex64,
@@ -103,7 +104,7 @@ def build_mixed_iti(pde_problem, return_top_T=False, device=None, tol: float = 1
     coeffs, op_kind = _coefficients(pde_problem, dev)
     out = _nosource_merge(T, dom.L, True, dev, return_top_T)
     del T
-    f, multi = st._src3(src, nl, n_pts, torch.complex128, dev)
+    f, multi = upload.result()
     nbr, bnode = _node_pairing(dom, dev)
     QH32 = torch.as_tensor(np.ascontiguousarray(pde_problem.QH), device=dev).to(torch.complex64)
     state = ItiMixedState(

@@ -83,6 +83,44 @@ def _src3(src, n_leaves, n_pts, dtype, dev):
     return s, True
 
 
+class _SourceUpload:
+    """The source's host -> device copy, started before the build so that the
+    copy engine moves it while the build's kernels run.  A page-locked,
+    contiguous CPU tensor of the working dtype is copied on a side stream
+    (which first waits for the work already queued on the current stream,
+    as the destination block may come from memory that work still uses);
+    ``result()`` makes the current stream wait for that copy — a device-side
+    wait, the host goes on — and returns (tensor, was_multi) as ``_src3``.
+    Any other source is converted by ``_src3`` when ``result()`` is called."""
+
+    def __init__(self, src, n_leaves, n_pts, dtype, dev):
+        self.args = (src, n_leaves, n_pts, dtype, dev)
+        self.out = None
+        self.event = None
+        if (isinstance(src, torch.Tensor) and src.device.type == "cpu" and src.dtype == dtype
+                and src.is_contiguous() and src.is_pinned() and dev.type == "cuda"):
+            main = torch.cuda.current_stream(dev)
+            side = torch.cuda.Stream(device=dev)
+            dst = torch.empty(src.shape, dtype=dtype, device=dev)
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                dst.copy_(src, non_blocking=True)
+            dst.record_stream(side)   # the block is not reused before the copy ends, even if the build fails
+            self.event = torch.cuda.Event()
+            self.event.record(side)
+            self.out = dst
+
+    def result(self):
+        if self.out is None:
+            return _src3(*self.args)
+        src, n_leaves, n_pts, dtype, dev = self.args
+        torch.cuda.current_stream(dev).wait_event(self.event)
+        s = self.out
+        if s.dim() == 2:
+            return s.unsqueeze(-1), False
+        return s, True
+
+
 def _coefficients(pde_problem, dev):
     cs, ops = pde_problem.active_coefficients()
     if not cs:

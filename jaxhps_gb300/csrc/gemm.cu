@@ -129,6 +129,196 @@ gemm_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, long long lda
   }
 }
 
+// FP32 8x8 register tiles with 16-byte shared-memory loads.  Thread (tx, ty)
+// owns rows {4ty .. 4ty+3} and {BM/2 + 4ty ..} and columns {4tx .. 4tx+3}
+// and {BN/2 + 4tx ..}: each k step reads its 8 A and 8 B values with four
+// 16-byte loads (a warp's loads from one row of As or Bs cover one
+// contiguous 64- or 128-byte span), where gemm_kernel<float, .., 8, 8> uses
+// sixteen 4-byte loads.  A is stored transposed with a row pitch of BM + 4
+// floats, which makes the transposing stores conflict-free.  Global tiles
+// move as float4 where the rows allow it (vec_* flags, checked on the host).
+// The k order of every output's FMA chain is that of gemm_kernel, so the two
+// kernels give identical results.
+template <int BM, int BN>
+__global__ void __launch_bounds__((BM / 8) * (BN / 8), 65536 / ((BM / 8) * (BN / 8) * 128))   // <= 128 registers
+gemm_f32_v4_kernel(int M, int N, int K, float alpha, const float* __restrict__ A, long long lda, long long sA,
+                   const float* __restrict__ B, long long ldb, long long sB, float beta, const float* C,
+                   long long ldc, long long sC, float* D, long long ldd, long long sD, int use_c, int vec_a,
+                   int vec_b, int vec_cd) {
+  constexpr int BK = 8;
+  constexpr int NTX = BN / 8, NTY = BM / 8, NT = NTX * NTY;
+  constexpr int PA = BM + 4;
+  constexpr int A4 = BM * BK / 4 / NT;   // float4 chunks of the A tile per thread
+  constexpr int B4 = BK * BN / 4 / NT;
+  static_assert(A4 >= 1 && B4 >= 1 && A4 * 4 * NT == BM * BK && B4 * 4 * NT == BK * BN, "tile split");
+  __shared__ __align__(16) float As[2][BK][PA];
+  __shared__ __align__(16) float Bs[2][BK][BN];
+
+  const long long bz = blockIdx.z;
+  A += bz * sA;
+  B += bz * sB;
+  D += bz * sD;
+  if (use_c) C += bz * sC;
+  const int m0 = blockIdx.y * BM;
+  const int n0 = blockIdx.x * BN;
+  const int tid = threadIdx.x;
+  const int tx = tid % NTX;
+  const int ty = tid / NTX;
+
+  float4 ra[A4], rb[B4];
+  auto load_tiles = [&](int k0) {
+#pragma unroll
+    for (int l = 0; l < A4; ++l) {
+      const int f = tid + l * NT;
+      const int r = f / (BK / 4), c = (f % (BK / 4)) * 4;
+      const int gm = m0 + r, gk = k0 + c;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gm < M) {
+        const float* src = A + (long long)gm * lda + gk;
+        if (vec_a && gk + 3 < K) {
+          v = *reinterpret_cast<const float4*>(src);
+        } else {
+          if (gk < K) v.x = src[0];
+          if (gk + 1 < K) v.y = src[1];
+          if (gk + 2 < K) v.z = src[2];
+          if (gk + 3 < K) v.w = src[3];
+        }
+      }
+      ra[l] = v;
+    }
+#pragma unroll
+    for (int l = 0; l < B4; ++l) {
+      const int f = tid + l * NT;
+      const int r = f / (BN / 4), c = (f % (BN / 4)) * 4;
+      const int gk = k0 + r, gn = n0 + c;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gk < K) {
+        const float* src = B + (long long)gk * ldb + gn;
+        if (vec_b && gn + 3 < N) {
+          v = *reinterpret_cast<const float4*>(src);
+        } else {
+          if (gn < N) v.x = src[0];
+          if (gn + 1 < N) v.y = src[1];
+          if (gn + 2 < N) v.z = src[2];
+          if (gn + 3 < N) v.w = src[3];
+        }
+      }
+      rb[l] = v;
+    }
+  };
+  auto store_tiles = [&](int buf) {
+#pragma unroll
+    for (int l = 0; l < A4; ++l) {
+      const int f = tid + l * NT;
+      const int r = f / (BK / 4), c = (f % (BK / 4)) * 4;
+      As[buf][c + 0][r] = ra[l].x;
+      As[buf][c + 1][r] = ra[l].y;
+      As[buf][c + 2][r] = ra[l].z;
+      As[buf][c + 3][r] = ra[l].w;
+    }
+#pragma unroll
+    for (int l = 0; l < B4; ++l) {
+      const int f = tid + l * NT;
+      const int r = f / (BN / 4), c = (f % (BN / 4)) * 4;
+      *reinterpret_cast<float4*>(&Bs[buf][r][c]) = rb[l];
+    }
+  };
+
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+
+  const int ktiles = (K + BK - 1) / BK;
+  if (ktiles > 0) {
+    load_tiles(0);
+    store_tiles(0);
+    __syncthreads();
+  }
+  for (int kt = 0; kt < ktiles; ++kt) {
+    const int buf = kt & 1;
+    if (kt + 1 < ktiles) load_tiles((kt + 1) * BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][4 * ty]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][BM / 2 + 4 * ty]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][4 * tx]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][BN / 2 + 4 * tx]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    if (kt + 1 < ktiles) {
+      store_tiles(buf ^ 1);
+      __syncthreads();
+    }
+  }
+
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int gm = m0 + (i < 4 ? 4 * ty + i : BM / 2 + 4 * ty + i - 4);
+    if (gm >= M) continue;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int gn = n0 + h * (BN / 2) + 4 * tx;
+      float v[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = alpha * acc[i][4 * h + j];
+      if (vec_cd && gn + 3 < N) {
+        if (use_c) {
+          const float4 c = *reinterpret_cast<const float4*>(C + (long long)gm * ldc + gn);
+          v[0] = fmaf(beta, c.x, v[0]);
+          v[1] = fmaf(beta, c.y, v[1]);
+          v[2] = fmaf(beta, c.z, v[2]);
+          v[3] = fmaf(beta, c.w, v[3]);
+        }
+        *reinterpret_cast<float4*>(D + (long long)gm * ldd + gn) = make_float4(v[0], v[1], v[2], v[3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (gn + j >= N) continue;
+          float x = v[j];
+          if (use_c) x = fmaf(beta, C[(long long)gm * ldc + gn + j], x);
+          D[(long long)gm * ldd + gn + j] = x;
+        }
+      }
+    }
+  }
+}
+
+static inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+template <int BM, int BN>
+static cudaError_t launch_gemm_f32_v4(int M, int N, int K, float alpha, const float* A, long long lda, long long sA,
+                                      const float* B, long long ldb, long long sB, float beta, const float* C,
+                                      long long ldc, long long sC, float* D, long long ldd, long long sD, int batch,
+                                      cudaStream_t st) {
+  const int use_c = (C != nullptr);
+  constexpr int NT = (BM / 8) * (BN / 8);
+  // float4 rows: leading dimensions and batch strides multiples of 4 floats,
+  // base addresses 16-byte aligned (then every row start and k or n offset
+  // that is a multiple of 4 is 16-byte aligned too)
+  const int vec_a = (lda % 4 == 0) && (sA % 4 == 0) && aligned16(A);
+  const int vec_b = (ldb % 4 == 0) && (sB % 4 == 0) && aligned16(B);
+  const int vec_cd = (ldd % 4 == 0) && (sD % 4 == 0) && aligned16(D) &&
+                     (!use_c || ((ldc % 4 == 0) && (sC % 4 == 0) && aligned16(C)));
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, nb);
+    ProfScope ps(KC_GEMM, st, 2.0 * M * (double)N * K * nb);
+    note_launch();
+    // batch offsets keep the alignment: sA, sB, sC, sD are multiples of 4 when the flags are set
+    gemm_f32_v4_kernel<BM, BN><<<grid, NT, 0, st>>>(M, N, K, alpha, A + b0 * sA, lda, sA, B + b0 * sB, ldb, sB, beta,
+                                                    use_c ? C + b0 * sC : nullptr, ldc, sC, D + b0 * sD, ldd, sD,
+                                                    use_c, vec_a, vec_b, vec_cd);
+  }
+  return cudaGetLastError();
+}
+
 template <class T, int BM, int BN, int BK, int TM, int TN>
 static cudaError_t launch_gemm_cfg(int M, int N, int K, T alpha, const T* A, long long lda, long long sA,
                                    const T* B, long long ldb, long long sB, T beta, const T* C,
@@ -223,9 +413,10 @@ static cudaError_t launch_skinny(int M, int N, int K, T alpha, const T* A, long 
 }
 
 // Which products run on the tensor cores (gemm_tc.cu): 0 none, 1 the shapes
-// where they were measured faster (default), 2 every FP32 / complex64 product.
-// HPS_GEMM_TC=0 in the environment starts the process at 0; hps_gemm_policy()
-// changes it.
+// where they were measured faster (default), 2 every FP32 / complex64 product,
+// 3 none and the FP32 8x8 tiles with 4-byte shared loads (gemm_kernel) in
+// place of gemm_f32_v4_kernel, for comparisons.  HPS_GEMM_TC=0 in the
+// environment starts the process at 0; hps_gemm_policy() changes it.
 static std::atomic<int> g_policy{-1};
 
 static int gemm_policy() {
@@ -239,7 +430,7 @@ static int gemm_policy() {
 }
 
 int set_gemm_policy(int p) {
-  if (p < 0 || p > 2) return -1;
+  if (p < 0 || p > 3) return -1;
   const int old = gemm_policy();
   g_policy.store(p, std::memory_order_relaxed);
   return old;
@@ -272,21 +463,29 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
     if (alpha.y == 0.f && beta.y == 0.f && (pol == 2 || (pol == 1 && M >= 128 && N >= 128 && K >= 128)))
       return gemm_tf32x3_c64(M, N, K, alpha.x, A, lda, sA, B, ldb, sB, beta.x, C, ldc, sC, D, ldd, sD, batch, st);
   }
-  if (sizeof(T) == 4) {
+  if constexpr (std::is_same<T, float>::value) {
+    const bool v4 = (pol != 3);
     const long long tiles128 = (long long)((M + 127) / 128) * ((N + 127) / 128) * batch;
     if (M >= 96 && N >= 96 && tiles128 >= 120)
-      return launch_gemm_cfg<T, 128, 128, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
-                                                   ldc, sC, D, ldd, sD, batch, st);
+      return v4 ? launch_gemm_f32_v4<128, 128>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd,
+                                               sD, batch, st)
+                : launch_gemm_cfg<T, 128, 128, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D,
+                                                        ldd, sD, batch, st);
     // N <= 64 (many right-hand sides, leaf and merge blocks): 8x8 register
-    // tiles (16 shared loads per 64 FMAs instead of 8 per 16)
+    // tiles (4 16-byte shared loads per 64 FMAs where 4x4 tiles need 8 4-byte
+    // loads per 16)
     const long long tiles_m128 = (long long)((M + 127) / 128) * batch;
     if (N > 32 && N <= 64 && M >= 96 && tiles_m128 >= 152)
-      return launch_gemm_cfg<T, 128, 64, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
-                                                  ldc, sC, D, ldd, sD, batch, st);
+      return v4 ? launch_gemm_f32_v4<128, 64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD,
+                                              batch, st)
+                : launch_gemm_cfg<T, 128, 64, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D,
+                                                       ldd, sD, batch, st);
     const long long tiles_m64 = (long long)((M + 63) / 64) * batch;
     if (N > 32 && N <= 64 && M >= 32 && tiles_m64 >= 304)
-      return launch_gemm_cfg<T, 64, 64, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C,
-                                                 ldc, sC, D, ldd, sD, batch, st);
+      return v4 ? launch_gemm_f32_v4<64, 64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD,
+                                             batch, st)
+                : launch_gemm_cfg<T, 64, 64, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D,
+                                                      ldd, sD, batch, st);
     return launch_gemm_cfg<T, 64, 64, 8, 4, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
                                                sC, D, ldd, sD, batch, st);
   }

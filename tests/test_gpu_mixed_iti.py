@@ -66,3 +66,25 @@ def test_mixed_iti_helmholtz_scattering_vs_complex128(cuda):
             assert len(pde._state.history) <= 8
         del pde
     assert _rel(sols["mixed"], sols["float64"]) < 1e-10
+
+
+def test_mixed_iti_pinned_source_matches_numpy_source(cuda):
+    """A page-locked complex128 source (copied while the build runs) gives
+    the same solution, bit for bit, as the NumPy source."""
+    import torch
+    L, p, q, k = 3, 12, 10, 15.0
+    root = hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0)
+    dom = hps.Domain(p=p, q=q, root=root, L=L)
+    x = dom.interior_points
+    rng = np.random.default_rng(7)
+    Icoef = k ** 2 * (1 + 0.3 * np.exp(-(x ** 2).sum(-1) / 0.1))
+    ones = np.ones_like(Icoef)
+    f = rng.standard_normal(x.shape[:2] + (2,)) + 1j * rng.standard_normal(x.shape[:2] + (2,))
+    g = np.exp(1j * k * dom.boundary_points[:, 1] * 0.4)
+    sols = []
+    for src in (f, torch.as_tensor(f).pin_memory()):
+        pde = hps.PDEProblem(dom, source=src, D_xx_coefficients=ones, D_yy_coefficients=ones,
+                             I_coefficients=Icoef, use_ItI=True, eta=k)
+        hps.build_solver(pde, precision="mixed")
+        sols.append(hps.solve(pde, g).numpy())
+    assert np.array_equal(sols[0], sols[1])

@@ -201,3 +201,43 @@ def test_gemm_policy_every_product_on_tensor_cores(cuda, dt, m, n, k, batch):
     err = np.abs(tC.cpu().numpy() - ref).max() / np.abs(ref).max()
     assert err < 3e-6 * max(1.0, np.sqrt(2 * k / 64)), err
     assert L.hps_gemm_tc_status() == 0
+
+
+@pytest.mark.parametrize("m,n,k,batch,pad", [(196, 64, 196, 160, 0), (196, 56, 60, 200, 0), (56, 64, 256, 400, 0),
+                                             (130, 129, 67, 120, 0), (200, 37, 50, 200, 0), (100, 48, 33, 400, 1),
+                                             (97, 97, 9, 130, 3)])
+def test_gemm_f32_vector_tiles_match_scalar_tiles(cuda, m, n, k, batch, pad):
+    """The FP32 8x8 tiles with 16-byte shared loads (default) against the
+    same tiles with 4-byte loads (policy 3): the FMA order per output is the
+    same, so the results are identical, for tile-aligned and ragged M, N, K,
+    leading dimensions that are not multiples of 4 (pad > 0: scalar global
+    loads), a broadcast A and C == D in place.  Both against NumPy too."""
+    from jaxhps_gb300 import _native as nat
+
+    L = nat.load_library()
+    rng = np.random.default_rng(m + 3 * n + 7 * k)
+    A = rng.standard_normal((batch, m, k + pad)).astype(np.float32)
+    B = rng.standard_normal((batch, k, n + pad)).astype(np.float32)
+    Cm = rng.standard_normal((batch, m, n + pad)).astype(np.float32)
+    tA = torch.as_tensor(A, device=cuda)[:, :, :k]
+    tB = torch.as_tensor(B, device=cuda)[:, :, :n]
+    outs = []
+    for pol in (0, 3):
+        old = L.hps_gemm_policy(pol)
+        try:
+            tC = torch.as_tensor(Cm, device=cuda)[:, :, :n]
+            out = torch.empty((batch, m, n + pad), dtype=torch.float32, device=cuda)[:, :, :n]
+            nat.gemm(tA, tB, out, alpha=-0.75, beta=1.5, Cmat=tC)
+            nat.gemm(tA[0], tB, tC, alpha=1.0, beta=1.0, Cmat=tC)     # broadcast A, in place
+            torch.cuda.synchronize()
+        finally:
+            L.hps_gemm_policy(old)
+        outs.append((out.cpu().numpy(), tC.cpu().numpy()))
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][1], outs[1][1])
+    A64, B64, C64 = A[:, :, :k].astype(np.float64), B[:, :, :n].astype(np.float64), Cm[:, :, :n].astype(np.float64)
+    ref = -0.75 * A64 @ B64 + 1.5 * C64
+    ref2 = A64[0] @ B64 + C64
+    scale = max(1.0, np.abs(ref).max()) * max(1, k) ** 0.5
+    assert np.abs(outs[0][0] - ref).max() <= 2e-5 * scale * 10
+    assert np.abs(outs[0][1] - ref2).max() <= 2e-5 * scale * 10

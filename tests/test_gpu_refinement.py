@@ -107,3 +107,21 @@ def test_incremental_residual_matches_fp64(cuda, extra):
     scale_f = float(fl_d.abs().max())
     assert float((r64 - r64b).abs().max()) < 1e-10 * scale_r
     assert float((flux - flux_b).abs().max()) < 1e-10 * scale_f
+
+
+def test_pinned_source_upload_matches_numpy_source(cuda):
+    """A page-locked CPU source is copied on a side stream while the build
+    runs; the solution is bit-identical to the one from a NumPy source."""
+    L, p, q, ns = 3, 12, 10, 4
+    dom, pde, _ = _setup(L, p, q, ns, True, seed=5)
+    bp = dom.boundary_points
+    g = np.stack([np.cos(bp[:, 0]) * (k + 1) for k in range(ns)], -1)
+    hps.build_solver(pde, precision="mixed")
+    u_np = hps.solve(pde, g).numpy()
+    f_pin = torch.as_tensor(pde.source).pin_memory()
+    dom2, pde2, _ = _setup(L, p, q, ns, True, seed=5)
+    pde2.source = f_pin
+    hps.build_solver(pde2, precision="mixed")
+    u_pin = hps.solve(pde2, g).numpy()
+    assert np.array_equal(u_np, u_pin)
+    assert len(pde2._state.history) == len(pde._state.history)
