@@ -13,6 +13,8 @@
 #include <atomic>
 #include <type_traits>
 
+#include <cooperative_groups.h>
+
 #include "hps_common.cuh"
 
 #include "hps_internal.h"
@@ -139,12 +141,21 @@ gemm_kernel(int M, int N, int K, T alpha, const T* __restrict__ A, long long lda
 // move as float4 where the rows allow it (vec_* flags, checked on the host).
 // The k order of every output's FMA chain is that of gemm_kernel, so the two
 // kernels give identical results.
-template <int BM, int BN>
+//
+// SPLIT: split-K for products with few output tiles and a long K (the
+// correction's products at the top merge levels: a few tall N = 64 tiles,
+// K in the thousands).  The `splits` CTAs of a thread-block cluster share one
+// output tile, CTA r accumulating the K-slice r; each stores its partial tile
+// in shared memory and, after a cluster barrier, sums its BM / splits rows
+// of the tile over the partials of ranks 0, 1, ... in that order (reads
+// through distributed shared memory), so the result is deterministic and no
+// global workspace is needed.
+template <int BM, int BN, bool SPLIT = false>
 __global__ void __launch_bounds__((BM / 8) * (BN / 8), 65536 / ((BM / 8) * (BN / 8) * 128))   // <= 128 registers
 gemm_f32_v4_kernel(int M, int N, int K, float alpha, const float* __restrict__ A, long long lda, long long sA,
                    const float* __restrict__ B, long long ldb, long long sB, float beta, const float* C,
                    long long ldc, long long sC, float* D, long long ldd, long long sD, int use_c, int vec_a,
-                   int vec_b, int vec_cd) {
+                   int vec_b, int vec_cd, int splits) {
   constexpr int BK = 8;
   constexpr int NTX = BN / 8, NTY = BM / 8, NT = NTX * NTY;
   constexpr int PA = BM + 4;
@@ -160,7 +171,16 @@ gemm_f32_v4_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
   D += bz * sD;
   if (use_c) C += bz * sC;
   const int m0 = blockIdx.y * BM;
-  const int n0 = blockIdx.x * BN;
+  int tile_x = blockIdx.x, kbeg = 0, kend = K;
+  if constexpr (SPLIT) {
+    // cluster dims (splits, 1, 1): the CTAs of a cluster are consecutive in x
+    const int r = (int)(blockIdx.x % (unsigned)splits);
+    tile_x = (int)(blockIdx.x / (unsigned)splits);
+    const int kc = ((K + splits - 1) / splits + BK - 1) / BK * BK;   // multiple of BK: float4 loads stay aligned
+    kbeg = min(K, r * kc);
+    kend = min(K, kbeg + kc);
+  }
+  const int n0 = tile_x * BN;
   const int tid = threadIdx.x;
   const int tx = tid % NTX;
   const int ty = tid / NTX;
@@ -175,13 +195,13 @@ gemm_f32_v4_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (gm < M) {
         const float* src = A + (long long)gm * lda + gk;
-        if (vec_a && gk + 3 < K) {
+        if (vec_a && gk + 3 < kend) {
           v = *reinterpret_cast<const float4*>(src);
         } else {
-          if (gk < K) v.x = src[0];
-          if (gk + 1 < K) v.y = src[1];
-          if (gk + 2 < K) v.z = src[2];
-          if (gk + 3 < K) v.w = src[3];
+          if (gk < kend) v.x = src[0];
+          if (gk + 1 < kend) v.y = src[1];
+          if (gk + 2 < kend) v.z = src[2];
+          if (gk + 3 < kend) v.w = src[3];
         }
       }
       ra[l] = v;
@@ -192,7 +212,7 @@ gemm_f32_v4_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
       const int r = f / (BN / 4), c = (f % (BN / 4)) * 4;
       const int gk = k0 + r, gn = n0 + c;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gk < K) {
+      if (gk < kend) {
         const float* src = B + (long long)gk * ldb + gn;
         if (vec_b && gn + 3 < N) {
           v = *reinterpret_cast<const float4*>(src);
@@ -230,15 +250,15 @@ gemm_f32_v4_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
 
-  const int ktiles = (K + BK - 1) / BK;
+  const int ktiles = (kend - kbeg + BK - 1) / BK;
   if (ktiles > 0) {
-    load_tiles(0);
+    load_tiles(kbeg);
     store_tiles(0);
     __syncthreads();
   }
   for (int kt = 0; kt < ktiles; ++kt) {
     const int buf = kt & 1;
-    if (kt + 1 < ktiles) load_tiles((kt + 1) * BK);
+    if (kt + 1 < ktiles) load_tiles(kbeg + (kt + 1) * BK);
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][4 * ty]);
@@ -256,6 +276,36 @@ gemm_f32_v4_kernel(int M, int N, int K, float alpha, const float* __restrict__ A
       store_tiles(buf ^ 1);
       __syncthreads();
     }
+  }
+
+  if constexpr (SPLIT) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ __align__(16) float part[BM * BN];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = i < 4 ? 4 * ty + i : BM / 2 + 4 * ty + i - 4;
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+        *reinterpret_cast<float4*>(&part[row * BN + h * (BN / 2) + 4 * tx]) =
+            make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
+    }
+    cluster.sync();
+    const int rank = (int)cluster.block_rank();
+    const int rows = BM / splits;
+    for (int e = tid; e < rows * BN; e += NT) {
+      const int row = rank * rows + e / BN, col = e % BN;
+      float sum = 0.f;
+      for (int q = 0; q < splits; ++q) sum += *cluster.map_shared_rank(&part[row * BN + col], q);
+      const int gm = m0 + row, gn = n0 + col;
+      if (gm < M && gn < N) {
+        float x = alpha * sum;
+        if (use_c) x = fmaf(beta, C[(long long)gm * ldc + gn], x);
+        D[(long long)gm * ldd + gn] = x;
+      }
+    }
+    cluster.sync();   // the partial tiles stay alive until every CTA has read them
+    return;
   }
 
 #pragma unroll
@@ -314,7 +364,46 @@ static cudaError_t launch_gemm_f32_v4(int M, int N, int K, float alpha, const fl
     // batch offsets keep the alignment: sA, sB, sC, sD are multiples of 4 when the flags are set
     gemm_f32_v4_kernel<BM, BN><<<grid, NT, 0, st>>>(M, N, K, alpha, A + b0 * sA, lda, sA, B + b0 * sB, ldb, sB, beta,
                                                     use_c ? C + b0 * sC : nullptr, ldc, sC, D + b0 * sD, ldd, sD,
-                                                    use_c, vec_a, vec_b, vec_cd);
+                                                    use_c, vec_a, vec_b, vec_cd, 1);
+  }
+  return cudaGetLastError();
+}
+
+// Split-K launch of gemm_f32_v4_kernel<BM, BN, true>: clusters of `splits`
+// CTAs (2, 4 or 8, dividing BM) along x, one cluster per output tile.
+template <int BM, int BN>
+static cudaError_t launch_gemm_f32_v4_split(int M, int N, int K, float alpha, const float* A, long long lda,
+                                            long long sA, const float* B, long long ldb, long long sB, float beta,
+                                            const float* C, long long ldc, long long sC, float* D, long long ldd,
+                                            long long sD, int batch, int splits, cudaStream_t st) {
+  if (splits < 2 || splits > 8 || BM % splits != 0) return cudaErrorInvalidValue;
+  const int use_c = (C != nullptr);
+  constexpr int NT = (BM / 8) * (BN / 8);
+  const int vec_a = (lda % 4 == 0) && (sA % 4 == 0) && aligned16(A);
+  const int vec_b = (ldb % 4 == 0) && (sB % 4 == 0) && aligned16(B);
+  const int vec_cd = (ldd % 4 == 0) && (sD % 4 == 0) && aligned16(D) &&
+                     (!use_c || ((ldc % 4 == 0) && (sC % 4 == 0) && aligned16(C)));
+  const int tiles_n = (N + BN - 1) / BN;
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(tiles_n * splits), (unsigned)((M + BM - 1) / BM), (unsigned)nb);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)splits;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    ProfScope ps(KC_GEMM, st, 2.0 * M * (double)N * K * nb);
+    note_launch();
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, gemm_f32_v4_kernel<BM, BN, true>, M, N, K, alpha, A + b0 * sA,
+                                             lda, sA, B + b0 * sB, ldb, sB, beta, use_c ? C + b0 * sC : nullptr,
+                                             ldc, sC, D + b0 * sD, ldd, sD, use_c, vec_a, vec_b, vec_cd, splits);
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
@@ -486,6 +575,16 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
                                              batch, st)
                 : launch_gemm_cfg<T, 64, 64, 8, 8, 8>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D,
                                                       ldd, sD, batch, st);
+    // fewer 64 x 64 output tiles than two per SM and a long K: split K over
+    // the CTAs of a cluster, up to about four CTAs per SM, K-slices of at
+    // least 128
+    const long long tiles64 = tiles_m64 * ((N + 63) / 64);
+    if (v4 && N > 8 && K >= 512 && tiles64 < 2 * 152) {
+      int S = 8;
+      while (S > 2 && (tiles64 * S > 4 * 152 || K / S < 128)) S >>= 1;
+      return launch_gemm_f32_v4_split<64, 64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD,
+                                              batch, S, st);
+    }
     return launch_gemm_cfg<T, 64, 64, 8, 4, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc,
                                                sC, D, ldd, sD, batch, st);
   }

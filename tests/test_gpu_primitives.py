@@ -241,3 +241,37 @@ def test_gemm_f32_vector_tiles_match_scalar_tiles(cuda, m, n, k, batch, pad):
     scale = max(1.0, np.abs(ref).max()) * max(1, k) ** 0.5
     assert np.abs(outs[0][0] - ref).max() <= 2e-5 * scale * 10
     assert np.abs(outs[0][1] - ref2).max() <= 2e-5 * scale * 10
+
+
+@pytest.mark.parametrize("m,n,k,batch,pad", [(3584, 64, 3584, 1, 0), (1792, 64, 1792, 4, 0), (896, 64, 896, 16, 0),
+                                             (100, 37, 2000, 3, 0), (64, 14, 600, 2, 0), (130, 96, 1031, 2, 1),
+                                             (70, 64, 515, 5, 3)])
+def test_gemm_f32_cluster_split_k(cuda, m, n, k, batch, pad):
+    """FP32 products with few output tiles and a long K run split-K over the
+    CTAs of a thread-block cluster (partial tiles reduced in rank order
+    through distributed shared memory): FP32 accuracy against NumPy, the
+    same bits on every run, ragged M / N / K, leading dimensions that are not
+    multiples of 4, a broadcast A and C == D in place."""
+    from jaxhps_gb300 import _native as nat
+
+    rng = np.random.default_rng(m + n + k)
+    A = rng.standard_normal((batch, m, k + pad)).astype(np.float32)
+    B = rng.standard_normal((batch, k, n + pad)).astype(np.float32)
+    Cm = rng.standard_normal((batch, m, n + pad)).astype(np.float32)
+    tA = torch.as_tensor(A, device=cuda)[:, :, :k]
+    tB = torch.as_tensor(B, device=cuda)[:, :, :n]
+    runs = []
+    for _ in range(2):
+        tC = torch.as_tensor(Cm, device=cuda)[:, :, :n]
+        out = torch.empty((batch, m, n + pad), dtype=torch.float32, device=cuda)[:, :, :n]
+        nat.gemm(tA, tB, out, alpha=0.5, beta=-1.0, Cmat=tC)
+        nat.gemm(tA[0], tB, tC, alpha=1.0, beta=1.0, Cmat=tC)
+        torch.cuda.synchronize()
+        runs.append((out.cpu().numpy(), tC.cpu().numpy()))
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+    A64, B64, C64 = A[:, :, :k].astype(np.float64), B[:, :, :n].astype(np.float64), Cm[:, :, :n].astype(np.float64)
+    ref = 0.5 * A64 @ B64 - C64
+    ref2 = A64[0] @ B64 + C64
+    scale = max(1.0, np.abs(ref).max()) * k ** 0.5
+    assert np.abs(runs[0][0] - ref).max() <= 2e-5 * scale * 10
+    assert np.abs(runs[0][1] - ref2).max() <= 2e-5 * scale * 10
