@@ -3,6 +3,8 @@
 // side orderings, interface flips, the exterior roll after a merge) is
 // precomputed on the host as small integer maps and applied here, so one
 // kernel serves 2D quad merges and 3D oct merges alike.
+#include <type_traits>
+
 #include "hps_common.cuh"
 #include "hps_internal.h"
 #include "../../include/jaxhps_gb300.h"
@@ -17,7 +19,25 @@ namespace hps {
 // Columns j < col_split go to out_lo[l][i][j], the rest to
 // out_hi[l][i][j-col_split].  One CTA per (row, leaf group); the operator
 // rows are staged in shared memory once and reused for the whole group.
+//
+// FP32 / complex64 output with real FP64 coefficients (the mixed-precision
+// builds): the sum is formed in double-float arithmetic on the FP32 pipe
+// (operands split into FP32 pairs once, while staging; TwoProd by FMA and
+// TwoSum per term, relative error below 2^-44) and rounded to FP32, which is
+// the FP64 sum rounded to FP32 except within 2^-44 of a rounding tie.  GB300
+// runs FP64 at 1/64 of the FP32 rate, so the FP64 form of this kernel was
+// bound by its 4 FP64 operations per element, not by its stores.
 // ---------------------------------------------------------------------------
+template <class T, class CT>
+__host__ __device__ constexpr bool assemble_in_pairs() {
+  return (std::is_same<T, float>::value || std::is_same<T, c64>::value) && std::is_same<CT, double>::value;
+}
+
+__device__ __forceinline__ float2 split_pair(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+
 template <class T, class CT>
 __global__ void leaf_assemble_kernel(int n_leaves, int n_pts, int row0, int col_split, int n_ops,
                                      const double* __restrict__ ops, const CT* __restrict__ coeffs,
@@ -27,6 +47,48 @@ __global__ void leaf_assemble_kernel(int n_leaves, int n_pts, int row0, int col_
   extern __shared__ double ds_smem[];  // [n_ops][n_pts] when staged
   const int i = blockIdx.x;
   const int row = row0 + i;
+  if constexpr (assemble_in_pairs<T, CT>()) {
+    if (staged) {
+      float2* dp = reinterpret_cast<float2*>(ds_smem);   // operator rows as pairs, [n_ops][n_pts]
+      float2* cp = dp + (size_t)n_ops * n_pts;            // coefficient pairs, [leaf in group][n_ops]
+      const int l0 = l_base + blockIdx.y * leaves_per_cta;
+      const int l1 = min(n_leaves, l0 + leaves_per_cta);
+      for (int e = threadIdx.x; e < n_ops * n_pts; e += blockDim.x) {
+        const int o = e / n_pts, j = e % n_pts;
+        dp[e] = split_pair(ops[((long long)o * n_pts + row) * n_pts + j]);
+      }
+      for (int e = threadIdx.x; e < (l1 - l0) * n_ops; e += blockDim.x) {
+        const int ll = e / n_ops, o = e % n_ops;
+        cp[e] = split_pair(coeffs[((long long)o * n_leaves + l0 + ll) * n_pts + row]);
+      }
+      __syncthreads();
+      for (int l = l0; l < l1; ++l) {
+        const float2* cl = cp + (size_t)(l - l0) * n_ops;
+        for (int j = threadIdx.x; j < n_pts; j += blockDim.x) {
+          float sh = 0.f, se = 0.f;
+          for (int o = 0; o < n_ops; ++o) {
+            const float2 c = cl[o], d = dp[o * n_pts + j];
+            const float pr = c.x * d.x;
+            float pe = fmaf(c.x, d.x, -pr);
+            pe = fmaf(c.x, d.y, pe);
+            pe = fmaf(c.y, d.x, pe);
+            const float t = sh + pr;
+            const float bb = t - sh;
+            const float err = (sh - (t - bb)) + (pr - bb);
+            sh = t;
+            se += err + pe;
+          }
+          const float r = sh + se;
+          T v;
+          if constexpr (std::is_same<T, float>::value) v = r;
+          else v = c64{r, 0.f};
+          if (j < col_split) out_lo[l * s_lo + (long long)i * ld_lo + j] = v;
+          else out_hi[l * s_hi + (long long)i * ld_hi + (j - col_split)] = v;
+        }
+      }
+      return;
+    }
+  }
   const double* ds;
   long long ds_ld;   // stride between operators
   if (staged) {
@@ -75,6 +137,7 @@ cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col
                           T* out_hi, long long ld_hi, long long s_hi, cudaStream_t st) {
   const int lpc = 32;
   size_t smem = sizeof(double) * (size_t)n_ops * n_pts;
+  if (assemble_in_pairs<T, CT>()) smem += sizeof(float2) * (size_t)lpc * n_ops;   // coefficient pairs
   const int staged = smem <= 200 * 1024;
   if (!staged) smem = 0;
   if (smem > 48 * 1024)
@@ -293,9 +356,9 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
                                     const T* __restrict__ hc, const int* __restrict__ int_c,
                                     const int* __restrict__ int_l, const int* __restrict__ ext_c,
                                     const int* __restrict__ ext_l, const int* __restrict__ loc, T* D, T* C,
-                                    T* B, T* Tout, T* dh, T* hext, int skip_zero, long long m_base) {
+                                    T* B, T* Tout, T* dh, T* hext, int skip_zero, long long m_base, int seg0) {
   const long long m = blockIdx.y + m_base;
-  const int seg = blockIdx.z;
+  const int seg = (int)blockIdx.z + seg0;
   const long long nbb = (long long)nb * nb;
   const T* Tm = Tc ? Tc + m * nch * nbb : nullptr;
   const T* hm = hc ? hc + m * nch * (long long)nb * ns : nullptr;
@@ -355,23 +418,59 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
   }
 }
 
+// Launch geometry of the merge gathers and the down-pass scatter: x blocks of
+// 256 threads over the largest segment of one merge.  When the launch would
+// hold far more CTAs than the GPU runs at once (152 SMs x 8 CTAs of 256
+// threads), each thread takes about four elements (the kernels stride over
+// their segment): these segments are short, and with one element per thread
+// scheduling the CTAs cost more than moving the data.
+static int gather_blocks(long long big, long long ctas_per_x) {
+  long long gx = (big + 255) / 256;
+  if (gx * ctas_per_x > 16LL * 152 * 8) gx = (big + 1023) / 1024;
+  if (gx < 1) gx = 1;
+  if (gx > 512) gx = 512;
+  return (int)gx;
+}
+
+// Segments 0-3 gather operator blocks (present with the children's
+// operators), 4-5 the children's h (present with hc): the first segment
+// launched and the number of segments, and the largest segment's size.
+static void gather_segments(bool ops, bool has_tout, bool has_h, long long n_int, long long n_ext, long long ns,
+                            int* seg0, int* nseg, long long* big) {
+  *seg0 = ops ? 0 : 4;
+  *nseg = (ops ? 4 : 0) + (has_h ? 2 : 0);
+  long long b = 0;
+  if (ops) {
+    b = n_int * n_int;
+    if (n_int * n_ext > b) b = n_int * n_ext;
+    if (has_tout && n_ext * n_ext > b) b = n_ext * n_ext;
+  }
+  if (has_h) {
+    const long long bh = (n_int > n_ext ? n_int : n_ext) * ns;
+    if (bh > b) b = bh;
+  }
+  *big = b;
+}
+
 template <class T>
 cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Tc, const T* hc,
                          const int* int_c, const int* int_l, const int* ext_c, const int* ext_l,
                          const int* loc, T* D, T* C, T* B, T* Tout, T* dh, T* hext, int skip_zero,
                          cudaStream_t st) {
-  long long big = Tc ? (long long)n_ext * n_ext : (long long)n_ext * ns;
-  int gx = (int)((big + 255) / 256);
-  if (gx > 512) gx = 512;
+  int seg0, nseg;
+  long long big;
+  gather_segments(Tc != nullptr, Tout != nullptr, hc != nullptr, n_int, n_ext, ns, &seg0, &nseg, &big);
+  if (nseg == 0 || big == 0) return cudaSuccess;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    const int gx = gather_blocks(big, (long long)nm * nseg);
     const double outs =
         Tc ? ((double)n_int * n_int + 2.0 * n_int * n_ext + (Tout ? (double)n_ext * n_ext : 0.0)) : 0.0;
-    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (outs + (double)(n_int + n_ext) * ns));
+    ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (outs + (hc ? (double)(n_int + n_ext) * ns : 0.0)));
     note_launch();
-    merge_gather_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Tc, hc, int_c, int_l,
-                                                            ext_c, ext_l, loc, D, C, B, Tout, dh, hext, skip_zero,
-                                                            m0);
+    merge_gather_kernel<T><<<dim3(gx, nm, nseg), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Tc, hc, int_c, int_l,
+                                                               ext_c, ext_l, loc, D, C, B, Tout, dh, hext, skip_zero,
+                                                               m0, seg0);
   }
   return cudaGetLastError();
 }
@@ -394,9 +493,9 @@ __global__ void merge_gather_iti_kernel(int nch, int nb, int n_int, int n_ext, i
                                         const T* __restrict__ hc, const int* __restrict__ int_c,
                                         const int* __restrict__ int_l, const int* __restrict__ ext_c,
                                         const int* __restrict__ ext_l, T* D, T* C, T* B, T* Tout, T* dh, T* hext,
-                                        int skip_zero, long long m_base) {
+                                        int skip_zero, long long m_base, int seg0) {
   const long long m = blockIdx.y + m_base;
-  const int seg = blockIdx.z;
+  const int seg = (int)blockIdx.z + seg0;
   const long long nbb = (long long)nb * nb;
   const T* Rm = Rc ? Rc + m * nch * nbb : nullptr;
   const T* hm = hc ? hc + m * nch * (long long)nb * ns : nullptr;
@@ -451,17 +550,20 @@ template <class T>
 cudaError_t merge_gather_iti(int n_merges, int nch, int nb, int n_int, int n_ext, int ns, const T* Rc, const T* hc,
                              const int* int_c, const int* int_l, const int* ext_c, const int* ext_l, T* D, T* C, T* B,
                              T* Tout, T* dh, T* hext, int skip_zero, cudaStream_t st) {
-  long long big = (long long)(n_ext > n_int ? n_ext : n_int) * (n_ext > n_int ? n_ext : n_int);
-  int gx = (int)((big + 255) / 256);
-  if (gx > 512) gx = 512;
+  int seg0, nseg;
+  long long big;
+  gather_segments(Rc != nullptr, Tout != nullptr, hc != nullptr, n_int, n_ext, ns, &seg0, &nseg, &big);
+  if (nseg == 0 || big == 0) return cudaSuccess;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    const int gx = gather_blocks(big, (long long)nm * nseg);
     ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * ((Rc ? (double)n_int * n_int + 2.0 * n_int * n_ext : 0.0) +
                                                        ((Rc && Tout) ? (double)n_ext * n_ext : 0.0) +
-                                                       (double)(n_int + n_ext) * ns));
+                                                       (hc ? (double)(n_int + n_ext) * ns : 0.0)));
     note_launch();
-    merge_gather_iti_kernel<T><<<dim3(gx, nm, 6), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Rc, hc, int_c, int_l, ext_c,
-                                                                ext_l, D, C, B, Tout, dh, hext, skip_zero, m0);
+    merge_gather_iti_kernel<T><<<dim3(gx, nm, nseg), 256, 0, st>>>(nch, nb, n_int, n_ext, ns, Rc, hc, int_c, int_l,
+                                                                   ext_c, ext_l, D, C, B, Tout, dh, hext, skip_zero,
+                                                                   m0, seg0);
   }
   return cudaGetLastError();
 }
@@ -505,10 +607,9 @@ template <class T>
 cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, int ns, const int* code,
                          const T* gpar, const T* gint, T* gch, cudaStream_t st) {
   long long cnt = (long long)nch * nb * ns;
-  int gx = (int)((cnt + 255) / 256);
-  if (gx > 256) gx = 256;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
+    const int gx = gather_blocks(cnt, nm);
     ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (double)cnt);
     note_launch();
     down_scatter_kernel<T><<<dim3(gx, nm), 256, 0, st>>>(nch, nb, n_ext, n_int, ns, code, gpar, gint, gch, m0);

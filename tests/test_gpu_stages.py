@@ -171,3 +171,55 @@ def test_iti_polynomial_known_answer_gpu(cuda):
     imp = dn + 1j * eta * (bp[:, 0] ** 3 + 3 * bp[:, 1] ** 2)
     u = hps.solve(pde, imp).numpy()
     assert np.abs(u - u_ex).max() < 1e-9
+
+
+def _mixed_coefficients(x):
+    """Every 2D operator kind, coefficients of different sizes and signs."""
+    return {"D_xx": 1.0 + 0.3 * np.sin(x[..., 0]), "D_xy": 0.2 * np.cos(x[..., 1]),
+            "D_yy": 1.5 + 0.1 * x[..., 0] * x[..., 1], "D_x": 3.0 * x[..., 1], "D_y": -2.0 * np.exp(x[..., 0]),
+            "I": -(50.0 + 20.0 * np.sin(2.0 * x[..., 1]))}
+
+
+def test_float32_leaf_operators_match_oracle(cuda):
+    """FP32 leaf solve, its operator rows assembled in double-float
+    arithmetic on the FP32 pipe: Y, T and the leaf inverse against the FP64
+    oracle to FP32-level accuracy, every operator kind."""
+    L, p, q = 2, 10, 8
+    rootn = hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0)
+    dom = hps.Domain(p=p, q=q, root=rootn, L=L)
+    coeffs = _mixed_coefficients(dom.interior_points)
+    pde = hps.PDEProblem(dom, **{f"{k}_coefficients": v for k, v in coeffs.items()})
+    Y, T, _, _, Aii = st._local_solve_dtn(pde, pde.P, pde.Q, cuda, torch.float32, keep_inverse=True,
+                                          want_source=False)
+    ref = O.Problem2D(rootn.bounds, L, p, q, coeffs, np.zeros(dom.interior_points.shape[:2]))
+    A = O.assemble_operator(ref.coeffs, ref.ops, dom.n_leaves, p * p)
+    Yr, Tr, _, _ = O.leaf_dtn(A, np.zeros((dom.n_leaves, p * p, 1)), ref.P, ref.Q)
+    # NumPy's float32 inverse of the same matrices: 1e-7 .. 2e-7 relative
+    assert _rel(Y, Yr) < 1e-5
+    assert _rel(T, Tr) < 1e-5
+    ncb = 4 * (p - 1)
+    eye = np.eye(p * p - ncb)
+    prod = np.einsum("lij,ljk->lik", Aii.double().cpu().numpy(), A[:, ncb:, ncb:])
+    assert np.abs(prod - eye).max() < 1e-5
+
+
+def test_complex64_iti_leaf_operators_match_oracle(cuda):
+    """complex64 ItI leaf solve with real coefficients (operator rows in
+    double-float, as the FP32 build): Y and T against the complex128 oracle."""
+    L, p, q, eta = 2, 10, 8, 6.0
+    rootn = hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0)
+    dom = hps.Domain(p=p, q=q, root=rootn, L=L)
+    x = dom.interior_points
+    coeffs = _mixed_coefficients(x)
+    coeffs["I"] = 36.0 * (1.0 + 0.3 * np.exp(-(x ** 2).sum(-1)))
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal(x.shape[:2]) + 1j * rng.standard_normal(x.shape[:2])
+    pde = hps.PDEProblem(dom, source=f, use_ItI=True, eta=eta, **{f"{k}_coefficients": v for k, v in coeffs.items()})
+    Y, T, v, h = st.local_solve_stage_uniform_2D_ItI(pde, device=cuda, dtype=torch.complex64)
+    ref = O.Problem2D(rootn.bounds, L, p, q, coeffs, f, iti=True, eta=eta)
+    A = O.assemble_operator(ref.coeffs, ref.ops, dom.n_leaves, p * p)
+    Yr, Tr, vr, hr = O.leaf_iti(A, ref.source, ref.P, ref.QH, ref.G)
+    # NumPy's complex64 inverse of the same matrices (condition ~5e3): 5e-7 .. 8e-7
+    assert _rel(Y, Yr) < 3e-5
+    assert _rel(T, Tr) < 3e-5
+    assert _rel(v, vr[..., 0]) < 3e-5
