@@ -272,3 +272,25 @@ def test_quad_merge_maps_iti_reproduce_oracle(nc):
             cd = maps.code[c, k]
             out[c, k] = g[cd] if cd >= 0 else gi[-cd - 1]
     assert np.allclose(out, ref)
+
+
+def test_source_upload_falls_back_for_unpinned_sources():
+    """The source upload takes the side-stream path only for a page-locked
+    CPU tensor of the working dtype bound for a CUDA device; NumPy arrays,
+    pageable tensors, other dtypes and CPU targets are converted as before
+    (values, shape and the multi-RHS flag unchanged)."""
+    import torch
+    from jaxhps_gb300 import _stages as st
+
+    rng = np.random.default_rng(0)
+    f2 = rng.standard_normal((4, 9))
+    f3 = rng.standard_normal((4, 9, 3))
+    cpu = torch.device("cpu")
+    for src, multi in ((f2, False), (f3, True), (torch.as_tensor(f3), True), (torch.as_tensor(f2, dtype=torch.float32), False)):
+        up = st._SourceUpload(src, 4, 9, torch.float64, cpu)
+        assert up.out is None and up.event is None
+        t, m = up.result()
+        assert m is multi
+        assert t.dtype == torch.float64 and t.shape == (4, 9, 1 if not multi else 3)
+        ref = np.asarray(src, dtype=np.float64)
+        np.testing.assert_array_equal(t.numpy(), ref if multi else ref[..., None])
