@@ -14,10 +14,12 @@ from jaxhps_gb300._index_maps import (colour_perm, merge_rects, oct_merge_maps_d
 from jaxhps_gb300._refinement import _domain_constants
 
 
-@pytest.mark.parametrize("kind", ["dtn", "iti", "oct"])
-def test_merge_rects_cover_exactly_the_nonzero_blocks(kind):
-    mp, iti = {"dtn": (quad_merge_maps_dtn(3), False), "iti": (quad_merge_maps_iti(3), True),
-               "oct": (oct_merge_maps_dtn(4), False)}[kind]
+@pytest.mark.parametrize("kind,size", [("dtn", 1), ("dtn", 3), ("dtn", 14), ("dtn", 56), ("iti", 1), ("iti", 3),
+                                       ("iti", 14), ("iti", 28), ("oct", 1), ("oct", 4), ("oct", 16), ("oct", 64)])
+def test_merge_rects_cover_exactly_the_nonzero_blocks(kind, size):
+    mp, iti = {"dtn": (quad_merge_maps_dtn, False), "iti": (quad_merge_maps_iti, True),
+               "oct": (oct_merge_maps_dtn, False)}[kind]
+    mp = mp(size)
     c_rects, b_rects = merge_rects(mp, iti)
     n_int, n_ext = mp.n_int, mp.n_ext
     Cm = np.zeros((n_int, n_ext), bool)
@@ -41,8 +43,8 @@ def test_merge_rects_cover_exactly_the_nonzero_blocks(kind):
     assert np.array_equal(Cr, Cm) and np.array_equal(Br, Bm)
 
 
-def test_two_colour_inverse_of_the_iti_merge_matrix():
-    nc = 3
+@pytest.mark.parametrize("nc", [1, 3, 8])
+def test_two_colour_inverse_of_the_iti_merge_matrix(nc):
     mp = quad_merge_maps_iti(nc)
     cp = colour_perm(mp)
     assert cp is not None and len(cp) == mp.n_int
