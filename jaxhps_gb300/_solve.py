@@ -3,7 +3,10 @@
 Propagates boundary data down the merge tree on the GPU and returns the
 leaf solutions, shape (n_leaves, p^d) or (n_leaves, p^d, nsrc), on
 ``host_device`` ("cpu" by default, as in the reference; pass a CUDA device
-or None to keep the result in device memory).
+or None to keep the result in device memory).  ``out``, a tensor of the
+result's shape and dtype (for example a page-locked CPU buffer that the
+caller reuses), receives the result instead, and is returned; it takes
+precedence over ``host_device``.  No counterpart in the reference.
 """
 
 from __future__ import annotations
@@ -14,7 +17,14 @@ import torch
 from . import _stages as st
 
 
-def solve(pde_problem, boundary_data, source=None, compute_device=None, host_device="cpu", **refine_kw):
+def solve(pde_problem, boundary_data, source=None, compute_device=None, host_device="cpu", out=None, **refine_kw):
+    if out is not None:
+        u = _solve(pde_problem, boundary_data, source, compute_device, None, **refine_kw)
+        return st._to_host(u, None, out=out)
+    return _solve(pde_problem, boundary_data, source, compute_device, host_device, **refine_kw)
+
+
+def _solve(pde_problem, boundary_data, source, compute_device, host_device, **refine_kw):
     dom = pde_problem.domain
     state = getattr(pde_problem, "_state", None)
     if state is not None and getattr(state, "iti", False):

@@ -60,11 +60,18 @@ def _is_complex(a) -> bool:
     return np.iscomplexobj(a)
 
 
-def _to_host(t: torch.Tensor, host_device):
-    """``t`` on ``host_device`` (None: left where it is).  Device -> CPU
-    copies land in page-locked memory (torch caches those blocks), which
-    the copy engines fill at full link speed; a pageable destination is
-    staged through a bounce buffer at a fraction of it."""
+def _to_host(t: torch.Tensor, host_device, out: torch.Tensor | None = None):
+    """``t`` on ``host_device`` (None: left where it is), or copied into
+    ``out`` (same shape and dtype) when given.  Device -> CPU copies land in
+    page-locked memory (torch caches those blocks), which the copy engines
+    fill at full link speed; a pageable destination is staged through a
+    bounce buffer at a fraction of it."""
+    if out is not None:
+        if tuple(out.shape) != tuple(t.shape) or out.dtype != t.dtype:
+            raise ValueError(f"out has shape {tuple(out.shape)} and dtype {out.dtype}; the result has "
+                             f"shape {tuple(t.shape)} and dtype {t.dtype}")
+        out.copy_(t)
+        return out
     if host_device is None:
         return t
     dev = torch.device(host_device)

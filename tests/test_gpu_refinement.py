@@ -125,3 +125,8 @@ def test_pinned_source_upload_matches_numpy_source(cuda):
     u_pin = hps.solve(pde2, g).numpy()
     assert np.array_equal(u_np, u_pin)
     assert len(pde2._state.history) == len(pde._state.history)
+    # the result read into a page-locked buffer the caller keeps
+    buf = torch.empty(u_np.shape, dtype=torch.float64).pin_memory()
+    hps.build_solver(pde2, precision="mixed")
+    r = hps.solve(pde2, g, out=buf)
+    assert r is buf and np.array_equal(buf.numpy(), u_np)

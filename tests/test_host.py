@@ -294,3 +294,20 @@ def test_source_upload_falls_back_for_unpinned_sources():
         assert t.dtype == torch.float64 and t.shape == (4, 9, 1 if not multi else 3)
         ref = np.asarray(src, dtype=np.float64)
         np.testing.assert_array_equal(t.numpy(), ref if multi else ref[..., None])
+
+
+def test_result_copy_into_caller_buffer():
+    """solve(out=...) ends in _to_host(out=...): the result is copied into
+    the caller's tensor, which is returned; a shape or dtype mismatch is an
+    error, not a silent reallocation."""
+    import torch
+    from jaxhps_gb300 import _stages as st
+
+    t = torch.arange(24, dtype=torch.float64).reshape(2, 3, 4)
+    out = torch.zeros(2, 3, 4, dtype=torch.float64)
+    r = st._to_host(t, None, out=out)
+    assert r is out and torch.equal(out, t)
+    with pytest.raises(ValueError):
+        st._to_host(t, None, out=torch.zeros(2, 3, 5, dtype=torch.float64))
+    with pytest.raises(ValueError):
+        st._to_host(t, None, out=torch.zeros(2, 3, 4, dtype=torch.float32))
