@@ -232,6 +232,19 @@ def cpu_threads():
 # ---------------------------------------------------------------------------
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest x over the ranks of the default process group (x itself
+    when there is none or it has one rank); every rank gets the result."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _cpu_sample(args):
     if args.workload == "helmholtz":
         L_s = min(args.ref_L, 4)
@@ -348,9 +361,7 @@ def main():
     launches = nat.launch_count() - launches0
     clk = clocks.stop()
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
     ms_per_step = ms / args.steps
     value = world * n_leaves / (ms_per_step / 1e3)
     iters = len(pde._state.history) if getattr(pde, "_state", None) is not None else None
@@ -389,6 +400,9 @@ def main():
             uh = estep()
         torch.cuda.synchronize()
         te = (time.perf_counter() - t0) / n_e2e
+        if world > 1:
+            barrier()
+            te = max_over_ranks(te, dev)
         e2e = {"value": world * n_leaves / te, "unit": "leaves/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": te * 1e3}
         del pde_h, uh, hu
