@@ -57,11 +57,13 @@ enum {
 /* Library version string (static storage). */
 HPS_API const char* hps_version(void);
 
-/* Number of CUDA kernels this library has enqueued since it was loaded. */
+/* Number of CUDA kernels this library has enqueued since it was loaded.
+ * No counterpart in the reference (instrumentation). */
 HPS_API long long hps_launch_count(void);
 
 /* Non-zero if a tensor-core GEMM launch of this process ever hit its bounded
- * wait (its output is then invalid).  Synchronises with the device. */
+ * wait (its output is then invalid).  Synchronises with the device.  No
+ * counterpart in the reference. */
 HPS_API int hps_gemm_tc_status(void);
 
 /* Which batched products run on the tcgen05 kernel: 0 none (SIMT kernels
@@ -80,12 +82,13 @@ HPS_API int hps_gemm_policy(int policy);
  * recorded on the launch's own stream.  hps_profile_end() synchronises on
  * those events and fills arrays of 8 entries indexed by class: summed kernel
  * time (ms), number of launches and summed algorithmic work (flops for 1, 2,
- * 4; bytes for 3), then disarms. */
+ * 4; bytes for 3), then disarms.  No counterpart in the reference. */
 HPS_API int hps_profile_begin(int class_mask);
 HPS_API int hps_profile_end(double* total_ms, long long* launches, double* work);
 
 /* Copies the last error message of this thread into buf (NUL-terminated).
- * Returns the full message length. */
+ * Returns the full message length.  No counterpart in the reference (whose
+ * stages raise Python exceptions; the Python layer raises NativeError). */
 HPS_API int hps_last_error(char* buf, size_t len);
 
 /* ---------------------------------------------------------------------------
@@ -103,7 +106,8 @@ HPS_API int hps_gemm_batched(int dtype, int m, int n, int k, const double* alpha
                      const void* C, long long ldc, long long strideC, void* D, long long ldd, long long strideD,
                      int batch, void* stream);
 
-/* Workspace bytes for hps_inverse_batched (0 for small n). */
+/* Workspace bytes for hps_inverse_batched (0 for small n); sizing only, the
+ * inverse replaces jnp.linalg.inv (local_solve/_uniform_2D_DtN.py:257). */
 HPS_API size_t hps_inverse_workspace_size(int dtype, int n, int batch);
 
 /* X[b] = inv(A[b]) by Gauss-Jordan elimination with partial pivoting.
@@ -133,7 +137,8 @@ HPS_API int hps_inverse_batched_static(int dtype, int n, const void* A, long lon
                                        void* X, long long ldx, long long strideX, int batch, int* info,
                                        void* stream);
 
-/* Element-type conversion of n contiguous elements (f64<->f32, c128<->c64). */
+/* Element-type conversion of n contiguous elements (f64<->f32, c128<->c64);
+ * the mixed-precision builds' casts, no counterpart in the reference. */
 HPS_API int hps_convert(int dtype_src, int dtype_dst, long long n, const void* src, void* dst, void* stream);
 
 /* ---------------------------------------------------------------------------
@@ -352,10 +357,13 @@ HPS_API int hps_residual_2d(const hps_residual2d_args* a, void* stream);
  *   a->r_int64 -= (A du_full)_int   (FP64, in/out; a->r_int gets its FP32 copy)
  *   a->flux    += Q du_full          (FP64, in/out)
  * with du_full = [P dg ; du], evaluated in double-float (FP32-pair)
- * arithmetic on the FP32 pipe. */
+ * arithmetic on the FP32 pipe.  Refinement only: no counterpart in the
+ * reference, which solves in FP64 directly. */
 HPS_API int hps_residual_update_2d(const hps_residual2d_args* a, const float* du, const float* dg, void* stream);
 
-/* u_full = [P g ; u_int] per leaf (FP64), exterior-first leaf order. */
+/* u_full = [P g ; u_int] per leaf (FP64), exterior-first leaf order: the
+ * leaf solution u = Y g + v of the down pass (down_pass/_uniform_2D_DtN.py
+ * :125-189) in the refinement's unknowns. */
 HPS_API int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
                               const double* g, double* u_full, void* stream);
 
@@ -387,7 +395,9 @@ HPS_API int hps_panel_map(int dtype, int mode, int batch, int n_out, int n_other
                           const void* M, const void* in, long long ld_in, long long stride_in, void* out,
                           long long ld_out, long long stride_out, void* stream);
 
-/* x[b][:] *= scale[b] (scale FP64 on the device) for n_per elements per batch. */
+/* x[b][:] *= scale[b] (scale FP64 on the device) for n_per elements per batch:
+ * the per-leaf side-length scaling of the adaptive leaf operators
+ * (local_solve/_adaptive_3D_DtN.py:130-168). */
 HPS_API int hps_scale_batched(int dtype, int batch, long long n_per, const double* scale, void* x, void* stream);
 
 /* ---------------------------------------------------------------------------
@@ -452,7 +462,8 @@ HPS_API int hps_mlp_backward(int n, const float* X, const float* params, const f
 HPS_API int hps_mlp_adam(float* params, const float* grad, float* m, float* v, float lr, float beta1, float beta2,
                          float eps, int step, void* stream);
 
-/* As hps_assemble_rows with complex128 coefficients and output. */
+/* As hps_assemble_rows with complex128 coefficients and output
+ * (assemble_diff_operator, local_solve/_uniform_2D_DtN.py:182-218). */
 HPS_API int hps_assemble_rows_complex(int n_leaves, int n_pts, int row0, int n_rows, int n_ops, const double* ops,
                                       const void* coeffs, void* out, long long ld, long long stride, void* stream);
 
@@ -462,6 +473,10 @@ HPS_API int hps_assemble_rows_complex(int n_leaves, int n_pts, int row0, int n_r
  * t_out = outgoing impedance QH u, t_in = incoming impedance state; hcorr is
  * minus the residual of the partner's interface equation t_in(a) + t_out(b) = 0
  * (the coupling of the ItI merges, merge/_uniform_2D_ItI.py:182-375). */
+HPS_API int hps_iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in,
+                            void* hcorr, int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry,
+                            void* stream);
+
 /* Residual of the ItI leaf and interface system (complex128; no counterpart
  * in the reference, which solves in complex128 directly).  Per leaf, with u
  * the values at all p^2 points (exterior-first) and t_in the incoming
@@ -506,7 +521,8 @@ HPS_API int hps_residual_iti_2d(const hps_residual_iti2d_args* a, void* stream);
 HPS_API int hps_interp_rows(long long n_rows, int n_src, const double* to_pts, const double* src_pts,
                             const double* src_weights, double* out, int rows_per_group, int transposed, void* stream);
 
-/* out[g][c] = in[g][idx[c]] for c < n_out (in: n_groups x n_in). */
+/* out[g][c] = in[g][idx[c]] for c < n_out (in: n_groups x n_in): the
+ * reordering step of interp_to_hps (_interpolation_methods.py:23-340). */
 HPS_API int hps_gather_cols(long long n_groups, int n_in, int n_out, const int* idx, const double* in, double* out,
                             void* stream);
 
@@ -525,22 +541,21 @@ HPS_API int hps_interp_from_leaves(int dim, long long n_targets, int nsrc, const
                                    const double* cell_origin, const double* cell_size, const double* f, double* out,
                                    void* stream);
 
-HPS_API int hps_iti_combine(long long n_nodes, int nsrc, const int* nbr, const void* t_out, const void* t_in,
-                            void* hcorr, int n_bdry, const int* bdry_node, const void* t_given, void* r_bdry,
-                            void* stream);
-
-/* r32 = f[:, n_cb:, :] rounded to FP32 (the residual at zero). */
+/* r32 = f[:, n_cb:, :] rounded to FP32 (the residual at zero).  Refinement
+ * only: no counterpart in the reference. */
 HPS_API int hps_interior_f32(long long n_leaves, int n_pts, int n_cb, int nsrc, const double* f, float* r32,
                              void* stream);
 
 /* hcorr[node] = (flux[node] + flux[nbr[node]]) / 2 (0 where nbr < 0);
  * r_bdry[b] = g_given[b] - g_state[bdry_node[b]] (g_given NULL: zero data).
- * Node = leaf*4q + k. */
+ * Node = leaf*4q + k.  Refinement only (the DtN interface equations that the
+ * reference's merges eliminate): no counterpart in the reference. */
 HPS_API int hps_flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr,
                              int n_bdry, const int* bdry_node, const double* g_given, const double* g_state,
                              float* r_bdry, void* stream);
 
-/* y += x elementwise (x FP32, y FP64). */
+/* y += x elementwise (x FP32, y FP64).  Refinement only: no counterpart in
+ * the reference. */
 HPS_API int hps_accumulate(long long n, const float* x, double* y, void* stream);
 
 /* y += x as hps_accumulate, and out[0] = max |x|, out[1] = max |y| after the
