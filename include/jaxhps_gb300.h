@@ -129,10 +129,14 @@ HPS_API int hps_inverse_batched(int dtype, int n, const void* A, long long lda, 
  * Scratch is a static device array of HPS_STATIC_SCRATCH_BYTES that every
  * GPU loading the library holds until exit; the call allocates nothing.
  * Returns HPS_ERR_WORKSPACE when hps_inverse_workspace_size(dtype, n, batch)
- * exceeds that size.  All calls share the array: calls that overlap on the
- * GPU (other streams or host threads, same device) race.  The first call on
- * a device looks up the array's address and should come before any stream
- * capture. */
+ * exceeds that size; that size counts 256 bytes of alignment slack, which the
+ * already aligned array does not need, so the usable limit is
+ * HPS_STATIC_SCRATCH_BYTES - 256 bytes of scratch proper.  All calls share the
+ * array: calls that overlap on the GPU (other streams or host threads, same
+ * device) race.  The first call on a device looks up the array's address and
+ * should come before any stream capture.  The address is kept per device
+ * index for the life of the process, which assumes the runtime's primary
+ * context throughout (no cudaDeviceReset between calls). */
 HPS_API int hps_inverse_batched_static(int dtype, int n, const void* A, long long lda, long long strideA,
                                        void* X, long long ldx, long long strideX, int batch, int* info,
                                        void* stream);

@@ -21,7 +21,12 @@
 //    same device) race on the scratch and must be serialised by the caller.
 //  * The device address of the array is looked up once per device, on the
 //    first call made with that device current (cudaGetSymbolAddress).  That
-//    first call should therefore come before any stream capture begins.
+//    first call should therefore come before any stream capture begins.  The
+//    address is cached per device index, which holds while the process keeps
+//    the runtime's primary context (a cudaDeviceReset would invalidate it).
+//  * The size check uses hps_inverse_workspace_size, which adds 256 bytes of
+//    alignment slack; the usable limit is therefore 256 bytes below the
+//    array's size.
 
 #include <cuda_runtime.h>
 

@@ -3,8 +3,12 @@ allocates nothing (its scratch is a fixed static device array).
 
 Checked through the C ABI against hps_inverse_batched with a caller
 workspace, on two calls in a row with different inputs (the second call
-runs on scratch that still holds the first call's contents), plus the
-size-limit rejection.  This file is named to be collected last.
+runs on scratch that still holds the first call's contents): both run the
+same kernels in the same order, so the results must be bitwise equal.  Each
+result is also compared with numpy.linalg.inv.  A larger call followed by a
+smaller one leaves stale data past the smaller call's scratch layout, which
+must not reach its result.  Plus the size-limit rejection.  This file is
+named to be collected last.
 """
 
 import ctypes as C
@@ -60,10 +64,31 @@ def test_static_inverse_matches_workspace_inverse(cuda, name, tdt, code, tol, n,
         nat.check(st, "hps_inverse_batched_static")
         torch.cuda.synchronize(cuda)
         assert (info.cpu().numpy() == 0).all() and (info_ref.cpu().numpy() == 0).all()
-        a, b = X.cpu().numpy(), X_ref.cpu().numpy()
+        assert torch.equal(X, X_ref), call
+        a = X.cpu().numpy()
         assert np.isfinite(a).all()
-        rel = np.abs(a - b).max() / np.abs(b).max()
-        assert rel < tol * 20, (call, rel)
+        ref = np.linalg.inv(A.cpu().numpy().astype(np.complex128 if tdt.is_complex else np.float64))
+        rel = np.abs(a - ref).max() / np.abs(ref).max()
+        assert rel < tol, (call, rel)
+
+
+def test_static_inverse_after_a_larger_call(cuda):
+    """A big call fills more of the shared scratch than the small call that
+    follows it reads; the small call's result must not depend on that."""
+    nat, f = _bind()
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    results = []
+    for n, batch in ((600, 3), (260, 2), (600, 3), (260, 2)):
+        A = _matrices(np.random.default_rng(n), batch, n, torch.float64).to(cuda)
+        X = torch.full_like(A, float("nan"))
+        info = torch.full((batch,), -7, dtype=torch.int32, device=cuda)
+        st = f(0, n, A.data_ptr(), A.stride(1), A.stride(0), X.data_ptr(), X.stride(1), X.stride(0), batch,
+               info.data_ptr(), stream)
+        nat.check(st, "hps_inverse_batched_static")
+        torch.cuda.synchronize(cuda)
+        assert (info.cpu().numpy() == 0).all()
+        results.append(X.clone())
+    assert torch.equal(results[0], results[2]) and torch.equal(results[1], results[3])
 
 
 def test_static_inverse_rejects_oversize(cuda):
