@@ -24,9 +24,17 @@ Metric: leaves/s = n_leaves / (t_build + t_solve).
           copy of the solution (into a page-locked buffer the caller keeps,
           solve(..., out=buf)) are inside the timed region.
 
-Prints one JSON line (rank 0).  ``--impl reference`` times the CPU
-restatement of the reference algorithm (the FP64 oracle; the reference's
-own JAX code cannot be installed on these machines) on a bounded sample.
+Accuracy: the mixed result is compared with the plain FP64 GPU path and,
+for ``poisson``, with the FP64 CPU oracle run on the same inputs at the same
+size (relative L2 and max-norm errors).
+
+``cpu_baseline`` / ``--impl reference``: the CPU restatement of the
+reference algorithm (the FP64 oracle; the reference's own JAX code cannot be
+installed on these machines).  For ``poisson`` it is the level-batched oracle
+(``oracle/hps_oracle_level.py``) on the full workload, on every host thread;
+for ``helmholtz`` the per-leaf loop oracle on an L=4 sample.
+
+Prints one JSON line (rank 0).
 """
 
 from __future__ import annotations
@@ -200,24 +208,35 @@ def cpu_oracle_sample_helmholtz(L_sample=4, p=16, q=14, k=40.0):
     return n / dt, dt, n
 
 
-def cpu_oracle_sample(L_sample=5, p=16, q=14, nsrc=64):
-    from oracle import hps_oracle as O
+def host_inputs(L, p, q, nsrc):
+    """The poisson workload's coefficient, sources and boundary data as NumPy
+    arrays (generated with torch on the CPU, the same formulas as on the GPU)."""
+    _, coeffs, f, g = make_inputs(L, p, q, nsrc, "cpu")
+    return coeffs["I_coefficients"].numpy(), f.numpy(), g.numpy()
 
-    root = (-1.0, 1.0, -1.0, 1.0)
-    pts = O.leaf_points_2D(O.uniform_leaf_bounds_2D(root, L_sample), p)
-    c = coefficient_c(pts, bump_centres())
-    a, zs, b = source_params(nsrc)
-    r2 = ((pts[:, :, None, None, :] - zs[None, None]) ** 2).sum(-1)
-    f = (a[None, None] * np.exp(-r2 / 0.1 ** 2)).sum(-1)
+
+def oracle_poisson(c, f, g, L, p, q, threads=None):
+    """Build + solve of the poisson workload by the level-batched FP64 oracle;
+    returns (solution, seconds)."""
+    from oracle import hps_oracle_level as OL
+
     ones = np.ones_like(c)
     t0 = time.perf_counter()
-    pr = O.Problem2D(root, L_sample, p, q, {"D_xx": ones, "D_yy": ones, "I": c}, f).build()
-    bp = pr.boundary_points
-    g = (bp[:, 0] ** 2 - bp[:, 1] ** 2)[:, None] * b[None, :]
-    pr.solve(g)
+    pr = OL.LevelProblem2D((-1.0, 1.0, -1.0, 1.0), L, p, q, {"D_xx": ones, "D_yy": ones, "I": c}, f, threads=threads)
+    pr.build()
+    u = pr.solve(g)
     dt = time.perf_counter() - t0
-    n = 4 ** L_sample
-    return n / dt, dt, n
+    pr.close()
+    return u, dt
+
+
+def oracle_thread_speedup(L=5, p=16, q=14, nsrc=64):
+    """Speed-up of the level-batched oracle on every host thread over one
+    thread, on an L=5 instance of the poisson workload."""
+    c, f, g = host_inputs(L, p, q, nsrc)
+    _, t1 = oracle_poisson(c, f, g, L, p, q, threads=1)
+    _, tn = oracle_poisson(c, f, g, L, p, q)
+    return t1 / tn
 
 
 def cpu_threads():
@@ -245,17 +264,11 @@ def max_over_ranks(x: float, device) -> float:
     return float(t.item())
 
 
-def _cpu_sample(args):
-    if args.workload == "helmholtz":
-        L_s = min(args.ref_L, 4)
-        v, dt, n = cpu_oracle_sample_helmholtz(L_s)
-        what = (f"complex128 NumPy/SciPy oracle (ItI), build+solve of the same problem at L={L_s} ({n} leaves, p=16, "
-                f"q=14, 1 RHS); Python loops over leaves and merges, OpenBLAS threads inside each call")
-    else:
-        v, dt, n = cpu_oracle_sample(args.ref_L)
-        what = (f"FP64 NumPy/SciPy oracle (CPU restatement of the reference algorithm), build+solve of the same "
-                f"problem at L={args.ref_L} ({n} leaves, p=16, q=14, 64 RHS); Python loops over leaves and "
-                f"merges, OpenBLAS threads inside each call (all threads measured 1.2x one thread)")
+def _cpu_sample_helmholtz(args):
+    L_s = min(args.ref_L, 4)
+    v, dt, n = cpu_oracle_sample_helmholtz(L_s)
+    what = (f"complex128 NumPy/SciPy oracle (ItI), build+solve of the same problem at L={L_s} ({n} leaves, p=16, "
+            f"q=14, 1 RHS); Python loops over leaves and merges, OpenBLAS threads inside each call")
     return v, dt, n, what
 
 
@@ -265,18 +278,34 @@ def run_reference(args):
         return 0
     wl = WORKLOADS[args.workload]
     vals = []
-    for i in range(args.warmup + args.steps):
-        v, dt, n, sample = _cpu_sample(args)
-        if i >= args.warmup:
-            vals.append(v)
-    value = float(np.median(vals))
+    if args.workload == "helmholtz":
+        for i in range(args.warmup + args.steps):
+            v, dt, n, sample = _cpu_sample_helmholtz(args)
+            if i >= args.warmup:
+                vals.append(v)
+        same, speedup = False, None
+    else:
+        L, p, q, ns = args.L, wl["p"], wl["q"], wl["nsrc"]
+        c, f, g = host_inputs(L, p, q, ns)
+        for i in range(args.warmup + args.steps):
+            _, dt = oracle_poisson(c, f, g, L, p, q)
+            if i >= args.warmup:
+                vals.append(4 ** L / dt)
+        same = True
+        speedup = oracle_thread_speedup(L=min(5, L), p=p, q=q, nsrc=ns)
+        sample = (f"the full workload (L={L}, {4 ** L} leaves, p={p}, q={q}, {ns} RHS) per step: level-batched FP64 "
+                  f"NumPy oracle (CPU restatement of the reference algorithm), LAPACK/BLAS batches on a thread pool "
+                  f"(one BLAS thread each) for levels of many small problems and BLAS on every thread for the top "
+                  f"merges; all threads run an L={min(5, L)} instance {speedup:.1f}x faster than one")
+    value = float(np.mean(vals))
     line = {
         "impl": "reference", "metric": "build+solve leaves/s", "value": value, "unit": "leaves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "dtype": "c128" if args.workload == "helmholtz" else "f64", "data": "synthetic",
-        "config": {"workload": wl["name"], **{k: wl[k] for k in ("L", "p", "q", "nsrc")}},
+        "config": {"workload": wl["name"], "L": args.L, "p": wl["p"], "q": wl["q"], "nsrc": wl["nsrc"]},
+        "same_config": same,
         "cpu_baseline": {"value": value, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "thread_speedup": speedup},
         "e2e": {"value": value, "unit": "leaves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's JAX package cannot be installed offline here; its algorithm is timed as the "
                 "oracle port",
@@ -294,7 +323,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["float64", "float32", "mixed"])
     ap.add_argument("--fp64-steps", dest="fp64_steps", type=int, default=1)
     ap.add_argument("--L", type=int, default=None)
-    ap.add_argument("--ref-L", dest="ref_L", type=int, default=5)
+    ap.add_argument("--ref-L", dest="ref_L", type=int, default=4, help="helmholtz CPU sample level")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--breakdown", action="store_true")
@@ -310,6 +339,7 @@ def main():
 
     import jaxhps_gb300 as hps
     from jaxhps_gb300 import _native as nat
+    from jaxhps_gb300 import _phases as phases
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -407,13 +437,26 @@ def main():
             te = max_over_ranks(te, dev)
         e2e = {"value": world * n_leaves / te, "unit": "leaves/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": te * 1e3}
+        # where an end-to-end call spends its time: CUDA events at the phase
+        # boundaries of build_solver / solve, a separate pass after the timed one
+        phase_ms: dict = {}
+        n_ph = 3
+        phases.enable()
+        for _ in range(n_ph):
+            phases.mark("start")
+            estep()
+            for k, v in phases.collect().items():
+                phase_ms[k] = phase_ms.get(k, 0.0) + v / n_ph
+        phases.disable()
+        e2e["phases_ms"] = phase_ms
         del pde_h, uh, hu
         nat.release_workspace()
         torch.cuda.empty_cache()
 
     # the plain FP64 GPU path on the same problem: its rate, and the error of
     # this run's solution against it
-    err, fp64 = None, None
+    err, fp64, u64_host = None, None, None
+    u_host = u.cpu().numpy()
     if args.precision != "float64":
         pde64 = hps.PDEProblem(dom, source=f, **coeffs)
         torch.cuda.synchronize()
@@ -424,6 +467,7 @@ def main():
         b1.record()
         torch.cuda.synchronize()
         err = float(((u - u64).abs().max() / u64.abs().max()).item())
+        u64_host = u64.cpu().numpy()
         if args.fp64_steps <= 0:
             ms64 = b0.elapsed_time(b1)
             fp64 = {"value": n_leaves / (ms64 / 1e3), "unit": "leaves/s", "ms_per_step": ms64,
@@ -444,6 +488,8 @@ def main():
         del pde64, u64
         nat.release_workspace()
         torch.cuda.empty_cache()
+    del u
+    torch.cuda.empty_cache()
 
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -487,10 +533,33 @@ def main():
     roofline["avg_launch_ms"] = avg_ms
     roofline["share_of_step"] = k_ms / ms
 
-    cpu = None
+    # the FP64 CPU oracle on the same inputs at the same size: the accuracy
+    # reference and, timed, the CPU baseline
+    cpu, acc = None, {}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, dt, n, what = _cpu_sample(args)
-        cpu = {"value": v, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port", "sample": f"{what}, {dt:.1f} s"}
+        if args.workload == "helmholtz":
+            v, dt, n, what = _cpu_sample_helmholtz(args)
+            cpu = {"value": v, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
+                   "sample": f"{what}, {dt:.1f} s"}
+        else:
+            c_h = coeffs["I_coefficients"].cpu().numpy()
+            u_o, dt = oracle_poisson(c_h, f.cpu().numpy(), g.cpu().numpy(), L, p, q)
+            speedup = oracle_thread_speedup(L=min(5, L), p=p, q=q, nsrc=ns)
+            cpu = {"value": n_leaves / dt, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
+                   "thread_speedup": speedup,
+                   "sample": (f"the full workload (L={L}, {n_leaves} leaves, {ns} RHS) once, {dt:.1f} s: "
+                              f"level-batched FP64 NumPy oracle on every host thread (an L={min(5, L)} instance runs "
+                              f"{speedup:.1f}x faster on all threads than on one)")}
+
+            def errs(a, b):
+                return {"rel_l2": float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel())),
+                        "rel_linf": float(np.abs(a - b).max() / np.abs(b).max())}
+
+            e = errs(u_host, u_o)
+            acc = {"rel_l2_vs_oracle": e["rel_l2"], "rel_linf_vs_oracle": e["rel_linf"]}
+            if u64_host is not None:
+                acc["fp64_path_vs_oracle"] = errs(u64_host, u_o)
+            del u_o
 
     if args.workload == "helmholtz":
         dtype = {"float64": "c128", "float32": "c64", "mixed": "c64+c128-refinement"}[args.precision]
@@ -503,7 +572,7 @@ def main():
         "config": {"workload": wl["name"], "L": L, "n_leaves": n_leaves, "p": p, "q": q, "nsrc": ns,
                    "precision": args.precision, "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (operator set is several GB)"},
-        "rel_err_vs_fp64": err, "refinement_iterations": iters, "fp64_path": fp64,
+        "rel_err_vs_fp64": err, **acc, "refinement_iterations": iters, "fp64_path": fp64,
         "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernel_classes": breakdown,
         "cpu_baseline": cpu, "clocks": clk,
     }

@@ -66,6 +66,24 @@ HPS_API long long hps_launch_count(void);
  * counterpart in the reference. */
 HPS_API int hps_gemm_tc_status(void);
 
+/* hps_gemm_tc_status, and the flag cleared: the Python build and solve call
+ * it after their work so that a flag raised by one call is reported once.
+ * Synchronises with the device.  No counterpart in the reference. */
+HPS_API int hps_gemm_tc_status_reset(void);
+
+/* Poll limits of the library's bounded device waits, on the current device:
+ * the multi-CTA inverse panel's grid barrier (default 2^24 polls of >= 100 ns;
+ * a barrier that runs out marks its matrix with info = -1 and the inverse's
+ * remaining kernels run to completion on in-range indices) and the
+ * tensor-core GEMM's mbarrier waits (default 2^22 polls, never set below
+ * 2^20: a CTA that gives up waits once more, with the same limit, for its
+ * MMAs in flight before freeing their tensor memory).  A negative value keeps
+ * a limit; the previous values are returned through the pointers that are
+ * not NULL.  Process-wide for the device, not meant to change while work is
+ * in flight.  No counterpart in the reference (it has no device waits). */
+HPS_API int hps_set_spin_limits(long long panel_barrier_polls, long long tc_wait_polls, long long* prev_panel,
+                                long long* prev_tc);
+
 /* Which batched products run on the tcgen05 kernel: 0 none (SIMT kernels
  * only), 1 the shapes where it was measured faster (default; HPS_GEMM_TC=0 in
  * the environment starts a process at 0), 2 every FP32 and complex64 product

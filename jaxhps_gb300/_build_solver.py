@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import torch
 
+from . import _native as nat
 from . import _stages as st
 from ._discretization_tree import DiscretizationNode2D
 
@@ -22,8 +23,21 @@ _PREC = {"float64": torch.float64, "float32": torch.float32, "mixed": torch.floa
 
 def build_solver(pde_problem, return_top_T: bool = False, compute_device=None, host_device=None,
                  precision: str = "float64", **refine_kw):
+    """Builds the solver operators (see the module docstring).  After the
+    build, the status words of every batched inverse and the tensor-core
+    GEMM's timeout flag are checked (one device sync): a singular leaf or
+    merge matrix raises SingularPivotError, a bounded device wait that ran
+    out raises DeviceWaitTimeout (both from ``_native``)."""
     if precision not in _PREC:
         raise ValueError(f"precision must be one of {sorted(_PREC)}")
+    pde_problem._leaf_info = None
+    out = _build(pde_problem, return_top_T, compute_device, precision, **refine_kw)
+    st.check_infos([pde_problem._leaf_info], "leaf inverse")
+    nat.raise_on_tc_timeout("build_solver")
+    return out
+
+
+def _build(pde_problem, return_top_T, compute_device, precision, **refine_kw):
     dom = pde_problem.domain
     if precision == "mixed":
         if pde_problem.use_ItI:

@@ -34,6 +34,21 @@ class NativeError(RuntimeError):
     """A native-library call returned a non-zero status."""
 
 
+class SingularPivotError(NativeError):
+    """A batched inverse met an exactly zero pivot (info > 0): the matrix is
+    singular and the operators built from it are not finite."""
+
+
+class DeviceWaitTimeout(NativeError):
+    """A bounded device wait ran out (info = -1 from a multi-CTA inverse
+    panel, or the tensor-core GEMM's flag); the results are invalid."""
+
+
+class RefinementNotConverged(NativeError):
+    """Iterative refinement used its step budget without reaching the
+    requested tolerance."""
+
+
 vp = C.c_void_p
 ci = C.c_int
 cll = C.c_longlong
@@ -188,6 +203,10 @@ def _declare(lib):
     lib.hps_assemble_rows_complex.restype = ci
     lib.hps_gemm_tc_status.argtypes = []
     lib.hps_gemm_tc_status.restype = ci
+    lib.hps_gemm_tc_status_reset.argtypes = []
+    lib.hps_gemm_tc_status_reset.restype = ci
+    lib.hps_set_spin_limits.argtypes = [cll, cll, P(cll), P(cll)]
+    lib.hps_set_spin_limits.restype = ci
     lib.hps_mlp_param_count.argtypes = []
     lib.hps_mlp_param_count.restype = ci
     lib.hps_mlp_sample_points.argtypes = [ci, vp, vp, vp]
@@ -212,7 +231,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_gemm_tc_status_reset", "hps_set_spin_limits", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
 )
 
 
@@ -246,6 +265,23 @@ def check(status: int, what: str) -> None:
         buf = C.create_string_buffer(1024)
         load_library().hps_last_error(buf, 1024)
         raise NativeError(f"{what} failed with status {status}: {buf.value.decode(errors='replace')}")
+
+
+def set_spin_limits(panel_barrier_polls: int = -1, tc_wait_polls: int = -1):
+    """Sets the bounded waits' poll limits on the current device (negative:
+    keep); returns the previous (panel_barrier_polls, tc_wait_polls)."""
+    a, b = C.c_longlong(0), C.c_longlong(0)
+    check(lib().hps_set_spin_limits(int(panel_barrier_polls), int(tc_wait_polls), C.byref(a), C.byref(b)),
+          "hps_set_spin_limits")
+    return int(a.value), int(b.value)
+
+
+def raise_on_tc_timeout(what: str) -> None:
+    """Reads and clears the tensor-core GEMM's timeout flag (one device sync);
+    raises DeviceWaitTimeout when a wait ran out since the last check."""
+    torch.cuda.current_stream().synchronize()
+    if lib().hps_gemm_tc_status_reset() != 0:
+        raise DeviceWaitTimeout(f"{what}: a tensor-core GEMM's bounded wait ran out; the results are invalid")
 
 
 def launch_count() -> int:

@@ -32,6 +32,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from . import _phases as phases
 from . import _stages as st
 from ._grid_creation_2D import rearrange_indices_ext_int, uniform_leaf_bounds_2D
 from ._index_maps import quad_merge_maps_dtn
@@ -243,6 +244,7 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
         consts=consts, nbr=consts["nbr"], bnode=consts["bnode"], tol=tol, max_iters=max_iters)
     pde_problem._state = state
     pde_problem._precision = "mixed"
+    phases.mark("build")
     pde_problem.Y = Y
     pde_problem.S_lst = S_lst
     pde_problem.D_inv_lst = Dinv_lst
@@ -250,6 +252,14 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     if return_top_T:
         return Tc[0]
     return None
+
+
+def raise_not_converged(history, tol, max_iters, what: str) -> None:
+    """Refinement ran max_iters steps without its last correction falling to
+    tol times the solution (max norms): the result is not FP64-accurate."""
+    last = f"{history[-1]:.2e}" if history else "none"
+    raise nat.RefinementNotConverged(f"{what}: iterative refinement did not converge in {max_iters} steps "
+                                     f"(last correction / solution = {last}, tolerance {tol:.1e})")
 
 
 def _res_args(state: MixedState, u_int, g, r32, flux, r64=None, u_full=None, zero_source=False):
@@ -318,6 +328,7 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
         else:
             raise ValueError("boundary data and source have different numbers of right-hand sides")
     g_given = g_given.contiguous()
+    phases.mark("boundary_h2d")
     nl, p, q = state.n_leaves, state.p, state.q
     n_i = p * p - 4 * (p - 1)
     u_int = torch.zeros((nl, n_i, ns), dtype=torch.float64, device=dev)
@@ -349,9 +360,13 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
             _residual(state, u_int, g, r32, flux, r64=r64)
         else:
             _residual_update(state, du, dg, r64, r32, flux)
+    else:
+        raise_not_converged(state.history, tol, max_iters, "mixed-precision DtN solve")
+    nat.raise_on_tc_timeout("mixed-precision DtN solve")
     u = torch.empty((nl, p * p, ns), dtype=torch.float64, device=dev)
     nat.check(L.hps_assemble_u_2d(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_int.data_ptr(), g.data_ptr(),
                                   u.data_ptr(), sp), "hps_assemble_u_2d")
     if not state.multi:
         u = u[..., 0]
+    phases.mark("refine")
     return st._to_host(u, host_device)

@@ -30,7 +30,7 @@ import torch
 from . import _native as nat
 from . import _stages as st
 from ._index_maps import oct_merge_maps_dtn, quad_merge_maps_dtn
-from ._refinement import leaf_gauss_nodes_2D, node_maps
+from ._refinement import leaf_gauss_nodes_2D, node_maps, raise_not_converged
 
 
 def _maps_for_ext(dim: int) -> Callable:
@@ -263,6 +263,9 @@ def solve_mixed_dense(pde_problem, boundary_data, source=None, host_device="cpu"
         if step <= tol * size:
             break
         _residual(state, u_int, g, ub, r64, r32, flux)
+    else:
+        raise_not_converged(state.history, tol, max_iters, "mixed-precision 3D solve")
+    nat.raise_on_tc_timeout("mixed-precision 3D solve")
     u = torch.empty((nl, n_pts, ns), dtype=torch.float64, device=dev)
     nat.gemm(state.P64, g, u[:, :n_cb, :])
     u[:, n_cb:, :].copy_(u_int)

@@ -35,7 +35,7 @@ from . import _stages as st
 from ._index_maps import quad_merge_maps_iti
 from ._nosource import _nosource_merge
 from ._pdeproblem import COEFF_NAMES_2D
-from ._refinement import OP_KIND_2D, _domain_constants
+from ._refinement import OP_KIND_2D, _domain_constants, raise_not_converged
 from ._refinement_dense import _node_pairing
 
 
@@ -203,6 +203,9 @@ def solve_mixed_iti(pde_problem, boundary_data, source=None, host_device="cpu", 
         if step <= tol * size:
             break
         _residual(state, u, t, r32, t_out)
+    else:
+        raise_not_converged(state.history, tol, max_iters, "mixed-precision ItI solve")
+    nat.raise_on_tc_timeout("mixed-precision ItI solve")
     if not state.multi:
         u = u[..., 0]
     return st._to_host(u, host_device)

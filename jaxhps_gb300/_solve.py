@@ -14,14 +14,20 @@ from __future__ import annotations
 import numpy as np
 import torch
 
+from . import _native as nat
+from . import _phases as phases
 from . import _stages as st
 
 
 def solve(pde_problem, boundary_data, source=None, compute_device=None, host_device="cpu", out=None, **refine_kw):
     if out is not None:
         u = _solve(pde_problem, boundary_data, source, compute_device, None, **refine_kw)
-        return st._to_host(u, None, out=out)
-    return _solve(pde_problem, boundary_data, source, compute_device, host_device, **refine_kw)
+        res = st._to_host(u, None, out=out)
+    else:
+        res = _solve(pde_problem, boundary_data, source, compute_device, host_device, **refine_kw)
+    phases.mark("result_d2h")
+    nat.raise_on_tc_timeout("solve")
+    return res
 
 
 def _solve(pde_problem, boundary_data, source, compute_device, host_device, **refine_kw):

@@ -17,6 +17,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
+from . import _phases as phases
 from ._index_maps import colour_perm, merge_rects, quad_merge_maps_dtn
 
 # Block-structured merge products (merge_rects); HPS_MERGE_RECTS=0 selects the
@@ -110,8 +111,15 @@ class _SourceUpload:
             side = torch.cuda.Stream(device=dev)
             dst = torch.empty(src.shape, dtype=dtype, device=dev)
             side.wait_stream(main)
+            timed = phases.enabled()
             with torch.cuda.stream(side):
+                if timed:
+                    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    t0.record()
                 dst.copy_(src, non_blocking=True)
+                if timed:
+                    t1.record()
+                    phases.side("source_h2d", t0, t1)
             dst.record_stream(side)   # the block is not reused before the copy ends, even if the build fails
             self.event = torch.cuda.Event()
             self.event.record(side)
@@ -136,6 +144,7 @@ def _coefficients(pde_problem, dev):
     ctype = torch.complex128 if cplx else torch.float64
     coeffs = torch.stack([_as_tensor(c, ctype, dev) for c in cs]).contiguous()
     ops_t = torch.as_tensor(np.stack(ops)).to(device=dev, dtype=torch.float64).contiguous()
+    phases.mark("coefficients_h2d")
     return ops_t, coeffs, cplx
 
 
@@ -254,6 +263,7 @@ def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None,
     out = (Y, T, v, h)
     if keep_inverse:
         out = out + (Binv,)
+    pde_problem._leaf_info = info
     return out
 
 
@@ -262,11 +272,26 @@ def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None,
 # ---------------------------------------------------------------------------
 
 
+def check_infos(infos, what: str = "batched inverse") -> None:
+    """Status words of batched inverses: -1 marks a matrix whose multi-CTA
+    panel barrier timed out (its result is invalid), k > 0 an exactly zero
+    pivot at column k (the matrix is singular).  One device sync for all."""
+    infos = [i for i in (infos or []) if i is not None and i.numel()]
+    if not infos:
+        return
+    lo, hi = (int(x) for x in torch.stack([torch.stack([i.min(), i.max()]) for i in infos]).aminmax())
+    if lo < 0:
+        raise nat.DeviceWaitTimeout(f"{what}: a multi-CTA panel barrier timed out; results are invalid")
+    if hi > 0:
+        bad = next(i for i in infos if int(i.max()) > 0)
+        m = int(torch.nonzero(bad > 0)[0, 0])
+        raise nat.SingularPivotError(f"{what}: matrix {m} of a batch is singular (zero pivot at column "
+                                     f"{int(bad[m]) - 1})")
+
+
 def raise_on_sync_timeout(infos) -> None:
-    """The blocked inverse marks a matrix whose multi-CTA panel barrier timed
-    out with info = -1 (its result is invalid).  One device sync."""
-    if infos and int(torch.stack([i.min() for i in infos]).min()) < 0:
-        raise nat.NativeError("blocked inverse: a multi-CTA panel barrier timed out; results are invalid")
+    """check_infos for the merge inverses (kept name)."""
+    check_infos(infos, "merge inverse")
 
 
 def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False,

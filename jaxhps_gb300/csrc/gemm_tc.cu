@@ -26,7 +26,13 @@ namespace hps {
 constexpr int TC_BM = 128;
 constexpr int TC_BK = 32;
 constexpr int TC_NT = 256;
-constexpr long long TC_SPIN_LIMIT = 1ll << 22;   // try_wait polls: well under a second
+// try_wait polls before an mbarrier wait gives up (default 2^22: well under
+// a second).  A device variable so that hps_set_spin_limits can change it;
+// TC_SPIN_FLOOR bounds it from below, because a CTA that gives up waits a
+// second time, with the same limit, for its MMAs in flight before it frees
+// the tensor memory they write.
+static __device__ long long g_tc_spin_limit = 1ll << 22;
+constexpr long long TC_SPIN_FLOOR = 1ll << 20;
 
 // Set by a CTA whose mbarrier wait ran out (a static device flag: the
 // library allocates no device memory).
@@ -68,7 +74,8 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
 // Bounded wait for the completion of the phase with the given parity.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);
-  for (long long it = 0; it < TC_SPIN_LIMIT; ++it) {
+  const long long limit = *(volatile long long*)&g_tc_spin_limit;
+  for (long long it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -389,6 +396,26 @@ int gemm_tc_error() {
   int h = 0;
   cudaMemcpyFromSymbol(&h, g_tc_err, sizeof(int));
   return h;
+}
+
+int gemm_tc_error_reset() {
+  int h = 0;
+  cudaMemcpyFromSymbol(&h, g_tc_err, sizeof(int));
+  const int zero_flag = 0;
+  cudaMemcpyToSymbol(g_tc_err, &zero_flag, sizeof(int));
+  return h;
+}
+
+cudaError_t set_tc_spin_limit(long long polls, long long* previous) {
+  long long old = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&old, g_tc_spin_limit, sizeof(old));
+  if (e != cudaSuccess) return e;
+  if (previous) *previous = old;
+  if (polls >= 0) {
+    if (polls < TC_SPIN_FLOOR) polls = TC_SPIN_FLOOR;
+    e = cudaMemcpyToSymbol(g_tc_spin_limit, &polls, sizeof(polls));
+  }
+  return e;
 }
 
 template <int BN, bool CPLX>

@@ -33,6 +33,12 @@ cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long
                             const c64* B, long long ldb, long long sB, float beta, const c64* C, long long ldc,
                             long long sC, c64* D, long long ldd, long long sD, int batch, cudaStream_t st);
 int gemm_tc_error();
+// Reads the flag and clears it (both synchronise with the device).
+int gemm_tc_error_reset();
+// Spin limits of the bounded waits on the current device (polls < 0: keep);
+// the previous value is returned through `previous` when it is not null.
+cudaError_t set_tc_spin_limit(long long polls, long long* previous);
+cudaError_t set_panel_spin_limit(long long polls, long long* previous);
 // Sets the tensor-core policy of gemm_batched (0, 1, 2); returns the old one.
 int set_gemm_policy(int p);
 

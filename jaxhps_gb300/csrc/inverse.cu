@@ -445,9 +445,13 @@ static GjeWs gje_layout(size_t es, int n) {
   return w;
 }
 
+// Copies A into the tableau, clears the used flags and sets piv and rinv to
+// the identity permutation: a panel that gives up after a barrier timeout
+// leaves its piv entries unwritten, and the later kernels index rows and
+// columns through piv / rinv, which therefore always hold indices below n.
 template <class T>
 __global__ void gje_copy_in_kernel(int n, const T* __restrict__ A, long long lda, long long sA, T* Mat,
-                                   unsigned char* used) {
+                                   unsigned char* used, int* piv, int* rinv) {
   const long long b = blockIdx.y;
   const long long nn = (long long)n * n;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nn;
@@ -456,7 +460,11 @@ __global__ void gje_copy_in_kernel(int n, const T* __restrict__ A, long long lda
     Mat[b * nn + e] = A[b * sA + i * lda + j];
   }
   if (blockIdx.x == 0)
-    for (int i = threadIdx.x; i < n; i += blockDim.x) used[b * n + i] = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      used[b * n + i] = 0;
+      piv[b * n + i] = i;
+      rinv[b * n + i] = i;
+    }
 }
 
 // Panel pivot selection: Gauss-Jordan restricted to the bw panel columns
@@ -626,7 +634,10 @@ gje_panel_kernel(int n, int k0, int bw, T* Mat, T* Pw, int use_smem, T* U, T* G,
 // error flag; the CTAs return and info[b] is set to -1.
 // --------------------------------------------------------------------------
 constexpr int CP_NT = 256;
-constexpr long long CP_SPIN_LIMIT = 1ll << 24;   // x >= 100 ns: a second or more
+// Polls of the grid barrier before it gives up (each poll sleeps >= 100 ns:
+// the default 2^24 is a second or more).  A device variable so that
+// hps_set_spin_limits can change it; read once per barrier.
+static __device__ long long g_cp_spin_limit = 1ll << 24;
 
 struct CoopHdr {
   unsigned count;
@@ -675,8 +686,9 @@ __device__ __forceinline__ bool coop_barrier(CoopHdr* hdr, unsigned nct) {
         atomicAdd(&hdr->gen, 1u);
       } else {
         long long it = 0;
+        const long long limit = *(volatile long long*)&g_cp_spin_limit;
         while (vh->gen == g) {
-          if (vh->err != 0 || ++it > CP_SPIN_LIMIT) {
+          if (vh->err != 0 || ++it > limit) {
             ok = 0;
             atomicExch(&hdr->err, 1);
             break;
@@ -1344,7 +1356,8 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
     if (gx > 1024) gx = 1024;
     note_launch();
     gje_copy_in_kernel<T><<<dim3(gx, nb), 256, 0, st>>>(n, A + (long long)b0 * sA, lda, sA,
-                                                        Mat + (long long)b0 * nn, used + (long long)b0 * n);
+                                                        Mat + (long long)b0 * nn, used + (long long)b0 * n,
+                                                        piv + (long long)b0 * n, rinv + (long long)b0 * n);
   }
   // Panel width: the widest of 32/16/8/4 whose panel fits in shared memory;
   // wider panels mean fewer (rank-bw) trailing GEMM updates.
@@ -1429,6 +1442,15 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
         X + (long long)b0 * sX, ldx, sX);
   }
   return cudaGetLastError();
+}
+
+cudaError_t set_panel_spin_limit(long long polls, long long* previous) {
+  long long old = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&old, g_cp_spin_limit, sizeof(old));
+  if (e != cudaSuccess) return e;
+  if (previous) *previous = old;
+  if (polls >= 0) e = cudaMemcpyToSymbol(g_cp_spin_limit, &polls, sizeof(polls));
+  return e;
 }
 
 #define HPS_INST_INV(T)                                                                       \

@@ -163,3 +163,24 @@ def test_package_grids_are_the_references(name, root):
     dom = hps.Domain(p=int(fx["p"]), q=int(fx["q"]), root=node, L=int(fx["L"]))
     assert np.array_equal(np.asarray(dom.interior_points), fx["interior_points"])
     assert np.array_equal(np.asarray(dom.boundary_points), fx["boundary_points"])
+
+
+@pytest.mark.parametrize("name,root", [("c1_dtn2d_L3_p8", (-1.0, 1.0, -1.0, 1.0)),
+                                       ("dtn2d_multisrc_L2_p10", (0.0, 1.0, -1.0, 1.0))])
+@pytest.mark.parametrize("threads", [1, 3])
+def test_level_batched_oracle_is_the_reference(name, root, threads):
+    """The level-batched oracle (the CPU baseline and the full-size accuracy
+    reference of bench.py) reproduces the reference's operators and solutions."""
+    from oracle import hps_oracle_level as OL
+
+    fx = load(name)
+    pr = OL.LevelProblem2D(root, int(fx["L"]), int(fx["p"]), int(fx["q"]), _ops_2d(fx), fx["source"],
+                           threads=threads).build()
+    multi = fx["source"].ndim == 3
+    _check_ops(fx, pr.S_lst, pr.g_lst, pr.T_top, squeeze=not multi)
+    if multi:
+        assert rel(pr.solve(fx["bdry"]), fx["soln"]) < TOL
+    else:
+        for k in (0, 1):
+            assert rel(pr.solve(fx[f"bdry_{k}"]), fx[f"soln_{k}"]) < TOL
+    pr.close()

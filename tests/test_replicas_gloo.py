@@ -51,7 +51,7 @@ def test_max_over_ranks_without_a_process_group():
 def test_reference_arm_under_torchrun_prints_once():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(_free_port()), str(ROOT / "bench.py"), "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0", "--ref-L", "2"]
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--L", "2"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -59,3 +59,4 @@ def test_reference_arm_under_torchrun_prints_once():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    assert d["same_config"] and d["config"]["L"] == 2 and d["cpu_baseline"]["thread_speedup"] > 0
