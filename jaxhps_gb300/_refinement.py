@@ -144,18 +144,6 @@ def _domain_constants(dom, dev):
     return consts
 
 
-def _coefficient_stack(pde_problem, dev):
-    cs, names = [], []
-    for name in COEFF_NAMES_2D:
-        c = getattr(pde_problem, f"{name}_coefficients")
-        if c is not None:
-            if st._is_complex(c):
-                raise NotImplementedError("mixed precision with complex coefficients is not implemented")
-            cs.append(st._as_tensor(c, torch.float64, dev))
-            names.append(name)
-    return torch.stack(cs).contiguous(), names
-
-
 def _refine_leaf_operators(dom, coeffs, op_kind, consts, Y, Aii_inv, Q_int):
     """One refinement step of the FP32 leaf solution operators.
 
@@ -209,11 +197,17 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     dev = st._device(device)
     p, q, n_leaves = dom.p, dom.q, dom.n_leaves
     n_cb = 4 * (p - 1)
+    # coefficients first: the source copy below shares the host-to-device copy
+    # engine, and the leaf stage needs the coefficients, not the source
+    ops_t, coeffs, cplx = st._coefficients(pde_problem, dev)
+    if cplx:
+        raise NotImplementedError("mixed precision with complex coefficients is not implemented")
+    names = [n for n in COEFF_NAMES_2D if getattr(pde_problem, f"{n}_coefficients") is not None]
     upload = st._SourceUpload(pde_problem.source, n_leaves, p * p, torch.float64, dev)
     Y, T, _, _, Aii = st._local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, dev, leaf_dtype,
-                                          keep_inverse=True, want_source=False)
+                                          keep_inverse=True, want_source=False,
+                                          coefficients=(ops_t, coeffs, cplx))
     Y, Aii = Y.float(), Aii.float()
-    coeffs, names = _coefficient_stack(pde_problem, dev)
     consts = _domain_constants(dom, dev)
     if leaf_refine and leaf_dtype == torch.float32:
         T = _refine_leaf_operators(dom, coeffs, [OP_KIND_2D[n] for n in names], consts, Y, Aii,

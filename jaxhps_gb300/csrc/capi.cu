@@ -578,10 +578,13 @@ int hps_gemm_tc_status(void) { return gemm_tc_error(); }
 
 int hps_gemm_tc_status_reset(void) { return gemm_tc_error_reset(); }
 
+int hps_inverse_policy(int policy) { return set_inverse_tc_policy(policy); }
+
 int hps_set_spin_limits(long long panel_barrier_polls, long long tc_wait_polls, long long* prev_panel,
                         long long* prev_tc) {
   cudaError_t e = set_panel_spin_limit(panel_barrier_polls, prev_panel);
   if (e == cudaSuccess) e = set_tc_spin_limit(tc_wait_polls, prev_tc);
+  if (e == cudaSuccess) e = set_itc_spin_limit(tc_wait_polls, nullptr);
   if (e != cudaSuccess) {
     set_error("hps_set_spin_limits: %s", cudaGetErrorString(e));
     return HPS_ERR_CUDA;

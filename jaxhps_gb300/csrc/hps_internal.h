@@ -39,6 +39,16 @@ int gemm_tc_error_reset();
 // the previous value is returned through `previous` when it is not null.
 cudaError_t set_tc_spin_limit(long long polls, long long* previous);
 cudaError_t set_panel_spin_limit(long long polls, long long* previous);
+cudaError_t set_itc_spin_limit(long long polls, long long* previous);
+
+// FP32 batched inverse with the tableau in tensor memory (inverse_tc.cu),
+// for 64 < n <= 256; used by inverse_batched<float> while
+// inverse_tc_policy() is 1.
+bool inverse_tc_supported(int n);
+cudaError_t inverse_tc_f32(int n, const float* A, long long lda, long long sA, float* X, long long ldx,
+                           long long sX, int batch, int* info, cudaStream_t st);
+int inverse_tc_policy();
+int set_inverse_tc_policy(int policy);
 // Sets the tensor-core policy of gemm_batched (0, 1, 2); returns the old one.
 int set_gemm_policy(int p);
 

@@ -1171,7 +1171,28 @@ int inverse_small_nmax(int dtype) {
   return 0;
 }
 
+// Which kernel inverts FP32 matrices of 64 < n <= 256: 1 (default) the
+// tensor-memory Gauss-Jordan kernel, 0 the SIMT kernels.  HPS_INVERSE_TC=0 in
+// the environment starts a process at 0.
+static int g_inverse_tc_policy = -1;
+
+int inverse_tc_policy() {
+  if (g_inverse_tc_policy < 0) {
+    const char* e = getenv("HPS_INVERSE_TC");
+    g_inverse_tc_policy = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_inverse_tc_policy;
+}
+
+int set_inverse_tc_policy(int policy) {
+  const int old = inverse_tc_policy();
+  if (policy != 0 && policy != 1) return -1;
+  g_inverse_tc_policy = policy;
+  return old;
+}
+
 size_t inverse_workspace_bytes(int dtype, int n, int batch) {
+  if (dtype == F32 && inverse_tc_policy() == 1 && inverse_tc_supported(n)) return 0;
   if (n <= inverse_small_nmax(dtype)) return 0;
   if ((dtype == F32 && sblock_fits<float>(n)) || (dtype == F64 && sblock_fits<double>(n)) ||
       (dtype == C64 && sblock_fits<c64>(n)))
@@ -1239,6 +1260,10 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
   ProfScope whole(KC_INVERSE, st, 2.0 * cplx * (double)n * n * n * batch);
   if (info) cudaMemsetAsync(info, 0, sizeof(int) * (size_t)batch, st);
   const int dtype = DTypeOf<T>::value;
+  if constexpr (DTypeOf<T>::value == F32) {
+    if (inverse_tc_policy() == 1 && inverse_tc_supported(n))
+      return inverse_tc_f32(n, (const float*)A, lda, sA, (float*)X, ldx, sX, batch, info, st);
+  }
   if constexpr (sizeof(T) <= 8) {
     if (sblock_fits<T>(n)) return launch_sblock<T>(n, A, lda, sA, X, ldx, sX, batch, info, st);
   }

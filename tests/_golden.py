@@ -31,6 +31,14 @@ def to_np(a) -> np.ndarray:
     return np.asarray(a)
 
 
+def same_points(a, b) -> bool:
+    """Grid points agree to a few units in the last place (the Gauss nodes
+    come from an eigenvalue solver whose last bits differ between CPU
+    architectures)."""
+    a, b = to_np(a), to_np(b)
+    return a.shape == b.shape and float(np.abs(a - b).max()) <= 1e-15 * max(1.0, float(np.abs(b).max()))
+
+
 def rel(a, b) -> float:
     """max |a - b| / max |b|."""
     a, b = to_np(a), to_np(b)

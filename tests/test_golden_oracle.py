@@ -12,7 +12,7 @@ factorisations).
 import numpy as np
 import pytest
 
-from _golden import load, matrix_err, rel
+from _golden import load, matrix_err, rel, same_points
 from oracle import hps_oracle as O
 
 TOL = 1e-11
@@ -46,8 +46,8 @@ def _check_ops(fx, S_lst, g_lst, T_top, squeeze):
 def test_c1_grids_operators_and_solutions():
     fx = load("c1_dtn2d_L3_p8")
     ref = O.Problem2D((-1.0, 1.0, -1.0, 1.0), 3, 8, 6, _ops_2d(fx), fx["source"]).build()
-    assert np.array_equal(ref.points, fx["interior_points"])
-    assert np.array_equal(ref.boundary_points, fx["boundary_points"])
+    assert same_points(ref.points, fx["interior_points"])
+    assert same_points(ref.boundary_points, fx["boundary_points"])
     _check_ops(fx, ref.S_lst, ref.g_lst, ref.T_top, squeeze=True)
     assert rel(ref.Y, fx["Y"]) < TOL
     assert rel(ref.v[..., 0], fx["v"]) < TOL
@@ -61,14 +61,14 @@ def test_c1_interpolation_to_a_regular_grid():
     fx = load("c1_dtn2d_L3_p8")
     bounds = O.uniform_leaf_bounds_2D((-1.0, 1.0, -1.0, 1.0), 3)
     vals, pts = O.oracle_interp_from_hps(bounds, 8, fx["soln_0"], [fx["interp_x"], fx["interp_y"]])
-    assert np.array_equal(pts, fx["interp_pts"])
+    assert same_points(pts, fx["interp_pts"])
     assert rel(vals, fx["interp_vals"]) < TOL
 
 
 def test_multisource_with_first_order_term():
     fx = load("dtn2d_multisrc_L2_p10")
     ref = O.Problem2D((0.0, 1.0, -1.0, 1.0), 2, 10, 8, _ops_2d(fx), fx["source"]).build()
-    assert np.array_equal(ref.points, fx["interior_points"])
+    assert same_points(ref.points, fx["interior_points"])
     _check_ops(fx, ref.S_lst, ref.g_lst, ref.T_top, squeeze=False)
     assert rel(ref.solve(fx["bdry"]), fx["soln"]) < TOL
 
@@ -88,7 +88,7 @@ def test_iti_operators_and_solution(name, nosource):
     fx = load(name)
     L, p, q, eta = int(fx["L"]), int(fx["p"]), int(fx["q"]), float(fx["eta"])
     ref = O.Problem2D((-1.0, 1.0, -1.0, 1.0), L, p, q, _ops_2d(fx), fx["source"], iti=True, eta=eta).build()
-    assert np.array_equal(ref.points, fx["interior_points"])
+    assert same_points(ref.points, fx["interior_points"])
     if not nosource:
         _check_ops(fx, ref.S_lst, ref.g_lst, ref.T_top, squeeze=True)
     assert rel(ref.solve(fx["bdry"]), fx["soln"]) < TOL
@@ -99,8 +99,8 @@ def test_3d_operators_and_solutions():
     ones = np.ones_like(fx["I_coefficients"])
     co = {"D_xx": ones, "D_yy": ones, "D_zz": ones, "I": fx["I_coefficients"]}
     ref = O.Problem3D((-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), 2, 6, 4, co, fx["source"]).build()
-    assert np.array_equal(ref.points, fx["interior_points"])
-    assert np.array_equal(ref.boundary_points, fx["boundary_points"])
+    assert same_points(ref.points, fx["interior_points"])
+    assert same_points(ref.boundary_points, fx["boundary_points"])
     _check_ops(fx, ref.S_lst, ref.g_lst, ref.T_top, squeeze=True)
     for k in (0, 1):
         assert rel(ref.solve(fx[f"bdry_{k}"]), fx[f"soln_{k}"]) < TOL
@@ -122,7 +122,7 @@ def test_adaptive_3d_tree_and_solution():
     assert np.array_equal(np.array([lf.b for lf in leaves]), fx["leaf_bounds"])
     assert np.array_equal(np.array([lf.depth for lf in leaves]), fx["leaf_depths"])
     pts = O.leaf_points_3D(np.array([lf.b for lf in leaves]), p)
-    assert np.array_equal(pts, fx["interior_points"])
+    assert same_points(pts, fx["interior_points"])
     ones = np.ones(pts.shape[:2])
     O.oracle_adaptive_build_3D(root, p, q, {"D_xx": ones, "D_yy": ones, "D_zz": ones}, fx["source"])
     assert matrix_err(fx, "T_top", root.T) < TOL
@@ -140,7 +140,7 @@ def test_adaptive_2d_tree_and_solution():
     assert np.array_equal(np.array([lf.b for lf in leaves]), fx["leaf_bounds"])
     assert np.array_equal(np.array([lf.depth for lf in leaves]), fx["leaf_depths"])
     pts = O.leaf_points_2D(np.array([lf.b for lf in leaves]), p)
-    assert np.array_equal(pts, fx["interior_points"])
+    assert same_points(pts, fx["interior_points"])
     ones = np.ones(pts.shape[:2])
     O.oracle_adaptive_build_2D(root, p, q, {"D_xx": ones, "D_yy": ones}, fx["source"])
     assert rel(root.T, fx["T_top"]) < TOL
@@ -161,8 +161,8 @@ def test_package_grids_are_the_references(name, root):
     fx = load(name)
     node = hps.DiscretizationNode2D(*root) if len(root) == 4 else hps.DiscretizationNode3D(*root)
     dom = hps.Domain(p=int(fx["p"]), q=int(fx["q"]), root=node, L=int(fx["L"]))
-    assert np.array_equal(np.asarray(dom.interior_points), fx["interior_points"])
-    assert np.array_equal(np.asarray(dom.boundary_points), fx["boundary_points"])
+    assert same_points(dom.interior_points, fx["interior_points"])
+    assert same_points(dom.boundary_points, fx["boundary_points"])
 
 
 @pytest.mark.parametrize("name,root", [("c1_dtn2d_L3_p8", (-1.0, 1.0, -1.0, 1.0)),

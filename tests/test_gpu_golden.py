@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 import jaxhps_gb300 as hps
-from _golden import load, matrix_err, rel, to_np
+from _golden import load, matrix_err, rel, same_points, to_np
 
 pytestmark = pytest.mark.gpu
 
@@ -50,8 +50,8 @@ def _check_ops(fx, pde, T_top):
 
 def _uniform_2d(fx, root, **kw):
     dom = hps.Domain(p=int(fx["p"]), q=int(fx["q"]), root=hps.DiscretizationNode2D(*root), L=int(fx["L"]))
-    assert np.array_equal(to_np(dom.interior_points), fx["interior_points"])
-    assert np.array_equal(to_np(dom.boundary_points), fx["boundary_points"])
+    assert same_points(dom.interior_points, fx["interior_points"])
+    assert same_points(dom.boundary_points, fx["boundary_points"])
     return dom
 
 
@@ -71,7 +71,7 @@ def test_c1(cuda, precision):
         assert rel(u, fx[f"soln_{k}"]) < tol, k
     u0 = hps.solve(pde, fx["bdry_0"])
     vals, pts = dom.interp_from_interior_points(to_np(u0), fx["interp_x"], fx["interp_y"])
-    assert np.array_equal(to_np(pts), fx["interp_pts"])
+    assert same_points(pts, fx["interp_pts"])
     assert rel(vals, fx["interp_vals"]) < tol
 
 
@@ -126,8 +126,8 @@ def test_3d(cuda, precision):
     fx = load("dtn3d_L2_p6")
     root = hps.DiscretizationNode3D(-1.0, 1.0, -1.0, 1.0, -1.0, 1.0)
     dom = hps.Domain(p=int(fx["p"]), q=int(fx["q"]), root=root, L=int(fx["L"]))
-    assert np.array_equal(to_np(dom.interior_points), fx["interior_points"])
-    assert np.array_equal(to_np(dom.boundary_points), fx["boundary_points"])
+    assert same_points(dom.interior_points, fx["interior_points"])
+    assert same_points(dom.boundary_points, fx["boundary_points"])
     pde = hps.PDEProblem(dom, source=fx["source"], **_coeffs(fx, 3))
     T_top = hps.build_solver(pde, return_top_T=True, precision=precision)
     if precision == "float64":
@@ -161,7 +161,7 @@ def test_adaptive_3d_meshing_build_solve(cuda):
     dom = hps.Domain.from_adaptive_discretization(p=p, q=q, root=root, f=lambda x: _wave_lap(x, x0, a), tol=tol)
     b, d = _leaf_arrays(root, 3)
     assert np.array_equal(b, fx["leaf_bounds"]) and np.array_equal(d, fx["leaf_depths"])
-    assert np.array_equal(to_np(dom.interior_points), fx["interior_points"])
+    assert same_points(dom.interior_points, fx["interior_points"])
     pde = hps.PDEProblem(dom, source=fx["source"], **_coeffs(fx, 3))
     T_top = hps.build_solver(pde, return_top_T=True)
     assert matrix_err(fx, "T_top", T_top) < TOL64
@@ -176,7 +176,7 @@ def test_adaptive_2d_meshing_build_solve(cuda):
     dom = hps.Domain.from_adaptive_discretization(p=p, q=q, root=root, f=lambda x: _wave_lap(x, x0, a), tol=tol)
     b, d = _leaf_arrays(root, 2)
     assert np.array_equal(b, fx["leaf_bounds"]) and np.array_equal(d, fx["leaf_depths"])
-    assert np.array_equal(to_np(dom.interior_points), fx["interior_points"])
+    assert same_points(dom.interior_points, fx["interior_points"])
     pde = hps.PDEProblem(dom, source=fx["source"], **_coeffs(fx, 2))
     T_top = hps.build_solver(pde, return_top_T=True)
     assert rel(T_top, fx["T_top"]) < TOL64
