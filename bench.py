@@ -15,6 +15,21 @@ plane wave u_in at a seeded angle, zero incoming impedance data, eta = k;
 uniform quadtree L=8 (65536 leaves), p=16, q=14, one right-hand side.
 complex64 build + complex128 refinement against the plain complex128 path.
 
+Workload ``c1``: the same operator form at L=3, p=8, q=6 (64 leaves), the
+manufactured solution u = sin(pi x) sin(pi y) (c = 1 + 0.5 * 4 seeded
+bumps), plain FP64, boundary data u and x^2 - y^2: compared with the
+reference's own output (tests/golden/c1_dtn2d_L3_p8.npz) and the oracle.
+
+Workload ``c4``: 3D, [-1,1]^3, c = 1 + 0.3 * 6 seeded bumps, u = sin sin
+sin, uniform octree L=3 (512 leaves), p=10, q=8: FP32 build + FP64
+refinement against the plain FP64 GPU path.
+
+Workload ``c5``: adaptive octree meshing of f = Laplacian of
+arctan(50(|x - x0| - 0.7)), x0 = (-0.05,)*3, on [0,1]^3, p=10, q=8,
+tol 1e-5 (L-infinity): meshing time of the plain criterion and with the
+learned refinement proposal (trained first on other fronts), every accepted
+leaf judged by the plain criterion; then the FP64 build + solve on the tree.
+
 One step = build_solver + solve of all right-hand sides.
 Metric: leaves/s = n_leaves / (t_build + t_solve).
 
@@ -56,6 +71,10 @@ sys.path.insert(0, str(ROOT))
 WORKLOADS = {
     "poisson": dict(name="2D var-coeff DtN, uniform quadtree", L=7, p=16, q=14, nsrc=64),
     "helmholtz": dict(name="2D Helmholtz scattering ItI k=40, uniform quadtree", L=8, p=16, q=14, nsrc=1, k=40.0),
+    "c1": dict(name="2D var-coeff DtN, manufactured sin(pi x) sin(pi y), plain FP64", L=3, p=8, q=6, nsrc=1),
+    "c4": dict(name="3D var-coeff DtN, manufactured sin sin sin, uniform octree", L=3, p=10, q=8, nsrc=1),
+    "c5": dict(name="3D adaptive octree wavefront arctan(50(|x-x0|-0.7)), meshing with and without the MLP",
+               L=None, p=10, q=8, nsrc=1, tol=1e-5),
 }
 WORKLOAD = WORKLOADS["poisson"]
 
@@ -278,7 +297,28 @@ def run_reference(args):
         return 0
     wl = WORKLOADS[args.workload]
     vals = []
-    if args.workload == "helmholtz":
+    if args.workload in ("c4", "c5"):
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU oracle needs minutes per step at this size "
+                          "(c4: --workload c4 --oracle times it once beside the GPU run)"}))
+        return 0
+    if args.workload == "c1":
+        import jaxhps_gb300 as hps
+        from oracle import hps_oracle as O
+
+        L, p, q = wl["L"], wl["p"], wl["q"]
+        dom = hps.Domain(p=p, q=q, root=hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0), L=L)
+        c, f, g0, g1, _ = c1_inputs(dom)
+        ones = np.ones_like(c)
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            ref = O.Problem2D((-1.0, 1.0, -1.0, 1.0), L, p, q, {"D_xx": ones, "D_yy": ones, "I": c}, f).build()
+            ref.solve(g0)
+            ref.solve(g1)
+            if i >= args.warmup:
+                vals.append(4 ** L / (time.perf_counter() - t0))
+        same, speedup = True, None
+        sample = f"the full workload (L={L}, build + 2 solves) by the FP64 NumPy oracle, per-leaf loops"
+    elif args.workload == "helmholtz":
         for i in range(args.warmup + args.steps):
             v, dt, n, sample = _cpu_sample_helmholtz(args)
             if i >= args.warmup:
@@ -314,6 +354,319 @@ def run_reference(args):
     return 0
 
 
+def _errs(a, b) -> dict:
+    a, b = np.asarray(a), np.asarray(b)
+    return {"rel_l2": float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300)),
+            "rel_linf": float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))}
+
+
+def _time_steps(step, steps, warmup):
+    """CUDA-event time of `steps` calls after `warmup` untimed ones, with
+    clocks sampled during the timed region; returns (ms per step, clocks, last result)."""
+    import torch
+
+    out = None
+    for _ in range(warmup):
+        out = step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        out = step()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, clocks.stop(), out
+
+
+def _base_line(args, wl, metric, value, unit, ms, higher=True, dtype="f64", extra_config=None):
+    cfg = {"workload": wl["name"], **{k: wl[k] for k in ("L", "p", "q", "nsrc") if wl.get(k) is not None},
+           "parallelism": "single-gpu"}
+    cfg.update(extra_config or {})
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": higher, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic", "config": cfg}
+
+
+def c1_inputs(dom):
+    x = np.asarray(dom.interior_points)
+    bp = np.asarray(dom.boundary_points)
+    z = np.random.default_rng(0).uniform(-0.8, 0.8, (4, 2))
+    c = 1.0 + 0.5 * np.exp(-((x[..., None, :] - z) ** 2).sum(-1) / 0.2 ** 2).sum(-1)
+    u = np.sin(np.pi * x[..., 0]) * np.sin(np.pi * x[..., 1])
+    f = (c - 2 * np.pi ** 2) * u
+    g0 = np.sin(np.pi * bp[:, 0]) * np.sin(np.pi * bp[:, 1])
+    g1 = bp[:, 0] ** 2 - bp[:, 1] ** 2
+    return c, f, g0, g1, u
+
+
+def run_c1(args):
+    """c1: plain FP64 build + two solves, against the reference's own output."""
+    import torch
+
+    import jaxhps_gb300 as hps
+    from jaxhps_gb300 import _native as nat
+    from oracle import hps_oracle as O
+
+    wl = WORKLOADS["c1"]
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    L, p, q = wl["L"], wl["p"], wl["q"]
+    dom = hps.Domain(p=p, q=q, root=hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0), L=L)
+    c, f, g0, g1, u_ex = c1_inputs(dom)
+    ones = np.ones_like(c)
+    tc = {k: torch.as_tensor(v, device=dev) for k, v in (("c", c), ("f", f), ("g0", g0), ("g1", g1), ("one", ones))}
+    pde = hps.PDEProblem(dom, source=tc["f"], D_xx_coefficients=tc["one"], D_yy_coefficients=tc["one"],
+                         I_coefficients=tc["c"])
+
+    def step():
+        pde.reset()
+        hps.build_solver(pde, precision="float64")
+        return hps.solve(pde, tc["g0"], host_device=None), hps.solve(pde, tc["g1"], host_device=None)
+
+    l0 = nat.launch_count()
+    ms, clk, (u0, u1) = _time_steps(step, args.steps, args.warmup)
+    launches = (nat.launch_count() - l0) // (args.steps + args.warmup)
+    u0, u1 = u0.cpu().numpy(), u1.cpu().numpy()
+    acc = {}
+    fx_path = ROOT / "tests" / "golden" / "c1_dtn2d_L3_p8.npz"
+    if fx_path.exists():
+        with np.load(fx_path) as fx:
+            acc["vs_reference_output"] = {"g=u": _errs(u0, fx["soln_0"]), "g=x^2-y^2": _errs(u1, fx["soln_1"])}
+    t0 = time.perf_counter()
+    ref = O.Problem2D((-1.0, 1.0, -1.0, 1.0), L, p, q, {"D_xx": ones, "D_yy": ones, "I": c}, f).build()
+    r0, r1 = ref.solve(g0), ref.solve(g1)
+    dt = time.perf_counter() - t0
+    acc["vs_oracle"] = {"g=u": _errs(u0, r0), "g=x^2-y^2": _errs(u1, r1)}
+    acc["discretization_error_vs_exact"] = float(np.abs(u0 - u_ex).max())
+    # e2e through the public API from host buffers
+    hf, hc, ho = (torch.as_tensor(a).pin_memory() for a in (f, c, ones))
+    hg0, hg1 = torch.as_tensor(g0).pin_memory(), torch.as_tensor(g1).pin_memory()
+    hu0, hu1 = torch.empty(u0.shape, dtype=torch.float64).pin_memory(), torch.empty(u1.shape, dtype=torch.float64).pin_memory()
+    pde_h = hps.PDEProblem(dom, source=hf, D_xx_coefficients=ho, D_yy_coefficients=ho, I_coefficients=hc)
+
+    def estep():
+        pde_h.reset()
+        hps.build_solver(pde_h, precision="float64")
+        hps.solve(pde_h, hg0, out=hu0)
+        hps.solve(pde_h, hg1, out=hu1)
+
+    for _ in range(max(3, args.warmup)):
+        estep()
+    torch.cuda.synchronize()
+    n_e = max(5, args.steps)
+    te0 = time.perf_counter()
+    for _ in range(n_e):
+        estep()
+    torch.cuda.synchronize()
+    te = (time.perf_counter() - te0) / n_e
+    n = dom.n_leaves
+    line = _base_line(args, wl, "build+solve leaves/s", n / (ms / 1e3), "leaves/s", ms,
+                      extra_config={"precision": "float64", "solves_per_step": 2, "l2": "small problem (L2-resident)"})
+    line.update({
+        **acc,
+        "e2e": {"value": n / te, "unit": "leaves/s", "ms_per_step": te * 1e3,
+                "h2d_bytes_per_step": int(8 * (f.size + 2 * c.size + g0.size + g1.size)),
+                "d2h_bytes_per_step": int(8 * (u0.size + u1.size))},
+        "gpu_launches": launches * args.steps,
+        "cpu_baseline": {"value": n / dt, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
+                         "sample": f"the full workload (build + 2 solves) by the FP64 NumPy oracle, {dt * 1e3:.0f} ms"},
+        "clocks": clk,
+    })
+    print(json.dumps(line))
+    return 0
+
+
+def c4_inputs(dom):
+    x = np.asarray(dom.interior_points)
+    bp = np.asarray(dom.boundary_points)
+    z = np.random.default_rng(3).uniform(-0.8, 0.8, (6, 3))
+    c = 1.0 + 0.3 * np.exp(-((x[..., None, :] - z) ** 2).sum(-1) / 0.2 ** 2).sum(-1)
+    u = np.sin(np.pi * x[..., 0]) * np.sin(np.pi * x[..., 1]) * np.sin(np.pi * x[..., 2])
+    f = (c - 3 * np.pi ** 2) * u
+    g = np.sin(np.pi * bp[:, 0]) * np.sin(np.pi * bp[:, 1]) * np.sin(np.pi * bp[:, 2])
+    return c, f, g, u
+
+
+def run_c4(args):
+    """c4: 3D uniform octree, mixed precision against the plain FP64 GPU path."""
+    import torch
+
+    import jaxhps_gb300 as hps
+    from jaxhps_gb300 import _native as nat
+
+    wl = WORKLOADS["c4"]
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    L, p, q = wl["L"], wl["p"], wl["q"]
+    dom = hps.Domain(p=p, q=q, root=hps.DiscretizationNode3D(-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), L=L)
+    c, f, g, u_ex = c4_inputs(dom)
+    ones = np.ones_like(c)
+    kw = {k: torch.as_tensor(v, device=dev) for k, v in (("D_xx_coefficients", ones), ("D_yy_coefficients", ones),
+                                                          ("D_zz_coefficients", ones), ("I_coefficients", c))}
+    ft, gt = torch.as_tensor(f, device=dev), torch.as_tensor(g, device=dev)
+
+    def make_step(prec):
+        pde = hps.PDEProblem(dom, source=ft, **kw)
+
+        def step():
+            pde.reset()
+            hps.build_solver(pde, precision=prec)
+            return hps.solve(pde, gt, host_device=None)
+        return pde, step
+
+    pde, step = make_step(args.precision)
+    l0 = nat.launch_count()
+    ms, clk, u = _time_steps(step, args.steps, args.warmup)
+    launches = (nat.launch_count() - l0) // (args.steps + args.warmup)
+    iters = len(pde._state.history) if getattr(pde, "_state", None) is not None else None
+    u = u.cpu().numpy()
+    del pde, step
+    nat.release_workspace()
+    torch.cuda.empty_cache()
+    pde64, step64 = make_step("float64")
+    ms64, _, u64 = _time_steps(step64, max(1, args.fp64_steps), 1)
+    u64 = u64.cpu().numpy()
+    del pde64, step64
+    n = dom.n_leaves
+    line = _base_line(args, wl, "build+solve leaves/s", n / (ms / 1e3), "leaves/s", ms,
+                      dtype={"float64": "f64", "float32": "f32", "mixed": "f32+f64-refinement"}[args.precision],
+                      extra_config={"precision": args.precision, "l2": "operators of several GB (larger than L2)"})
+    line.update({
+        "rel_err_vs_fp64": _errs(u, u64), "refinement_iterations": iters,
+        "discretization_error_vs_exact": {"this_path": float(np.abs(u - u_ex).max()),
+                                          "fp64_path": float(np.abs(u64 - u_ex).max())},
+        "fp64_path": {"value": n / (ms64 / 1e3), "unit": "leaves/s", "ms_per_step": ms64,
+                      "speedup_of_this_path": ms64 / ms},
+        "gpu_launches": launches * args.steps, "clocks": clk,
+    })
+    if args.oracle:
+        from oracle import hps_oracle as O
+
+        t0 = time.perf_counter()
+        ref = O.Problem3D((-1.0, 1.0, -1.0, 1.0, -1.0, 1.0), L, p, q,
+                          {"D_xx": ones, "D_yy": ones, "D_zz": ones, "I": c}, f).build()
+        ur = ref.solve(g)
+        dt = time.perf_counter() - t0
+        line["rel_err_vs_oracle"] = _errs(u, ur)
+        line["fp64_path_vs_oracle"] = _errs(u64, ur)
+        line["cpu_baseline"] = {"value": n / dt, "unit": "leaves/s", "cores": cpu_threads(), "kind": "port",
+                                "sample": f"the full workload by the FP64 NumPy oracle, {dt:.1f} s"}
+    print(json.dumps(line))
+    return 0
+
+
+def wavefront_f(x0=(-0.05, -0.05, -0.05), a=50.0, R=0.7):
+    """f = Laplacian of arctan(a (|x - x0| - R)) in 3D, for NumPy or torch points."""
+    def f(x):
+        xp = np if isinstance(x, np.ndarray) else __import__("torch")
+        r = xp.sqrt(((x[..., 0] - x0[0]) ** 2 + (x[..., 1] - x0[1]) ** 2 + (x[..., 2] - x0[2]) ** 2))
+        s = a * (r - R)
+        return -2 * a ** 2 * s / (1 + s ** 2) ** 2 + 2 * a / (1 + s ** 2) / r
+    return f
+
+
+def wavefront_u(x0=(-0.05, -0.05, -0.05), a=50.0, R=0.7):
+    def u(x):
+        x = np.asarray(x)
+        return np.arctan(a * (np.sqrt(((x - np.asarray(x0)) ** 2).sum(-1)) - R))
+    return u
+
+
+def run_c5(args):
+    """c5: adaptive meshing with the plain criterion and with the learned
+    refinement proposal, then the FP64 build + solve on the plain tree."""
+    import torch
+
+    import jaxhps_gb300 as hps
+    from jaxhps_gb300 import _adaptive_discretization_3D as ad
+    from jaxhps_gb300 import refinement_mlp as rm
+    from jaxhps_gb300._discretization_tree import get_all_leaves
+
+    wl = WORKLOADS["c5"]
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    p, q, tol = wl["p"], wl["q"], wl["tol"]
+    f = wavefront_f()
+
+    def mesh(prop, stats=None):
+        root = hps.DiscretizationNode3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)
+        ad.generate_adaptive_mesh_level_restriction(root, f, tol, p, q, proposer=prop, stats=stats)
+        return root
+
+    # the proposer is trained on refine / keep labels of other fronts (untimed)
+    t_tr = time.perf_counter()
+    rec = rm.LabelRecorder(device=dev)
+    rng = np.random.default_rng(11)
+    for _ in range(args.train_fronts):
+        c0 = tuple(rng.uniform(-0.3, 0.4, 3))
+        ff = wavefront_f(c0, rng.uniform(20.0, 60.0), rng.uniform(0.4, 0.9))
+        root = hps.DiscretizationNode3D(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)
+        ad.generate_adaptive_mesh_level_restriction(root, ff, tol, p, q, proposer=rec)
+    X, y = rec.dataset()
+    net = rm.RefinementMLP(device=dev, seed=0)
+    net.train(X, y, epochs=40, batch=256, lr=2e-3)
+    t_tr = time.perf_counter() - t_tr
+    prop = rm.RefinementProposer(net, threshold=args.threshold)
+
+    res = {}
+    for name, pr in (("plain", None), ("mlp", prop)):
+        for _ in range(args.warmup):
+            mesh(pr)
+        torch.cuda.synchronize()
+        runs = []
+        for _ in range(args.steps):
+            st = {}
+            root = mesh(pr, st)
+            runs.append(st)
+        res[name] = (root, runs)
+    plain_s = float(np.median([r["seconds"] for r in res["plain"][1]]))
+    mlp_s = float(np.median([r["seconds"] for r in res["mlp"][1]]))
+    gn = res["plain"][1][-1]["global_norm"]
+    consts = ad._CheckConstants(p, dev)
+    judged = {}
+    for name, (root, _) in res.items():
+        leaves = get_all_leaves(root)
+        diff, ref, _ = ad.refinement_check(np.array([lf.bounds for lf in leaves]), f, consts, dev)
+        judged[name] = bool(np.all(diff / np.maximum(gn, ref) < tol))
+
+    def summary(runs):
+        r = runs[-1]
+        keys = ("rounds", "checked", "proposed", "leaves", "t_propose", "t_check", "t_edit")
+        return {**{k: r[k] for k in keys}, "seconds_median": float(np.median([x["seconds"] for x in runs])),
+                "rounds_detail": r["rounds_detail"]}
+
+    # FP64 build + solve on the plain tree
+    root = res["plain"][0]
+    dom = hps.Domain(p=p, q=q, root=root)
+    x = np.asarray(dom.interior_points)
+    ones = np.ones(x.shape[:2])
+    src = f(x)
+    pde = hps.PDEProblem(dom, source=src, D_xx_coefficients=ones, D_yy_coefficients=ones, D_zz_coefficients=ones)
+    bl = dom.get_adaptive_boundary_data_lst(wavefront_u())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    hps.build_solver(pde)
+    u = hps.solve(pde, bl)
+    torch.cuda.synchronize()
+    t_bs = time.perf_counter() - t0
+    err = float(np.abs(np.asarray(u) - wavefront_u()(x)).max())
+    line = _base_line(args, wl, "adaptive meshing seconds (learned proposal)", mlp_s, "s", mlp_s * 1e3, higher=False,
+                      extra_config={"tol": tol, "criterion": "L-infinity", "proposal_threshold": args.threshold,
+                                    "l2": "meshing: f evaluated per round on the GPU"})
+    line.update({
+        "plain_meshing_seconds": plain_s, "speedup_of_proposal": plain_s / mlp_s,
+        "plain": summary(res["plain"][1]), "mlp": summary(res["mlp"][1]),
+        "every_leaf_passes_plain_criterion": judged,
+        "training": {"fronts": args.train_fronts, "labels": int(X.shape[0]), "seconds": t_tr},
+        "build_solve_fp64": {"leaves": dom.n_leaves, "seconds": t_bs, "leaves_per_s": dom.n_leaves / t_bs,
+                             "max_error_vs_exact_u": err},
+    })
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -328,12 +681,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--breakdown", action="store_true")
     ap.add_argument("--workload", default="poisson", choices=sorted(WORKLOADS))
+    ap.add_argument("--oracle", action="store_true", help="c4: also run the FP64 CPU oracle (minutes)")
+    ap.add_argument("--train-fronts", dest="train_fronts", type=int, default=6, help="c5: fronts to train on")
+    ap.add_argument("--threshold", type=float, default=0.9, help="c5: proposal probability threshold")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.L is None:
         args.L = wl["L"]
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload in ("c1", "c4", "c5"):
+        return {"c1": run_c1, "c4": run_c4, "c5": run_c5}[args.workload](args)
 
     import torch
 

@@ -187,7 +187,12 @@ def generate_adaptive_mesh_level_restriction(root: DiscretizationNode3D, f_fn: C
                                              device=None, stats: dict | None = None) -> None:
     """Refines ``root`` in place (:34-210).  ``stats`` (optional dict) receives
     the number of rounds, of fully checked nodes, of nodes refined on the
-    proposer's word, and the wall time."""
+    proposer's word, the wall time, and the wall time per phase summed over
+    the rounds (``t_propose``: the proposer's features and network;
+    ``t_check``: f at the check points and the batched criterion on the GPU,
+    with the device sync that returns its verdicts; ``t_edit``: the host-side
+    tree edits, level restriction included) with the same split per round in
+    ``rounds_detail``."""
     t0 = time.perf_counter()
     dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
     nat.lib()
@@ -206,8 +211,10 @@ def generate_adaptive_mesh_level_restriction(root: DiscretizationNode3D, f_fn: C
         global_nrm = float(evaluate_f(f_fn, pts1).max().item())
     queue: List[DiscretizationNode3D] = list(get_all_leaves(root))
     n_rounds = n_checked = n_proposed = 0
+    detail = []
     while queue:
         n_rounds += 1
+        ta = time.perf_counter()
         to_refine = np.zeros(len(queue), dtype=bool)
         check_idx = np.arange(len(queue))
         if proposer is not None:
@@ -215,6 +222,7 @@ def generate_adaptive_mesh_level_restriction(root: DiscretizationNode3D, f_fn: C
             to_refine |= sure
             n_proposed += int(sure.sum())
             check_idx = np.nonzero(~sure)[0]
+        tb = time.perf_counter()
         if len(check_idx):
             bounds = np.array([queue[i].bounds for i in check_idx])
             diff, ref, l2 = refinement_check(bounds, f_fn, consts, dev, want_l2=l2_norm)
@@ -228,6 +236,7 @@ def generate_adaptive_mesh_level_restriction(root: DiscretizationNode3D, f_fn: C
             to_refine[check_idx] = fails
             if proposer is not None:
                 proposer.record(queue, check_idx, fails)
+        tc = time.perf_counter()
         new_queue: List[DiscretizationNode3D] = []
         for i, node in enumerate(queue):
             if not to_refine[i]:
@@ -243,7 +252,10 @@ def generate_adaptive_mesh_level_restriction(root: DiscretizationNode3D, f_fn: C
                         if n is not None:
                             pending.append(n)
                             new_queue.extend(n.children)
+        detail.append(dict(queued=len(queue), checked=int(len(check_idx)), refined=int(to_refine.sum()),
+                           t_propose=tb - ta, t_check=tc - tb, t_edit=time.perf_counter() - tc))
         queue = new_queue
     if stats is not None:
         stats.update(rounds=n_rounds, checked=n_checked, proposed=n_proposed, seconds=time.perf_counter() - t0,
-                     leaves=len(get_all_leaves(root)), global_norm=global_nrm, tol=tol)
+                     leaves=len(get_all_leaves(root)), global_norm=global_nrm, tol=tol, rounds_detail=detail,
+                     **{k: sum(d[k] for d in detail) for k in ("t_propose", "t_check", "t_edit")})
