@@ -76,23 +76,28 @@ HPS_API int hps_gemm_tc_status_reset(void);
  * a barrier that runs out marks its matrix with info = -1 and the inverse's
  * remaining kernels run to completion on in-range indices) and the
  * tensor-core kernels' mbarrier waits (GEMM and tensor-memory inverse;
- * default 2^22 polls, never set below
- * 2^20: a CTA that gives up waits once more, with the same limit, for its
- * MMAs in flight before freeing their tensor memory).  A negative value keeps
- * a limit; the previous values are returned through the pointers that are
- * not NULL.  Process-wide for the device, not meant to change while work is
- * in flight.  No counterpart in the reference (it has no device waits). */
-/* Which kernel inverts FP32 matrices of 64 < n <= 256 in hps_inverse_batched
- * (and the leaf stage): 1 (default) the kernel that keeps the Gauss-Jordan
- * tableau in tensor memory and runs its trailing updates as 3xTF32 tcgen05
- * MMAs (no workspace), 0 the SIMT kernels.  Returns the previous policy, or -1
- * for an invalid one.  HPS_INVERSE_TC=0 in the environment starts a process at
- * 0.  Process-wide; not meant to change while work is in flight.  No
- * counterpart in the reference (which calls jnp.linalg.inv). */
-HPS_API int hps_inverse_policy(int policy);
-
+ * default 2^22 polls, never set below 2^20: a CTA that gives up waits once
+ * more, with the same limit, for its MMAs in flight before freeing their
+ * tensor memory).  A negative value keeps a limit; the previous values are
+ * returned through the pointers that are not NULL.  Process-wide for the
+ * device, not meant to change while work is in flight.  No counterpart in
+ * the reference (it has no device waits). */
 HPS_API int hps_set_spin_limits(long long panel_barrier_polls, long long tc_wait_polls, long long* prev_panel,
                                 long long* prev_tc);
+
+/* Which FP32 inversions of 64 < n <= 224 use the kernel that keeps the
+ * Gauss-Jordan tableau in tensor memory and runs its rank-32 trailing updates
+ * as tcgen05 MMAs on operands split into three TF32 parts (no workspace):
+ * 0 none (SIMT kernels only), 1 (default) the leaf stage's inverses of
+ * hps_local_solve_dtn, 2 every one, hps_inverse_batched and the merges
+ * included (the tensor core accumulates the update in FP32 with its own
+ * rounding, which on the merges' interface matrices costs the mixed-precision
+ * solve refinement steps; 2 is for tests and measurements).  Returns the
+ * previous policy, or -1 for an invalid one.  HPS_INVERSE_TC=0 in the
+ * environment starts a process at 0.  Process-wide; not meant to change while
+ * work is in flight.  No counterpart in the reference (which calls
+ * jnp.linalg.inv). */
+HPS_API int hps_inverse_policy(int policy);
 
 /* Which batched products run on the tcgen05 kernel: 0 none (SIMT kernels
  * only), 1 the shapes where it was measured faster (default; HPS_GEMM_TC=0 in

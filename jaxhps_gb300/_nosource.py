@@ -9,12 +9,19 @@ up passes (up_pass/_uniform_2D_DtN.py:8-173, up_pass/_uniform_2D_ItI.py
 
 Stored on the problem: ``Y``, ``Phi`` (DtN: inv(A_ii), which maps the
 interior source to the interior particular solution; ItI: the source columns
-of inv(B)), ``S_lst``, ``D_inv_lst`` and ``BD_inv_lst`` (per level; rows of
-B D^-1 in the merged exterior's final order, interface columns in the order
-of S's rows).
+of inv(B)), ``S_lst``, ``D_inv_lst`` and ``BD_inv_lst``.  The up pass works
+on an internal layout (rows of B D^-1 in the merged exterior's final,
+rolled order; ItI interface unknowns in the order of S's rows), kept as
+``_D_inv_int`` / ``_BD_inv_int``; ``D_inv_lst`` and ``BD_inv_lst`` present
+them in the reference's layout (merge/_nosource_uniform_2D_DtN.py:238-248,
+merge/_nosource_uniform_2D_ItI.py: B D^-1 before the roll of the merged
+exterior, ItI interface unknowns in the h_int order b5, d8, b6, d7, a5, c6,
+c7, a8), converted when an element is read.
 """
 
 from __future__ import annotations
+
+from collections.abc import Sequence
 
 import numpy as np
 import torch
@@ -43,6 +50,56 @@ def nosource_local_solve_stage_uniform_2D_ItI(pde_problem, device=None, host_dev
         pde_problem.source = src
     n_cb = pde_problem.P.shape[0]
     return Y, T, Binv[:, :, n_cb:]
+
+
+def _iti_order(nc: int) -> np.ndarray:
+    """Position in the reference's h_int order of each interface unknown in
+    S's row order (the row permutation of merge/_uniform_2D_ItI.py:360-373)."""
+    return np.concatenate([np.arange(0, nc), np.arange(4 * nc, 5 * nc), np.arange(5 * nc, 6 * nc),
+                           np.arange(2 * nc, 3 * nc), np.arange(3 * nc, 4 * nc), np.arange(6 * nc, 7 * nc),
+                           np.arange(7 * nc, 8 * nc), np.arange(nc, 2 * nc)])
+
+
+def public_D_inv(Dinv: torch.Tensor, iti: bool) -> torch.Tensor:
+    """D^-1 of one level in the reference's layout."""
+    if not iti:
+        return Dinv
+    inv = torch.as_tensor(np.argsort(_iti_order(Dinv.shape[-1] // 8)), device=Dinv.device)
+    return Dinv.index_select(-2, inv).index_select(-1, inv)
+
+
+def public_BD_inv(BDinv: torch.Tensor, iti: bool) -> torch.Tensor:
+    """B D^-1 of one level in the reference's layout: rows before the roll of
+    the merged exterior by -nc, ItI columns in the h_int order."""
+    nc = BDinv.shape[-2] // 8
+    out = torch.roll(BDinv, nc, dims=-2)
+    if iti:
+        inv = torch.as_tensor(np.argsort(_iti_order(BDinv.shape[-1] // 8)), device=BDinv.device)
+        out = out.index_select(-1, inv)
+    return out
+
+
+class LayoutList(Sequence):
+    """A read-only list whose items are converted from an internal list when
+    they are read (the reference's layout of D^-1 / B D^-1)."""
+
+    def __init__(self, items, convert):
+        self._items, self._convert = items, convert
+
+    def __len__(self):
+        return len(self._items)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self._convert(x) for x in self._items[i]]
+        return self._convert(self._items[i])
+
+
+def store_operators(pde_problem, Dinv_lst, BDinv_lst, iti: bool) -> None:
+    """Internal lists for the up pass, reference-layout views as the public attributes."""
+    pde_problem._D_inv_int, pde_problem._BD_inv_int = Dinv_lst, BDinv_lst
+    pde_problem.D_inv_lst = LayoutList(Dinv_lst, lambda t: public_D_inv(t, iti))
+    pde_problem.BD_inv_lst = LayoutList(BDinv_lst, lambda t: public_BD_inv(t, iti))
 
 
 def _nosource_merge(T_arr, l: int, iti: bool, device=None, return_T: bool = False):
@@ -87,7 +144,8 @@ def nosource_build_solver(pde_problem, return_top_T: bool = False, device=None, 
         Y, T, Phi = nosource_local_solve_stage_uniform_2D_DtN(pde_problem, device=device, dtype=dtype)
     pde_problem.Y, pde_problem.Phi, pde_problem.v = Y, Phi, None
     out = _nosource_merge(T, dom.L, pde_problem.use_ItI, device, return_top_T)
-    pde_problem.S_lst, pde_problem.D_inv_lst, pde_problem.BD_inv_lst = out[0], out[1], out[2]
+    pde_problem.S_lst = out[0]
+    store_operators(pde_problem, out[1], out[2], pde_problem.use_ItI)
     pde_problem.g_tilde_lst = []
     pde_problem._precision = "nosource"
     if return_top_T:
@@ -96,7 +154,7 @@ def nosource_build_solver(pde_problem, return_top_T: bool = False, device=None, 
 
 
 def _up_pass(source, pde_problem, iti: bool, device=None, return_h_last: bool = False):
-    if getattr(pde_problem, "Phi", None) is None or not getattr(pde_problem, "D_inv_lst", None):
+    if getattr(pde_problem, "Phi", None) is None or not getattr(pde_problem, "_D_inv_int", None):
         raise ValueError("solve(..., source=...) needs a solver built without a source (build_solver on a "
                          "PDEProblem whose source is None)")
     Phi = pde_problem.Phi
@@ -115,7 +173,7 @@ def _up_pass(source, pde_problem, iti: bool, device=None, return_h_last: bool = 
     h = torch.empty((nl, Q.shape[0], ns), dtype=dtype, device=dev)
     nat.gemm(Q, v, h)
     g_lst = []
-    for Dinv, BDinv in zip(pde_problem.D_inv_lst, pde_problem.BD_inv_lst):
+    for Dinv, BDinv in zip(pde_problem._D_inv_int, pde_problem._BD_inv_int):
         nc = BDinv.shape[1] // 8
         maps = quad_merge_maps_iti(nc) if iti else quad_merge_maps_dtn(nc)
         g_t, h = st.up_level(h, Dinv, BDinv, maps, b_is_bd_inv=True, iti=iti)

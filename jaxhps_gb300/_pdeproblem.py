@@ -100,6 +100,8 @@ class PDEProblem:
         self.g_tilde_lst: List = []
         self.D_inv_lst: List = []
         self.BD_inv_lst: List = []
+        self._D_inv_int: List = []
+        self._BD_inv_int: List = []
         self.Phi = None
         self._state = None
 

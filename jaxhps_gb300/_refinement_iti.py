@@ -33,7 +33,7 @@ import torch
 from . import _native as nat
 from . import _stages as st
 from ._index_maps import quad_merge_maps_iti
-from ._nosource import _nosource_merge
+from ._nosource import _nosource_merge, store_operators
 from ._pdeproblem import COEFF_NAMES_2D
 from ._refinement import OP_KIND_2D, _domain_constants, raise_not_converged
 from ._refinement_dense import _node_pairing
@@ -115,7 +115,8 @@ def build_mixed_iti(pde_problem, return_top_T=False, device=None, tol: float = 1
     pde_problem._state = state
     pde_problem._precision = "mixed"
     pde_problem.Y = Y
-    pde_problem.S_lst, pde_problem.D_inv_lst, pde_problem.BD_inv_lst = out[0], out[1], out[2]
+    pde_problem.S_lst = out[0]
+    store_operators(pde_problem, out[1], out[2], True)
     pde_problem.g_tilde_lst = []
     if return_top_T:
         return out[3]

@@ -218,8 +218,9 @@ static int leaf_dtn_impl(const hps_leaf_dtn_args* a, cudaStream_t st) {
     e = leaf_assemble<T, double>(nl, np, ncb, ni, ncb, a->n_ops, a->ops, (const double*)a->coeffs, Aie, ncb,
                                  (long long)ni * ncb, Aii, ni, (long long)ni * ni, st);
   HPS_CHECK(e);
+  // the leaf blocks may use the tensor-memory kernel (FP32, 64 < n <= 224)
   HPS_CHECK(inverse_batched<T>(ni, Aii, ni, (long long)ni * ni, Aii, ni, (long long)ni * ni, nl, a->info, invws,
-                               invb, st));
+                               invb, st, true));
   const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
   const T* P = (const T*)a->P;
   const T* Q = (const T*)a->Q;

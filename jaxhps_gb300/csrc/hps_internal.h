@@ -22,7 +22,7 @@ size_t inverse_workspace_bytes(int dtype, int n, int batch);
 template <class T>
 cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
                             long long sX, int batch, int* info, void* ws, size_t ws_bytes,
-                            cudaStream_t st);
+                            cudaStream_t st, bool tensor_memory = false);
 
 // FP32 GEMM on the tensor cores (TF32 split into hi + lo, three products);
 // gemm_tc_error() reports whether a CTA's bounded wait ever ran out.
@@ -42,8 +42,8 @@ cudaError_t set_panel_spin_limit(long long polls, long long* previous);
 cudaError_t set_itc_spin_limit(long long polls, long long* previous);
 
 // FP32 batched inverse with the tableau in tensor memory (inverse_tc.cu),
-// for 64 < n <= 256; used by inverse_batched<float> while
-// inverse_tc_policy() is 1.
+// for 64 < n <= 224; used by inverse_batched<float> for the calls that pass
+// tensor_memory = true while inverse_tc_policy() is 1, for every call at 2.
 bool inverse_tc_supported(int n);
 cudaError_t inverse_tc_f32(int n, const float* A, long long lda, long long sA, float* X, long long ldx,
                            long long sX, int batch, int* info, cudaStream_t st);

@@ -1171,9 +1171,14 @@ int inverse_small_nmax(int dtype) {
   return 0;
 }
 
-// Which kernel inverts FP32 matrices of 64 < n <= 256: 1 (default) the
-// tensor-memory Gauss-Jordan kernel, 0 the SIMT kernels.  HPS_INVERSE_TC=0 in
-// the environment starts a process at 0.
+// Which inversions of FP32 matrices of 64 < n <= 224 run on the
+// tensor-memory Gauss-Jordan kernel (inverse_tc.cu): 0 none, 1 (default) the
+// leaf stage's (the callers that pass tensor_memory = true), 2 every one
+// (hps_inverse_batched and the merges too; for tests and measurements: the
+// tensor core accumulates the update in FP32 with its own rounding, which on
+// the merges' interface matrices costs the mixed-precision solve one or two
+// refinement steps).  HPS_INVERSE_TC=0 in the environment starts a process
+// at 0.
 static int g_inverse_tc_policy = -1;
 
 int inverse_tc_policy() {
@@ -1186,13 +1191,17 @@ int inverse_tc_policy() {
 
 int set_inverse_tc_policy(int policy) {
   const int old = inverse_tc_policy();
-  if (policy != 0 && policy != 1) return -1;
+  if (policy < 0 || policy > 2) return -1;
   g_inverse_tc_policy = policy;
   return old;
 }
 
+static bool inverse_tc_takes(int n, bool tensor_memory) {
+  const int p = inverse_tc_policy();
+  return inverse_tc_supported(n) && (p == 2 || (p == 1 && tensor_memory));
+}
+
 size_t inverse_workspace_bytes(int dtype, int n, int batch) {
-  if (dtype == F32 && inverse_tc_policy() == 1 && inverse_tc_supported(n)) return 0;
   if (n <= inverse_small_nmax(dtype)) return 0;
   if ((dtype == F32 && sblock_fits<float>(n)) || (dtype == F64 && sblock_fits<double>(n)) ||
       (dtype == C64 && sblock_fits<c64>(n)))
@@ -1252,7 +1261,7 @@ cudaError_t inverse_small<c128>(int n, const c128* A, long long lda, long long s
 template <class T>
 cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
                             long long sX, int batch, int* info, void* ws, size_t ws_bytes,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool tensor_memory) {
   if (n <= 0 || batch <= 0) return cudaSuccess;
   // one profiler record for the whole inversion (its panel kernels and the
   // GEMM updates nested below): 2 n^3 flops per matrix, x4 for complex
@@ -1261,7 +1270,7 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
   if (info) cudaMemsetAsync(info, 0, sizeof(int) * (size_t)batch, st);
   const int dtype = DTypeOf<T>::value;
   if constexpr (DTypeOf<T>::value == F32) {
-    if (inverse_tc_policy() == 1 && inverse_tc_supported(n))
+    if (inverse_tc_takes(n, tensor_memory))
       return inverse_tc_f32(n, (const float*)A, lda, sA, (float*)X, ldx, sX, batch, info, st);
   }
   if constexpr (sizeof(T) <= 8) {
@@ -1480,7 +1489,7 @@ cudaError_t set_panel_spin_limit(long long polls, long long* previous) {
 
 #define HPS_INST_INV(T)                                                                       \
   template cudaError_t inverse_batched<T>(int, const T*, long long, long long, T*, long long, \
-                                          long long, int, int*, void*, size_t, cudaStream_t);
+                                          long long, int, int*, void*, size_t, cudaStream_t, bool);
 HPS_INST_INV(float)
 HPS_INST_INV(double)
 HPS_INST_INV(c64)

@@ -237,8 +237,15 @@ def case_iti_nosource(jh):
     f = rng.standard_normal(x.shape[:2]) + 1j * rng.standard_normal(x.shape[:2])
     g = np.exp(1j * bp[:, 0]) * (1 + bp[:, 1])
     u = jh.solve(pde_problem=pde, boundary_data=J(g), source=J(f))
-    return dict(L=2, p=8, q=6, k=k, eta=k, interior_points=x, boundary_points=bp, I_coefficients=Icoef, source=f,
-                bdry=g, soln=_np(u))
+    out = dict(L=2, p=8, q=6, k=k, eta=k, interior_points=x, boundary_points=bp, I_coefficients=Icoef, source=f,
+               bdry=g, soln=_np(u))
+    for i, S in enumerate(pde.S_lst):
+        out[f"S_{i}"] = _np(S)
+    for i, D in enumerate(pde.D_inv_lst):
+        out[f"D_inv_{i}"] = _np(D)
+    for i, B in enumerate(pde.BD_inv_lst):
+        out[f"BD_inv_{i}"] = _np(B)
+    return out
 
 
 # ---------------------------------------------------------------------------

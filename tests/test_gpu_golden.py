@@ -117,6 +117,10 @@ def test_iti_nosource_up_pass(cuda):
     dom = _uniform_2d(fx, (-1.0, 1.0, -1.0, 1.0))
     pde = hps.PDEProblem(dom, use_ItI=True, eta=float(fx["eta"]), **_coeffs(fx, 2))
     hps.build_solver(pde)
+    for i in range(len(pde.S_lst)):
+        assert rel(pde.S_lst[i], fx[f"S_{i}"]) < TOL64
+        assert rel(pde.D_inv_lst[i], fx[f"D_inv_{i}"]) < TOL64
+        assert rel(pde.BD_inv_lst[i], fx[f"BD_inv_{i}"]) < TOL64
     u = hps.solve(pde, fx["bdry"], source=fx["source"])
     assert rel(u, fx["soln"]) < TOL64
 
