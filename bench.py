@@ -682,6 +682,8 @@ def main():
     ap.add_argument("--breakdown", action="store_true")
     ap.add_argument("--workload", default="poisson", choices=sorted(WORKLOADS))
     ap.add_argument("--oracle", action="store_true", help="c4: also run the FP64 CPU oracle (minutes)")
+    ap.add_argument("--no-autotune", dest="no_autotune", action="store_true",
+                    help="skip the GEMM autotuner (built-in kernel choices)")
     ap.add_argument("--train-fronts", dest="train_fronts", type=int, default=6, help="c5: fronts to train on")
     ap.add_argument("--threshold", type=float, default=0.9, help="c5: proposal probability threshold")
     args = ap.parse_args()
@@ -722,6 +724,22 @@ def main():
         pde.reset()
         hps.build_solver(pde, precision=args.precision)
         return hps.solve(pde, g, host_device=None)
+
+    # tile shapes and kernels of the products from the project's autotuner
+    # (untimed): every variant timed on every product shape of one step
+    tuning = None
+    if not args.no_autotune:
+        from jaxhps_gb300 import autotune
+
+        rep = autotune.tune(step, reps=3)
+        names = {}
+        for sh in rep["shapes"]:
+            names[sh["variant_name"]] = names.get(sh["variant_name"], 0) + 1
+        tuning = {"shapes": len(rep["shapes"]), "seconds": rep["seconds"], "variants": names,
+                  "builtin_ms_sum": rep["builtin_total_ms"], "tuned_ms_sum": rep["tuned_total_ms"]}
+        pde.reset()
+        nat.release_workspace()
+        torch.cuda.empty_cache()
 
     for _ in range(args.warmup):
         step()
@@ -932,7 +950,7 @@ def main():
                    "l2": "inputs larger than L2 (operator set is several GB)"},
         "rel_err_vs_fp64": err, **acc, "refinement_iterations": iters, "fp64_path": fp64,
         "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernel_classes": breakdown,
-        "cpu_baseline": cpu, "clocks": clk,
+        "cpu_baseline": cpu, "clocks": clk, "autotune": tuning,
     }
     if rank == 0:
         print(json.dumps(line))

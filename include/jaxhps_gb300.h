@@ -109,6 +109,26 @@ HPS_API int hps_inverse_policy(int policy);
  * No counterpart in the reference. */
 HPS_API int hps_gemm_policy(int policy);
 
+/* Autotuning of the FP32 batched products (the leaf, merge, refinement and
+ * down-pass products; not the N <= 8 ones).  Kernel variants: 0 tcgen05
+ * 3xTF32, 1 / 2 / 3 SIMT 8x8 register tiles of 128x128 / 128x64 / 64x64,
+ * 4 / 5 / 6 64x64 tiles with K split over a 2 / 4 / 8-CTA cluster, 7 SIMT 4x4
+ * register tiles of 64x64.  hps_gemm_tune_set stores the variant for an
+ * (M, N, K, batch) shape (-1 removes it); products of a stored shape run that
+ * variant, the others the built-in rules.  hps_gemm_tune_clear empties the
+ * table.  hps_gemm_force_variant(v) runs every FP32 product with variant v
+ * (-1: off; for timing), returning the previous one.  hps_gemm_shapes(mode,
+ * out, cap): mode 1 clears the record and starts recording the distinct
+ * product shapes, 0 stops, -1 only reads; returns the number recorded and
+ * writes up to cap of them to out, 13 values each (M, N, K, batch, lda,
+ * strideA, ldb, strideB, ldc, strideC, ldd, strideD, has C).  The table and
+ * switches are process-wide.  jaxhps_gb300/autotune.py drives them.  No
+ * counterpart in the reference (XLA chooses its own kernels). */
+HPS_API int hps_gemm_tune_set(int M, int N, int K, int batch, int variant);
+HPS_API int hps_gemm_tune_clear(void);
+HPS_API int hps_gemm_force_variant(int variant);
+HPS_API long long hps_gemm_shapes(int mode, long long* out, long long cap);
+
 /* Live profiler.  hps_profile_begin(mask) arms CUDA-event timing of every
  * later launch whose kernel class c has bit (1 << c) set in mask (classes:
  * 1 GEMM, 2 inverse, 3 gather/scatter/assembly, 4 refinement residual),

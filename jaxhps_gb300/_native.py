@@ -205,6 +205,14 @@ def _declare(lib):
     lib.hps_gemm_tc_status.restype = ci
     lib.hps_gemm_tc_status_reset.argtypes = []
     lib.hps_gemm_tc_status_reset.restype = ci
+    lib.hps_gemm_tune_set.argtypes = [ci, ci, ci, ci, ci]
+    lib.hps_gemm_tune_set.restype = ci
+    lib.hps_gemm_tune_clear.argtypes = []
+    lib.hps_gemm_tune_clear.restype = ci
+    lib.hps_gemm_force_variant.argtypes = [ci]
+    lib.hps_gemm_force_variant.restype = ci
+    lib.hps_gemm_shapes.argtypes = [ci, P(cll), cll]
+    lib.hps_gemm_shapes.restype = cll
     lib.hps_inverse_policy.argtypes = [ci]
     lib.hps_inverse_policy.restype = ci
     lib.hps_set_spin_limits.argtypes = [cll, cll, P(cll), P(cll)]
@@ -233,7 +241,7 @@ EXPORTED_SYMBOLS = (
     "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
-    "hps_scale_batched", "hps_gemm_tc_status", "hps_gemm_tc_status_reset", "hps_set_spin_limits", "hps_inverse_policy", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
+    "hps_scale_batched", "hps_gemm_tc_status", "hps_gemm_tc_status_reset", "hps_set_spin_limits", "hps_inverse_policy", "hps_gemm_tune_set", "hps_gemm_tune_clear", "hps_gemm_force_variant", "hps_gemm_shapes", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
 )
 
 

@@ -534,6 +534,23 @@ long long hps_launch_count(void) { return g_launches.load(std::memory_order_rela
 
 int hps_gemm_policy(int policy) { return set_gemm_policy(policy); }
 
+int hps_gemm_tune_set(int M, int N, int K, int batch, int variant) {
+  if (gemm_tune_set(M, N, K, batch, variant) != 0) {
+    set_error("hps_gemm_tune_set: variant %d out of range", variant);
+    return HPS_ERR_ARG;
+  }
+  return HPS_OK;
+}
+
+int hps_gemm_tune_clear(void) {
+  gemm_tune_clear();
+  return HPS_OK;
+}
+
+int hps_gemm_force_variant(int variant) { return gemm_force_variant(variant); }
+
+long long hps_gemm_shapes(int mode, long long* out, long long cap) { return gemm_shapes(mode, out, cap); }
+
 int hps_interp_rows(long long n_rows, int n_src, const double* to_pts, const double* src_pts,
                     const double* src_weights, double* out, int rows_per_group, int transposed, void* stream) {
   if (n_rows < 0 || n_src <= 0 || !to_pts || !src_pts || !src_weights || !out || rows_per_group <= 0 ||

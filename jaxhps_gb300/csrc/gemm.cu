@@ -11,7 +11,11 @@
 #include <stdlib.h>
 
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
+#include <vector>
 
 #include <cooperative_groups.h>
 
@@ -525,11 +529,126 @@ int set_gemm_policy(int p) {
   return old;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuning of the FP32 products.  A tuner (jaxhps_gb300/autotune.py) records
+// the shapes a build + solve issues (hps_gemm_shapes), times every kernel
+// variant below on each shape (hps_gemm_force_variant) and stores the fastest
+// per (M, N, K, batch) (hps_gemm_tune_set); gemm_batched<float> then runs the
+// stored variant and falls back to the measured rules below for other shapes.
+// ---------------------------------------------------------------------------
+enum GemmVariant {
+  GV_TC = 0,          // tcgen05 3xTF32 (gemm_tc.cu)
+  GV_V4_128x128 = 1,  // SIMT 8x8 register tiles, 128 x 128 CTA tile
+  GV_V4_128x64 = 2,
+  GV_V4_64x64 = 3,
+  GV_SPLIT2 = 4,      // 64 x 64 tiles, K split over a 2-CTA cluster
+  GV_SPLIT4 = 5,
+  GV_SPLIT8 = 6,
+  GV_GENERIC = 7,     // SIMT 4x4 register tiles, 64 x 64
+  GV_COUNT = 8
+};
+
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int>, int> g_tune;
+static std::atomic<int> g_tune_size{0};
+static std::atomic<int> g_force_variant{-1};
+static std::atomic<int> g_shape_log{0};
+static std::vector<std::vector<long long>> g_shapes;
+
+int gemm_tune_set(int M, int N, int K, int batch, int variant) {
+  if (variant >= GV_COUNT) return -1;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  const auto key = std::make_tuple(M, N, K, batch);
+  if (variant < 0) g_tune.erase(key);
+  else g_tune[key] = variant;
+  g_tune_size.store((int)g_tune.size());
+  return 0;
+}
+
+void gemm_tune_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  g_tune_size.store(0);
+}
+
+int gemm_force_variant(int variant) {
+  if (variant >= GV_COUNT) return -2;
+  return g_force_variant.exchange(variant < 0 ? -1 : variant);
+}
+
+long long gemm_shapes(int mode, long long* out, long long cap) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (mode == 1) {
+    g_shapes.clear();
+    g_shape_log.store(1);
+  } else if (mode == 0) {
+    g_shape_log.store(0);
+  }
+  if (out)
+    for (long long i = 0; i < (long long)g_shapes.size() && i < cap; ++i)
+      for (int j = 0; j < 13; ++j) out[i * 13 + j] = g_shapes[(size_t)i][(size_t)j];
+  return (long long)g_shapes.size();
+}
+
+static void log_shape(int M, int N, int K, int batch, long long lda, long long sA, long long ldb, long long sB,
+                      long long ldc, long long sC, long long ldd, long long sD, bool has_c) {
+  std::vector<long long> e{M, N, K, batch, lda, sA, ldb, sB, ldc, sC, ldd, sD, has_c ? 1 : 0};
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (const auto& x : g_shapes)
+    if (x == e) return;
+  g_shapes.push_back(e);
+}
+
+static int tuned_variant(int M, int N, int K, int batch) {
+  const int f = g_force_variant.load(std::memory_order_relaxed);
+  if (f >= 0) return f;
+  if (g_tune_size.load(std::memory_order_relaxed) == 0) return -1;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  const auto it = g_tune.find(std::make_tuple(M, N, K, batch));
+  return it == g_tune.end() ? -1 : it->second;
+}
+
+static cudaError_t run_variant_f32(int v, int M, int N, int K, float alpha, const float* A, long long lda,
+                                   long long sA, const float* B, long long ldb, long long sB, float beta,
+                                   const float* C, long long ldc, long long sC, float* D, long long ldd,
+                                   long long sD, int batch, cudaStream_t st) {
+  switch (v) {
+    case GV_TC:
+      return gemm_tf32x3(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+    case GV_V4_128x128:
+      return launch_gemm_f32_v4<128, 128>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD,
+                                          batch, st);
+    case GV_V4_128x64:
+      return launch_gemm_f32_v4<128, 64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD,
+                                         batch, st);
+    case GV_V4_64x64:
+      return launch_gemm_f32_v4<64, 64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD,
+                                        batch, st);
+    case GV_SPLIT2:
+    case GV_SPLIT4:
+    case GV_SPLIT8:
+      return launch_gemm_f32_v4_split<64, 64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD,
+                                              batch, 2 << (v - GV_SPLIT2), st);
+    default:
+      return launch_gemm_cfg<float, 64, 64, 8, 4, 4>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D,
+                                                     ldd, sD, batch, st);
+  }
+}
+
 template <class T>
 cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda, long long sA,
                          const T* B, long long ldb, long long sB, T beta, const T* C, long long ldc,
                          long long sC, T* D, long long ldd, long long sD, int batch, cudaStream_t st) {
   if (M <= 0 || N <= 0 || batch <= 0) return cudaSuccess;
+  if constexpr (std::is_same<T, float>::value) {
+    if (!(N <= 8 && K >= 32)) {
+      if (g_shape_log.load(std::memory_order_relaxed))
+        log_shape(M, N, K, batch, lda, sA, ldb, sB, ldc, sC, ldd, sD, C != nullptr);
+      const int v = tuned_variant(M, N, K, batch);
+      if (v >= 0)
+        return run_variant_f32(v, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+    }
+  }
   if (N <= 8 && K >= 32) {
     if (N == 1)
       return launch_skinny<T, 1>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);

@@ -49,6 +49,13 @@ cudaError_t inverse_tc_f32(int n, const float* A, long long lda, long long sA, f
                            long long sX, int batch, int* info, cudaStream_t st);
 int inverse_tc_policy();
 int set_inverse_tc_policy(int policy);
+
+// Autotuning table of the FP32 products (gemm.cu): per-shape kernel variant,
+// a forced variant for timing, and the shape recorder.
+int gemm_tune_set(int M, int N, int K, int batch, int variant);
+void gemm_tune_clear();
+int gemm_force_variant(int variant);
+long long gemm_shapes(int mode, long long* out, long long cap);
 // Sets the tensor-core policy of gemm_batched (0, 1, 2); returns the old one.
 int set_gemm_policy(int p);
 
