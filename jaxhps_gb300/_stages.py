@@ -39,6 +39,10 @@ def colour_perm_device(maps, dev):
 
 REAL_TO_COMPLEX = {torch.float64: torch.complex128, torch.float32: torch.complex64}
 
+# Device bytes the leaf stage's workspace (the assembled leaf operators) may
+# take at once; above it the leaves go in chunks.
+LEAF_WORKSPACE_BUDGET = 16 << 30
+
 
 def _device(device) -> torch.device:
     if device is None or (isinstance(device, str) and device == "cuda"):
@@ -200,9 +204,33 @@ def _local_solve_dtn(pde_problem, P_np, Q_np, device, dtype, keep_inverse, sourc
         source=nat.ptr(f), P=P.data_ptr(), Q=Q.data_ptr(), Y=Y.data_ptr(), T=T.data_ptr(), v=nat.ptr(v),
         h=nat.ptr(h), Aii_inv=Aii.data_ptr(), info=info.data_ptr(), workspace=None, workspace_bytes=0)
     wsb = L.hps_local_solve_dtn_workspace_size(C.byref(a))
-    ws = nat.workspace(wsb, dev)
-    a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
-    nat.check(L.hps_local_solve_dtn(C.byref(a), nat.stream_ptr()), "hps_local_solve_dtn")
+    if wsb <= LEAF_WORKSPACE_BUDGET or n_leaves == 1:
+        ws = nat.workspace(wsb, dev)
+        a.workspace, a.workspace_bytes = ws.data_ptr(), ws.numel()
+        nat.check(L.hps_local_solve_dtn(C.byref(a), nat.stream_ptr()), "hps_local_solve_dtn")
+    else:
+        # the assembled leaf operators of every leaf would not fit the budget:
+        # leaves in chunks (the reference chunks its leaf stage as well,
+        # _device_config.py:65-90), one workspace reused by all chunks
+        chunk = max(1, int(n_leaves * LEAF_WORKSPACE_BUDGET // wsb))
+        es = torch.empty((), dtype=dtype).element_size()
+        for lo in range(0, n_leaves, chunk):
+            hi = min(n_leaves, lo + chunk)
+            cc = coeffs[:, lo:hi].contiguous()
+            b = nat.LeafDtnArgs(
+                dtype=a.dtype, coef_complex=a.coef_complex, n_leaves=hi - lo, n_pts=n_pts, n_cb=n_cb, n_gauss=ng,
+                nsrc=ns, n_ops=a.n_ops, ops=a.ops, coeffs=cc.data_ptr(),
+                source=None if f is None else f.data_ptr() + lo * n_pts * ns * es, P=a.P, Q=a.Q,
+                Y=Y.data_ptr() + lo * n_pts * ng * es, T=T.data_ptr() + lo * ng * ng * es,
+                v=None if v is None else v.data_ptr() + lo * n_pts * ns * es,
+                h=None if h is None else h.data_ptr() + lo * ng * ns * es,
+                Aii_inv=Aii.data_ptr() + lo * n_i * n_i * es, info=info.data_ptr() + lo * 4, workspace=None,
+                workspace_bytes=0)
+            wsc = L.hps_local_solve_dtn_workspace_size(C.byref(b))
+            ws = nat.workspace(wsc, dev)
+            b.workspace, b.workspace_bytes = ws.data_ptr(), ws.numel()
+            nat.check(L.hps_local_solve_dtn(C.byref(b), nat.stream_ptr()), "hps_local_solve_dtn")
+            del cc
     if v is not None and not multi:
         v, h = v[..., 0], h[..., 0]
     out = (Y, T, v, h)
