@@ -780,6 +780,7 @@ def main():
     ms_per_step = ms / args.steps
     value = world * n_leaves / (ms_per_step / 1e3)
     iters = len(pde._state.history) if getattr(pde, "_state", None) is not None else None
+    history = [float(h) for h in pde._state.history] if iters else None
     pde.reset()                      # the comparison run below needs the memory
     nat.release_workspace()
     torch.cuda.empty_cache()
@@ -955,7 +956,8 @@ def main():
         "config": {"workload": wl["name"], "L": L, "n_leaves": n_leaves, "p": p, "q": q, "nsrc": ns,
                    "precision": args.precision, "parallelism": "replicas" if world > 1 else "single-gpu",
                    "l2": "inputs larger than L2 (operator set is several GB)"},
-        "rel_err_vs_fp64": err, **acc, "refinement_iterations": iters, "fp64_path": fp64,
+        "rel_err_vs_fp64": err, **acc, "refinement_iterations": iters,
+        "refinement_history": history, "fp64_path": fp64,
         "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernel_classes": breakdown,
         "cpu_baseline": cpu, "clocks": clk, "autotune": tuning,
     }

@@ -13,7 +13,8 @@ every leaf) in FP64, starting from zero, iterating
                                  down pass (hps_down_level)
     x += dx                      FP64 (hps_accumulate)
 
-until max|du| <= tol * max|u|.  J is the system the reference's FP64 direct
+until the remaining error is at most tol * max|u| (``converged``: the last
+correction, or the contraction-rate estimate of what is left).  J is the system the reference's FP64 direct
 solver solves exactly: leaf collocation rows (local_solve/_uniform_2D_DtN.py:
 228-273), continuity of the outward normal derivative across interfaces
 (the merge equations, merge/_schur_complement.py:182-237) and the Dirichlet
@@ -248,6 +249,26 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     return None
 
 
+def converged(history, tol: float) -> bool:
+    """True once the refinement's remaining error is at most tol (max norms,
+    relative to the solution).  ``history`` holds max|dx_k| / max|x| of every
+    correction so far.  Refinement converges linearly: with contraction rho,
+    the error left after correction k is about rho / (1 - rho) * |dx_k|, so
+    once two corrections give rho = |dx_k| / |dx_(k-1)| < 1/4 that estimate
+    decides, which ends one correction before the next one would itself fall
+    below tol.  Without a rate (first correction) or with slow contraction
+    (rho >= 1/4, e.g. at the rounding floor), the last correction must be
+    below tol."""
+    h = history[-1]
+    if h <= tol:
+        return True
+    if len(history) >= 2 and history[-2] > 0.0:
+        rho = h / history[-2]
+        if rho < 0.25 and rho / (1.0 - rho) * h <= tol:
+            return True
+    return False
+
+
 def raise_not_converged(history, tol, max_iters, what: str) -> None:
     """Refinement ran max_iters steps without its last correction falling to
     tol times the solution (max norms): the result is not FP64-accurate."""
@@ -346,7 +367,7 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
         nat.check(L.hps_accumulate(dg.numel(), dg.data_ptr(), g.data_ptr(), sp), "hps_accumulate")
         step, size = nat.accumulate_max(du, u_int, maxima)
         state.history.append(step / max(size, 1e-300))
-        if step <= tol * size:
+        if converged(state.history, tol):
             break
         if it == 0:
             # the first correction is the size of the solution: recompute the

@@ -11,7 +11,8 @@ assembled once in FP64 (hps_assemble_rows) and kept for the residuals.
 
 Solve: x = (u_int, g) in FP64 from zero, iterating r = b - J x (FP64
 strided GEMMs), dx = M r (FP32 leaf inverse, up pass, down pass), x += dx,
-until max|du| <= tol * max|u|.  J is the system the reference's FP64 direct
+until the remaining error is at most tol * max|u|
+(``_refinement.converged``).  J is the system the reference's FP64 direct
 solver solves exactly: leaf collocation rows (local_solve/_uniform_3D_DtN.py
 :13-106 with get_DtN, local_solve/_uniform_2D_DtN.py:228-273), continuity
 of the outward normal derivative across interfaces (the merge equations,
@@ -30,7 +31,7 @@ import torch
 from . import _native as nat
 from . import _stages as st
 from ._index_maps import oct_merge_maps_dtn, quad_merge_maps_dtn
-from ._refinement import leaf_gauss_nodes_2D, node_maps, raise_not_converged
+from ._refinement import converged, leaf_gauss_nodes_2D, node_maps, raise_not_converged
 
 
 def _maps_for_ext(dim: int) -> Callable:
@@ -260,7 +261,7 @@ def solve_mixed_dense(pde_problem, boundary_data, source=None, host_device="cpu"
         nat.check(L.hps_accumulate(dg.numel(), dg.data_ptr(), g.data_ptr(), sp), "hps_accumulate")
         step, size = nat.accumulate_max(du, u_int, maxima)
         state.history.append(step / max(size, 1e-300))
-        if step <= tol * size:
+        if converged(state.history, tol):
             break
         _residual(state, u_int, g, ub, r64, r32, flux)
     else:

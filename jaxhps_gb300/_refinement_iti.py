@@ -17,7 +17,7 @@ tensor-product derivatives, no stored per-leaf rows) and applies M:
     v  = inv(B) r_leaf,  h = QH v + hcorr  (hcorr: the interface residuals),
     up pass with D^-1, B D^-1; down pass from the boundary residual -> dt,
     du = Y dt + v;  u += du, t += dt
-until max|du| <= tol max|u|.
+until the remaining error is at most tol max|u| (``_refinement.converged``).
 """
 
 from __future__ import annotations
@@ -35,7 +35,7 @@ from . import _stages as st
 from ._index_maps import quad_merge_maps_iti
 from ._nosource import _nosource_merge, store_operators
 from ._pdeproblem import COEFF_NAMES_2D
-from ._refinement import OP_KIND_2D, _domain_constants, raise_not_converged
+from ._refinement import OP_KIND_2D, _domain_constants, converged, raise_not_converged
 from ._refinement_dense import _node_pairing
 
 
@@ -201,7 +201,7 @@ def solve_mixed_iti(pde_problem, boundary_data, source=None, host_device="cpu", 
         _accumulate(dt, t)
         step, size = nat.accumulate_max(du, u, maxima, pairs=True)
         state.history.append(step / max(size, 1e-300))
-        if step <= tol * size:
+        if converged(state.history, tol):
             break
         _residual(state, u, t, r32, t_out)
     else:
