@@ -99,6 +99,19 @@ HPS_API int hps_set_spin_limits(long long panel_barrier_polls, long long tc_wait
  * jnp.linalg.inv). */
 HPS_API int hps_inverse_policy(int policy);
 
+/* Whether the FP32 interface-matrix inverses of the DtN merges
+ * (hps_merge_level_dtn, n >= 224) use the recursive 2 x 2 block inversion:
+ * two half-size inversions and six half-size batched products per level,
+ * down to blocks of n < 224 inverted by pivoted Gauss-Jordan, with no
+ * pivoting across blocks (the leading blocks of an interface matrix are
+ * interface operators themselves).  1 on (default; HPS_INVERSE_RECURSIVE=0 in
+ * the environment starts a process at 0), 0 off (pivoted Gauss-Jordan over the
+ * whole matrix), -1 query.  Returns the previous policy.  hps_inverse_batched
+ * itself always pivots over the whole matrix.  Process-wide; not meant to
+ * change while work is in flight.  No counterpart in the reference (which
+ * calls jnp.linalg.inv). */
+HPS_API int hps_inverse_block_policy(int policy);
+
 /* Which batched products run on the tcgen05 kernel: 0 none (SIMT kernels
  * only), 1 the shapes where it was measured faster (default; HPS_GEMM_TC=0 in
  * the environment starts a process at 0), 2 every FP32 and complex64 product
@@ -171,6 +184,16 @@ HPS_API size_t hps_inverse_workspace_size(int dtype, int n, int batch);
 HPS_API int hps_inverse_batched(int dtype, int n, const void* A, long long lda, long long strideA, void* X,
                         long long ldx, long long strideX, int batch, int* info, void* workspace,
                         size_t workspace_bytes, void* stream);
+
+/* The inverse hps_merge_level_dtn applies to its interface matrices: as
+ * hps_inverse_batched, except that FP32 matrices of n >= 224 use the
+ * recursive 2 x 2 block inversion while hps_inverse_block_policy is 1 (zero
+ * pivots of its blocks reported in info with the block's column offset).
+ * Same workspace size.  Replaces jnp.linalg.inv at
+ * merge/_schur_complement.py:146. */
+HPS_API int hps_inverse_interface(int dtype, int n, const void* A, long long lda, long long strideA, void* X,
+                                  long long ldx, long long strideX, int batch, int* info, void* workspace,
+                                  size_t workspace_bytes, void* stream);
 
 /* Size of the fixed scratch behind hps_inverse_batched_static: 64 MiB. */
 #define HPS_STATIC_SCRATCH_BYTES (64u << 20)
@@ -417,6 +440,27 @@ HPS_API int hps_residual_2d(const hps_residual2d_args* a, void* stream);
  * arithmetic on the FP32 pipe.  Refinement only: no counterpart in the
  * reference, which solves in FP64 directly. */
 HPS_API int hps_residual_update_2d(const hps_residual2d_args* a, const float* du, const float* dg, void* stream);
+
+/* hps_residual_2d with the FP64 leaf-row residual r also stored as an FP32
+ * pair: a->r_int = fl32(r) and r_lo = fl32(r - a->r_int) (a->r_int64 may be
+ * NULL).  The starting point of hps_residual_update_2d_df.  Refinement only:
+ * no counterpart in the reference. */
+HPS_API int hps_residual_2d_df(const hps_residual2d_args* a, float* r_lo, void* stream);
+
+/* The incremental update of hps_residual_update_2d with the leaf-row
+ * residual held as an FP32 pair (a->r_int = hi, r_lo = lo, both in/out; no
+ * FP64 arithmetic on it) and a->flux += Q du_full (FP64, in/out); a->r_int64,
+ * a->coeffs and the FP64 operators are not read: `prep` holds them as FP32
+ * pairs, written once per solve by hps_residual_df_prepare (its size in bytes
+ * from hps_residual_df_prep_size).  Each thread keeps one grid line in
+ * registers.  Supported for q = p - 2 with p in 8, 10, 12, 14, 16
+ * (hps_residual_df_supported); HPS_ERR_ARG otherwise.  Refinement only: no
+ * counterpart in the reference. */
+HPS_API size_t hps_residual_df_prep_size(int n_leaves, int p, int q, int n_ops);
+HPS_API int hps_residual_df_prepare(const hps_residual2d_args* a, float* prep, void* stream);
+HPS_API int hps_residual_update_2d_df(const hps_residual2d_args* a, const float* prep, const float* du,
+                                      const float* dg, float* r_lo, void* stream);
+HPS_API int hps_residual_df_supported(int p, int q);
 
 /* u_full = [P g ; u_int] per leaf (FP64), exterior-first leaf order: the
  * leaf solution u = Y g + v of the down pass (down_pass/_uniform_2D_DtN.py

@@ -166,6 +166,20 @@ def _declare(lib):
     lib.hps_accumulate.restype = ci
     lib.hps_residual_update_2d.argtypes = [P(Residual2DArgs), vp, vp, vp]
     lib.hps_residual_update_2d.restype = ci
+    lib.hps_residual_2d_df.argtypes = [P(Residual2DArgs), vp, vp]
+    lib.hps_residual_2d_df.restype = ci
+    lib.hps_residual_update_2d_df.argtypes = [P(Residual2DArgs), vp, vp, vp, vp, vp]
+    lib.hps_residual_update_2d_df.restype = ci
+    lib.hps_residual_df_prep_size.argtypes = [ci, ci, ci, ci]
+    lib.hps_residual_df_prep_size.restype = csz
+    lib.hps_residual_df_prepare.argtypes = [P(Residual2DArgs), vp, vp]
+    lib.hps_residual_df_prepare.restype = ci
+    lib.hps_inverse_interface.argtypes = lib.hps_inverse_batched.argtypes
+    lib.hps_inverse_interface.restype = ci
+    lib.hps_inverse_block_policy.argtypes = [ci]
+    lib.hps_inverse_block_policy.restype = ci
+    lib.hps_residual_df_supported.argtypes = [ci, ci]
+    lib.hps_residual_df_supported.restype = ci
     lib.hps_assemble_u_2d.argtypes = [ci, ci, ci, ci, vp, vp, vp, vp, vp]
     lib.hps_assemble_u_2d.restype = ci
     lib.hps_interior_f32.argtypes = [cll, ci, ci, ci, vp, vp, vp]
@@ -238,7 +252,8 @@ EXPORTED_SYMBOLS = (
     "hps_inverse_batched", "hps_convert", "hps_local_solve_dtn_workspace_size", "hps_local_solve_dtn",
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
     "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
-    "hps_accumulate", "hps_residual_update_2d", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
+    "hps_accumulate", "hps_residual_update_2d", "hps_residual_2d_df", "hps_residual_update_2d_df",
+    "hps_residual_df_supported", "hps_residual_df_prep_size", "hps_inverse_block_policy", "hps_inverse_interface", "hps_residual_df_prepare", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
     "hps_scale_batched", "hps_gemm_tc_status", "hps_gemm_tc_status_reset", "hps_set_spin_limits", "hps_inverse_policy", "hps_gemm_tune_set", "hps_gemm_tune_clear", "hps_gemm_force_variant", "hps_gemm_shapes", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
@@ -383,8 +398,9 @@ def gemm(A, B, out, alpha=1.0, beta=0.0, Cmat=None, batch=None):
     return out
 
 
-def inverse(A, out=None, info=None):
-    """Batched inverse of a (batch, n, n) tensor (out may be A)."""
+def inverse(A, out=None, info=None, entry="hps_inverse_batched"):
+    """Batched inverse of a (batch, n, n) tensor (out may be A); entry
+    "hps_inverse_interface" selects the merge interface-matrix inverse."""
     L = lib()
     if A.dim() == 2:
         A = A.unsqueeze(0)
@@ -394,8 +410,8 @@ def inverse(A, out=None, info=None):
     dt = TORCH_TO_HPS[A.dtype]
     wsb = L.hps_inverse_workspace_size(dt, n, b)
     ws = workspace(wsb, A.device) if wsb else None
-    check(L.hps_inverse_batched(dt, n, A.data_ptr(), A.stride(1), A.stride(0), out.data_ptr(), out.stride(1),
-                                out.stride(0), b, ptr(info), ptr(ws), wsb, stream_ptr()), "hps_inverse_batched")
+    check(getattr(L, entry)(dt, n, A.data_ptr(), A.stride(1), A.stride(0), out.data_ptr(), out.stride(1),
+                            out.stride(0), b, ptr(info), ptr(ws), wsb, stream_ptr()), entry)
     return out
 
 

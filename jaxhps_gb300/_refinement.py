@@ -7,16 +7,19 @@ solver, used here as an approximate inverse M of the discrete system J.
 Solve: x = (interior values u_int of every leaf, Gauss boundary values g of
 every leaf) in FP64, starting from zero, iterating
 
-    r  = b - J x                 FP64 residual (hps_residual_2d,
-                                 hps_flux_combine)
+    r  = b - J x                 FP64 residual after the first correction
+                                 (hps_residual_2d_df), then kept current by
+                                 r -= J dx in double-float with r held as
+                                 an FP32 pair (hps_residual_update_2d_df);
+                                 interface terms by hps_flux_combine
     dx = M r                     FP32: leaf inverse, up pass (hps_up_level),
                                  down pass (hps_down_level)
     x += dx                      FP64 (hps_accumulate)
 
 until the remaining error is at most tol * max|u| (``converged``: the last
-correction, or the contraction-rate estimate of what is left).  J is the system the reference's FP64 direct
-solver solves exactly: leaf collocation rows (local_solve/_uniform_2D_DtN.py:
-228-273), continuity of the outward normal derivative across interfaces
+correction, or the contraction-rate estimate of what is left).  J is the
+system the reference's FP64 direct solver solves exactly: leaf collocation
+rows (local_solve/_uniform_2D_DtN.py:228-273), continuity of the outward normal derivative across interfaces
 (the merge equations, merge/_schur_complement.py:182-237) and the Dirichlet
 data on the domain boundary.  The fixed point is therefore the FP64 discrete
 solution; each iteration contracts the error by roughly the FP32 solver's
@@ -150,7 +153,7 @@ def _refine_leaf_operators(dom, coeffs, op_kind, consts, Y, Aii_inv, Q_int):
 
     Y_int solves A_ii Y_int = W, W = -A_ie P.  With the FP32 solution Y0,
     R = W - A_ii Y0 and T0 = Q [P ; Y0] are evaluated in double-float
-    arithmetic (hps_residual_update_2d applied to the 4q Gauss-data columns),
+    arithmetic (the residual update applied to the 4q Gauss-data columns),
     then Y_int = Y0 + inv(A_ii) R and T = T0 + Q_int inv(A_ii) R in FP32.
     FP32 evaluation of W and Q Y cancels terms ~1e8 times larger than the
     DtN map's smallest eigenvalues (the near-constant modes); this step
@@ -161,18 +164,25 @@ def _refine_leaf_operators(dom, coeffs, op_kind, consts, Y, Aii_inv, Q_int):
     dev = Y.device
     Y0 = Y[:, n_cb:, :].contiguous()
     dg = torch.eye(nq, dtype=torch.float32, device=dev).expand(n_leaves, nq, nq).contiguous()
-    r64 = torch.zeros(Y0.shape, dtype=torch.float64, device=dev)
-    r32 = torch.empty(Y0.shape, dtype=torch.float32, device=dev)
+    pairs = bool(nat.lib().hps_residual_df_supported(p, q))
+    r64 = None if pairs else torch.zeros(Y0.shape, dtype=torch.float64, device=dev)
+    r_lo = torch.zeros(Y0.shape, dtype=torch.float32, device=dev) if pairs else None
+    r32 = torch.zeros(Y0.shape, dtype=torch.float32, device=dev)
     T0 = torch.zeros((n_leaves, nq, nq), dtype=torch.float64, device=dev)
     a = nat.Residual2DArgs(
         n_leaves=n_leaves, p=p, q=q, nsrc=nq, n_ops=len(op_kind), coeffs=coeffs.data_ptr(),
         inv_half=consts["inv_half"].data_ptr(), D1=consts["D1"].data_ptr(), D2=consts["D2"].data_ptr(),
         Pside=consts["Pside"].data_ptr(), Qside=consts["Qside"].data_ptr(), perm=consts["perm"].data_ptr(),
-        u_int=None, g=None, f=None, r_int=r32.data_ptr(), r_int64=r64.data_ptr(), flux=T0.data_ptr(), u_full=None)
+        u_int=None, g=None, f=None, r_int=r32.data_ptr(), r_int64=nat.ptr(r64), flux=T0.data_ptr(), u_full=None)
     for i, k in enumerate(op_kind):
         a.op_kind[i] = k
-    nat.check(nat.lib().hps_residual_update_2d(C.byref(a), Y0.data_ptr(), dg.data_ptr(), nat.stream_ptr()),
-              "hps_residual_update_2d")
+    if pairs:
+        prep = _df_prepare(a)
+        nat.check(nat.lib().hps_residual_update_2d_df(C.byref(a), prep.data_ptr(), Y0.data_ptr(), dg.data_ptr(),
+                                                      r_lo.data_ptr(), nat.stream_ptr()), "hps_residual_update_2d_df")
+    else:
+        nat.check(nat.lib().hps_residual_update_2d(C.byref(a), Y0.data_ptr(), dg.data_ptr(), nat.stream_ptr()),
+                  "hps_residual_update_2d")
     dY = torch.empty_like(r32)
     nat.gemm(Aii_inv, r32, dY)                      # dY = inv(A_ii) R
     Y_int = Y[:, n_cb:, :]
@@ -290,10 +300,14 @@ def _res_args(state: MixedState, u_int, g, r32, flux, r64=None, u_full=None, zer
     return a
 
 
-def _residual(state: MixedState, u_int, g, r32, flux, u_full=None, zero_source=False, r64=None):
-    """FP64 residual of the discrete system at (u_int, g); zero_source drops f."""
+def _residual(state: MixedState, u_int, g, r32, flux, u_full=None, zero_source=False, r64=None, r_lo=None):
+    """FP64 residual of the discrete system at (u_int, g); zero_source drops f.
+    With r_lo the leaf-row residual is also stored as the FP32 pair (r32, r_lo)."""
     a = _res_args(state, u_int, g, r32, flux, r64=r64, u_full=u_full, zero_source=zero_source)
-    nat.check(nat.lib().hps_residual_2d(C.byref(a), nat.stream_ptr()), "hps_residual_2d")
+    if r_lo is not None:
+        nat.check(nat.lib().hps_residual_2d_df(C.byref(a), r_lo.data_ptr(), nat.stream_ptr()), "hps_residual_2d_df")
+    else:
+        nat.check(nat.lib().hps_residual_2d(C.byref(a), nat.stream_ptr()), "hps_residual_2d")
 
 
 def _residual_update(state: MixedState, du, dg, r64, r32, flux):
@@ -301,6 +315,27 @@ def _residual_update(state: MixedState, du, dg, r64, r32, flux):
     a = _res_args(state, None, None, r32, flux, r64=r64)
     nat.check(nat.lib().hps_residual_update_2d(C.byref(a), du.data_ptr(), dg.data_ptr(), nat.stream_ptr()),
               "hps_residual_update_2d")
+
+
+def _df_prepare(a) -> torch.Tensor:
+    """The FP32-pair operator and coefficient table of the pair residual
+    (hps_residual_df_prepare) for the problem described by the args ``a``."""
+    L = nat.lib()
+    nbytes = L.hps_residual_df_prep_size(a.n_leaves, a.p, a.q, a.n_ops)
+    if nbytes == 0:
+        raise ValueError(f"the pair residual does not serve p = {a.p}, q = {a.q}")
+    prep = torch.empty(nbytes // 4, dtype=torch.float32, device=torch.device("cuda", torch.cuda.current_device()))
+    nat.check(L.hps_residual_df_prepare(C.byref(a), prep.data_ptr(), nat.stream_ptr()), "hps_residual_df_prepare")
+    return prep
+
+
+def _residual_update_df(state: MixedState, prep, du, dg, r_lo, r32, flux):
+    """(r32, r_lo) -= (A du)_int as an FP32 pair, flux += Q du_full
+    (double-float arithmetic, one grid line per thread); ``prep`` from
+    _df_prepare."""
+    a = _res_args(state, None, None, r32, flux)
+    nat.check(nat.lib().hps_residual_update_2d_df(C.byref(a), prep.data_ptr(), du.data_ptr(), dg.data_ptr(),
+                                                  r_lo.data_ptr(), nat.stream_ptr()), "hps_residual_update_2d_df")
 
 
 def correction(state: MixedState, r32, hcorr, rb32):
@@ -349,8 +384,13 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
     u_int = torch.zeros((nl, n_i, ns), dtype=torch.float64, device=dev)
     g = torch.zeros((nl, 4 * q, ns), dtype=torch.float64, device=dev)
     r32 = torch.empty((nl, n_i, ns), dtype=torch.float32, device=dev)
-    r64 = torch.empty((nl, n_i, ns), dtype=torch.float64, device=dev)
+    # the leaf-row residual between updates: an FP32 pair (r32, r_lo) where the
+    # pair kernel serves (p, q), else FP64
+    pairs = bool(L.hps_residual_df_supported(p, q))
+    r64 = None if pairs else torch.empty((nl, n_i, ns), dtype=torch.float64, device=dev)
+    r_lo = torch.empty((nl, n_i, ns), dtype=torch.float32, device=dev) if pairs else None
     flux = torch.zeros((nl, 4 * q, ns), dtype=torch.float64, device=dev)
+    prep = _df_prepare(_res_args(state, None, None, r32, flux)) if pairs else None
     hcorr = torch.empty((nl, 4 * q, ns), dtype=torch.float32, device=dev)
     rb32 = torch.empty((g_given.shape[0], ns), dtype=torch.float32, device=dev)
     sp = nat.stream_ptr()
@@ -372,7 +412,9 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
         if it == 0:
             # the first correction is the size of the solution: recompute the
             # residual from scratch in FP64
-            _residual(state, u_int, g, r32, flux, r64=r64)
+            _residual(state, u_int, g, r32, flux, r64=r64, r_lo=r_lo)
+        elif pairs:
+            _residual_update_df(state, prep, du, dg, r_lo, r32, flux)
         else:
             _residual_update(state, du, dg, r64, r32, flux)
     else:

@@ -78,7 +78,7 @@ cudaError_t convert(long long n, const S* src, D* dst, cudaStream_t st);
 cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds, const double* coeffs,
                         const double* inv_half, const double* D1, const double* D2, const double* Pside,
                         const double* Qside, const int* perm, const double* u_int, const double* g,
-                        const double* f, float* r_int, double* r_int64, double* flux, double* u_full,
+                        const double* f, float* r_int, double* r_int64, float* r_lo, double* flux, double* u_full,
                         int need_uy, cudaStream_t st);
 cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr, int n_bdry,
                          const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
@@ -104,6 +104,14 @@ cudaError_t jx_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsign
                          const double* coeffs, const double* inv_half, const double* D1, const double* D2,
                          const double* Pside, const double* Qside, const int* perm, const float* du, const float* dg,
                          double* r_int, float* r32, double* flux, int need_uy, cudaStream_t st);
+bool jx_df_supported(int p, int q);
+size_t jx_df_prep_floats(int n_leaves, int p, int q, int n_ops);
+cudaError_t jx_df_prepare(int n_leaves, int p, int q, int n_ops, unsigned long long kinds, const double* coeffs,
+                          const double* inv_half, const double* D1, const double* D2, const double* Pside,
+                          const double* Qside, const int* perm, float* prep, cudaStream_t st);
+cudaError_t jx_df_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
+                            const float* prep, const double* inv_half, const int* perm, const float* du,
+                            const float* dg, float* r_hi, float* r_lo, double* flux, int need_uy, cudaStream_t st);
 cudaError_t assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
                           const double* g, double* u_full, cudaStream_t st);
 cudaError_t interior_f32(long long n_leaves, int pp, int ncb, int nsrc, const double* f, float* r32, cudaStream_t st);
@@ -220,7 +228,7 @@ static int leaf_dtn_impl(const hps_leaf_dtn_args* a, cudaStream_t st) {
   HPS_CHECK(e);
   // the leaf blocks may use the tensor-memory kernel (FP32, 64 < n <= 224)
   HPS_CHECK(inverse_batched<T>(ni, Aii, ni, (long long)ni * ni, Aii, ni, (long long)ni * ni, nl, a->info, invws,
-                               invb, st, true));
+                               invb, st, INV_TENSOR_MEMORY));
   const T one_ = one<T>(), zero_ = zero<T>(), mone = make_scalar<T>(-1.0, 0.0);
   const T* P = (const T*)a->P;
   const T* Q = (const T*)a->Q;
@@ -374,8 +382,9 @@ static int merge_impl(const hps_merge_args* a, cudaStream_t st, bool iti) {
     HPS_CHECK(gemm_batched<T>(nx, nx, nx, mone, X21, nx, sx, Pm, nx, sx, zero_, nullptr, 0, 0, Wm, nx, sx, nm, st));
     HPS_CHECK(perm_scatter<T>(nm, ni, nx, nx, D, sD, cp, nx, nx, Wm, sx, 1, st));
   } else {
+    // interface matrices: the recursive block inversion may serve FP32
     HPS_CHECK(inverse_batched<T>(ni, D, ni, (long long)ni * ni, D, ni, (long long)ni * ni, nm, a->info, invws, invb,
-                                 st));
+                                 st, INV_BLOCK_RECURSIVE));
   }
   T* S = (T*)a->S;
   const long long sDD = (long long)ni * ni, sC = (long long)ni * ne, sB = (long long)ne * ni, sT = (long long)ne * ne;
@@ -466,9 +475,9 @@ static int gemm_entry(int m, int n, int k, const double* alpha, const void* A, l
 
 template <class T>
 static int inverse_entry(int n, const void* A, long long lda, long long sA, void* X, long long ldx, long long sX,
-                         int batch, int* info, void* ws, size_t wsb, void* stream) {
+                         int batch, int* info, void* ws, size_t wsb, void* stream, int flags) {
   HPS_CHECK(inverse_batched<T>(n, (const T*)A, lda, sA, (T*)X, ldx, sX, batch, info, ws, wsb,
-                               (cudaStream_t)stream));
+                               (cudaStream_t)stream, flags));
   return HPS_OK;
 }
 
@@ -598,6 +607,8 @@ int hps_gemm_tc_status_reset(void) { return gemm_tc_error_reset(); }
 
 int hps_inverse_policy(int policy) { return set_inverse_tc_policy(policy); }
 
+int hps_inverse_block_policy(int policy) { return set_inverse_rec_policy(policy); }
+
 int hps_set_spin_limits(long long panel_barrier_polls, long long tc_wait_polls, long long* prev_panel,
                         long long* prev_tc) {
   cudaError_t e = set_panel_spin_limit(panel_barrier_polls, prev_panel);
@@ -680,7 +691,23 @@ int hps_inverse_batched(int dtype, int n, const void* A, long long lda, long lon
     return HPS_ERR_WORKSPACE;
   }
   DISPATCH(dtype, inverse_entry, n, A, lda, strideA, X, ldx, strideX, batch, info, workspace, workspace_bytes,
-           stream)
+           stream, 0)
+}
+
+int hps_inverse_interface(int dtype, int n, const void* A, long long lda, long long strideA, void* X, long long ldx,
+                          long long strideX, int batch, int* info, void* workspace, size_t workspace_bytes,
+                          void* stream) {
+  if (n < 0 || batch < 0 || !A || !X) {
+    set_error("hps_inverse_interface: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (workspace_bytes < inverse_workspace_bytes(dtype, n, batch)) {
+    set_error("hps_inverse_interface: workspace too small (%zu < %zu)", workspace_bytes,
+              inverse_workspace_bytes(dtype, n, batch));
+    return HPS_ERR_WORKSPACE;
+  }
+  DISPATCH(dtype, inverse_entry, n, A, lda, strideA, X, ldx, strideX, batch, info, workspace, workspace_bytes,
+           stream, INV_BLOCK_RECURSIVE)
 }
 
 int hps_convert(int ds, int dd, long long n, const void* src, void* dst, void* stream) {
@@ -899,6 +926,59 @@ int hps_residual_update_2d(const hps_residual2d_args* a, const float* du, const 
   return HPS_OK;
 }
 
+int hps_residual_df_supported(int p, int q) { return jx_df_supported(p, q) ? 1 : 0; }
+
+size_t hps_residual_df_prep_size(int n_leaves, int p, int q, int n_ops) {
+  if (n_leaves <= 0 || n_ops <= 0 || n_ops > 10 || !jx_df_supported(p, q)) return 0;
+  return jx_df_prep_floats(n_leaves, p, q, n_ops) * sizeof(float);
+}
+
+static int check_df_args(const hps_residual2d_args* a, const char* who) {
+  if (!a || a->n_leaves <= 0 || a->p < 3 || a->q <= 0 || a->nsrc <= 0 || a->n_ops <= 0 || !a->inv_half ||
+      !a->perm) {
+    set_error("%s: invalid arguments", who);
+    return HPS_ERR_ARG;
+  }
+  if (!jx_df_supported(a->p, a->q)) {
+    set_error("%s: p = %d, q = %d not supported (q = p - 2 with p in 8, 10, 12, 14, 16)", who, a->p, a->q);
+    return HPS_ERR_ARG;
+  }
+  return HPS_OK;
+}
+
+int hps_residual_df_prepare(const hps_residual2d_args* a, float* prep, void* stream) {
+  if (check_df_args(a, "hps_residual_df_prepare") != HPS_OK) return HPS_ERR_ARG;
+  if (!prep || !a->coeffs || !a->D1 || !a->D2 || !a->Pside || !a->Qside) {
+    set_error("hps_residual_df_prepare: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  unsigned long long kinds = 0;
+  int need_uy = 0;
+  if (pack_op_kinds(a, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
+  HPS_CHECK(jx_df_prepare(a->n_leaves, a->p, a->q, a->n_ops, kinds, a->coeffs, a->inv_half, a->D1, a->D2, a->Pside,
+                          a->Qside, a->perm, prep, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_residual_update_2d_df(const hps_residual2d_args* a, const float* prep, const float* du, const float* dg,
+                              float* r_lo, void* stream) {
+  if (check_df_args(a, "hps_residual_update_2d_df") != HPS_OK) return HPS_ERR_ARG;
+  if (!prep || !du || !dg || !a->r_int || !r_lo || !a->flux) {
+    set_error("hps_residual_update_2d_df: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if ((a->nsrc + 15) / 16 > 65535) {
+    set_error("hps_residual_update_2d_df: too many right-hand sides");
+    return HPS_ERR_ARG;
+  }
+  unsigned long long kinds = 0;
+  int need_uy = 0;
+  if (pack_op_kinds(a, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
+  HPS_CHECK(jx_df_update_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, prep, a->inv_half, a->perm, du, dg,
+                            a->r_int, r_lo, a->flux, need_uy, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
 int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
                       const double* g, double* u_full, void* stream) {
   if (n_leaves <= 0 || p < 3 || q <= 0 || nsrc <= 0 || !Pside || !u_int || !g || !u_full) {
@@ -1106,8 +1186,28 @@ int hps_residual_2d(const hps_residual2d_args* a, void* stream) {
   int need_uy = 0;
   if (pack_op_kinds(a, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
   HPS_CHECK(residual_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, a->coeffs, a->inv_half, a->D1, a->D2,
-                        a->Pside, a->Qside, a->perm, a->u_int, a->g, a->f, a->r_int, a->r_int64, a->flux, a->u_full,
-                        need_uy, (cudaStream_t)stream));
+                        a->Pside, a->Qside, a->perm, a->u_int, a->g, a->f, a->r_int, a->r_int64, nullptr, a->flux,
+                        a->u_full, need_uy, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_residual_2d_df(const hps_residual2d_args* a, float* r_lo, void* stream) {
+  if (!a || a->n_leaves <= 0 || a->p < 3 || a->q <= 0 || a->nsrc <= 0 || a->n_ops <= 0 ||
+      !a->coeffs || !a->inv_half || !a->D1 || !a->D2 || !a->Pside || !a->Qside || !a->perm || !a->u_int || !a->g ||
+      !a->r_int || !r_lo || !a->flux) {
+    set_error("hps_residual_2d_df: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  if (a->n_leaves > 2147483647 || (a->nsrc + 15) / 16 > 65535) {
+    set_error("hps_residual_2d_df: too many right-hand sides");
+    return HPS_ERR_ARG;
+  }
+  unsigned long long kinds = 0;
+  int need_uy = 0;
+  if (pack_op_kinds(a, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
+  HPS_CHECK(residual_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, a->coeffs, a->inv_half, a->D1, a->D2,
+                        a->Pside, a->Qside, a->perm, a->u_int, a->g, a->f, a->r_int, a->r_int64, r_lo, a->flux,
+                        a->u_full, need_uy, (cudaStream_t)stream));
   return HPS_OK;
 }
 

@@ -18,11 +18,18 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
 
 // Batched inverse by Gauss-Jordan elimination with partial (row) pivoting.
 // X may alias A.  info[b] = 0 on success, k+1 if the k-th pivot was zero.
+// flags: INV_TENSOR_MEMORY lets FP32 blocks of 64 < n <= 224 use the
+// tensor-memory kernel (while inverse_tc_policy() is 1); INV_BLOCK_RECURSIVE
+// lets FP32 matrices of n >= 224 use the recursive 2 x 2 block inversion
+// (pivots within its smallest blocks only; while inverse_rec_policy() is 1).
+enum InverseFlags : int { INV_TENSOR_MEMORY = 1, INV_BLOCK_RECURSIVE = 2 };
 size_t inverse_workspace_bytes(int dtype, int n, int batch);
 template <class T>
 cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
                             long long sX, int batch, int* info, void* ws, size_t ws_bytes,
-                            cudaStream_t st, bool tensor_memory = false);
+                            cudaStream_t st, int flags = 0);
+int inverse_rec_policy();
+int set_inverse_rec_policy(int policy);
 
 // FP32 GEMM on the tensor cores (TF32 split into hi + lo, three products);
 // gemm_tc_error() reports whether a CTA's bounded wait ever ran out.

@@ -1201,13 +1201,156 @@ static bool inverse_tc_takes(int n, bool tensor_memory) {
   return inverse_tc_supported(n) && (p == 2 || (p == 1 && tensor_memory));
 }
 
-size_t inverse_workspace_bytes(int dtype, int n, int batch) {
+static size_t flat_workspace_bytes(int dtype, int n, int batch) {
   if (n <= inverse_small_nmax(dtype)) return 0;
   if ((dtype == F32 && sblock_fits<float>(n)) || (dtype == F64 && sblock_fits<double>(n)) ||
       (dtype == C64 && sblock_fits<c64>(n)))
     return 0;
   const size_t es = dtype_size(dtype);
   return gje_layout(es, n).per * (size_t)batch + 256;
+}
+
+// ---------------------------------------------------------------------------
+// Recursive 2 x 2 block inversion (FP32, n >= REC_MIN).  With A split at h1
+// into [[A11, A12], [A21, A22]] and the Schur complement S = A22 - A21 W,
+// W = A11^-1 A12, V = A21 A11^-1:
+//     A^-1 = [[A11^-1 + W S^-1 V, -W S^-1], [-S^-1 V, S^-1]],
+// i.e. two half-size inversions (recursively) and six half-size products, all
+// batched over the matrices of the call: 2 n^3 flops as Gauss-Jordan, but
+// carried by the GEMM kernels instead of n dependent pivot columns.  Pivots
+// are searched within the blocks the recursion ends at (n < REC_MIN, the
+// Gauss-Jordan kernels), not across them, which suits the interface matrices
+// of the DtN merges (their leading blocks are themselves interface operators
+// of the same kind); a zero pivot in a block is reported through info with
+// the block's column offset.  Used for FP32 while inverse_rec_policy() is 1.
+// ---------------------------------------------------------------------------
+template <class T>
+static cudaError_t inverse_batched_flat(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
+                                        long long sX, int batch, int* info, void* ws, size_t ws_bytes,
+                                        cudaStream_t st, bool tensor_memory);
+
+constexpr int REC_MIN = 224;
+static int g_inverse_rec_policy = -1;
+
+int inverse_rec_policy() {
+  if (g_inverse_rec_policy < 0) {
+    const char* e = getenv("HPS_INVERSE_RECURSIVE");
+    g_inverse_rec_policy = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_inverse_rec_policy;
+}
+
+int set_inverse_rec_policy(int policy) {
+  const int old = inverse_rec_policy();
+  if (policy == 0 || policy == 1) g_inverse_rec_policy = policy;
+  return old;
+}
+
+static int rec_split(int n) { return (n / 2) & ~3; }
+
+// FP32 workspace of the recursion below for (n, batch): W, S, V of this level,
+// the block info scratch, then the larger of the two half-size sub-problems.
+static size_t rec_workspace_bytes(int n, int batch) {
+  if (n < REC_MIN) return al256(sizeof(int) * (size_t)batch) + flat_workspace_bytes(F32, n, batch);
+  const int h1 = rec_split(n), h2 = n - h1;
+  const size_t lvl = al256(sizeof(float) * (size_t)batch * ((size_t)h1 * h2 + (size_t)h2 * h2 + (size_t)h2 * h1)) +
+                     al256(sizeof(int) * (size_t)batch);
+  const size_t a = rec_workspace_bytes(h1, batch), b = rec_workspace_bytes(h2, batch);
+  return lvl + (a > b ? a : b) + 256;
+}
+
+size_t inverse_workspace_bytes(int dtype, int n, int batch) {
+  const size_t flat = flat_workspace_bytes(dtype, n, batch);
+  if (dtype != F32 || n < REC_MIN) return flat;
+  const size_t rec = rec_workspace_bytes(n, batch);
+  return rec > flat ? rec : flat;
+}
+
+// info[b] = tmp[b] (+ column offset for a zero pivot) where info[b] is still 0
+__global__ void info_merge_kernel(int batch, const int* __restrict__ tmp, int* info, int offset) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch && info[b] == 0 && tmp[b] != 0) info[b] = tmp[b] > 0 ? tmp[b] + offset : tmp[b];
+}
+
+static cudaError_t info_merge(int batch, const int* tmp, int* info, int offset, cudaStream_t st) {
+  note_launch();
+  info_merge_kernel<<<(batch + 255) / 256, 256, 0, st>>>(batch, tmp, info, offset);
+  return cudaGetLastError();
+}
+
+// X = A^-1 for a batch of FP32 matrices (X may alias A with ldx == lda, sX == sA);
+// info[b] receives the first zero pivot (1-based, in A's columns) or -1.
+static cudaError_t inverse_rec_f32(int n, const float* A, long long lda, long long sA, float* X, long long ldx,
+                                   long long sX, int batch, int* info, unsigned char* ws, size_t ws_bytes,
+                                   int col0, cudaStream_t st) {
+  if (n < REC_MIN) {
+    // a block the recursion ends at: pivoted Gauss-Jordan, info via scratch
+    int* tinfo = reinterpret_cast<int*>(ws);
+    const size_t ib = al256(sizeof(int) * (size_t)batch);
+    cudaError_t e = inverse_batched_flat<float>(n, A, lda, sA, X, ldx, sX, batch, info ? tinfo : nullptr, ws + ib,
+                                                ws_bytes - ib, st, false);
+    if (e != cudaSuccess || !info) return e;
+    return info_merge(batch, tinfo, info, col0, st);
+  }
+  const int h1 = rec_split(n), h2 = n - h1;
+  const long long sW = (long long)h1 * h2, sS = (long long)h2 * h2, sV = (long long)h2 * h1;
+  float* W = reinterpret_cast<float*>(ws);
+  float* S = W + sW * batch;
+  float* V = S + sS * batch;
+  const size_t lvl = al256(sizeof(float) * (size_t)batch * (size_t)(sW + sS + sV)) + al256(sizeof(int) * (size_t)batch);
+  unsigned char* sub = ws + lvl;
+  const size_t sub_bytes = ws_bytes - lvl;
+  const float* A12 = A + h1;
+  const float* A21 = A + (long long)h1 * lda;
+  const float* A22 = A21 + h1;
+  float* X11 = X;
+  float* X12 = X + h1;
+  float* X21 = X + (long long)h1 * ldx;
+  float* X22 = X21 + h1;
+  cudaError_t e;
+  // X11 = A11^-1
+  if ((e = inverse_rec_f32(h1, A, lda, sA, X11, ldx, sX, batch, info, sub, sub_bytes, col0, st)) != cudaSuccess) return e;
+  // W = X11 A12;  S = A22 - A21 W
+  if ((e = gemm_batched<float>(h1, h2, h1, 1.f, X11, ldx, sX, A12, lda, sA, 0.f, nullptr, 0, 0, W, h2, sW, batch,
+                               st)) != cudaSuccess) return e;
+  if ((e = gemm_batched<float>(h2, h2, h1, -1.f, A21, lda, sA, W, h2, sW, 1.f, A22, lda, sA, S, h2, sS, batch,
+                               st)) != cudaSuccess) return e;
+  // V = A21 X11 (before X21 overwrites A21 when X aliases A)
+  if ((e = gemm_batched<float>(h2, h1, h1, 1.f, A21, lda, sA, X11, ldx, sX, 0.f, nullptr, 0, 0, V, h1, sV, batch,
+                               st)) != cudaSuccess) return e;
+  // X22 = S^-1
+  if ((e = inverse_rec_f32(h2, S, h2, sS, X22, ldx, sX, batch, info, sub, sub_bytes, col0 + h1, st)) != cudaSuccess)
+    return e;
+  // X12 = -W X22;  X21 = -X22 V;  X11 -= X12 V
+  if ((e = gemm_batched<float>(h1, h2, h2, -1.f, W, h2, sW, X22, ldx, sX, 0.f, nullptr, 0, 0, X12, ldx, sX, batch,
+                               st)) != cudaSuccess) return e;
+  if ((e = gemm_batched<float>(h2, h1, h2, -1.f, X22, ldx, sX, V, h1, sV, 0.f, nullptr, 0, 0, X21, ldx, sX, batch,
+                               st)) != cudaSuccess) return e;
+  return gemm_batched<float>(h1, h1, h2, -1.f, X12, ldx, sX, V, h1, sV, 1.f, X11, ldx, sX, X11, ldx, sX, batch, st);
+}
+
+template <class T>
+cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
+                            long long sX, int batch, int* info, void* ws, size_t ws_bytes,
+                            cudaStream_t st, int flags) {
+  const bool tensor_memory = (flags & INV_TENSOR_MEMORY) != 0;
+  if constexpr (DTypeOf<T>::value == F32) {
+    if ((flags & INV_BLOCK_RECURSIVE) && n >= REC_MIN && batch > 0 && inverse_rec_policy() == 1 &&
+        !inverse_tc_takes(n, tensor_memory)) {
+      const size_t need = rec_workspace_bytes(n, batch);
+      if (ws == nullptr || ws_bytes < need) {
+        set_error("inverse: workspace too small (%zu < %zu)", ws_bytes, need);
+        return cudaErrorInvalidValue;
+      }
+      ProfScope whole(KC_INVERSE, st, 2.0 * (double)n * n * n * batch);
+      if (info) cudaMemsetAsync(info, 0, sizeof(int) * (size_t)batch, st);
+      unsigned char* base = reinterpret_cast<unsigned char*>(
+          (reinterpret_cast<uintptr_t>(ws) + 255) & ~uintptr_t(255));
+      return inverse_rec_f32(n, (const float*)A, lda, sA, (float*)X, ldx, sX, batch, info, base,
+                             ws_bytes - (size_t)(base - reinterpret_cast<unsigned char*>(ws)), 0, st);
+    }
+  }
+  return inverse_batched_flat<T>(n, A, lda, sA, X, ldx, sX, batch, info, ws, ws_bytes, st, tensor_memory);
 }
 
 template <class T, int NMAX>
@@ -1259,9 +1402,9 @@ cudaError_t inverse_small<c128>(int n, const c128* A, long long lda, long long s
 }
 
 template <class T>
-cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
-                            long long sX, int batch, int* info, void* ws, size_t ws_bytes,
-                            cudaStream_t st, bool tensor_memory) {
+static cudaError_t inverse_batched_flat(int n, const T* A, long long lda, long long sA, T* X, long long ldx,
+                                        long long sX, int batch, int* info, void* ws, size_t ws_bytes,
+                                        cudaStream_t st, bool tensor_memory) {
   if (n <= 0 || batch <= 0) return cudaSuccess;
   // one profiler record for the whole inversion (its panel kernels and the
   // GEMM updates nested below): 2 n^3 flops per matrix, x4 for complex
@@ -1489,7 +1632,7 @@ cudaError_t set_panel_spin_limit(long long polls, long long* previous) {
 
 #define HPS_INST_INV(T)                                                                       \
   template cudaError_t inverse_batched<T>(int, const T*, long long, long long, T*, long long, \
-                                          long long, int, int*, void*, size_t, cudaStream_t, bool);
+                                          long long, int, int*, void*, size_t, cudaStream_t, int);
 HPS_INST_INV(float)
 HPS_INST_INV(double)
 HPS_INST_INV(c64)

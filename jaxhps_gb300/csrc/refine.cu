@@ -12,6 +12,7 @@
 // structure of the spectral operators: derivatives are 1D Chebyshev
 // differentiation along one grid axis (p MACs per point and operator)
 // instead of dense p^2 x p^2 products.
+#include "df32.cuh"
 #include "hps_common.cuh"
 #include "hps_internal.h"
 
@@ -34,7 +35,7 @@ residual_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lon
                    const double* __restrict__ Pside_g, const double* __restrict__ Qside_g,
                    const int* __restrict__ perm_g, const double* __restrict__ u_int,
                    const double* __restrict__ g, const double* __restrict__ f, float* r_int, double* r_int64,
-                   double* flux, double* u_full, int need_uy) {
+                   float* r_lo, double* flux, double* u_full, int need_uy) {
   extern __shared__ double sm[];
   const int pp = p * p;
   const int ncb = 4 * (p - 1);
@@ -145,8 +146,10 @@ residual_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lon
       acc = fma(-c, fld, acc);
     }
     const long long o = ((long long)l * ni + i) * nsrc + s0 + s;
-    r_int[o] = (float)acc;
+    const float rh = (float)acc;
+    r_int[o] = rh;
     if (r_int64) r_int64[o] = acc;
+    if (r_lo) r_lo[o] = (float)(acc - (double)rh);   // the residual as an FP32 pair
   }
   // outward normal derivatives at the Chebyshev points of each side
   // (rows of N, _precompute_operators_2D.py:132-163):
@@ -201,7 +204,7 @@ size_t residual_2d_smem(int p, int q, int need_uy) {
 cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds, const double* coeffs,
                         const double* inv_half, const double* D1, const double* D2, const double* Pside,
                         const double* Qside, const int* perm, const double* u_int, const double* g,
-                        const double* f, float* r_int, double* r_int64, double* flux, double* u_full,
+                        const double* f, float* r_int, double* r_int64, float* r_lo, double* flux, double* u_full,
                         int need_uy, cudaStream_t st) {
   const size_t smem = residual_2d_smem(p, q, need_uy);
   if (smem > 48 * 1024)
@@ -211,8 +214,8 @@ cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigne
   ProfScope ps(KC_RESIDUAL, st, work);
   note_launch();
   residual_2d_kernel<<<grid, RES_NT, smem, st>>>(n_leaves, p, q, nsrc, n_ops, kinds, coeffs, inv_half, D1, D2,
-                                                 Pside, Qside, perm, u_int, g, f, r_int, r_int64, flux, u_full,
-                                                 need_uy);
+                                                 Pside, Qside, perm, u_int, g, f, r_int, r_int64, r_lo, flux,
+                                                 u_full, need_uy);
   return cudaGetLastError();
 }
 
@@ -632,44 +635,6 @@ cudaError_t accumulate(long long n, const float* x, double* y, cudaStream_t st) 
 // every correction after the first is at most a few percent of the solution,
 // so the pair arithmetic's rounding enters the residual far below FP64 level.
 // ---------------------------------------------------------------------------
-struct df32 {
-  float hi, lo;
-};
-
-__device__ __forceinline__ df32 df_split(double x) {
-  const float h = __double2float_rn(x);
-  return df32{h, __double2float_rn(x - (double)h)};
-}
-__device__ __forceinline__ double df_join(float s, float e) { return (double)s + (double)e; }
-
-// (s, e) with |e| <= |s| ulp-wise; FastTwoSum on the FP32 pipe
-__device__ __forceinline__ df32 df_norm(float s, float e) {
-  const float h = s + e;
-  return df32{h, e - (h - s)};
-}
-
-// a * b for pairs, renormalised (FP32 pipe only)
-__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
-  const float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, e);
-  e = fmaf(a.lo, b.hi, e);
-  return df_norm(p, e);
-}
-
-// (s, e) += a * b ; s carries the running sum, e the low-order terms
-__device__ __forceinline__ void df_mac(float& s, float& e, df32 a, df32 b) {
-  const float p = a.hi * b.hi;
-  float pe = fmaf(a.hi, b.hi, -p);
-  pe = fmaf(a.hi, b.lo, pe);
-  pe = fmaf(a.lo, b.hi, pe);
-  const float t = s + p;
-  const float bb = t - s;
-  const float err = (s - (t - bb)) + (p - bb);
-  s = t;
-  e += err + pe;
-}
-
 __global__ void __launch_bounds__(RES_NT)
 jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned long long kinds,
                     const double* __restrict__ coeffs, const double* __restrict__ inv_half,

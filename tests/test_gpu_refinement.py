@@ -109,6 +109,51 @@ def test_incremental_residual_matches_fp64(cuda, extra):
     assert float((flux - flux_b).abs().max()) < 1e-10 * scale_f
 
 
+@pytest.mark.parametrize("p,ns,extra", [(10, 5, False), (16, 20, False), (12, 3, True), (16, 64, True)])
+def test_pair_residual_update_matches_fp64(cuda, p, ns, extra):
+    """The FP32-pair residual: its FP64 start equals hps_residual_2d split in
+    two, and after r -= J dx (one grid line per thread) it equals the FP64
+    residual at x + dx, within the update's rounding relative to |J dx|; the
+    update agrees with the FP64-storage update kernel."""
+    L, q = 2, p - 2
+    assert hps._native.lib().hps_residual_df_supported(p, q) == 1
+    dom, pde, ref = _setup(L, p, q, ns, extra, seed=7)
+    hps.build_solver(pde, precision="mixed")
+    state = pde._state
+    rng = np.random.default_rng(8)
+    nl, ncb = dom.n_leaves, 4 * (p - 1)
+    ni = p * p - ncb
+    u = torch.as_tensor(rng.standard_normal((nl, ni, ns)), device=cuda)
+    g = torch.as_tensor(rng.standard_normal((nl, 4 * q, ns)), device=cuda)
+    du = torch.as_tensor(1e-2 * rng.standard_normal((nl, ni, ns)), device=cuda, dtype=torch.float32)
+    dg = torch.as_tensor(1e-2 * rng.standard_normal((nl, 4 * q, ns)), device=cuda, dtype=torch.float32)
+    r32 = torch.empty((nl, ni, ns), dtype=torch.float32, device=cuda)
+    r_lo = torch.empty_like(r32)
+    r64 = torch.empty((nl, ni, ns), dtype=torch.float64, device=cuda)
+    flux = torch.empty((nl, 4 * q, ns), dtype=torch.float64, device=cuda)
+    rf._residual(state, u, g, r32, flux, r64=r64, r_lo=r_lo)
+    pair = r32.double() + r_lo.double()
+    assert float((pair - r64).abs().max()) <= 2.0 ** -46 * float(r64.abs().max())
+    flux_old = flux.clone()
+    r32_old = torch.empty_like(r32)
+    rf._residual_update(state, du, dg, r64, r32_old, flux_old)
+    prep = rf._df_prepare(rf._res_args(state, None, None, r32, flux))
+    rf._residual_update_df(state, prep, du, dg, r_lo, r32, flux)
+    r64b = torch.empty_like(r64)
+    flux_b = torch.empty_like(flux)
+    rf._residual(state, u + du.double(), g + dg.double(), r32_old, flux_b, r64=r64b)
+    ref_d = torch.empty_like(r64)
+    fl_d = torch.empty_like(flux)
+    rf._residual(state, du.double(), dg.double(), r32_old, fl_d, r64=ref_d, zero_source=True)
+    scale_r = float(ref_d.abs().max())
+    scale_f = float(fl_d.abs().max())
+    pair = r32.double() + r_lo.double()
+    assert float((pair - r64b).abs().max()) < 1e-10 * scale_r
+    assert float((pair - r64).abs().max()) < 1e-12 * scale_r
+    assert float((flux - flux_b).abs().max()) < 1e-10 * scale_f
+    assert float((flux - flux_old).abs().max()) < 1e-12 * scale_f
+
+
 def test_pinned_source_upload_matches_numpy_source(cuda):
     """A page-locked CPU source is copied on a side stream while the build
     runs; the solution is bit-identical to the one from a NumPy source."""
