@@ -126,7 +126,10 @@ HPS_API int hps_gemm_policy(int policy);
  * down-pass products; not the N <= 8 ones).  Kernel variants: 0 tcgen05
  * 3xTF32, 1 / 2 / 3 SIMT 8x8 register tiles of 128x128 / 128x64 / 64x64,
  * 4 / 5 / 6 64x64 tiles with K split over a 2 / 4 / 8-CTA cluster, 7 SIMT 4x4
- * register tiles of 64x64.  hps_gemm_tune_set stores the variant for an
+ * register tiles of 64x64, 8 the warp-specialised TMA + tcgen05 3xTF32 kernel
+ * for N <= 64 (16-byte aligned operands; other shapes run variant 3; policy 1
+ * also picks it for such products with at least 608 row tiles of 128).
+ * hps_gemm_tune_set stores the variant for an
  * (M, N, K, batch) shape (-1 removes it); products of a stored shape run that
  * variant, the others the built-in rules.  hps_gemm_tune_clear empties the
  * table.  hps_gemm_force_variant(v) runs every FP32 product with variant v

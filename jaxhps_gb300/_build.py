@@ -77,7 +77,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB_PATH.with_suffix(".so.tmp")
-    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcuda"]
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

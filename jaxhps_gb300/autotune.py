@@ -12,7 +12,8 @@ before its built-in rules.  ``save`` / ``load`` keep a table in a JSON file.
 Variants (``hps_gemm_tune_set`` in include/jaxhps_gb300.h): 0 tcgen05
 3xTF32; 1 / 2 / 3 SIMT 8x8 register tiles of 128x128 / 128x64 / 64x64;
 4 / 5 / 6 64x64 tiles with K split over a 2 / 4 / 8-CTA cluster; 7 SIMT 4x4
-register tiles of 64x64.  All variants compute the same product; only the
+register tiles of 64x64; 8 the warp-specialised TMA + tcgen05 3xTF32 kernel
+for N <= 64 (other shapes run variant 3).  All variants compute the same product; only the
 order of the FP32 additions differs.  No counterpart in the reference.
 """
 
@@ -37,6 +38,7 @@ VARIANTS = {
     5: "64x64 split-K x4",
     6: "64x64 split-K x8",
     7: "SIMT 4x4 tiles 64x64",
+    8: "TMA + tcgen05 3xTF32, warp-specialised",
 }
 
 Shape = Tuple[int, ...]   # (M, N, K, batch, lda, sA, ldb, sB, ldc, sC, ldd, sD, has_C)

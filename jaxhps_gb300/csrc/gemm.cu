@@ -545,7 +545,8 @@ enum GemmVariant {
   GV_SPLIT4 = 5,
   GV_SPLIT8 = 6,
   GV_GENERIC = 7,     // SIMT 4x4 register tiles, 64 x 64
-  GV_COUNT = 8
+  GV_TMA = 8,         // warp-specialised TMA + tcgen05 3xTF32, N <= 64 (gemm_tc.cu)
+  GV_COUNT = 9
 };
 
 static std::mutex g_tune_mu;
@@ -612,6 +613,12 @@ static cudaError_t run_variant_f32(int v, int M, int N, int K, float alpha, cons
                                    long long sA, const float* B, long long ldb, long long sB, float beta,
                                    const float* C, long long ldc, long long sC, float* D, long long ldd,
                                    long long sD, int batch, cudaStream_t st) {
+  if (v == GV_TMA) {
+    // layouts the TMA kernel does not take run the 64 x 64 SIMT tiles
+    const cudaError_t e = gemm_tma_f32(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
+    if (e != cudaErrorNotSupported) return e;
+    v = GV_V4_64x64;
+  }
   switch (v) {
     case GV_TC:
       return gemm_tf32x3(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch, st);
@@ -660,6 +667,13 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
   }
   const int pol = gemm_policy();
   if constexpr (std::is_same<T, float>::value) {
+    // many small products with few right-hand-side columns (the leaf
+    // solves): the streaming TMA kernel, one persistent CTA per SM
+    if (pol == 1 && N > 8 && N <= 64 && (long long)((M + 127) / 128) * batch >= 4 * 152) {
+      const cudaError_t e = gemm_tma_f32(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch,
+                                         st);
+      if (e != cudaErrorNotSupported) return e;
+    }
     // measured: the tensor-core kernel wins once tiles are wide (N >= 128)
     // and have enough K-steps to amortise its pipeline prologue and epilogue;
     // below that the 8x8-register SIMT tiles are as fast or faster

@@ -18,8 +18,12 @@
 // a device error flag (gemm_tc_error) and the CTA winds down.  The accumulator
 // is read back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, i.e.
 // tile rows 32w..32w+31).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "hps_common.cuh"
 #include "hps_internal.h"
+#include "tc_common.cuh"
 
 namespace hps {
 
@@ -472,6 +476,393 @@ cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long
                                 2 * sC, Df, 2 * ldd, 2 * sD, batch, st);
   return launch_tc<64, true>(M, 2 * N, 2 * K, alpha, Af, 2 * lda, 2 * sA, Bf, 2 * ldb, 2 * sB, beta, Cf, 2 * ldc,
                              2 * sC, Df, 2 * ldd, 2 * sD, batch, st);
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised TMA + tcgen05 kernel for the batched products with few
+// right-hand-side columns (N <= 64): the leaf solves v = inv(A_ii) r, the
+// leaf operators Y = inv(A_ii) W, du = Y g + v, h = Q v.  These are
+// HBM-bound (each leaf's A is read once, ~20 flops per byte), so the kernel is
+// built to stream: a persistent CTA per SM, a ring of LT_NS stages filled by
+// the tensor memory accelerator (cp.async.bulk.tensor; A tiles land directly
+// in the 128-byte-swizzled K-major layout, B tiles row-major), and five
+// roles that never meet at a CTA barrier:
+//   warp 0     producer: one lane issues the TMA loads of each K-tile (A box
+//              32 x 128, B box 64 x 32) against the stage's `full` barrier;
+//   warp 1     MMA: one lane issues, per K-tile, the three TF32 products
+//              A_hi B_hi + A_hi B_lo + A_lo B_hi (the split-operand method of
+//              Ootomo & Yokota, as gemm_tf32x3_kernel) as 4 x 3
+//              tcgen05.mma 128 x 64 x 8 into a TMEM accumulator, commits the
+//              stage back to the producer (`empty`) and, after the last
+//              K-tile, the accumulator to the epilogue (`accf`);
+//   warps 2-5  converters: split the landed A tile into TF32 hi (in place)
+//              and lo, transpose B into K-major hi / lo, then release the
+//              stage to the MMA warp (`conv`);
+//   warps 6-9  epilogue: read the accumulator with tcgen05.ld (warp w owns
+//              TMEM lanes 32 (w % 4) ..), hand it back (`acce`), and write
+//              alpha acc + beta C row by row.
+// Two accumulators (128 TMEM columns) let the MMAs of the next 128-row tile
+// start while the epilogue drains the previous one.  M and K tails come from
+// the TMA's zero fill; N < 64 from the zero-filled B columns.  Every wait is
+// bounded (g_tc_spin_limit polls); a wait that runs out sets g_tc_err, every
+// role winds down, the CTA waits (bounded) for its loads and MMAs in flight
+// and frees its tensor memory.
+// ---------------------------------------------------------------------------
+constexpr int LT_BM = 128, LT_BN = 64, LT_BK = 32, LT_NS = 3, LT_NT = 320;
+constexpr int LT_A_BYTES = LT_BM * LT_BK * 4;         // 16 KB
+constexpr int LT_B_BYTES = LT_BN * LT_BK * 4;         // 8 KB
+constexpr int LT_OFF_ALO = LT_A_BYTES;
+constexpr int LT_OFF_BHI = 2 * LT_A_BYTES;
+constexpr int LT_OFF_BLO = LT_OFF_BHI + LT_B_BYTES;
+constexpr int LT_OFF_BRAW = LT_OFF_BLO + LT_B_BYTES;  // B as loaded: 32 rows (k) of 64 floats (n)
+constexpr int LT_STAGE = LT_OFF_BRAW + LT_B_BYTES;    // 56 KB, a multiple of 1024
+constexpr size_t LT_SMEM = LT_NS * (size_t)LT_STAGE + 1024;
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 3D tiled TMA load of one box into shared memory, completing on `bar`
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// The CTA's failure flag read once per lane and agreed across the warp, so
+// that a warp leaves its loop as a whole.
+__device__ __forceinline__ bool warp_flag(volatile int* f) { return __any_sync(0xffffffffu, *f != 0); }
+
+// Bounded wait by a whole warp: every lane polls (its own acquire), then the
+// warp agrees (a lane that gave up makes the wait fail for all).
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
+  const bool ok = mbar_wait(bar, parity);
+  return __all_sync(0xffffffffu, ok);
+}
+
+__global__ void __launch_bounds__(LT_NT, 1)
+gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+                float alpha, float beta, const float* C, long long ldc, long long sC, float* D, long long ldd,
+                long long sD, int batch, int a_batched, int b_batched, int vec_out) {
+  extern __shared__ unsigned char lt_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(lt_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t full[LT_NS], conv[LT_NS], empty[LT_NS], accf[2], acce[2];
+  __shared__ uint32_t armed[LT_NS], committed[LT_NS], acc_committed[2];
+  __shared__ uint32_t tmem_s;
+  __shared__ int fail_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int i = 0; i < LT_NS; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&conv[i], 4);
+      mbar_init(&empty[i], 1);
+      armed[i] = committed[i] = 0;
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&accf[i], 1);
+      mbar_init(&acce[i], 4);
+      acc_committed[i] = 0;
+    }
+    fail_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_s)),
+                 "r"(2 * LT_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_s;
+  const int tiles_m = (M + LT_BM - 1) / LT_BM;
+  const long long n_units = (long long)batch * tiles_m;
+  const int nk = (K + LT_BK - 1) / LT_BK;
+  volatile int* fail = &fail_s;
+
+  // Each role runs its loop with the whole warp converged: every lane polls
+  // the barrier (each its own acquire), the warp agrees on the outcome, and
+  // one lane issues the TMA loads, MMAs and commits.
+  if (warp == 0) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmA)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmB)) : "memory");
+    }
+    uint32_t it = 0;
+    for (long long u = blockIdx.x; u < n_units && !warp_flag(fail); u += gridDim.x) {
+      const int b = (int)(u / tiles_m), m0 = (int)(u % tiles_m) * LT_BM;
+      for (int kt = 0; kt < nk; ++kt, ++it) {
+        const int s = it % LT_NS;
+        const uint32_t use = it / LT_NS;
+        if (use > 0 && !warp_wait(&empty[s], (use - 1) & 1)) {
+          *fail = 1;
+          break;
+        }
+        if (lane == 0) {
+          unsigned char* sb = smem + s * LT_STAGE;
+          mbar_expect_tx(&full[s], LT_A_BYTES + LT_B_BYTES);
+          armed[s] += 1;
+          tma_load_3d(sb, &tmA, kt * LT_BK, m0, a_batched ? b : 0, &full[s]);
+          tma_load_3d(sb + LT_OFF_BRAW, &tmB, 0, kt * LT_BK, b_batched ? b : 0, &full[s]);
+        }
+        __syncwarp();
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    constexpr uint32_t idesc = make_idesc_tf32(LT_BM, LT_BN);
+    uint32_t it = 0, acc_it = 0;
+    for (long long u = blockIdx.x; u < n_units && !warp_flag(fail); u += gridDim.x, ++acc_it) {
+      const int a = acc_it & 1;
+      const uint32_t ause = acc_it >> 1;
+      if (ause > 0 && !warp_wait(&acce[a], (ause - 1) & 1)) {
+        *fail = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t dt = tmem + (uint32_t)(a * LT_BN);
+      bool ok = true;
+      for (int kt = 0; kt < nk; ++kt, ++it) {
+        const int s = it % LT_NS;
+        if (!warp_wait(&conv[s], (it / LT_NS) & 1)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        if (lane == 0) {
+          const uint32_t a_hi = smem_u32(smem + s * LT_STAGE), a_lo = a_hi + LT_OFF_ALO;
+          const uint32_t b_hi = a_hi + LT_OFF_BHI, b_lo = a_hi + LT_OFF_BLO;
+#pragma unroll
+          for (int kk = 0; kk < LT_BK / 8; ++kk) {
+            const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
+            mma_tf32(dt, make_desc_sw128(a_hi + off), make_desc_sw128(b_hi + off), idesc,
+                     (kt > 0 || kk > 0) ? 1u : 0u);
+            mma_tf32(dt, make_desc_sw128(a_hi + off), make_desc_sw128(b_lo + off), idesc, 1u);
+            mma_tf32(dt, make_desc_sw128(a_lo + off), make_desc_sw128(b_hi + off), idesc, 1u);
+          }
+          mma_commit(&empty[s]);
+          committed[s] += 1;
+        }
+        __syncwarp();
+      }
+      if (!ok) {
+        *fail = 1;
+        break;
+      }
+      if (lane == 0) {
+        mma_commit(&accf[a]);
+        acc_committed[a] += 1;
+      }
+      __syncwarp();
+    }
+  } else if (warp < 6) {
+    // ---------------- converters (128 threads) ----------------
+    const int ct = tid - 64;
+    uint32_t it = 0;
+    for (long long u = blockIdx.x; u < n_units && !warp_flag(fail); u += gridDim.x) {
+      bool ok = true;
+      for (int kt = 0; kt < nk; ++kt, ++it) {
+        const int s = it % LT_NS;
+        if (!warp_wait(&full[s], (it / LT_NS) & 1)) {
+          ok = false;
+          break;
+        }
+        unsigned char* sb = smem + s * LT_STAGE;
+        // A: TF32 hi in place (the swizzle is a permutation of 16-byte chunks,
+        // so the split is layout-free), lo into A_lo at the same offsets
+#pragma unroll
+        for (int i = 0; i < LT_A_BYTES / 16 / 128; ++i) {
+          const int off = (ct + 128 * i) * 16;
+          const float4 x = *reinterpret_cast<const float4*>(sb + off);
+          uint4 h, l;
+          h.x = f32_to_tf32(x.x); l.x = f32_to_tf32(x.x - __uint_as_float(h.x));
+          h.y = f32_to_tf32(x.y); l.y = f32_to_tf32(x.y - __uint_as_float(h.y));
+          h.z = f32_to_tf32(x.z); l.z = f32_to_tf32(x.z - __uint_as_float(h.z));
+          h.w = f32_to_tf32(x.w); l.w = f32_to_tf32(x.w - __uint_as_float(h.w));
+          *reinterpret_cast<uint4*>(sb + off) = h;
+          *reinterpret_cast<uint4*>(sb + LT_OFF_ALO + off) = l;
+        }
+        // B: row-major 32 x 64 -> K-major (row n, 32 k) swizzled hi / lo;
+        // item f takes column n = f % 64 and k = 4 (f / 64) .. +3
+        const float* rb = reinterpret_cast<const float*>(sb + LT_OFF_BRAW);
+#pragma unroll
+        for (int i = 0; i < LT_BN * LT_BK / 4 / 128; ++i) {
+          const int f = ct + 128 * i;
+          const int nn = f % LT_BN, kq = (f / LT_BN) * 4;
+          const float4 x = make_float4(rb[(kq + 0) * LT_BN + nn], rb[(kq + 1) * LT_BN + nn], rb[(kq + 2) * LT_BN + nn],
+                                       rb[(kq + 3) * LT_BN + nn]);
+          store_split4(sb + LT_OFF_BHI, sb + LT_OFF_BLO, nn, kq, x);
+        }
+        // generic-proxy stores -> visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&conv[s]);
+        __syncwarp();
+      }
+      if (!ok) {
+        *fail = 1;
+        break;
+      }
+    }
+  } else {
+    // ---------------- epilogue (128 threads) ----------------
+    const int q = warp & 3;
+    uint32_t acc_it = 0;
+    for (long long u = blockIdx.x; u < n_units && !warp_flag(fail); u += gridDim.x, ++acc_it) {
+      const int a = acc_it & 1;
+      if (!warp_wait(&accf[a], (acc_it >> 1) & 1)) {
+        *fail = 1;
+        break;
+      }
+      tc_fence_after();
+      const long long b = u / tiles_m;
+      const int row = (int)(u % tiles_m) * LT_BM + q * 32 + lane;
+      float v0[32], v1[32];
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * LT_BN);
+      tc::tmem_ld32(taddr, v0);
+      tc::tmem_ld32(taddr + 32, v1);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[a]);
+      __syncwarp();
+      if (row < M) {
+        const float* Cr = C ? C + b * sC + (long long)row * ldc : nullptr;
+        float* Dr = D + b * sD + (long long)row * ldd;
+        if (vec_out) {
+#pragma unroll
+          for (int c = 0; c < LT_BN; c += 4) {
+            if (c < N) {
+              float4 x = make_float4(c < 32 ? v0[c] : v1[c - 32], c < 32 ? v0[c + 1] : v1[c - 31],
+                                     c < 32 ? v0[c + 2] : v1[c - 30], c < 32 ? v0[c + 3] : v1[c - 29]);
+              x.x *= alpha;
+              x.y *= alpha;
+              x.z *= alpha;
+              x.w *= alpha;
+              if (Cr) {
+                const float4 y = *reinterpret_cast<const float4*>(Cr + c);
+                x.x = fmaf(beta, y.x, x.x);
+                x.y = fmaf(beta, y.y, x.y);
+                x.z = fmaf(beta, y.z, x.z);
+                x.w = fmaf(beta, y.w, x.w);
+              }
+              *reinterpret_cast<float4*>(Dr + c) = x;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < LT_BN; ++c) {
+            if (c < N) {
+              float x = alpha * (c < 32 ? v0[c] : v1[c - 32]);
+              if (Cr) x = fmaf(beta, Cr[c], x);
+              Dr[c] = x;
+            }
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (fail_s && tid == 0) {
+    atomicExch(&g_tc_err, 1);
+    // give the loads and MMAs in flight a second bounded chance to finish
+    // before the CTA leaves and frees the tensor memory they write
+    for (int s = 0; s < LT_NS; ++s) {
+      if (armed[s]) mbar_wait(&full[s], (armed[s] - 1) & 1);
+      if (committed[s]) mbar_wait(&empty[s], (committed[s] - 1) & 1);
+    }
+    for (int a = 0; a < 2; ++a)
+      if (acc_committed[a]) mbar_wait(&accf[a], (acc_committed[a] - 1) & 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * LT_BN) : "memory");
+  }
+}
+
+// The layouts the TMA kernel takes: 16-byte aligned bases, row strides and
+// batch strides (or a broadcast operand), N <= 64.
+bool gemm_tma_supported(int M, int N, int K, const float* A, long long lda, long long sA, const float* B,
+                        long long ldb, long long sB, int batch) {
+  auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+  if (M <= 0 || N <= 0 || N > LT_BN || K <= 0 || batch <= 0) return false;
+  if (!al16(A) || !al16(B) || lda % 4 || ldb % 4 || lda < K || ldb < N) return false;
+  if (batch > 1 && ((sA != 0 && sA % 4) || (sB != 0 && sB % 4))) return false;
+  return true;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point: the
+// library does not link the driver library, so it still loads (to report its
+// symbols and errors) on a machine without a GPU driver.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    cudaGetLastError();
+  }
+  return fn;
+}
+
+static bool encode_map(CUtensorMap* map, const float* base, long long d0, long long d1, long long d2, long long ld,
+                       long long sb, int box0, int box1, bool swizzle) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+  if (!encode) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+  // the batch stride of a single-entry (or broadcast) third dimension is never
+  // used; any valid multiple of 16 bytes will do
+  const long long sbb = (d2 > 1) ? sb * 4 : ((ld * 4 * d1 + 15) / 16) * 16;
+  const cuuint64_t strides[2] = {(cuuint64_t)(ld * 4), (cuuint64_t)sbb};
+  const cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims,
+                                            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                            swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+cudaError_t gemm_tma_f32(int M, int N, int K, float alpha, const float* A, long long lda, long long sA,
+                         const float* B, long long ldb, long long sB, float beta, const float* C, long long ldc,
+                         long long sC, float* D, long long ldd, long long sD, int batch, cudaStream_t st) {
+  if (M <= 0 || N <= 0 || batch <= 0) return cudaSuccess;
+  if (!gemm_tma_supported(M, N, K, A, lda, sA, B, ldb, sB, batch)) return cudaErrorNotSupported;
+  const int a_batched = (batch > 1 && sA != 0) ? 1 : 0, b_batched = (batch > 1 && sB != 0) ? 1 : 0;
+  CUtensorMap tmA, tmB;
+  if (!encode_map(&tmA, A, K, M, a_batched ? batch : 1, lda, sA, LT_BK, LT_BM, true) ||
+      !encode_map(&tmB, B, N, K, b_batched ? batch : 1, ldb, sB, LT_BN, LT_BK, false))
+    return cudaErrorNotSupported;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+  }
+  cudaError_t e = cudaFuncSetAttribute(gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LT_SMEM);
+  if (e != cudaSuccess) return e;
+  const long long units = (long long)batch * ((M + LT_BM - 1) / LT_BM);
+  const unsigned grid = (unsigned)(units < sms ? units : sms);
+  auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+  const int vec_out = al16(D) && ldd % 4 == 0 && (batch == 1 || sD % 4 == 0) && N % 4 == 0 &&
+                      (!C || (al16(C) && ldc % 4 == 0 && (batch == 1 || sC % 4 == 0)));
+  ProfScope ps(KC_GEMM, st, 2.0 * (double)M * N * K * batch);
+  note_launch();
+  gemm_tma_kernel<<<grid, LT_NT, LT_SMEM, st>>>(tmA, tmB, M, N, K, alpha, beta, C, ldc, sC, D, ldd, sD, batch,
+                                               a_batched, b_batched, vec_out);
+  return cudaGetLastError();
 }
 
 }  // namespace hps

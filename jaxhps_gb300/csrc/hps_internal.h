@@ -39,6 +39,13 @@ cudaError_t gemm_tf32x3(int M, int N, int K, float alpha, const float* A, long l
 cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long long lda, long long sA,
                             const c64* B, long long ldb, long long sB, float beta, const c64* C, long long ldc,
                             long long sC, c64* D, long long ldd, long long sD, int batch, cudaStream_t st);
+// Warp-specialised TMA + tcgen05 3xTF32 kernel for N <= 64 (gemm_tc.cu):
+// cudaErrorNotSupported for layouts it does not take (gemm_tma_supported).
+bool gemm_tma_supported(int M, int N, int K, const float* A, long long lda, long long sA, const float* B,
+                        long long ldb, long long sB, int batch);
+cudaError_t gemm_tma_f32(int M, int N, int K, float alpha, const float* A, long long lda, long long sA,
+                         const float* B, long long ldb, long long sB, float beta, const float* C, long long ldc,
+                         long long sC, float* D, long long ldd, long long sD, int batch, cudaStream_t st);
 int gemm_tc_error();
 // Reads the flag and clears it (both synchronise with the device).
 int gemm_tc_error_reset();

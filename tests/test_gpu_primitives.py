@@ -275,3 +275,45 @@ def test_gemm_f32_cluster_split_k(cuda, m, n, k, batch, pad):
     scale = max(1.0, np.abs(ref).max()) * k ** 0.5
     assert np.abs(runs[0][0] - ref).max() <= 2e-5 * scale * 10
     assert np.abs(runs[0][1] - ref2).max() <= 2e-5 * scale * 10
+
+
+@pytest.mark.parametrize("M,N,K,batch,bcastA,viewA,inplace", [
+    (196, 64, 196, 600, False, False, False),   # the leaf solve v = inv(A_ii) r: two row tiles, K tail
+    (196, 56, 56, 300, False, True, True),      # du = Y_int g + v: A a row-offset view, C aliasing D, N tail
+    (56, 64, 196, 300, True, False, False),     # h = Q_int v: broadcast A, one partial row tile
+    (300, 48, 100, 5, False, False, False),
+    (128, 64, 32, 1, False, False, True),
+    (200, 16, 12, 7, False, False, False),      # K shorter than one K-tile
+])
+def test_gemm_tma_warp_specialised(cuda, M, N, K, batch, bcastA, viewA, inplace):
+    """Variant 8 (TMA loads, warp-specialised tcgen05 3xTF32) against an FP64
+    product, FP32-level tolerance (1e-5 relative), with the operand layouts
+    the leaf products use; no bounded wait may run out."""
+    from jaxhps_gb300 import _native as nat
+
+    lib = nat.lib()
+    g = torch.Generator(device=cuda).manual_seed(M * 7 + N)
+    if bcastA:
+        A = torch.randn(M, K, device=cuda, generator=g)
+        A64 = A.double().expand(batch, M, K)
+    elif viewA:
+        big = torch.randn(batch, M + 60, K, device=cuda, generator=g)
+        A = big[:, 60:, :]
+        A64 = A.double()
+    else:
+        A = torch.randn(batch, M, K, device=cuda, generator=g)
+        A64 = A.double()
+    B = torch.randn(batch, K, N, device=cuda, generator=g)
+    Cm = torch.randn(batch, M, N, device=cuda, generator=g)
+    ref = (A64 @ B.double()) * 0.75 + Cm.double() * 1.5
+    lib.hps_gemm_tc_status_reset()
+    old = lib.hps_gemm_force_variant(8)
+    try:
+        D = Cm.clone() if inplace else torch.full((batch, M, N), float("nan"), device=cuda)
+        nat.gemm(A, B, D, alpha=0.75, beta=1.5, Cmat=D if inplace else Cm, batch=batch)
+        torch.cuda.synchronize()
+    finally:
+        lib.hps_gemm_force_variant(old)
+    err = float((D.double() - ref).abs().max() / ref.abs().max())
+    assert err < 1e-5, err
+    assert lib.hps_gemm_tc_status() == 0
