@@ -46,10 +46,13 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ uint32_t f32_to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return r;
+// x = hi + lo with hi the TF32 value nearest to x (ties away from zero: add
+// half a TF32 unit to the bit pattern, clear the 13 dropped bits; two integer
+// operations on the full-rate pipes) and lo = x - hi, exact (at most 13
+// significant bits; the tensor core reads its leading 11).
+__device__ __forceinline__ void split_tf32(float x, uint32_t& h, uint32_t& l) {
+  h = (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
+  l = __float_as_uint(x - __uint_as_float(h));
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
@@ -119,10 +122,10 @@ __device__ __forceinline__ uint32_t sw128_off(int r, int k) {
 __device__ __forceinline__ void store_split4(unsigned char* hi_base, unsigned char* lo_base, int r, int k,
                                              float4 x) {
   uint4 h, l;
-  h.x = f32_to_tf32(x.x); l.x = f32_to_tf32(x.x - __uint_as_float(h.x));
-  h.y = f32_to_tf32(x.y); l.y = f32_to_tf32(x.y - __uint_as_float(h.y));
-  h.z = f32_to_tf32(x.z); l.z = f32_to_tf32(x.z - __uint_as_float(h.z));
-  h.w = f32_to_tf32(x.w); l.w = f32_to_tf32(x.w - __uint_as_float(h.w));
+  split_tf32(x.x, h.x, l.x);
+  split_tf32(x.y, h.y, l.y);
+  split_tf32(x.z, h.z, l.z);
+  split_tf32(x.w, h.w, l.w);
   const uint32_t o = sw128_off(r, k);
   *reinterpret_cast<uint4*>(hi_base + o) = h;
   *reinterpret_cast<uint4*>(lo_base + o) = l;
@@ -491,31 +494,33 @@ cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long
 //              32 x 128, B box 64 x 32) against the stage's `full` barrier;
 //   warp 1     MMA: one lane issues, per K-tile, the three TF32 products
 //              A_hi B_hi + A_hi B_lo + A_lo B_hi (the split-operand method of
-//              Ootomo & Yokota, as gemm_tf32x3_kernel) as 4 x 3
-//              tcgen05.mma 128 x 64 x 8 into a TMEM accumulator, commits the
-//              stage back to the producer (`empty`) and, after the last
-//              K-tile, the accumulator to the epilogue (`accf`);
+//              Ootomo & Yokota, as gemm_tf32x3_kernel) as 4 x (one
+//              tcgen05.mma 128 x 128 x 8 of A_hi against [B_hi | B_lo] and one
+//              128 x 64 x 8 of A_lo against B_hi) into a TMEM accumulator of
+//              128 columns, commits the stage back to the producer (`empty`)
+//              and, after the last K-tile, the accumulator to the epilogue
+//              (`accf`);
 //   warps 2-5  converters: split the landed A tile into TF32 hi (in place)
 //              and lo, transpose B into K-major hi / lo, then release the
 //              stage to the MMA warp (`conv`);
 //   warps 6-9  epilogue: read the accumulator with tcgen05.ld (warp w owns
-//              TMEM lanes 32 (w % 4) ..), hand it back (`acce`), and write
-//              alpha acc + beta C row by row.
-// Two accumulators (128 TMEM columns) let the MMAs of the next 128-row tile
+//              TMEM lanes 32 (w % 4) ..), add its two halves, hand it back
+//              (`acce`), and write alpha acc + beta C row by row.
+// Two accumulators (256 TMEM columns) let the MMAs of the next 128-row tile
 // start while the epilogue drains the previous one.  M and K tails come from
 // the TMA's zero fill; N < 64 from the zero-filled B columns.  Every wait is
 // bounded (g_tc_spin_limit polls); a wait that runs out sets g_tc_err, every
 // role winds down, the CTA waits (bounded) for its loads and MMAs in flight
 // and frees its tensor memory.
 // ---------------------------------------------------------------------------
-constexpr int LT_BM = 128, LT_BN = 64, LT_BK = 32, LT_NS = 3, LT_NT = 320;
+constexpr int LT_BM = 128, LT_BN = 64, LT_BK = 32, LT_NS = 4, LT_NT = 320;
 constexpr int LT_A_BYTES = LT_BM * LT_BK * 4;         // 16 KB
 constexpr int LT_B_BYTES = LT_BN * LT_BK * 4;         // 8 KB
 constexpr int LT_OFF_ALO = LT_A_BYTES;
 constexpr int LT_OFF_BHI = 2 * LT_A_BYTES;
 constexpr int LT_OFF_BLO = LT_OFF_BHI + LT_B_BYTES;
 constexpr int LT_OFF_BRAW = LT_OFF_BLO + LT_B_BYTES;  // B as loaded: 32 rows (k) of 64 floats (n)
-constexpr int LT_STAGE = LT_OFF_BRAW + LT_B_BYTES;    // 56 KB, a multiple of 1024
+constexpr int LT_STAGE = LT_OFF_BRAW + LT_B_BYTES;    // 56 KB, a multiple of 1024 (four stages: 224 KB)
 constexpr size_t LT_SMEM = LT_NS * (size_t)LT_STAGE + 1024;
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -572,7 +577,7 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_s)),
-                 "r"(2 * LT_BN)
+                 "r"(4 * LT_BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -616,7 +621,11 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
-    constexpr uint32_t idesc = make_idesc_tf32(LT_BM, LT_BN);
+    // per 8-deep K step: A_hi [B_hi | B_lo] as one N = 128 product (B_lo is
+    // stored right after B_hi: 64 more K-major rows) into columns 0..127 of the
+    // accumulator, then A_lo B_hi into columns 0..63; the epilogue adds the halves
+    constexpr uint32_t idesc_hb = make_idesc_tf32(LT_BM, 2 * LT_BN);
+    constexpr uint32_t idesc_lb = make_idesc_tf32(LT_BM, LT_BN);
     uint32_t it = 0, acc_it = 0;
     for (long long u = blockIdx.x; u < n_units && !warp_flag(fail); u += gridDim.x, ++acc_it) {
       const int a = acc_it & 1;
@@ -626,7 +635,7 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         break;
       }
       tc_fence_after();
-      const uint32_t dt = tmem + (uint32_t)(a * LT_BN);
+      const uint32_t dt = tmem + (uint32_t)(a * 2 * LT_BN);
       bool ok = true;
       for (int kt = 0; kt < nk; ++kt, ++it) {
         const int s = it % LT_NS;
@@ -641,10 +650,9 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
 #pragma unroll
           for (int kk = 0; kk < LT_BK / 8; ++kk) {
             const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
-            mma_tf32(dt, make_desc_sw128(a_hi + off), make_desc_sw128(b_hi + off), idesc,
+            mma_tf32(dt, make_desc_sw128(a_hi + off), make_desc_sw128(b_hi + off), idesc_hb,
                      (kt > 0 || kk > 0) ? 1u : 0u);
-            mma_tf32(dt, make_desc_sw128(a_hi + off), make_desc_sw128(b_lo + off), idesc, 1u);
-            mma_tf32(dt, make_desc_sw128(a_lo + off), make_desc_sw128(b_hi + off), idesc, 1u);
+            mma_tf32(dt, make_desc_sw128(a_lo + off), make_desc_sw128(b_hi + off), idesc_lb, 1u);
           }
           mma_commit(&empty[s]);
           committed[s] += 1;
@@ -681,10 +689,10 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
           const int off = (ct + 128 * i) * 16;
           const float4 x = *reinterpret_cast<const float4*>(sb + off);
           uint4 h, l;
-          h.x = f32_to_tf32(x.x); l.x = f32_to_tf32(x.x - __uint_as_float(h.x));
-          h.y = f32_to_tf32(x.y); l.y = f32_to_tf32(x.y - __uint_as_float(h.y));
-          h.z = f32_to_tf32(x.z); l.z = f32_to_tf32(x.z - __uint_as_float(h.z));
-          h.w = f32_to_tf32(x.w); l.w = f32_to_tf32(x.w - __uint_as_float(h.w));
+          split_tf32(x.x, h.x, l.x);
+          split_tf32(x.y, h.y, l.y);
+          split_tf32(x.z, h.z, l.z);
+          split_tf32(x.w, h.w, l.w);
           *reinterpret_cast<uint4*>(sb + off) = h;
           *reinterpret_cast<uint4*>(sb + LT_OFF_ALO + off) = l;
         }
@@ -723,10 +731,16 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       tc_fence_after();
       const long long b = u / tiles_m;
       const int row = (int)(u % tiles_m) * LT_BM + q * 32 + lane;
-      float v0[32], v1[32];
-      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * LT_BN);
+      float v0[32], v1[32], w[32];
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * 2 * LT_BN);
       tc::tmem_ld32(taddr, v0);
+      tc::tmem_ld32(taddr + 2 * 32, w);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v0[j] += w[j];
       tc::tmem_ld32(taddr + 32, v1);
+      tc::tmem_ld32(taddr + 3 * 32, w);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) v1[j] += w[j];
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acce[a]);
@@ -783,7 +797,7 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * LT_BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(4 * LT_BN) : "memory");
   }
 }
 
