@@ -500,10 +500,10 @@ cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long
 //              128 columns, commits the stage back to the producer (`empty`)
 //              and, after the last K-tile, the accumulator to the epilogue
 //              (`accf`);
-//   warps 2-5  converters: split the landed A tile into TF32 hi (in place)
+//   warps 2-9  converters: split the landed A tile into TF32 hi (in place)
 //              and lo, transpose B into K-major hi / lo, then release the
 //              stage to the MMA warp (`conv`);
-//   warps 6-9  epilogue: read the accumulator with tcgen05.ld (warp w owns
+//   warps 10-13 epilogue: read the accumulator with tcgen05.ld (warp w owns
 //              TMEM lanes 32 (w % 4) ..), add its two halves, hand it back
 //              (`acce`), and write alpha acc + beta C row by row.
 // Two accumulators (256 TMEM columns) let the MMAs of the next 128-row tile
@@ -513,7 +513,10 @@ cudaError_t gemm_tf32x3_c64(int M, int N, int K, float alpha, const c64* A, long
 // role winds down, the CTA waits (bounded) for its loads and MMAs in flight
 // and frees its tensor memory.
 // ---------------------------------------------------------------------------
-constexpr int LT_BM = 128, LT_BN = 64, LT_BK = 32, LT_NS = 4, LT_NT = 320;
+constexpr int LT_BM = 128, LT_BN = 64, LT_BK = 32, LT_NS = 4;
+constexpr int LT_CW = 8;                           // converter warps
+constexpr int LT_CT = LT_CW * 32;
+constexpr int LT_NT = (2 + LT_CW + 4) * 32;           // 448
 constexpr int LT_A_BYTES = LT_BM * LT_BK * 4;         // 16 KB
 constexpr int LT_B_BYTES = LT_BN * LT_BK * 4;         // 8 KB
 constexpr int LT_OFF_ALO = LT_A_BYTES;
@@ -563,7 +566,7 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
   if (tid == 0) {
     for (int i = 0; i < LT_NS; ++i) {
       mbar_init(&full[i], 1);
-      mbar_init(&conv[i], 4);
+      mbar_init(&conv[i], LT_CW);
       mbar_init(&empty[i], 1);
       armed[i] = committed[i] = 0;
     }
@@ -669,8 +672,8 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
       }
       __syncwarp();
     }
-  } else if (warp < 6) {
-    // ---------------- converters (128 threads) ----------------
+  } else if (warp < 2 + LT_CW) {
+    // ---------------- converters (LT_CT threads) ----------------
     const int ct = tid - 64;
     uint32_t it = 0;
     for (long long u = blockIdx.x; u < n_units && !warp_flag(fail); u += gridDim.x) {
@@ -685,8 +688,8 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         // A: TF32 hi in place (the swizzle is a permutation of 16-byte chunks,
         // so the split is layout-free), lo into A_lo at the same offsets
 #pragma unroll
-        for (int i = 0; i < LT_A_BYTES / 16 / 128; ++i) {
-          const int off = (ct + 128 * i) * 16;
+        for (int i = 0; i < LT_A_BYTES / 16 / LT_CT; ++i) {
+          const int off = (ct + LT_CT * i) * 16;
           const float4 x = *reinterpret_cast<const float4*>(sb + off);
           uint4 h, l;
           split_tf32(x.x, h.x, l.x);
@@ -700,8 +703,8 @@ gemm_tma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__
         // item f takes column n = f % 64 and k = 4 (f / 64) .. +3
         const float* rb = reinterpret_cast<const float*>(sb + LT_OFF_BRAW);
 #pragma unroll
-        for (int i = 0; i < LT_BN * LT_BK / 4 / 128; ++i) {
-          const int f = ct + 128 * i;
+        for (int i = 0; i < LT_BN * LT_BK / 4 / LT_CT; ++i) {
+          const int f = ct + LT_CT * i;
           const int nn = f % LT_BN, kq = (f / LT_BN) * 4;
           const float4 x = make_float4(rb[(kq + 0) * LT_BN + nn], rb[(kq + 1) * LT_BN + nn], rb[(kq + 2) * LT_BN + nn],
                                        rb[(kq + 3) * LT_BN + nn]);
