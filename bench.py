@@ -674,6 +674,51 @@ def run_c5(args):
     return 0
 
 
+CLASS_NAMES = {1: "gemm (SIMT tiles, 3xTF32 tcgen05 kernel)", 2: "inverse (merge interfaces; leaf blocks off the "
+                "tensor cores)", 3: "gather/scatter/assembly", 4: "residual_2d_kernel (FP64 residual)",
+               5: "gemm_tma_kernel (TMA + tcgen05, N <= 64 products)", 6: "jx_df_kernel (FP32-pair residual update)",
+               7: "inv_tc_kernel (leaf inverses, tensor memory)"}
+BYTES_CLASSES = (3, 5, 6)
+
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# the ncu captures summarised under profiles/, for the classes whose launches
+# have one shape per step (workload, L, class) -> bytes
+NCU_TRAFFIC = {}
+
+
+def class_roofline(nat, c, v, step_ms, peaks, mhz, res_bytes, workload, L):
+    """Roofline record of one kernel class from the live profiler's totals
+    (summed CUDA-event ms, launches, algorithmic work)."""
+    k_ms, k_n, k_work = v
+    avg_ms = k_ms / max(k_n, 1)
+    if c in BYTES_CLASSES or c == 4:
+        per = res_bytes if c == 4 else k_work / max(k_n, 1)
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = per / (avg_ms / 1e3) / 1e9
+        r = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+             "traffic": NCU_TRAFFIC.get((workload, L, c)), "kernel": CLASS_NAMES[c], "bytes_per_launch": per,
+             "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured" if peaks else "fallback 6800 GB/s"}
+        if c == 4:
+            r["flops_per_launch"] = k_work / max(k_n, 1)
+            r["fp64_tflops"] = k_work / (k_ms / 1e3) / 1e12
+    else:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        achieved = k_work / (k_ms / 1e3) / 1e12
+        # FP32 / TF32 arithmetic: besides the bf16 tensor peak the contract
+        # names, the FP32 FMA rate (152 SMs x 128 lanes x 2 flop x the sampled
+        # SM clock) bounds the SIMT kernels
+        fp32_peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+        r = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+             "traffic": NCU_TRAFFIC.get((workload, L, c)), "kernel": CLASS_NAMES[c],
+             "flops_per_launch": k_work / max(k_n, 1),
+             "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured" if peaks else "fallback",
+             "fp32_simt_peak_tflops": fp32_peak, "frac_of_fp32_simt": achieved / fp32_peak}
+    r["avg_launch_ms"] = avg_ms
+    r["launches_in_timed_region"] = k_n
+    r["share_of_step"] = k_ms / step_ms
+    return r
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -759,7 +804,8 @@ def main():
     clocks = ClockSampler()
     clocks.start()
     launches0 = nat.launch_count()
-    nat.profile_begin(nat.KC_GEMM, nat.KC_INVERSE, nat.KC_MOVE, nat.KC_RESIDUAL)
+    nat.profile_begin(nat.KC_GEMM, nat.KC_INVERSE, nat.KC_MOVE, nat.KC_RESIDUAL, nat.KC_GEMM_TMA,
+                      nat.KC_RESIDUAL_DF, nat.KC_INVERSE_TC)
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -879,43 +925,16 @@ def main():
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
         peaks = json.loads(pk.read_text())
-    names = {nat.KC_GEMM: "gemm_kernel", nat.KC_INVERSE: "inverse (inv_reg_kernel / gje_panel_kernel)",
-             nat.KC_MOVE: "gather/scatter/assembly", nat.KC_RESIDUAL: "residual_2d_kernel (FP64)"}
-    breakdown = {names[c]: {"ms_per_step": v[0] / args.steps, "share": v[0] / ms, "launches_per_step":
-                            v[1] / args.steps} for c, v in classes.items()}
+    breakdown = {CLASS_NAMES[c]: {"ms_per_step": v[0] / args.steps, "share": v[0] / ms, "launches_per_step":
+                                  v[1] / args.steps} for c, v in classes.items()}
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    n_i = p * p - 4 * (p - 1)
+    # algorithmic bytes of one FP64 residual launch: read u_int, g, f, coefficients; write r (pair), flux
+    res_bytes = n_leaves * ns * (n_i * 8 + 4 * q * 8 + p * p * 8 + n_i * 8 + 4 * q * 8) + 3 * n_leaves * p * p * 8
+    rooflines = {CLASS_NAMES[c]: class_roofline(nat, c, v, ms, peaks, mhz, res_bytes, args.workload, L)
+                 for c, v in classes.items()}
     dom_cls = max(classes, key=lambda c: classes[c][0])
-    k_ms, k_n, k_work = classes[dom_cls]
-    avg_ms = k_ms / max(k_n, 1)
-    if dom_cls in (nat.KC_MOVE, nat.KC_RESIDUAL):
-        if dom_cls == nat.KC_RESIDUAL:
-            # algorithmic bytes of one residual launch: read u_int, g, f, coefficients; write r (FP32), flux
-            n_i = p * p - 4 * (p - 1)
-            per = n_leaves * ns * (n_i * 8 + 4 * q * 8 + p * p * 8 + n_i * 4 + 4 * q * 8) + 3 * n_leaves * p * p * 8
-        else:
-            per = k_work / max(k_n, 1)
-        peak = peaks.get("hbm_gbs", 6800.0)
-        achieved = per / (avg_ms / 1e3) / 1e9
-        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": None, "kernel": names[dom_cls], "bytes_per_launch": per,
-                    "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured" if peaks else "fallback 6800 GB/s"}
-        if dom_cls == nat.KC_RESIDUAL:
-            roofline["flops_per_launch"] = k_work / max(k_n, 1)
-            roofline["fp64_tflops"] = k_work / (k_ms / 1e3) / 1e12
-    else:
-        peak = peaks.get("bf16_tflops", 1900.0)
-        achieved = k_work / (k_ms / 1e3) / 1e12
-        # the class runs FP32 / complex64 arithmetic on the SIMT pipe (and the
-        # 3xTF32 tensor-core kernel): its own ceiling is the FP32 FMA rate,
-        # 152 SMs x 128 lanes x 2 flop x the sampled SM clock
-        mhz = (clk or {}).get("sm_mhz") or 2070.0
-        fp32_peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
-        roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak, "traffic": None, "kernel": names[dom_cls],
-                    "flops_per_launch": k_work / max(k_n, 1),
-                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured" if peaks else "fallback",
-                    "fp32_simt_peak_tflops": fp32_peak, "frac_of_fp32_simt": achieved / fp32_peak}
-    roofline["avg_launch_ms"] = avg_ms
-    roofline["share_of_step"] = k_ms / ms
+    roofline = dict(rooflines[CLASS_NAMES[dom_cls]])
 
     # the FP64 CPU oracle on the same inputs at the same size: the accuracy
     # reference and, timed, the CPU baseline
@@ -959,6 +978,7 @@ def main():
         "rel_err_vs_fp64": err, **acc, "refinement_iterations": iters,
         "refinement_history": history, "fp64_path": fp64,
         "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "kernel_classes": breakdown,
+        "kernel_rooflines": rooflines,
         "cpu_baseline": cpu, "clocks": clk, "autotune": tuning,
     }
     if rank == 0:

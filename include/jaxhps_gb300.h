@@ -147,11 +147,15 @@ HPS_API long long hps_gemm_shapes(int mode, long long* out, long long cap);
 
 /* Live profiler.  hps_profile_begin(mask) arms CUDA-event timing of every
  * later launch whose kernel class c has bit (1 << c) set in mask (classes:
- * 1 GEMM, 2 inverse, 3 gather/scatter/assembly, 4 refinement residual),
- * recorded on the launch's own stream.  hps_profile_end() synchronises on
- * those events and fills arrays of 8 entries indexed by class: summed kernel
- * time (ms), number of launches and summed algorithmic work (flops for 1, 2,
- * 4; bytes for 3), then disarms.  No counterpart in the reference. */
+ * 1 GEMM (SIMT and the 3xTF32 tcgen05 kernel), 2 inverse, 3
+ * gather/scatter/assembly, 4 FP64 refinement residual, 5 the TMA GEMM of the
+ * N <= 64 products, 6 the FP32-pair residual update, 7 the tensor-memory leaf
+ * inverse), recorded on the launch's own stream.  A launch inside another
+ * recorded one (an inversion's products) counts for the outer one only.
+ * hps_profile_end() synchronises on those events and fills arrays of 8
+ * entries indexed by class: summed kernel time (ms), number of launches and
+ * summed algorithmic work (flops for 1, 2, 4, 7; bytes for 3, 5, 6), then
+ * disarms.  No counterpart in the reference. */
 HPS_API int hps_profile_begin(int class_mask);
 HPS_API int hps_profile_end(double* total_ms, long long* launches, double* work);
 
@@ -470,6 +474,15 @@ HPS_API int hps_residual_df_supported(int p, int q);
  * :125-189) in the refinement's unknowns. */
 HPS_API int hps_assemble_u_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const double* u_int,
                               const double* g, double* u_full, void* stream);
+
+/* The device address of page-locked host memory (cudaHostAlloc'd or
+ * registered; mapped for the device), or HPS_ERR_ARG when `host` is not such
+ * memory.  A kernel may write its output there directly: hps_assemble_u_2d
+ * with u_full in a caller's page-locked buffer forms the solution and moves it
+ * to the host in one pass, without a device copy or a separate transfer
+ * (synchronise the stream before reading it).  No counterpart in the
+ * reference. */
+HPS_API int hps_mapped_pointer(const void* host, void** device);
 
 /* out[l][i][j] = sum_o coeffs[o][l][row0+i] * ops[o][row0+i][j] for rows
  * row0 .. row0+n_rows-1 of every leaf's operator A (FP64; row stride ld,

@@ -176,6 +176,8 @@ def _declare(lib):
     lib.hps_residual_df_prepare.restype = ci
     lib.hps_inverse_interface.argtypes = lib.hps_inverse_batched.argtypes
     lib.hps_inverse_interface.restype = ci
+    lib.hps_mapped_pointer.argtypes = [vp, P(vp)]
+    lib.hps_mapped_pointer.restype = ci
     lib.hps_inverse_block_policy.argtypes = [ci]
     lib.hps_inverse_block_policy.restype = ci
     lib.hps_residual_df_supported.argtypes = [ci, ci]
@@ -253,7 +255,7 @@ EXPORTED_SYMBOLS = (
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
     "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
     "hps_accumulate", "hps_residual_update_2d", "hps_residual_2d_df", "hps_residual_update_2d_df",
-    "hps_residual_df_supported", "hps_residual_df_prep_size", "hps_inverse_block_policy", "hps_inverse_interface", "hps_residual_df_prepare", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
+    "hps_residual_df_supported", "hps_residual_df_prep_size", "hps_inverse_block_policy", "hps_inverse_interface", "hps_mapped_pointer", "hps_residual_df_prepare", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
     "hps_scale_batched", "hps_gemm_tc_status", "hps_gemm_tc_status_reset", "hps_set_spin_limits", "hps_inverse_policy", "hps_gemm_tune_set", "hps_gemm_tune_clear", "hps_gemm_force_variant", "hps_gemm_shapes", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
@@ -314,7 +316,7 @@ def launch_count() -> int:
     return int(load_library().hps_launch_count())
 
 
-KC_GEMM, KC_INVERSE, KC_MOVE, KC_RESIDUAL = 1, 2, 3, 4
+KC_GEMM, KC_INVERSE, KC_MOVE, KC_RESIDUAL, KC_GEMM_TMA, KC_RESIDUAL_DF, KC_INVERSE_TC = 1, 2, 3, 4, 5, 6, 7
 
 
 def profile_begin(*kernel_classes: int) -> None:
@@ -396,6 +398,17 @@ def gemm(A, B, out, alpha=1.0, beta=0.0, Cmat=None, batch=None):
     check(L.hps_gemm_batched(dt, m, n, k, al, A.data_ptr(), lda, sA, B.data_ptr(), ldb, sB, be, cp, ldc, sC,
                              out.data_ptr(), ldd, sD, nb, stream_ptr()), "hps_gemm_batched")
     return out
+
+
+def mapped_pointer(t: torch.Tensor):
+    """Device address of a page-locked CPU tensor's memory, or None when the
+    tensor is not page-locked (mapped) memory."""
+    if t.device.type != "cpu" or not t.is_pinned():
+        return None
+    dp = C.c_void_p()
+    if lib().hps_mapped_pointer(t.data_ptr(), C.byref(dp)) != 0:
+        return None
+    return dp.value
 
 
 def inverse(A, out=None, info=None, entry="hps_inverse_batched"):

@@ -359,7 +359,11 @@ def correction(state: MixedState, r32, hcorr, rb32):
     return du, gch
 
 
-def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=None, max_iters=None):
+def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=None, max_iters=None, out=None):
+    """The refined solve.  ``out``: a page-locked, contiguous FP64 CPU tensor of
+    the result's shape receives the solution straight from the assembly
+    kernel (written through its device mapping: no device-side result and no
+    separate copy); it is returned once the stream has finished."""
     state: MixedState = pde_problem._state
     if source is not None:
         raise ValueError("the mixed-precision solver takes the source at build time")
@@ -420,6 +424,16 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
     else:
         raise_not_converged(state.history, tol, max_iters, "mixed-precision DtN solve")
     nat.raise_on_tc_timeout("mixed-precision DtN solve")
+    shape = (nl, p * p, ns) if state.multi else (nl, p * p)
+    dst = None
+    if (out is not None and tuple(out.shape) == shape and out.dtype == torch.float64 and out.is_contiguous()):
+        dst = nat.mapped_pointer(out)
+    if dst is not None:
+        phases.mark("refine")
+        nat.check(L.hps_assemble_u_2d(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_int.data_ptr(), g.data_ptr(),
+                                      dst, sp), "hps_assemble_u_2d")
+        torch.cuda.current_stream(dev).synchronize()
+        return out
     u = torch.empty((nl, p * p, ns), dtype=torch.float64, device=dev)
     nat.check(L.hps_assemble_u_2d(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_int.data_ptr(), g.data_ptr(),
                                   u.data_ptr(), sp), "hps_assemble_u_2d")

@@ -6,7 +6,10 @@ leaf solutions, shape (n_leaves, p^d) or (n_leaves, p^d, nsrc), on
 or None to keep the result in device memory).  ``out``, a tensor of the
 result's shape and dtype (for example a page-locked CPU buffer that the
 caller reuses), receives the result instead, and is returned; it takes
-precedence over ``host_device``.  No counterpart in the reference.
+precedence over ``host_device``.  After a mixed-precision DtN build a
+page-locked, contiguous ``out`` is written by the solution's assembly kernel
+itself through the buffer's device mapping (no device-side result, no
+separate copy).  No counterpart in the reference.
 """
 
 from __future__ import annotations
@@ -21,8 +24,13 @@ from . import _stages as st
 
 def solve(pde_problem, boundary_data, source=None, compute_device=None, host_device="cpu", out=None, **refine_kw):
     if out is not None:
+        state = getattr(pde_problem, "_state", None)
+        if (state is not None and getattr(state, "mixed", False) and not getattr(state, "iti", False)
+                and not getattr(state, "dense", False)):
+            # the refined DtN solve writes a page-locked `out` directly
+            refine_kw = dict(refine_kw, out=out)
         u = _solve(pde_problem, boundary_data, source, compute_device, None, **refine_kw)
-        res = st._to_host(u, None, out=out)
+        res = out if u is out else st._to_host(u, None, out=out)
     else:
         res = _solve(pde_problem, boundary_data, source, compute_device, host_device, **refine_kw)
     phases.mark("result_d2h")

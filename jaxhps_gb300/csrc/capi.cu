@@ -928,6 +928,22 @@ int hps_residual_update_2d(const hps_residual2d_args* a, const float* du, const 
 
 int hps_residual_df_supported(int p, int q) { return jx_df_supported(p, q) ? 1 : 0; }
 
+int hps_mapped_pointer(const void* host, void** device) {
+  if (!host || !device) {
+    set_error("hps_mapped_pointer: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  *device = nullptr;
+  const cudaError_t e = cudaHostGetDevicePointer(device, const_cast<void*>(host), 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *device = nullptr;
+    set_error("hps_mapped_pointer: not page-locked host memory mapped for the device (%s)", cudaGetErrorString(e));
+    return HPS_ERR_ARG;
+  }
+  return HPS_OK;
+}
+
 size_t hps_residual_df_prep_size(int n_leaves, int p, int q, int n_ops) {
   if (n_leaves <= 0 || n_ops <= 0 || n_ops > 10 || !jx_df_supported(p, q)) return 0;
   return jx_df_prep_floats(n_leaves, p, q, n_ops) * sizeof(float);

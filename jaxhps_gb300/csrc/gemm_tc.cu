@@ -875,7 +875,10 @@ cudaError_t gemm_tma_f32(int M, int N, int K, float alpha, const float* A, long 
   auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
   const int vec_out = al16(D) && ldd % 4 == 0 && (batch == 1 || sD % 4 == 0) && N % 4 == 0 &&
                       (!C || (al16(C) && ldc % 4 == 0 && (batch == 1 || sC % 4 == 0)));
-  ProfScope ps(KC_GEMM, st, 2.0 * (double)M * N * K * batch);
+  // algorithmic bytes: A and B once (a broadcast operand once in all), C, D
+  const double bytes = 4.0 * ((double)M * K * (a_batched ? batch : 1) + (double)K * N * (b_batched ? batch : 1) +
+                              (double)M * N * batch * (C ? 2.0 : 1.0));
+  ProfScope ps(KC_GEMM_TMA, st, bytes);
   note_launch();
   gemm_tma_kernel<<<grid, LT_NT, LT_SMEM, st>>>(tmA, tmB, M, N, K, alpha, beta, C, ldc, sC, D, ldd, sD, batch,
                                                a_batched, b_batched, vec_out);

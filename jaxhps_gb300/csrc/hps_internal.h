@@ -81,7 +81,18 @@ int inverse_small_nmax(int dtype);
 void note_launch();
 
 // Kernel classes for the live profiler (hps_profile_begin/end).
-enum KernelClass : int { KC_GEMM = 1, KC_INVERSE = 2, KC_MOVE = 3, KC_RESIDUAL = 4 };
+// 5-7 single out the kernels that carry most of a mixed-precision step: the
+// TMA GEMM (work in algorithmic bytes), the FP32-pair residual update (bytes)
+// and the tensor-memory leaf inverse (flops).
+enum KernelClass : int {
+  KC_GEMM = 1,
+  KC_INVERSE = 2,
+  KC_MOVE = 3,
+  KC_RESIDUAL = 4,
+  KC_GEMM_TMA = 5,
+  KC_RESIDUAL_DF = 6,
+  KC_INVERSE_TC = 7
+};
 
 // RAII scope placed around one kernel launch (or a sequence of them): when
 // the profiler is armed for `cls`, records a CUDA event pair on `st` around

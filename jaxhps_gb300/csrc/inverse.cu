@@ -1409,11 +1409,12 @@ static cudaError_t inverse_batched_flat(int n, const T* A, long long lda, long l
   // one profiler record for the whole inversion (its panel kernels and the
   // GEMM updates nested below): 2 n^3 flops per matrix, x4 for complex
   const double cplx = (sizeof(T) == 16 || DTypeOf<T>::value == C64) ? 4.0 : 1.0;
-  ProfScope whole(KC_INVERSE, st, 2.0 * cplx * (double)n * n * n * batch);
+  const bool on_tc = DTypeOf<T>::value == F32 && inverse_tc_takes(n, tensor_memory);
+  ProfScope whole(on_tc ? KC_INVERSE_TC : KC_INVERSE, st, 2.0 * cplx * (double)n * n * n * batch);
   if (info) cudaMemsetAsync(info, 0, sizeof(int) * (size_t)batch, st);
   const int dtype = DTypeOf<T>::value;
   if constexpr (DTypeOf<T>::value == F32) {
-    if (inverse_tc_takes(n, tensor_memory))
+    if (on_tc)
       return inverse_tc_f32(n, (const float*)A, lda, sA, (float*)X, ldx, sX, batch, info, st);
   }
   if constexpr (sizeof(T) <= 8) {

@@ -51,8 +51,10 @@ residual_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lon
   double* Qs = Ps + p * q;                // q*p
   int* perm = reinterpret_cast<int*>(Qs + q * p);  // pp
 
-  const long long l = blockIdx.x;
-  const int s0 = blockIdx.y * RES_SC;
+  // the right-hand-side chunks of a leaf are consecutive blocks (shared L2 rows)
+  const int nch = (nsrc + RES_SC - 1) / RES_SC;
+  const long long l = blockIdx.x / nch;
+  const int s0 = (int)(blockIdx.x % nch) * RES_SC;
   const int sc = min(RES_SC, nsrc - s0);
   const int tid = threadIdx.x;
   const double ih = inv_half[l];
@@ -209,7 +211,9 @@ cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigne
   const size_t smem = residual_2d_smem(p, q, need_uy);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(residual_2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 grid(n_leaves, (nsrc + RES_SC - 1) / RES_SC);
+  const long long nblk = (long long)n_leaves * ((nsrc + RES_SC - 1) / RES_SC);
+  if (nblk > 2147483647ll) return cudaErrorInvalidValue;
+  const unsigned grid = (unsigned)nblk;
   const double work = 2.0 * n_leaves * (double)nsrc * (p * p * (double)p * (n_ops + 2) + 8.0 * p * q);
   ProfScope ps(KC_RESIDUAL, st, work);
   note_launch();
@@ -259,8 +263,10 @@ residual_iti_2d_kernel(int n_leaves, int p, int q, int nsrc, int SC, int n_ops, 
   double* Qs = Ps + p * q;
   int* perm = reinterpret_cast<int*>(Qs + q * p);
 
-  const long long l = blockIdx.x;
-  const int s0 = blockIdx.y * SC;
+  // the right-hand-side chunks of a leaf are consecutive blocks (shared L2 rows)
+  const int nch = (nsrc + SC - 1) / SC;
+  const long long l = blockIdx.x / nch;
+  const int s0 = (int)(blockIdx.x % nch) * SC;
   const int sc = min(SC, nsrc - s0);
   const int tid = threadIdx.x;
   const double ih = inv_half[l];
@@ -423,7 +429,9 @@ cudaError_t residual_iti_2d(int n_leaves, int p, int q, int nsrc, int n_ops, uns
     cudaFuncSetAttribute(residual_iti_2d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(residual_iti_2d_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
-  dim3 grid(n_leaves, (nsrc + SC - 1) / SC);
+  const long long nblk = (long long)n_leaves * ((nsrc + SC - 1) / SC);
+  if (nblk > 2147483647ll) return cudaErrorInvalidValue;
+  const unsigned grid = (unsigned)nblk;
   const double work = 8.0 * n_leaves * (double)nsrc * (p * p * (double)p * (n_ops + 2) + 8.0 * p * q);
   ProfScope ps(KC_RESIDUAL, st, work);
   note_launch();
@@ -659,8 +667,10 @@ jx_update_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lo
   float* gs = reinterpret_cast<float*>(Qs + q * p);  // nq * SC
   int* perm = reinterpret_cast<int*>(gs + nq * RES_SC);
 
-  const long long l = blockIdx.x;
-  const int s0 = blockIdx.y * RES_SC;
+  // the right-hand-side chunks of a leaf are consecutive blocks (shared L2 rows)
+  const int nch = (nsrc + RES_SC - 1) / RES_SC;
+  const long long l = blockIdx.x / nch;
+  const int s0 = (int)(blockIdx.x % nch) * RES_SC;
   const int sc = min(RES_SC, nsrc - s0);
   const int tid = threadIdx.x;
   const double ih = inv_half[l];
@@ -814,7 +824,9 @@ cudaError_t jx_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsign
   const size_t smem = jx_update_2d_smem(p, q, need_uy, n_ops);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(jx_update_2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 grid(n_leaves, (nsrc + RES_SC - 1) / RES_SC);
+  const long long nblk = (long long)n_leaves * ((nsrc + RES_SC - 1) / RES_SC);
+  if (nblk > 2147483647ll) return cudaErrorInvalidValue;
+  const unsigned grid = (unsigned)nblk;
   const int ni = p * p - 4 * (p - 1);
   const double work = 2.0 * n_leaves * (double)nsrc * ((double)ni * p * n_ops + 8.0 * p * q);
   ProfScope ps(KC_RESIDUAL, st, work);

@@ -165,8 +165,11 @@ jx_df_kernel(int n_leaves, int nsrc, int n_ops, unsigned long long kinds, const 
   float* ndl = ndh + 4 * P * SC;
   int* perm = reinterpret_cast<int*>(ndl + 4 * P * SC);
 
-  const long long l = blockIdx.x;
-  const int s0 = blockIdx.y * SC;
+  // the right-hand-side chunks of a leaf are consecutive blocks, so that they
+  // run together and share each 256-byte row segment in L2
+  const int nch = (nsrc + SC - 1) / SC;
+  const long long l = blockIdx.x / nch;
+  const int s0 = (int)(blockIdx.x % nch) * SC;
   const int sc = min(SC, nsrc - s0);
   const int tid = threadIdx.x;
   const df32 ihd = df_split(inv_half[l]), mihd = df32{-ihd.hi, -ihd.lo};
@@ -409,10 +412,15 @@ cudaError_t launch_jx_df(int n_leaves, int nsrc, int n_ops, unsigned long long k
   const size_t smem = jx_df_smem<P, Q>(n_ops, need_uy);
   cudaError_t e = cudaFuncSetAttribute(jx_df_kernel<P, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 grid(n_leaves, (nsrc + DF_SC - 1) / DF_SC);
-  constexpr int NI = P * P - 4 * (P - 1);
-  const double work = 2.0 * n_leaves * (double)nsrc * ((double)NI * P * n_ops + 8.0 * P * Q);
-  ProfScope ps(KC_RESIDUAL, st, work);
+  const long long nblk = (long long)n_leaves * ((nsrc + DF_SC - 1) / DF_SC);
+  if (nblk > 2147483647ll) return cudaErrorInvalidValue;
+  const unsigned grid = (unsigned)nblk;
+  // algorithmic bytes: du, dg, the residual pair read and written, the flux
+  // (FP64) read and written, this leaf's coefficient pairs
+  constexpr int NI = P * P - 4 * (P - 1), NQ = 4 * Q, NL2 = (P - 2) * (P - 2);
+  const double bytes = (double)n_leaves * ((double)nsrc * (4.0 * NI + 4.0 * NQ + 16.0 * NI + 16.0 * NQ) +
+                                           8.0 * n_ops * NL2);
+  ProfScope ps(KC_RESIDUAL_DF, st, bytes);
   note_launch();
   jx_df_kernel<P, Q><<<grid, DF_NT, smem, st>>>(n_leaves, nsrc, n_ops, kinds, prep, inv_half, perm, du, dg, r_hi,
                                                 r_lo, flux, need_uy);

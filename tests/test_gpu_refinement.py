@@ -175,3 +175,21 @@ def test_pinned_source_upload_matches_numpy_source(cuda):
     hps.build_solver(pde2, precision="mixed")
     r = hps.solve(pde2, g, out=buf)
     assert r is buf and np.array_equal(buf.numpy(), u_np)
+
+
+def test_solution_assembled_into_caller_buffers(cuda):
+    """One right-hand side: a page-locked `out` is written by the assembly
+    kernel through its device mapping, a pageable one by a copy; both equal
+    the solution returned on the host, bit for bit."""
+    L, p, q = 3, 12, 10
+    dom, pde, _ = _setup(L, p, q, None, False, seed=9)
+    bp = dom.boundary_points
+    g = np.cos(bp[:, 0]) - bp[:, 1]
+    hps.build_solver(pde, precision="mixed")
+    u_ref = hps.solve(pde, g).numpy()
+    pinned = torch.full(u_ref.shape, float("nan"), dtype=torch.float64).pin_memory()
+    pageable = torch.full(u_ref.shape, float("nan"), dtype=torch.float64)
+    assert hps.solve(pde, g, out=pinned) is pinned
+    assert hps.solve(pde, g, out=pageable) is pageable
+    assert np.array_equal(pinned.numpy(), u_ref)
+    assert np.array_equal(pageable.numpy(), u_ref)
