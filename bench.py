@@ -681,9 +681,11 @@ CLASS_NAMES = {1: "gemm (SIMT tiles, 3xTF32 tcgen05 kernel)", 2: "inverse (merge
 BYTES_CLASSES = (3, 5, 6)
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# the ncu captures summarised under profiles/, for the classes whose launches
-# have one shape per step (workload, L, class) -> bytes
-NCU_TRAFFIC = {}
+# the ncu capture summarised in profiles/traffic_poisson_L5_mixed.md (L = 5),
+# scaled by the number of leaves to L = 7 (the leaf kernels' traffic grows in
+# proportion), for the classes with one launch shape per step:
+# (workload, L, class) -> bytes
+NCU_TRAFFIC = {("poisson", 7, 4): 16 * 355.4e6, ("poisson", 7, 6): 16 * 453.6e6, ("poisson", 7, 7): 16 * 255.0e6}
 
 
 def class_roofline(nat, c, v, step_ms, peaks, mhz, res_bytes, workload, L):
