@@ -1229,6 +1229,185 @@ static cudaError_t inverse_batched_flat(int n, const T* A, long long lda, long l
                                         long long sX, int batch, int* info, void* ws, size_t ws_bytes,
                                         cudaStream_t st, bool tensor_memory);
 
+// ---------------------------------------------------------------------------
+// Block Gauss-Jordan inversion of one FP32 matrix per CTA, n <= 128, for the
+// interface blocks the recursive inversion ends at (and the n <= 128 merge
+// interfaces).  The matrix lives in registers (thread (ty, tx) of a 16 x 32
+// grid owns rows ty + 16 a, columns tx + 32 c); each of the n / 16 steps
+// publishes the 16-wide column and row blocks to shared memory, one warp
+// inverts the 16 x 16 diagonal block (Gauss-Jordan with partial pivoting
+// inside the block), the CTA forms the new row block R = P M_k. and every
+// thread updates its elements:
+//     M_ij -= M_ik R_kj,  M_kj = R_kj,  M_ik = -M_ik P,  M_kk = P.
+// Pivots are searched within the 16 x 16 blocks only (as in the recursion
+// above); a zero pivot sets info to its column (1-based).  Three barriers per
+// 16 columns where the per-column kernels need one or two per column.
+// ---------------------------------------------------------------------------
+constexpr int B16_NT = 512, B16_TY = 16, B16_TX = 32, B16_B = 16, B16_NMAX = 128;
+constexpr int B16_RM = B16_NMAX / B16_TY, B16_RN = B16_NMAX / B16_TX;   // 8 x 4 elements per thread
+
+__global__ void __launch_bounds__(B16_NT, 1)
+inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long sA, float* X, long long ldx,
+                   long long sX, int* info) {
+  __shared__ float Cb[B16_NMAX][B16_B + 1];   // the step's column block (old values)
+  __shared__ float Rk[B16_B][B16_NMAX + 1];   // the step's row block, then R = P M_k.
+  __shared__ float Pk[B16_B][B16_B + 1];      // inverse of the diagonal block
+  __shared__ int s_info;
+  const long long bb = blockIdx.x;
+  const float* Ab = A + bb * sA;
+  const int tid = threadIdx.x, ty = tid / B16_TX, tx = tid % B16_TX, lane = tid & 31, warp = tid >> 5;
+  float m[B16_RM][B16_RN];
+#pragma unroll
+  for (int a = 0; a < B16_RM; ++a)
+#pragma unroll
+    for (int c = 0; c < B16_RN; ++c) {
+      const int i = ty + B16_TY * a, j = tx + B16_TX * c;
+      m[a][c] = (i < n && j < n) ? Ab[(long long)i * lda + j] : 0.f;
+    }
+  if (tid == 0) s_info = 0;
+  for (int k0 = 0; k0 < n; k0 += B16_B) {
+    const int bs = min(B16_B, n - k0);
+    // (1) publish the column block and the row block
+#pragma unroll
+    for (int a = 0; a < B16_RM; ++a)
+#pragma unroll
+      for (int c = 0; c < B16_RN; ++c) {
+        const int i = ty + B16_TY * a, j = tx + B16_TX * c;
+        if (i < n && j >= k0 && j < k0 + bs) Cb[i][j - k0] = m[a][c];
+        if (j < n && i >= k0 && i < k0 + bs) Rk[i - k0][j] = m[a][c];
+      }
+    __syncthreads();
+    // (2) warp 0 inverts the diagonal block: lane r holds row r of [M_kk | I]
+    if (warp == 0) {
+      float d[B16_B], e[B16_B];
+#pragma unroll
+      for (int j = 0; j < B16_B; ++j) {
+        d[j] = (lane < bs && j < bs) ? Cb[k0 + lane][j] : 0.f;
+        e[j] = (lane == j) ? 1.f : 0.f;
+      }
+      bool used = lane >= bs;
+      int mycol = 0;
+#pragma unroll
+      for (int c = 0; c < B16_B; ++c) {
+        if (c < bs) {
+          float v = used ? -1.f : fabsf(d[c]);
+          if (v != v) v = INFINITY;   // a NaN pivot is taken (and poisons the result) rather than skipped
+          int who = lane;
+#pragma unroll
+          for (int off = 16; off; off >>= 1) {
+            const float ov = __shfl_xor_sync(0xffffffffu, v, off);
+            const int ow = __shfl_xor_sync(0xffffffffu, who, off);
+            if (ov > v || (ov == v && ow < who)) {
+              v = ov;
+              who = ow;
+            }
+          }
+          if (!(v > 0.f) && lane == 0 && s_info == 0) s_info = k0 + c + 1;
+          const float pv = __shfl_sync(0xffffffffu, d[c], who);
+          const float pinv = (v > 0.f) ? 1.f / pv : 0.f;
+          if (lane == who) {
+            used = true;
+            mycol = c;
+#pragma unroll
+            for (int j = 0; j < B16_B; ++j) {
+              d[j] *= pinv;
+              e[j] *= pinv;
+            }
+          }
+          const float f = (lane == who) ? 0.f : d[c];
+#pragma unroll
+          for (int j = 0; j < B16_B; ++j) {
+            const float pd = __shfl_sync(0xffffffffu, d[j], who);
+            const float pe = __shfl_sync(0xffffffffu, e[j], who);
+            d[j] = fmaf(-f, pd, d[j]);
+            e[j] = fmaf(-f, pe, e[j]);
+          }
+        }
+      }
+      // the pivot row of column c holds row c of the inverse
+      if (lane < bs) {
+#pragma unroll
+        for (int j = 0; j < B16_B; ++j) Pk[mycol][j] = e[j];
+      }
+    }
+    __syncthreads();
+    // (3) R = P M_k. into registers of the threads that own those columns:
+    // thread (ty, tx) forms R[ty][j] for its columns j (bs <= 16 rows)
+    float r_new[B16_RN];
+#pragma unroll
+    for (int c = 0; c < B16_RN; ++c) {
+      const int j = tx + B16_TX * c;
+      float acc = 0.f;
+      if (ty < bs && j < n) {
+#pragma unroll
+        for (int d = 0; d < B16_B; ++d)
+          if (d < bs) acc = fmaf(Pk[ty][d], Rk[d][j], acc);
+      }
+      r_new[c] = acc;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < B16_RN; ++c) {
+      const int j = tx + B16_TX * c;
+      if (ty < bs && j < n) Rk[ty][j] = r_new[c];
+    }
+    __syncthreads();
+    // (4) every element from the snapshots in shared memory
+#pragma unroll
+    for (int a = 0; a < B16_RM; ++a) {
+      const int i = ty + B16_TY * a;
+      if (i >= n) continue;
+      const bool ib = i >= k0 && i < k0 + bs;
+      float ci[B16_B];
+#pragma unroll
+      for (int d = 0; d < B16_B; ++d) ci[d] = (d < bs && !ib) ? Cb[i][d] : 0.f;
+#pragma unroll
+      for (int c = 0; c < B16_RN; ++c) {
+        const int j = tx + B16_TX * c;
+        if (j >= n) continue;
+        const bool jb = j >= k0 && j < k0 + bs;
+        float v;
+        if (ib) {
+          v = jb ? Pk[i - k0][j - k0] : Rk[i - k0][j];
+        } else if (jb) {
+          v = 0.f;
+#pragma unroll
+          for (int d = 0; d < B16_B; ++d)
+            if (d < bs) v = fmaf(-ci[d], Pk[d][j - k0], v);
+        } else {
+          v = m[a][c];
+#pragma unroll
+          for (int d = 0; d < B16_B; ++d)
+            if (d < bs) v = fmaf(-ci[d], Rk[d][j], v);
+        }
+        m[a][c] = v;
+      }
+    }
+    __syncthreads();   // the next step overwrites Cb, Rk and Pk
+  }
+  if (tid == 0 && info) info[bb] = s_info;
+  float* Xb = X + bb * sX;
+#pragma unroll
+  for (int a = 0; a < B16_RM; ++a)
+#pragma unroll
+    for (int c = 0; c < B16_RN; ++c) {
+      const int i = ty + B16_TY * a, j = tx + B16_TX * c;
+      if (i < n && j < n) Xb[(long long)i * ldx + j] = m[a][c];
+    }
+}
+
+static cudaError_t launch_block16(int n, const float* A, long long lda, long long sA, float* X, long long ldx,
+                                  long long sX, int batch, int* info, cudaStream_t st) {
+  for (int b0 = 0; b0 < batch; b0 += 1 << 30) {
+    const int nb = batch - b0;
+    ProfScope ps(KC_INVERSE, st, 2.0 * (double)n * n * n * nb);
+    note_launch();
+    inv_block16_kernel<<<nb, B16_NT, 0, st>>>(n, A + (long long)b0 * sA, lda, sA, X + (long long)b0 * sX, ldx, sX,
+                                              info ? info + b0 : nullptr);
+  }
+  return cudaGetLastError();
+}
+
 constexpr int REC_MIN = 224;
 static int g_inverse_rec_policy = -1;
 
@@ -1284,11 +1463,14 @@ static cudaError_t inverse_rec_f32(int n, const float* A, long long lda, long lo
                                    long long sX, int batch, int* info, unsigned char* ws, size_t ws_bytes,
                                    int col0, cudaStream_t st) {
   if (n < REC_MIN) {
-    // a block the recursion ends at: pivoted Gauss-Jordan, info via scratch
+    // a block the recursion ends at: block Gauss-Jordan (n <= 128) or the
+    // pivoted per-column kernels; info via scratch
     int* tinfo = reinterpret_cast<int*>(ws);
     const size_t ib = al256(sizeof(int) * (size_t)batch);
-    cudaError_t e = inverse_batched_flat<float>(n, A, lda, sA, X, ldx, sX, batch, info ? tinfo : nullptr, ws + ib,
-                                                ws_bytes - ib, st, false);
+    cudaError_t e = (n <= B16_NMAX)
+                        ? launch_block16(n, A, lda, sA, X, ldx, sX, batch, info ? tinfo : nullptr, st)
+                        : inverse_batched_flat<float>(n, A, lda, sA, X, ldx, sX, batch, info ? tinfo : nullptr,
+                                                      ws + ib, ws_bytes - ib, st, false);
     if (e != cudaSuccess || !info) return e;
     return info_merge(batch, tinfo, info, col0, st);
   }
@@ -1335,6 +1517,12 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
                             cudaStream_t st, int flags) {
   const bool tensor_memory = (flags & INV_TENSOR_MEMORY) != 0;
   if constexpr (DTypeOf<T>::value == F32) {
+    // interface matrices of n <= 128: one block Gauss-Jordan CTA each
+    if ((flags & INV_BLOCK_RECURSIVE) && n > 0 && n <= B16_NMAX && batch > 0 && inverse_rec_policy() == 1 &&
+        !inverse_tc_takes(n, tensor_memory)) {
+      ProfScope whole(KC_INVERSE, st, 2.0 * (double)n * n * n * batch);
+      return launch_block16(n, (const float*)A, lda, sA, (float*)X, ldx, sX, batch, info, st);
+    }
     if ((flags & INV_BLOCK_RECURSIVE) && n >= REC_MIN && batch > 0 && inverse_rec_policy() == 1 &&
         !inverse_tc_takes(n, tensor_memory)) {
       const size_t need = rec_workspace_bytes(n, batch);

@@ -82,7 +82,7 @@ def test_mixed_solve_with_block_inverse_matches_oracle(cuda, L, nsrc):
     assert len(hist[1]) <= len(hist[0]) + 1, hist
 
 
-@pytest.mark.parametrize("n,batch", [(224, 3), (448, 2), (900, 1)])
+@pytest.mark.parametrize("n,batch", [(56, 5), (100, 3), (112, 300), (128, 2), (224, 3), (448, 2), (900, 1)])
 def test_interface_inverse_matches_numpy(cuda, n, batch):
     """The block recursion on diagonally dominant matrices (no row
     permutation: pivots stay within blocks), out of place and in place."""
@@ -100,6 +100,22 @@ def test_interface_inverse_matches_numpy(cuda, n, batch):
     Xe = np.linalg.inv(A.astype(np.float64))
     assert _rel(X, Xe) < 2e-5 * 20
     assert np.array_equal(tA.cpu().numpy(), X)
+
+
+@pytest.mark.parametrize("n,col", [(112, 37), (448, 300)])
+def test_block_inverse_reports_a_singular_interface_block_at_its_column(cuda, n, col):
+    """A zero column: info > 0 for that matrix only, the other inverted exactly."""
+    D = torch.eye(n, dtype=torch.float32, device=cuda).repeat(2, 1, 1).contiguous()
+    D[1, :, col] = 0.0
+    info = torch.zeros(2, dtype=torch.int32, device=cuda)
+    old = nat.lib().hps_inverse_block_policy(1)
+    try:
+        X = nat.inverse(D, info=info, entry="hps_inverse_interface")
+    finally:
+        nat.lib().hps_inverse_block_policy(old)
+    inf = info.cpu().numpy()
+    assert inf[0] == 0 and inf[1] > 0
+    assert torch.equal(X[0], torch.eye(n, dtype=torch.float32, device=cuda))
 
 
 def test_block_inverse_reports_a_singular_interface_block(cuda):
