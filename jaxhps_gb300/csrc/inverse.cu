@@ -1234,9 +1234,10 @@ static cudaError_t inverse_batched_flat(int n, const T* A, long long lda, long l
 // interface blocks the recursive inversion ends at (and the n <= 128 merge
 // interfaces).  The matrix lives in registers (thread (ty, tx) of a 16 x 32
 // grid owns rows ty + 16 a, columns tx + 32 c); each of the n / 16 steps
-// publishes the 16-wide column and row blocks to shared memory, one warp
+// publishes the 16-wide column and row blocks to shared memory, the CTA
 // inverts the 16 x 16 diagonal block (Gauss-Jordan with partial pivoting
-// inside the block), the CTA forms the new row block R = P M_k. and every
+// inside the block, one element of [M_kk | I] per thread), forms the new row
+// block R = P M_k. and every
 // thread updates its elements:
 //     M_ij -= M_ik R_kj,  M_kj = R_kj,  M_ik = -M_ik P,  M_kk = P.
 // Pivots are searched within the 16 x 16 blocks only (as in the recursion
@@ -1252,6 +1253,9 @@ inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long 
   __shared__ float Cb[B16_NMAX][B16_B + 1];   // the step's column block (old values)
   __shared__ float Rk[B16_B][B16_NMAX + 1];   // the step's row block, then R = P M_k.
   __shared__ float Pk[B16_B][B16_B + 1];      // inverse of the diagonal block
+  __shared__ float Ag[2][B16_B][2 * B16_B + 1];   // [M_kk | I] under elimination, two copies
+  __shared__ int used_s[B16_B], rowof_s[B16_B], piv_s;
+  __shared__ float pinv_s;
   __shared__ int s_info;
   const long long bb = blockIdx.x;
   const float* Ab = A + bb * sA;
@@ -1277,20 +1281,24 @@ inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long 
         if (j < n && i >= k0 && i < k0 + bs) Rk[i - k0][j] = m[a][c];
       }
     __syncthreads();
-    // (2) warp 0 inverts the diagonal block: lane r holds row r of [M_kk | I]
-    if (warp == 0) {
-      float d[B16_B], e[B16_B];
-#pragma unroll
-      for (int j = 0; j < B16_B; ++j) {
-        d[j] = (lane < bs && j < bs) ? Cb[k0 + lane][j] : 0.f;
-        e[j] = (lane == j) ? 1.f : 0.f;
-      }
-      bool used = lane >= bs;
-      int mycol = 0;
-#pragma unroll
-      for (int c = 0; c < B16_B; ++c) {
-        if (c < bs) {
-          float v = used ? -1.f : fabsf(d[c]);
+    // (2) the diagonal block by Gauss-Jordan on [M_kk | I] with one element
+    // per thread (16 x 32 = 512), ping-ponging between two copies: per pivot,
+    // warp 0 picks the largest unused row of the column, then every thread
+    // forms its element of the next copy (two barriers per pivot, a short
+    // loop body)
+    {
+      const int r = tid >> 5, c = tid & 31;
+      float v0;
+      if (c < B16_B) v0 = (r < bs && c < bs) ? Cb[k0 + r][c] : (r == c ? 1.f : 0.f);
+      else v0 = (c - B16_B == r) ? 1.f : 0.f;
+      Ag[0][r][c] = v0;
+      if (tid < B16_B) used_s[tid] = 0;
+      __syncthreads();
+#pragma unroll 1
+      for (int k = 0; k < B16_B; ++k) {
+        const int cur = k & 1;
+        if (warp == 0) {
+          float v = (lane < B16_B && !used_s[lane]) ? fabsf(Ag[cur][lane][k]) : -1.f;
           if (v != v) v = INFINITY;   // a NaN pivot is taken (and poisons the result) rather than skipped
           int who = lane;
 #pragma unroll
@@ -1302,33 +1310,24 @@ inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long 
               who = ow;
             }
           }
-          if (!(v > 0.f) && lane == 0 && s_info == 0) s_info = k0 + c + 1;
-          const float pv = __shfl_sync(0xffffffffu, d[c], who);
-          const float pinv = (v > 0.f) ? 1.f / pv : 0.f;
-          if (lane == who) {
-            used = true;
-            mycol = c;
-#pragma unroll
-            for (int j = 0; j < B16_B; ++j) {
-              d[j] *= pinv;
-              e[j] *= pinv;
-            }
-          }
-          const float f = (lane == who) ? 0.f : d[c];
-#pragma unroll
-          for (int j = 0; j < B16_B; ++j) {
-            const float pd = __shfl_sync(0xffffffffu, d[j], who);
-            const float pe = __shfl_sync(0xffffffffu, e[j], who);
-            d[j] = fmaf(-f, pd, d[j]);
-            e[j] = fmaf(-f, pe, e[j]);
+          if (lane == 0) {
+            if (!(v > 0.f) && k < bs && s_info == 0) s_info = k0 + k + 1;
+            piv_s = who;
+            pinv_s = (v > 0.f) ? 1.f / Ag[cur][who][k] : 0.f;
+            used_s[who] = 1;
+            rowof_s[k] = who;
           }
         }
+        __syncthreads();
+        const int pr = piv_s;
+        const float pinv = pinv_s;
+        const float pv = Ag[cur][pr][c] * pinv;
+        Ag[cur ^ 1][r][c] = (r == pr) ? pv : fmaf(-Ag[cur][r][k], pv, Ag[cur][r][c]);
+        __syncthreads();
       }
-      // the pivot row of column c holds row c of the inverse
-      if (lane < bs) {
-#pragma unroll
-        for (int j = 0; j < B16_B; ++j) Pk[mycol][j] = e[j];
-      }
+      // the pivot row of column k holds row k of the inverse (16 pivots: the
+      // result is in copy 0)
+      if (r < bs && c < bs) Pk[r][c] = Ag[0][rowof_s[r]][B16_B + c];
     }
     __syncthreads();
     // (3) R = P M_k. into registers of the threads that own those columns:
@@ -1517,8 +1516,9 @@ cudaError_t inverse_batched(int n, const T* A, long long lda, long long sA, T* X
                             cudaStream_t st, int flags) {
   const bool tensor_memory = (flags & INV_TENSOR_MEMORY) != 0;
   if constexpr (DTypeOf<T>::value == F32) {
-    // interface matrices of n <= 128: one block Gauss-Jordan CTA each
-    if ((flags & INV_BLOCK_RECURSIVE) && n > 0 && n <= B16_NMAX && batch > 0 && inverse_rec_policy() == 1 &&
+    // interface matrices of 64 < n <= 128: one block Gauss-Jordan CTA each
+    // (measured: below 64 the per-column register kernel is as fast)
+    if ((flags & INV_BLOCK_RECURSIVE) && n > 64 && n <= B16_NMAX && batch > 0 && inverse_rec_policy() == 1 &&
         !inverse_tc_takes(n, tensor_memory)) {
       ProfScope whole(KC_INVERSE, st, 2.0 * (double)n * n * n * batch);
       return launch_block16(n, (const float*)A, lda, sA, (float*)X, ldx, sX, batch, info, st);
