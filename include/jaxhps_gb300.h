@@ -450,9 +450,22 @@ HPS_API int hps_residual_update_2d(const hps_residual2d_args* a, const float* du
 
 /* hps_residual_2d with the FP64 leaf-row residual r also stored as an FP32
  * pair: a->r_int = fl32(r) and r_lo = fl32(r - a->r_int) (a->r_int64 may be
- * NULL).  The starting point of hps_residual_update_2d_df.  Refinement only:
- * no counterpart in the reference. */
-HPS_API int hps_residual_2d_df(const hps_residual2d_args* a, float* r_lo, void* stream);
+ * NULL).  With u_int32 not NULL the interior values are read from it (FP32,
+ * same layout) instead of a->u_int.  The starting point of
+ * hps_residual_update_2d_df.  Refinement only: no counterpart in the
+ * reference. */
+HPS_API int hps_residual_2d_df(const hps_residual2d_args* a, const float* u_int32, float* r_lo, void* stream);
+
+/* y += x with y held as an FP32 pair (y_hi, y_lo; TwoSum, no FP64
+ * arithmetic) and out[0] = max |x|, out[1] = max |y_hi| (FP64, device); n a
+ * multiple of 4, arrays 16-byte aligned.  The refined solution's interior
+ * accumulator.  No counterpart in the reference. */
+HPS_API int hps_accumulate_max_df(long long n, const float* x, float* y_hi, float* y_lo, double* out, void* stream);
+
+/* hps_assemble_u_2d with the interior values given as an FP32 pair
+ * (u_hi + u_lo, summed in FP64).  No counterpart in the reference. */
+HPS_API int hps_assemble_u_2d_df(int n_leaves, int p, int q, int nsrc, const double* Pside, const float* u_hi,
+                                 const float* u_lo, const double* g, double* u_full, void* stream);
 
 /* The incremental update of hps_residual_update_2d with the leaf-row
  * residual held as an FP32 pair (a->r_int = hi, r_lo = lo, both in/out; no

@@ -166,7 +166,11 @@ def _declare(lib):
     lib.hps_accumulate.restype = ci
     lib.hps_residual_update_2d.argtypes = [P(Residual2DArgs), vp, vp, vp]
     lib.hps_residual_update_2d.restype = ci
-    lib.hps_residual_2d_df.argtypes = [P(Residual2DArgs), vp, vp]
+    lib.hps_residual_2d_df.argtypes = [P(Residual2DArgs), vp, vp, vp]
+    lib.hps_accumulate_max_df.argtypes = [cll, vp, vp, vp, vp, vp]
+    lib.hps_accumulate_max_df.restype = ci
+    lib.hps_assemble_u_2d_df.argtypes = [ci, ci, ci, ci, vp, vp, vp, vp, vp, vp]
+    lib.hps_assemble_u_2d_df.restype = ci
     lib.hps_residual_2d_df.restype = ci
     lib.hps_residual_update_2d_df.argtypes = [P(Residual2DArgs), vp, vp, vp, vp, vp]
     lib.hps_residual_update_2d_df.restype = ci
@@ -255,7 +259,8 @@ EXPORTED_SYMBOLS = (
     "hps_local_solve_iti_workspace_size", "hps_local_solve_iti", "hps_merge_level_dtn_workspace_size",
     "hps_merge_level_dtn", "hps_merge_level_iti", "hps_down_level", "hps_up_level", "hps_residual_2d", "hps_flux_combine",
     "hps_accumulate", "hps_residual_update_2d", "hps_residual_2d_df", "hps_residual_update_2d_df",
-    "hps_residual_df_supported", "hps_residual_df_prep_size", "hps_inverse_block_policy", "hps_inverse_interface", "hps_mapped_pointer", "hps_residual_df_prepare", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
+    "hps_residual_df_supported", "hps_residual_df_prep_size", "hps_inverse_block_policy", "hps_inverse_interface", "hps_mapped_pointer", "hps_accumulate_max_df",
+    "hps_assemble_u_2d_df", "hps_residual_df_prepare", "hps_assemble_u_2d", "hps_interior_f32", "hps_assemble_rows",
     "hps_refine_points_3d", "hps_refine_check_3d", "hps_mlp_param_count", "hps_mlp_sample_points",
     "hps_mlp_features", "hps_mlp_forward", "hps_mlp_bce", "hps_mlp_backward", "hps_mlp_adam", "hps_panel_map",
     "hps_scale_batched", "hps_gemm_tc_status", "hps_gemm_tc_status_reset", "hps_set_spin_limits", "hps_inverse_policy", "hps_gemm_tune_set", "hps_gemm_tune_clear", "hps_gemm_force_variant", "hps_gemm_shapes", "hps_iti_combine", "hps_residual_iti_2d", "hps_gemm_policy", "hps_accumulate_max", "hps_refine_points_2d", "hps_refine_check_2d", "hps_interp_rows", "hps_gather_cols", "hps_interp_from_leaves", "hps_assemble_rows_complex",
@@ -398,6 +403,15 @@ def gemm(A, B, out, alpha=1.0, beta=0.0, Cmat=None, batch=None):
     check(L.hps_gemm_batched(dt, m, n, k, al, A.data_ptr(), lda, sA, B.data_ptr(), ldb, sB, be, cp, ldc, sC,
                              out.data_ptr(), ldd, sD, nb, stream_ptr()), "hps_gemm_batched")
     return out
+
+
+def accumulate_max_df(x: torch.Tensor, y_hi: torch.Tensor, y_lo: torch.Tensor, out: torch.Tensor):
+    """(y_hi, y_lo) += x in double-float and (max |x|, max |y|) as two Python
+    floats (one device sync)."""
+    check(lib().hps_accumulate_max_df(x.numel(), x.data_ptr(), y_hi.data_ptr(), y_lo.data_ptr(), out.data_ptr(),
+                                      stream_ptr()), "hps_accumulate_max_df")
+    mx, my = out.tolist()
+    return mx, my
 
 
 def mapped_pointer(t: torch.Tensor):

@@ -300,12 +300,15 @@ def _res_args(state: MixedState, u_int, g, r32, flux, r64=None, u_full=None, zer
     return a
 
 
-def _residual(state: MixedState, u_int, g, r32, flux, u_full=None, zero_source=False, r64=None, r_lo=None):
+def _residual(state: MixedState, u_int, g, r32, flux, u_full=None, zero_source=False, r64=None, r_lo=None,
+              u32=None):
     """FP64 residual of the discrete system at (u_int, g); zero_source drops f.
-    With r_lo the leaf-row residual is also stored as the FP32 pair (r32, r_lo)."""
+    With r_lo the leaf-row residual is also stored as the FP32 pair (r32, r_lo);
+    u32 (FP32) then may give the interior values in place of u_int."""
     a = _res_args(state, u_int, g, r32, flux, r64=r64, u_full=u_full, zero_source=zero_source)
     if r_lo is not None:
-        nat.check(nat.lib().hps_residual_2d_df(C.byref(a), r_lo.data_ptr(), nat.stream_ptr()), "hps_residual_2d_df")
+        nat.check(nat.lib().hps_residual_2d_df(C.byref(a), nat.ptr(u32), r_lo.data_ptr(), nat.stream_ptr()),
+                  "hps_residual_2d_df")
     else:
         nat.check(nat.lib().hps_residual_2d(C.byref(a), nat.stream_ptr()), "hps_residual_2d")
 
@@ -385,12 +388,17 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
     phases.mark("boundary_h2d")
     nl, p, q = state.n_leaves, state.p, state.q
     n_i = p * p - 4 * (p - 1)
-    u_int = torch.zeros((nl, n_i, ns), dtype=torch.float64, device=dev)
+    # the leaf-row residual between updates and the interior solution: FP32
+    # pairs (r32, r_lo), (u_hi, u_lo) where the pair kernels serve (p, q), else FP64
+    pairs = bool(L.hps_residual_df_supported(p, q))
+    if pairs:
+        u_int = None
+        u_hi = torch.zeros((nl, n_i, ns), dtype=torch.float32, device=dev)
+        u_lo = torch.zeros((nl, n_i, ns), dtype=torch.float32, device=dev)
+    else:
+        u_int = torch.zeros((nl, n_i, ns), dtype=torch.float64, device=dev)
     g = torch.zeros((nl, 4 * q, ns), dtype=torch.float64, device=dev)
     r32 = torch.empty((nl, n_i, ns), dtype=torch.float32, device=dev)
-    # the leaf-row residual between updates: an FP32 pair (r32, r_lo) where the
-    # pair kernel serves (p, q), else FP64
-    pairs = bool(L.hps_residual_df_supported(p, q))
     r64 = None if pairs else torch.empty((nl, n_i, ns), dtype=torch.float64, device=dev)
     r_lo = torch.empty((nl, n_i, ns), dtype=torch.float32, device=dev) if pairs else None
     flux = torch.zeros((nl, 4 * q, ns), dtype=torch.float64, device=dev)
@@ -409,14 +417,19 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
                                      rb32.data_ptr(), sp), "hps_flux_combine")
         du, dg = correction(state, r32, hcorr, rb32)
         nat.check(L.hps_accumulate(dg.numel(), dg.data_ptr(), g.data_ptr(), sp), "hps_accumulate")
-        step, size = nat.accumulate_max(du, u_int, maxima)
+        if pairs:
+            step, size = nat.accumulate_max_df(du, u_hi, u_lo, maxima)
+        else:
+            step, size = nat.accumulate_max(du, u_int, maxima)
         state.history.append(step / max(size, 1e-300))
         if converged(state.history, tol):
             break
         if it == 0:
             # the first correction is the size of the solution: recompute the
             # residual from scratch in FP64
-            _residual(state, u_int, g, r32, flux, r64=r64, r_lo=r_lo)
+            # (with pairs the interior solution is still du of the first
+            # correction, exactly u_hi)
+            _residual(state, u_int, g, r32, flux, r64=r64, r_lo=r_lo, u32=u_hi if pairs else None)
         elif pairs:
             _residual_update_df(state, prep, du, dg, r_lo, r32, flux)
         else:
@@ -428,15 +441,21 @@ def solve_mixed(pde_problem, boundary_data, source=None, host_device="cpu", tol=
     dst = None
     if (out is not None and tuple(out.shape) == shape and out.dtype == torch.float64 and out.is_contiguous()):
         dst = nat.mapped_pointer(out)
+    def assemble(target):
+        if pairs:
+            nat.check(L.hps_assemble_u_2d_df(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_hi.data_ptr(),
+                                             u_lo.data_ptr(), g.data_ptr(), target, sp), "hps_assemble_u_2d_df")
+        else:
+            nat.check(L.hps_assemble_u_2d(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_int.data_ptr(),
+                                          g.data_ptr(), target, sp), "hps_assemble_u_2d")
+
     if dst is not None:
         phases.mark("refine")
-        nat.check(L.hps_assemble_u_2d(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_int.data_ptr(), g.data_ptr(),
-                                      dst, sp), "hps_assemble_u_2d")
+        assemble(dst)
         torch.cuda.current_stream(dev).synchronize()
         return out
     u = torch.empty((nl, p * p, ns), dtype=torch.float64, device=dev)
-    nat.check(L.hps_assemble_u_2d(nl, p, q, ns, state.consts["Pside"].data_ptr(), u_int.data_ptr(), g.data_ptr(),
-                                  u.data_ptr(), sp), "hps_assemble_u_2d")
+    assemble(u.data_ptr())
     if not state.multi:
         u = u[..., 0]
     phases.mark("refine")

@@ -79,7 +79,10 @@ cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigne
                         const double* inv_half, const double* D1, const double* D2, const double* Pside,
                         const double* Qside, const int* perm, const double* u_int, const double* g,
                         const double* f, float* r_int, double* r_int64, float* r_lo, double* flux, double* u_full,
-                        int need_uy, cudaStream_t st);
+                        int need_uy, cudaStream_t st, const float* u_int32 = nullptr);
+cudaError_t accumulate_pair_max(long long n, const float* x, float* hi, float* lo, double* out, cudaStream_t st);
+cudaError_t assemble_u_pair_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const float* u_hi,
+                               const float* u_lo, const double* g, double* u_full, cudaStream_t st);
 cudaError_t flux_combine(long long n_nodes, int nsrc, const int* nbr, const double* flux, float* hcorr, int n_bdry,
                          const int* bdry_node, const double* g_given, const double* g_state, float* r_bdry,
                          cudaStream_t st);
@@ -1207,10 +1210,10 @@ int hps_residual_2d(const hps_residual2d_args* a, void* stream) {
   return HPS_OK;
 }
 
-int hps_residual_2d_df(const hps_residual2d_args* a, float* r_lo, void* stream) {
+int hps_residual_2d_df(const hps_residual2d_args* a, const float* u_int32, float* r_lo, void* stream) {
   if (!a || a->n_leaves <= 0 || a->p < 3 || a->q <= 0 || a->nsrc <= 0 || a->n_ops <= 0 ||
-      !a->coeffs || !a->inv_half || !a->D1 || !a->D2 || !a->Pside || !a->Qside || !a->perm || !a->u_int || !a->g ||
-      !a->r_int || !r_lo || !a->flux) {
+      !a->coeffs || !a->inv_half || !a->D1 || !a->D2 || !a->Pside || !a->Qside || !a->perm ||
+      (!a->u_int && !u_int32) || !a->g || !a->r_int || !r_lo || !a->flux) {
     set_error("hps_residual_2d_df: invalid arguments");
     return HPS_ERR_ARG;
   }
@@ -1223,7 +1226,26 @@ int hps_residual_2d_df(const hps_residual2d_args* a, float* r_lo, void* stream) 
   if (pack_op_kinds(a, &kinds, &need_uy) != HPS_OK) return HPS_ERR_ARG;
   HPS_CHECK(residual_2d(a->n_leaves, a->p, a->q, a->nsrc, a->n_ops, kinds, a->coeffs, a->inv_half, a->D1, a->D2,
                         a->Pside, a->Qside, a->perm, a->u_int, a->g, a->f, a->r_int, a->r_int64, r_lo, a->flux,
-                        a->u_full, need_uy, (cudaStream_t)stream));
+                        a->u_full, need_uy, (cudaStream_t)stream, u_int32));
+  return HPS_OK;
+}
+
+int hps_accumulate_max_df(long long n, const float* x, float* y_hi, float* y_lo, double* out, void* stream) {
+  if (n < 0 || n % 4 || !x || !y_hi || !y_lo || !out) {
+    set_error("hps_accumulate_max_df: invalid arguments (n a multiple of 4, 16-byte aligned arrays)");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(accumulate_pair_max(n, x, y_hi, y_lo, out, (cudaStream_t)stream));
+  return HPS_OK;
+}
+
+int hps_assemble_u_2d_df(int n_leaves, int p, int q, int nsrc, const double* Pside, const float* u_hi,
+                         const float* u_lo, const double* g, double* u_full, void* stream) {
+  if (n_leaves <= 0 || p < 3 || q <= 0 || nsrc <= 0 || !Pside || !u_hi || !u_lo || !g || !u_full) {
+    set_error("hps_assemble_u_2d_df: invalid arguments");
+    return HPS_ERR_ARG;
+  }
+  HPS_CHECK(assemble_u_pair_2d(n_leaves, p, q, nsrc, Pside, u_hi, u_lo, g, u_full, (cudaStream_t)stream));
   return HPS_OK;
 }
 

@@ -35,7 +35,7 @@ residual_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lon
                    const double* __restrict__ Pside_g, const double* __restrict__ Qside_g,
                    const int* __restrict__ perm_g, const double* __restrict__ u_int,
                    const double* __restrict__ g, const double* __restrict__ f, float* r_int, double* r_int64,
-                   float* r_lo, double* flux, double* u_full, int need_uy) {
+                   float* r_lo, double* flux, double* u_full, int need_uy, const float* __restrict__ u_int32) {
   extern __shared__ double sm[];
   const int pp = p * p;
   const int ncb = 4 * (p - 1);
@@ -77,7 +77,8 @@ residual_2d_kernel(int n_leaves, int p, int q, int nsrc, int n_ops, unsigned lon
   // interior values
   for (int e = tid; e < ni * RES_SC; e += RES_NT) {
     const int i = e / RES_SC, s = e % RES_SC;
-    u[perm[ncb + i] * RES_SC + s] = (s < sc) ? u_int[(l * ni + i) * nsrc + s0 + s] : 0.0;
+    const long long o = (l * ni + i) * nsrc + s0 + s;
+    u[perm[ncb + i] * RES_SC + s] = (s < sc) ? (u_int32 ? (double)u_int32[o] : u_int[o]) : 0.0;
   }
   // Chebyshev boundary values u_b = P g: side t-th point interpolated from
   // the side's q Gauss values; the four corners average their two sides
@@ -207,7 +208,7 @@ cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigne
                         const double* inv_half, const double* D1, const double* D2, const double* Pside,
                         const double* Qside, const int* perm, const double* u_int, const double* g,
                         const double* f, float* r_int, double* r_int64, float* r_lo, double* flux, double* u_full,
-                        int need_uy, cudaStream_t st) {
+                        int need_uy, cudaStream_t st, const float* u_int32) {
   const size_t smem = residual_2d_smem(p, q, need_uy);
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(residual_2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -219,7 +220,7 @@ cudaError_t residual_2d(int n_leaves, int p, int q, int nsrc, int n_ops, unsigne
   note_launch();
   residual_2d_kernel<<<grid, RES_NT, smem, st>>>(n_leaves, p, q, nsrc, n_ops, kinds, coeffs, inv_half, D1, D2,
                                                  Pside, Qside, perm, u_int, g, f, r_int, r_int64, r_lo, flux,
-                                                 u_full, need_uy);
+                                                 u_full, need_uy, u_int32);
   return cudaGetLastError();
 }
 

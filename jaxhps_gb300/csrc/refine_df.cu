@@ -477,4 +477,110 @@ cudaError_t jx_df_update_2d(int n_leaves, int p, int q, int nsrc, int n_ops, uns
   return cudaErrorInvalidValue;
 }
 
+// ---------------------------------------------------------------------------
+// The refined solution's interior values as an FP32 pair (hi, lo): the
+// corrections are accumulated by TwoSum on the FP32 pipe (the FP64 version
+// spends its time on the 1/64-rate FP64 add and conversion), with the
+// convergence maxima max |dx| and max |x| (of hi) as integer bit patterns.
+// ---------------------------------------------------------------------------
+__global__ void accumulate_pair_max_kernel(long long n, const float4* __restrict__ x, float4* hi, float4* lo,
+                                           unsigned long long* out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ unsigned int sx[32], sy[32];
+  unsigned int bx = 0, by = 0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += stride) {
+    const float4 d = x[e];
+    float4 h = hi[e], l = lo[e];
+    const float dv[4] = {d.x, d.y, d.z, d.w};
+    float hv[4] = {h.x, h.y, h.z, h.w}, lv[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float t = hv[j] + dv[j];
+      const float bb = t - hv[j];
+      const float err = (hv[j] - (t - bb)) + (dv[j] - bb);
+      const df32 r = df_norm(t, lv[j] + err);
+      hv[j] = r.hi;
+      lv[j] = r.lo;
+      bx = max(bx, __float_as_uint(dv[j]) & 0x7fffffffu);
+      by = max(by, __float_as_uint(r.hi) & 0x7fffffffu);
+    }
+    hi[e] = make_float4(hv[0], hv[1], hv[2], hv[3]);
+    lo[e] = make_float4(lv[0], lv[1], lv[2], lv[3]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    bx = max(bx, __shfl_xor_sync(0xffffffffu, bx, o));
+    by = max(by, __shfl_xor_sync(0xffffffffu, by, o));
+  }
+  if (lane == 0) {
+    sx[warp] = bx;
+    sy[warp] = by;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int ax = sx[0], ay = sy[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      ax = max(ax, sx[w]);
+      ay = max(ay, sy[w]);
+    }
+    // as FP64 bit patterns, the layout the FP64 version reports
+    atomicMax(out, (unsigned long long)__double_as_longlong((double)__uint_as_float(ax)));
+    atomicMax(out + 1, (unsigned long long)__double_as_longlong((double)__uint_as_float(ay)));
+  }
+}
+
+cudaError_t accumulate_pair_max(long long n, const float* x, float* hi, float* lo, double* out, cudaStream_t st) {
+  if (n % 4 || (reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(hi) | reinterpret_cast<uintptr_t>(lo)) & 15)
+    return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(out, 0, 2 * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  long long g = (n / 4 + 255) / 256;
+  if (g > 8192) g = 8192;
+  if (g < 1) g = 1;
+  ProfScope ps(KC_MOVE, st, 20.0 * (double)n);
+  note_launch();
+  accumulate_pair_max_kernel<<<(int)g, 256, 0, st>>>(n / 4, reinterpret_cast<const float4*>(x),
+                                                     reinterpret_cast<float4*>(hi), reinterpret_cast<float4*>(lo),
+                                                     reinterpret_cast<unsigned long long*>(out));
+  return cudaGetLastError();
+}
+
+// u_full[l][k] = (P g)[k] on the Chebyshev boundary and hi + lo on the
+// interior (FP64), exterior-first leaf order
+__global__ void assemble_u_pair_2d_kernel(int n_leaves, int p, int q, int nsrc, const double* __restrict__ Pside,
+                                          const float* __restrict__ u_hi, const float* __restrict__ u_lo,
+                                          const double* __restrict__ g, double* u_full) {
+  const int pp = p * p, ncb = 4 * (p - 1), ni = pp - ncb, nq = 4 * q;
+  const long long l = blockIdx.x;
+  for (int e = threadIdx.x; e < pp * nsrc; e += blockDim.x) {
+    const int k = e / nsrc, s = e % nsrc;
+    double v;
+    if (k >= ncb) {
+      const long long o = (l * ni + (k - ncb)) * nsrc + s;
+      v = (double)u_hi[o] + (double)u_lo[o];
+    } else {
+      double acc = 0.0;
+      int cnt = 0;
+      for (int side = 0; side < 4; ++side) {
+        int t = k - side * (p - 1);
+        if (side == 3 && k == 0) t = p - 1;
+        if (t < 0 || t > p - 1) continue;
+        if (side == 3 && t == p - 1 && k != 0) continue;
+        for (int j = 0; j < q; ++j) acc = fma(Pside[t * q + j], g[(l * nq + side * q + j) * nsrc + s], acc);
+        ++cnt;
+      }
+      v = (cnt == 2) ? 0.5 * acc : acc;
+    }
+    u_full[(l * pp + k) * nsrc + s] = v;
+  }
+}
+
+cudaError_t assemble_u_pair_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const float* u_hi,
+                               const float* u_lo, const double* g, double* u_full, cudaStream_t st) {
+  ProfScope ps(KC_MOVE, st, 8.0 * n_leaves * (double)p * p * nsrc * 2.0);
+  note_launch();
+  assemble_u_pair_2d_kernel<<<n_leaves, 256, 0, st>>>(n_leaves, p, q, nsrc, Pside, u_hi, u_lo, g, u_full);
+  return cudaGetLastError();
+}
+
 }  // namespace hps

@@ -193,3 +193,24 @@ def test_solution_assembled_into_caller_buffers(cuda):
     assert hps.solve(pde, g, out=pageable) is pageable
     assert np.array_equal(pinned.numpy(), u_ref)
     assert np.array_equal(pageable.numpy(), u_ref)
+
+
+def test_pair_accumulator_matches_fp64(cuda):
+    """(hi, lo) += dx over several corrections of shrinking size equals the
+    FP64 sum to double-float rounding; the maxima are max |dx| and max |x|."""
+    from jaxhps_gb300 import _native as nat
+
+    rng = np.random.default_rng(12)
+    n = 4 * 12345
+    hi = torch.zeros(n, dtype=torch.float32, device=cuda)
+    lo = torch.zeros_like(hi)
+    ref = np.zeros(n)
+    out = torch.empty(2, dtype=torch.float64, device=cuda)
+    for k in range(5):
+        dx = (rng.standard_normal(n) * 10.0 ** (-3 * k)).astype(np.float32)
+        mx, my = nat.accumulate_max_df(torch.as_tensor(dx, device=cuda), hi, lo, out)
+        ref += dx.astype(np.float64)
+        assert mx == float(np.abs(dx).max())
+        assert abs(my - np.abs(ref).max()) <= 1e-6 * np.abs(ref).max()
+    got = hi.double().cpu().numpy() + lo.double().cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-14 * np.abs(ref).max()
