@@ -5,6 +5,8 @@ direct solver with the public API of meliao/jaxhps:
     PDEProblem, build_solver, solve, solve_subtree, upward_pass_subtree,
     downward_pass_subtree
 
+plus ``save_solver`` / ``load_solver`` (the built operator set as one file).
+
 The leaf solves, merges and down pass run as hand-written sm_103a CUDA
 kernels behind a C ABI (include/jaxhps_gb300.h); host code here only builds
 the small FP64 operators, the index maps and the device buffers.
@@ -23,6 +25,7 @@ from ._pdeproblem import PDEProblem
 from ._build_solver import build_solver
 from ._solve import solve
 from ._subtree import downward_pass_subtree, solve_subtree, upward_pass_subtree
+from ._checkpoint import load_solver, save_solver
 
 
 def local_solve_chunksize_2D(p: int, dtype=None) -> int:
@@ -50,6 +53,8 @@ __all__ = [
     "solve_subtree",
     "upward_pass_subtree",
     "downward_pass_subtree",
+    "save_solver",
+    "load_solver",
     "local_solve_chunksize_2D",
     "local_solve_chunksize_3D",
 ]

@@ -15,6 +15,7 @@ from __future__ import annotations
 import torch
 
 from . import _native as nat
+from . import _phases as phases
 from . import _stages as st
 from ._discretization_tree import DiscretizationNode2D
 
@@ -37,6 +38,7 @@ def build_solver(pde_problem, return_top_T: bool = False, compute_device=None, h
     return out
 
 
+@phases.ranged("build_solver")
 def _build(pde_problem, return_top_T, compute_device, precision, **refine_kw):
     dom = pde_problem.domain
     if precision == "mixed":

@@ -3,12 +3,26 @@ solve (coefficient upload, build, boundary upload, refinement, result copy),
 for reports of where an end-to-end call spends its time.  Disabled unless a
 caller enables it; when enabled each mark records one event on the current
 stream (no synchronisation), and copies on side streams record their own
-start/end pair.  No counterpart in the reference.
+start/end pair.
+
+Optional NVTX ranges around the stages (``build_solver``, ``solve``, the
+leaf stage, each merge and down-pass level, each refinement correction), so
+a profiler's timeline and its range filters name them.  Off unless the
+environment sets ``HPS_NVTX=1`` or a caller calls ``enable_nvtx()``: a
+profiler filter on an enclosing range of the caller's own then sees the
+same range stack as without them.  No counterpart in the reference (its
+examples time whole calls with ``timeit``).
 """
 
 from __future__ import annotations
 
+import contextlib
+import functools
+import os
+
 import torch
+
+_nvtx = os.environ.get("HPS_NVTX", "0") not in ("", "0")
 
 _marks = None
 _side = None
@@ -56,3 +70,36 @@ def collect() -> dict:
         out[name + " (side stream)"] = out.get(name + " (side stream)", 0.0) + a.elapsed_time(b)
     _marks, _side = [], []
     return out
+
+
+def enable_nvtx(on: bool = True) -> None:
+    global _nvtx
+    _nvtx = bool(on)
+
+
+def nvtx_enabled() -> bool:
+    return _nvtx
+
+
+@contextlib.contextmanager
+def nvtx(name: str):
+    """An NVTX push/pop range named ``name`` around the body, when enabled."""
+    if not _nvtx:
+        yield
+        return
+    torch.cuda.nvtx.range_push(name)
+    try:
+        yield
+    finally:
+        torch.cuda.nvtx.range_pop()
+
+
+def ranged(name: str):
+    """Decorator: the function's calls run inside ``nvtx(name)``."""
+    def deco(fn):
+        @functools.wraps(fn)
+        def wrapper(*args, **kwargs):
+            with nvtx(name):
+                return fn(*args, **kwargs)
+        return wrapper
+    return deco

@@ -300,6 +300,7 @@ def _res_args(state: MixedState, u_int, g, r32, flux, r64=None, u_full=None, zer
     return a
 
 
+@phases.ranged("FP64 residual")
 def _residual(state: MixedState, u_int, g, r32, flux, u_full=None, zero_source=False, r64=None, r_lo=None,
               u32=None):
     """FP64 residual of the discrete system at (u_int, g); zero_source drops f.
@@ -332,6 +333,7 @@ def _df_prepare(a) -> torch.Tensor:
     return prep
 
 
+@phases.ranged("pair residual update")
 def _residual_update_df(state: MixedState, prep, du, dg, r_lo, r32, flux):
     """(r32, r_lo) -= (A du)_int as an FP32 pair, flux += Q du_full
     (double-float arithmetic, one grid line per thread); ``prep`` from
@@ -341,6 +343,7 @@ def _residual_update_df(state: MixedState, prep, du, dg, r_lo, r32, flux):
                                                   r_lo.data_ptr(), nat.stream_ptr()), "hps_residual_update_2d_df")
 
 
+@phases.ranged("correction (FP32 operators)")
 def correction(state: MixedState, r32, hcorr, rb32):
     """dx = M r with the FP32 operators: returns (du_int, dg) in FP32."""
     v = torch.empty_like(r32)

@@ -38,6 +38,7 @@ def solve(pde_problem, boundary_data, source=None, compute_device=None, host_dev
     return res
 
 
+@phases.ranged("solve")
 def _solve(pde_problem, boundary_data, source, compute_device, host_device, **refine_kw):
     dom = pde_problem.domain
     state = getattr(pde_problem, "_state", None)

@@ -168,6 +168,7 @@ def local_solve_stage_uniform_2D_DtN(pde_problem, host_device=None, device=None,
     return _local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, device, dtype, keep_inverse)
 
 
+@phases.ranged("leaf solve (DtN)")
 def _local_solve_dtn(pde_problem, P_np, Q_np, device, dtype, keep_inverse, source=None, want_source=True,
                      coefficients=None):
     """``coefficients`` = (ops, coeffs, is_complex) overrides the problem's own
@@ -247,6 +248,7 @@ def local_solve_stage_uniform_3D_DtN(pde_problem, host_device=None, device=None,
     return _local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, device, dtype, keep_inverse)
 
 
+@phases.ranged("leaf solve (ItI)")
 def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None, dtype=torch.complex128,
                                      keep_inverse: bool = False):
     """Leaf ItI solve (reference local_solve/_uniform_2D_ItI.py:10-186).
@@ -322,6 +324,7 @@ def raise_on_sync_timeout(infos) -> None:
     check_infos(infos, "merge inverse")
 
 
+@phases.ranged("merge level")
 def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False, keep_BD_inv=False,
                     keep_B=False, iti=False, need_T=True, infos=None):
     """One batched merge level.  T_children: (n_merges*nch, nb, nb);
@@ -373,6 +376,7 @@ def merge_level_dtn(T_children: torch.Tensor, h_children, maps, keep_D_inv=False
     return S, g_t, T_out, h_out, D_inv, BD_inv
 
 
+@phases.ranged("up level")
 def up_level(h_children, D_inv, B, maps, b_is_bd_inv: bool = False, iti: bool = False):
     """One up-pass level with stored D_inv and B, or B D_inv with
     ``b_is_bd_inv`` (reference up_pass/_uniform_2D_DtN.py:8-173,
@@ -451,6 +455,7 @@ def merge_stage_uniform_2D_DtN(T_arr, h_arr, l: int, device=None, host_device=No
 # ---------------------------------------------------------------------------
 
 
+@phases.ranged("down level")
 def down_level(S, g_tilde, g_parent, maps):
     """One level of boundary-data propagation (n_merges parents -> nch*n_merges children)."""
     L = nat.lib()
