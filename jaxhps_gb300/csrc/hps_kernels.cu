@@ -51,8 +51,12 @@ __global__ void leaf_assemble_kernel(int n_leaves, int n_pts, int row0, int col_
     if (staged) {
       float2* dp = reinterpret_cast<float2*>(ds_smem);   // operator rows as pairs, [n_ops][n_pts]
       float2* cp = dp + (size_t)n_ops * n_pts;            // coefficient pairs, [leaf in group][n_ops]
+      int* nzc = reinterpret_cast<int*>(cp + (size_t)leaves_per_cta * n_ops);   // nonzero columns
+      unsigned char* nzf = reinterpret_cast<unsigned char*>(nzc + n_pts);        // column flags
+      __shared__ int nnz_s;
       const int l0 = l_base + blockIdx.y * leaves_per_cta;
       const int l1 = min(n_leaves, l0 + leaves_per_cta);
+      if (threadIdx.x == 0) nnz_s = 0;
       for (int e = threadIdx.x; e < n_ops * n_pts; e += blockDim.x) {
         const int o = e / n_pts, j = e % n_pts;
         dp[e] = split_pair(ops[((long long)o * n_pts + row) * n_pts + j]);
@@ -62,29 +66,46 @@ __global__ void leaf_assemble_kernel(int n_leaves, int n_pts, int row0, int col_
         cp[e] = split_pair(coeffs[((long long)o * n_leaves + l0 + ll) * n_pts + row]);
       }
       __syncthreads();
-      for (int l = l0; l < l1; ++l) {
-        const float2* cl = cp + (size_t)(l - l0) * n_ops;
-        for (int j = threadIdx.x; j < n_pts; j += blockDim.x) {
-          float sh = 0.f, se = 0.f;
-          for (int o = 0; o < n_ops; ++o) {
-            const float2 c = cl[o], d = dp[o * n_pts + j];
-            const float pr = c.x * d.x;
-            float pe = fmaf(c.x, d.x, -pr);
-            pe = fmaf(c.x, d.y, pe);
-            pe = fmaf(c.y, d.x, pe);
-            const float t = sh + pr;
-            const float bb = t - sh;
-            const float err = (sh - (t - bb)) + (pr - bb);
-            sh = t;
-            se += err + pe;
-          }
-          const float r = sh + se;
-          T v;
-          if constexpr (std::is_same<T, float>::value) v = r;
-          else v = c64{r, 0.f};
-          if (j < col_split) out_lo[l * s_lo + (long long)i * ld_lo + j] = v;
-          else out_hi[l * s_hi + (long long)i * ld_hi + (j - col_split)] = v;
+      // The operators are differentiation matrices on a tensor grid: a row of
+      // D_xx or D_yy is nonzero only on the row's own grid lines, so most
+      // entries of the sum are exact zeros.  Those are stored directly; the
+      // nonzero columns (a zero FP32 head means a zero pair) are listed once
+      // and their sums spread over all threads of the CTA.
+      for (int j = threadIdx.x; j < n_pts; j += blockDim.x) {
+        bool nz = false;
+        for (int o = 0; o < n_ops; ++o) nz |= dp[o * n_pts + j].x != 0.f;
+        nzf[j] = nz;
+        if (nz) nzc[atomicAdd(&nnz_s, 1)] = j;
+      }
+      __syncthreads();
+      const int nnz = nnz_s;
+      auto store = [&](int l, int j, float r) {
+        T v;
+        if constexpr (std::is_same<T, float>::value) v = r;
+        else v = c64{r, 0.f};
+        if (j < col_split) out_lo[l * s_lo + (long long)i * ld_lo + j] = v;
+        else out_hi[l * s_hi + (long long)i * ld_hi + (j - col_split)] = v;
+      };
+      for (int l = l0; l < l1; ++l)
+        for (int j = threadIdx.x; j < n_pts; j += blockDim.x)
+          if (!nzf[j]) store(l, j, 0.f);
+      for (int w = threadIdx.x; w < (l1 - l0) * nnz; w += blockDim.x) {
+        const int ll = w / nnz, j = nzc[w - ll * nnz];
+        const float2* cl = cp + (size_t)ll * n_ops;
+        float sh = 0.f, se = 0.f;
+        for (int o = 0; o < n_ops; ++o) {
+          const float2 c = cl[o], d = dp[o * n_pts + j];
+          const float pr = c.x * d.x;
+          float pe = fmaf(c.x, d.x, -pr);
+          pe = fmaf(c.x, d.y, pe);
+          pe = fmaf(c.y, d.x, pe);
+          const float t = sh + pr;
+          const float bb = t - sh;
+          const float err = (sh - (t - bb)) + (pr - bb);
+          sh = t;
+          se += err + pe;
         }
+        store(l0 + ll, j, sh + se);
       }
       return;
     }
@@ -137,7 +158,8 @@ cudaError_t leaf_assemble(int n_leaves, int n_pts, int row0, int n_rows, int col
                           T* out_hi, long long ld_hi, long long s_hi, cudaStream_t st) {
   const int lpc = 32;
   size_t smem = sizeof(double) * (size_t)n_ops * n_pts;
-  if (assemble_in_pairs<T, CT>()) smem += sizeof(float2) * (size_t)lpc * n_ops;   // coefficient pairs
+  // coefficient pairs, the nonzero-column list and the column flags
+  if (assemble_in_pairs<T, CT>()) smem += sizeof(float2) * (size_t)lpc * n_ops + (sizeof(int) + 1) * (size_t)n_pts;
   const int staged = smem <= 200 * 1024;
   if (!staged) smem = 0;
   if (smem > 48 * 1024)
@@ -351,6 +373,16 @@ cudaError_t add_identity(int batch, int n, T* X, long long sX, cudaStream_t st) 
 //   Tout[e][f] = T_c[e][f] if e, f on the same child else 0   (the A blocks)
 //   dh[i]    = sum of the two children's h at i,   hext[e] = h_c(e)[e]
 // ---------------------------------------------------------------------------
+// Rows are handled by groups of gw lanes (gw = the column count rounded up to
+// a power of two, at most 32; several short rows share a warp): each group
+// looks up its row's child and local index once and strides over the
+// columns, so no element pays a division for its (row, column) pair.
+__device__ __forceinline__ int row_group_width(int cols) {
+  int w = 1;
+  while (w < cols && w < 32) w <<= 1;
+  return w;
+}
+
 template <class T>
 __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int ns, const T* __restrict__ Tc,
                                     const T* __restrict__ hc, const int* __restrict__ int_c,
@@ -362,64 +394,78 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
   const long long nbb = (long long)nb * nb;
   const T* Tm = Tc ? Tc + m * nch * nbb : nullptr;
   const T* hm = hc ? hc + m * nch * (long long)nb * ns : nullptr;
-  long long cnt;
+  int rows, cols;
   switch (seg) {
-    case 0: cnt = Tm ? (long long)n_int * n_int : 0; break;
-    case 1: cnt = Tm ? (long long)n_int * n_ext : 0; break;
-    case 2: cnt = Tm ? (long long)n_ext * n_int : 0; break;
-    case 3: cnt = (Tm && Tout) ? (long long)n_ext * n_ext : 0; break;
-    case 4: cnt = hm ? (long long)n_int * ns : 0; break;
-    default: cnt = hm ? (long long)n_ext * ns : 0; break;
+    case 0: rows = Tm ? n_int : 0; cols = n_int; break;
+    case 1: rows = Tm ? n_int : 0; cols = n_ext; break;
+    case 2: rows = Tm ? n_ext : 0; cols = n_int; break;
+    case 3: rows = (Tm && Tout) ? n_ext : 0; cols = n_ext; break;
+    case 4: rows = hm ? n_int : 0; cols = ns; break;
+    default: rows = hm ? n_ext : 0; cols = ns; break;
   }
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt;
-       e += (long long)gridDim.x * blockDim.x) {
-    T v = zero<T>();
+  const int gw = row_group_width(cols);
+  const int lane = threadIdx.x & 31, gl = lane & (gw - 1);
+  const int groups = (blockDim.x >> 5) * (32 / gw);
+  const int g = (threadIdx.x >> 5) * (32 / gw) + lane / gw;
+  for (int r = blockIdx.x * groups + g; r < rows; r += gridDim.x * groups) {
+    const long long o = (long long)r * cols;
     if (seg == 0) {
-      const int i = (int)(e / n_int), j = (int)(e % n_int);
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        const int c = int_c[2 * i + t];
-        if (c < 0) continue;
-        const int lj = loc[c * n_int + j];
-        if (lj >= 0) v = add(v, Tm[c * nbb + (long long)int_l[2 * i + t] * nb + lj]);
+      const int c0 = int_c[2 * r], c1 = int_c[2 * r + 1];
+      const T* t0 = c0 >= 0 ? Tm + c0 * nbb + (long long)int_l[2 * r] * nb : nullptr;
+      const T* t1 = c1 >= 0 ? Tm + c1 * nbb + (long long)int_l[2 * r + 1] * nb : nullptr;
+      const int* loc0 = loc + (c0 >= 0 ? c0 : 0) * n_int;
+      const int* loc1 = loc + (c1 >= 0 ? c1 : 0) * n_int;
+      T* out = D + m * n_int * (long long)n_int + o;
+      for (int j = gl; j < cols; j += gw) {
+        T v = zero<T>();
+        if (t0) { const int lj = loc0[j]; if (lj >= 0) v = add(v, t0[lj]); }
+        if (t1) { const int lj = loc1[j]; if (lj >= 0) v = add(v, t1[lj]); }
+        out[j] = v;
       }
-      D[m * n_int * (long long)n_int + e] = v;
     } else if (seg == 1) {
-      const int i = (int)(e / n_ext), x = (int)(e % n_ext);
-      const int c = ext_c[x];
-      const int li = loc[c * n_int + i];
-      if (li >= 0) v = Tm[c * nbb + (long long)li * nb + ext_l[x]];
-      if (li >= 0 || !(skip_zero & 1)) C[m * n_int * (long long)n_ext + e] = v;
-    } else if (seg == 2) {
-      const int x = (int)(e / n_int), j = (int)(e % n_int);
-      const int c = ext_c[x];
-      const int lj = loc[c * n_int + j];
-      if (lj >= 0) v = Tm[c * nbb + (long long)ext_l[x] * nb + lj];
-      if (lj >= 0 || !(skip_zero & 2)) B[m * n_ext * (long long)n_int + e] = v;
-    } else if (seg == 3) {
-      const int x = (int)(e / n_ext), y = (int)(e % n_ext);
-      const int c = ext_c[x];
-      if (ext_c[y] == c) v = Tm[c * nbb + (long long)ext_l[x] * nb + ext_l[y]];
-      Tout[m * n_ext * (long long)n_ext + e] = v;
-    } else if (seg == 4) {
-      const int i = (int)(e / ns), s = (int)(e % ns);
-#pragma unroll
-      for (int t = 0; t < 2; ++t) {
-        const int c = int_c[2 * i + t];
-        if (c < 0) continue;
-        v = add(v, hm[(c * (long long)nb + int_l[2 * i + t]) * ns + s]);
+      T* out = C + m * n_int * (long long)n_ext + o;
+      for (int x = gl; x < cols; x += gw) {
+        const int c = ext_c[x];
+        const int li = loc[c * n_int + r];
+        const T v = li >= 0 ? Tm[c * nbb + (long long)li * nb + ext_l[x]] : zero<T>();
+        if (li >= 0 || !(skip_zero & 1)) out[x] = v;
       }
-      dh[m * n_int * (long long)ns + e] = v;
+    } else if (seg == 2) {
+      const int c = ext_c[r];
+      const T* t = Tm + c * nbb + (long long)ext_l[r] * nb;
+      const int* lc = loc + c * n_int;
+      T* out = B + m * n_ext * (long long)n_int + o;
+      for (int j = gl; j < cols; j += gw) {
+        const int lj = lc[j];
+        if (lj >= 0) out[j] = t[lj];
+        else if (!(skip_zero & 2)) out[j] = zero<T>();
+      }
+    } else if (seg == 3) {
+      const int c = ext_c[r];
+      const T* t = Tm + c * nbb + (long long)ext_l[r] * nb;
+      T* out = Tout + m * n_ext * (long long)n_ext + o;
+      for (int y = gl; y < cols; y += gw) out[y] = ext_c[y] == c ? t[ext_l[y]] : zero<T>();
+    } else if (seg == 4) {
+      const int c0 = int_c[2 * r], c1 = int_c[2 * r + 1];
+      const T* h0 = c0 >= 0 ? hm + (c0 * (long long)nb + int_l[2 * r]) * ns : nullptr;
+      const T* h1 = c1 >= 0 ? hm + (c1 * (long long)nb + int_l[2 * r + 1]) * ns : nullptr;
+      T* out = dh + m * n_int * (long long)ns + o;
+      for (int s = gl; s < cols; s += gw) {
+        T v = zero<T>();
+        if (h0) v = add(v, h0[s]);
+        if (h1) v = add(v, h1[s]);
+        out[s] = v;
+      }
     } else {
-      const int x = (int)(e / ns), s = (int)(e % ns);
-      v = hm[(ext_c[x] * (long long)nb + ext_l[x]) * ns + s];
-      hext[m * n_ext * (long long)ns + e] = v;
+      const T* h = hm + (ext_c[r] * (long long)nb + ext_l[r]) * ns;
+      T* out = hext + m * n_ext * (long long)ns + o;
+      for (int s = gl; s < cols; s += gw) out[s] = h[s];
     }
   }
 }
 
-// Launch geometry of the merge gathers and the down-pass scatter: x blocks of
-// 256 threads over the largest segment of one merge.  When the launch would
+// Launch geometry of the ItI merge gather: x blocks of 256 threads over the
+// largest segment of one merge.  When the launch would
 // hold far more CTAs than the GPU runs at once (152 SMs x 8 CTAs of 256
 // threads), each thread takes about four elements (the kernels stride over
 // their segment): these segments are short, and with one element per thread
@@ -427,6 +473,21 @@ __global__ void merge_gather_kernel(int nch, int nb, int n_int, int n_ext, int n
 static int gather_blocks(long long big, long long ctas_per_x) {
   long long gx = (big + 255) / 256;
   if (gx * ctas_per_x > 16LL * 152 * 8) gx = (big + 1023) / 1024;
+  if (gx < 1) gx = 1;
+  if (gx > 512) gx = 512;
+  return (int)gx;
+}
+
+// Launch geometry of the row-wise gathers and the down-pass scatter: groups
+// of lanes per row as in the kernels (256 threads), one row per group; when
+// the launch would hold far more CTAs than the GPU runs at once each group
+// takes about four rows.
+static int row_blocks(long long rows, long long cols, long long ctas_per_x) {
+  long long gw = 1;
+  while (gw < cols && gw < 32) gw <<= 1;
+  const long long groups = 8 * (32 / gw);
+  long long gx = (rows + groups - 1) / groups;
+  if (gx * ctas_per_x > 16LL * 152 * 8) gx = (rows + 4 * groups - 1) / (4 * groups);
   if (gx < 1) gx = 1;
   if (gx > 512) gx = 512;
   return (int)gx;
@@ -461,9 +522,18 @@ cudaError_t merge_gather(int n_merges, int nch, int nb, int n_int, int n_ext, in
   long long big;
   gather_segments(Tc != nullptr, Tout != nullptr, hc != nullptr, n_int, n_ext, ns, &seg0, &nseg, &big);
   if (nseg == 0 || big == 0) return cudaSuccess;
+  // the row blocks of the widest segment launched (segments 0-3: the
+  // operator blocks, 4-5: h; rows x columns as in the kernel)
+  const long long seg_rows[6] = {n_int, n_int, n_ext, n_ext, n_int, n_ext};
+  const long long seg_cols[6] = {n_int, n_ext, n_int, n_ext, ns, ns};
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
-    const int gx = gather_blocks(big, (long long)nm * nseg);
+    int gx = 1;
+    for (int sg = seg0; sg < seg0 + nseg; ++sg) {
+      if (sg == 3 && !Tout) continue;
+      const int b = row_blocks(seg_rows[sg], seg_cols[sg], (long long)nm * nseg);
+      if (b > gx) gx = b;
+    }
     const double outs =
         Tc ? ((double)n_int * n_int + 2.0 * n_int * n_ext + (Tout ? (double)n_ext * n_ext : 0.0)) : 0.0;
     ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (outs + (hc ? (double)(n_int + n_ext) * ns : 0.0)));
@@ -590,26 +660,28 @@ __global__ void down_scatter_kernel(int nch, int nb, int n_ext, int n_int, int n
                                     const T* __restrict__ gpar, const T* __restrict__ gint, T* gch,
                                     long long m_base) {
   const long long m = blockIdx.y + m_base;
-  const long long cnt = (long long)nch * nb * ns;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int s = (int)(e % ns);
-    const int ck = (int)(e / ns);  // c*nb + k
-    const int cd = code[ck];
+  const int rows = nch * nb;   // child boundary points (c*nb + k)
+  const int gw = row_group_width(ns);
+  const int lane = threadIdx.x & 31, gl = lane & (gw - 1);
+  const int groups = (blockDim.x >> 5) * (32 / gw);
+  const int g = (threadIdx.x >> 5) * (32 / gw) + lane / gw;
+  for (int r = blockIdx.x * groups + g; r < rows; r += gridDim.x * groups) {
+    const int cd = code[r];
     // HPS_CODE_PAD marks padding slots of a child with fewer boundary points
-    const T v = (cd == HPS_CODE_PAD) ? zero<T>()
-                : (cd >= 0) ? gpar[(m * n_ext + cd) * ns + s] : gint[(m * n_int + (-cd - 1)) * ns + s];
-    gch[m * cnt + e] = v;
+    const T* src = (cd == HPS_CODE_PAD) ? nullptr
+                   : (cd >= 0) ? gpar + (m * n_ext + cd) * ns : gint + (m * n_int + (-cd - 1)) * ns;
+    T* out = gch + (m * rows + r) * (long long)ns;
+    for (int s = gl; s < ns; s += gw) out[s] = src ? src[s] : zero<T>();
   }
 }
 
 template <class T>
 cudaError_t down_scatter(int n_merges, int nch, int nb, int n_ext, int n_int, int ns, const int* code,
                          const T* gpar, const T* gint, T* gch, cudaStream_t st) {
-  long long cnt = (long long)nch * nb * ns;
+  const long long cnt = (long long)nch * nb * ns;
   for (int m0 = 0; m0 < n_merges; m0 += 65535) {
     const int nm = n_merges - m0 < 65535 ? n_merges - m0 : 65535;
-    const int gx = gather_blocks(cnt, nm);
+    const int gx = row_blocks((long long)nch * nb, ns, nm);
     ProfScope ps(KC_MOVE, st, 2.0 * sizeof(T) * nm * (double)cnt);
     note_launch();
     down_scatter_kernel<T><<<dim3(gx, nm), 256, 0, st>>>(nch, nb, n_ext, n_int, ns, code, gpar, gint, gch, m0);
