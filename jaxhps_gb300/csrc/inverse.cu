@@ -1234,14 +1234,14 @@ static cudaError_t inverse_batched_flat(int n, const T* A, long long lda, long l
 // interface blocks the recursive inversion ends at (and the n <= 128 merge
 // interfaces).  The matrix lives in registers (thread (ty, tx) of a 16 x 32
 // grid owns rows ty + 16 a, columns tx + 32 c); each of the n / 16 steps
-// publishes the 16-wide column and row blocks to shared memory, the CTA
-// inverts the 16 x 16 diagonal block (Gauss-Jordan with partial pivoting
-// inside the block, one element of [M_kk | I] per thread), forms the new row
-// block R = P M_k. and every
-// thread updates its elements:
+// publishes the 16-wide column and row blocks to shared memory, one warp
+// inverts the 16 x 16 diagonal block in registers (Gauss-Jordan with partial
+// pivoting inside the block, a column of [M_kk | I] per lane), the CTA forms
+// the new row block R = P M_k. and every thread updates its elements as an
+// outer product:
 //     M_ij -= M_ik R_kj,  M_kj = R_kj,  M_ik = -M_ik P,  M_kk = P.
 // Pivots are searched within the 16 x 16 blocks only (as in the recursion
-// above); a zero pivot sets info to its column (1-based).  Three barriers per
+// above); a zero pivot sets info to its column (1-based).  Six barriers per
 // 16 columns where the per-column kernels need one or two per column.
 // ---------------------------------------------------------------------------
 constexpr int B16_NT = 512, B16_TY = 16, B16_TX = 32, B16_B = 16, B16_NMAX = 128;
@@ -1253,9 +1253,8 @@ inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long 
   __shared__ float Cb[B16_NMAX][B16_B + 1];   // the step's column block (old values)
   __shared__ float Rk[B16_B][B16_NMAX + 1];   // the step's row block, then R = P M_k.
   __shared__ float Pk[B16_B][B16_B + 1];      // inverse of the diagonal block
-  __shared__ float Ag[2][B16_B][2 * B16_B + 1];   // [M_kk | I] under elimination, two copies
-  __shared__ int used_s[B16_B], rowof_s[B16_B], piv_s;
-  __shared__ float pinv_s;
+  __shared__ float Ag[1][B16_B][2 * B16_B + 1];   // [M_kk | I] after elimination
+  __shared__ int rowof_s[B16_B];
   __shared__ int s_info;
   const long long bb = blockIdx.x;
   const float* Ab = A + bb * sA;
@@ -1281,68 +1280,82 @@ inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long 
         if (j < n && i >= k0 && i < k0 + bs) Rk[i - k0][j] = m[a][c];
       }
     __syncthreads();
-    // (2) the diagonal block by Gauss-Jordan on [M_kk | I] with one element
-    // per thread (16 x 32 = 512), ping-ponging between two copies: per pivot,
-    // warp 0 picks the largest unused row of the column, then every thread
-    // forms its element of the next copy (two barriers per pivot, a short
-    // loop body)
-    {
-      const int r = tid >> 5, c = tid & 31;
-      float v0;
-      if (c < B16_B) v0 = (r < bs && c < bs) ? Cb[k0 + r][c] : (r == c ? 1.f : 0.f);
-      else v0 = (c - B16_B == r) ? 1.f : 0.f;
-      Ag[0][r][c] = v0;
-      if (tid < B16_B) used_s[tid] = 0;
-      __syncthreads();
+    // (2) the diagonal block by Gauss-Jordan on [M_kk | I] in warp 0: lane c
+    // holds column c of the 16 x 32 tableau in registers.  Per pivot, lane k
+    // scans its column for the largest unused row (the lowest such row on
+    // ties, a NaN taken as the largest) and every lane takes the pivot, the
+    // column-k factors and the pivot's reciprocal from lane k by shuffles,
+    // then eliminates its own column: no block barrier inside the 16 pivots.
+    if (warp == 0) {
+      float t[B16_B];
+#pragma unroll
+      for (int r = 0; r < B16_B; ++r) {
+        if (lane < B16_B) t[r] = (r < bs && lane < bs) ? Cb[k0 + r][lane] : (r == lane ? 1.f : 0.f);
+        else t[r] = (lane - B16_B == r) ? 1.f : 0.f;
+      }
+      unsigned used = 0;
 #pragma unroll 1
       for (int k = 0; k < B16_B; ++k) {
-        const int cur = k & 1;
-        if (warp == 0) {
-          float v = (lane < B16_B && !used_s[lane]) ? fabsf(Ag[cur][lane][k]) : -1.f;
-          if (v != v) v = INFINITY;   // a NaN pivot is taken (and poisons the result) rather than skipped
-          int who = lane;
+        float best = -1.f;
+        int who = 0;
 #pragma unroll
-          for (int off = 16; off; off >>= 1) {
-            const float ov = __shfl_xor_sync(0xffffffffu, v, off);
-            const int ow = __shfl_xor_sync(0xffffffffu, who, off);
-            if (ov > v || (ov == v && ow < who)) {
-              v = ov;
-              who = ow;
-            }
-          }
-          if (lane == 0) {
-            if (!(v > 0.f) && k < bs && s_info == 0) s_info = k0 + k + 1;
-            piv_s = who;
-            pinv_s = (v > 0.f) ? 1.f / Ag[cur][who][k] : 0.f;
-            used_s[who] = 1;
-            rowof_s[k] = who;
+        for (int r = 0; r < B16_B; ++r) {
+          float v = ((used >> r) & 1u) ? -1.f : fabsf(t[r]);
+          if (v != v) v = INFINITY;   // a NaN pivot is taken (and poisons the result) rather than skipped
+          if (v > best) {
+            best = v;
+            who = r;
           }
         }
-        __syncthreads();
-        const int pr = piv_s;
-        const float pinv = pinv_s;
-        const float pv = Ag[cur][pr][c] * pinv;
-        Ag[cur ^ 1][r][c] = (r == pr) ? pv : fmaf(-Ag[cur][r][k], pv, Ag[cur][r][c]);
-        __syncthreads();
+        best = __shfl_sync(0xffffffffu, best, k);
+        who = __shfl_sync(0xffffffffu, who, k);
+        float f[B16_B];
+#pragma unroll
+        for (int r = 0; r < B16_B; ++r) f[r] = __shfl_sync(0xffffffffu, t[r], k);
+        float prow = 0.f, fk = 0.f;   // this column's entry in the pivot row; column k's
+#pragma unroll
+        for (int r = 0; r < B16_B; ++r) {
+          prow = (r == who) ? t[r] : prow;
+          fk = (r == who) ? f[r] : fk;
+        }
+        const float pinv = (best > 0.f) ? 1.f / fk : 0.f;
+        const float pv = prow * pinv;
+#pragma unroll
+        for (int r = 0; r < B16_B; ++r) t[r] = (r == who) ? pv : fmaf(-f[r], pv, t[r]);
+        used |= 1u << who;
+        if (lane == 0) {
+          if (!(best > 0.f) && k < bs && s_info == 0) s_info = k0 + k + 1;
+          rowof_s[k] = who;
+        }
       }
-      // the pivot row of column k holds row k of the inverse (16 pivots: the
-      // result is in copy 0)
+#pragma unroll
+      for (int r = 0; r < B16_B; ++r) Ag[0][r][lane] = t[r];
+    }
+    __syncthreads();
+    {
+      // the pivot row of column k holds row k of the inverse
+      const int r = tid >> 5, c = tid & 31;
       if (r < bs && c < bs) Pk[r][c] = Ag[0][rowof_s[r]][B16_B + c];
     }
     __syncthreads();
     // (3) R = P M_k. into registers of the threads that own those columns:
     // thread (ty, tx) forms R[ty][j] for its columns j (bs <= 16 rows)
     float r_new[B16_RN];
+    {
+      float prow[B16_B];
 #pragma unroll
-    for (int c = 0; c < B16_RN; ++c) {
-      const int j = tx + B16_TX * c;
-      float acc = 0.f;
-      if (ty < bs && j < n) {
+      for (int d = 0; d < B16_B; ++d) prow[d] = (ty < bs && d < bs) ? Pk[ty][d] : 0.f;
 #pragma unroll
-        for (int d = 0; d < B16_B; ++d)
-          if (d < bs) acc = fmaf(Pk[ty][d], Rk[d][j], acc);
+      for (int c = 0; c < B16_RN; ++c) {
+        const int j = tx + B16_TX * c;
+        float acc = 0.f;
+        if (ty < bs && j < n) {
+#pragma unroll
+          for (int d = 0; d < B16_B; ++d)
+            if (d < bs) acc = fmaf(prow[d], Rk[d][j], acc);
+        }
+        r_new[c] = acc;
       }
-      r_new[c] = acc;
     }
     __syncthreads();
 #pragma unroll
@@ -1351,35 +1364,50 @@ inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long 
       if (ty < bs && j < n) Rk[ty][j] = r_new[c];
     }
     __syncthreads();
-    // (4) every element from the snapshots in shared memory
+    // (4) every element as an outer-product update from the snapshots in
+    // shared memory: per d, the 8 column-block values of this thread's rows
+    // and the 4 values of the new row block (or of P, in the block's own
+    // columns) of its columns, each loaded once:
+    //     rows outside the block:  M_ij = [j outside] M_ij - sum_d C_id R'_dj
+    //     rows inside the block:   M_ij = R'_(i-k0) j
+    // with R' = R outside the block's columns and P inside them.
 #pragma unroll
     for (int a = 0; a < B16_RM; ++a) {
       const int i = ty + B16_TY * a;
-      if (i >= n) continue;
       const bool ib = i >= k0 && i < k0 + bs;
-      float ci[B16_B];
-#pragma unroll
-      for (int d = 0; d < B16_B; ++d) ci[d] = (d < bs && !ib) ? Cb[i][d] : 0.f;
 #pragma unroll
       for (int c = 0; c < B16_RN; ++c) {
         const int j = tx + B16_TX * c;
-        if (j >= n) continue;
-        const bool jb = j >= k0 && j < k0 + bs;
-        float v;
-        if (ib) {
-          v = jb ? Pk[i - k0][j - k0] : Rk[i - k0][j];
-        } else if (jb) {
-          v = 0.f;
+        if (ib || (j >= k0 && j < k0 + bs)) m[a][c] = 0.f;
+      }
+    }
 #pragma unroll
-          for (int d = 0; d < B16_B; ++d)
-            if (d < bs) v = fmaf(-ci[d], Pk[d][j - k0], v);
-        } else {
-          v = m[a][c];
+    for (int d = 0; d < B16_B; ++d) {
+      if (d >= bs) break;
+      float cv[B16_RM], rv[B16_RN];
 #pragma unroll
-          for (int d = 0; d < B16_B; ++d)
-            if (d < bs) v = fmaf(-ci[d], Rk[d][j], v);
-        }
-        m[a][c] = v;
+      for (int a = 0; a < B16_RM; ++a) {
+        const int i = ty + B16_TY * a;
+        cv[a] = (i < n && !(i >= k0 && i < k0 + bs)) ? Cb[i][d] : 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < B16_RN; ++c) {
+        const int j = tx + B16_TX * c;
+        rv[c] = (j >= n) ? 0.f : (j >= k0 && j < k0 + bs) ? Pk[d][j - k0] : Rk[d][j];
+      }
+#pragma unroll
+      for (int a = 0; a < B16_RM; ++a)
+#pragma unroll
+        for (int c = 0; c < B16_RN; ++c) m[a][c] = fmaf(-cv[a], rv[c], m[a][c]);
+    }
+#pragma unroll
+    for (int a = 0; a < B16_RM; ++a) {
+      const int i = ty + B16_TY * a;
+      if (!(i >= k0 && i < k0 + bs)) continue;
+#pragma unroll
+      for (int c = 0; c < B16_RN; ++c) {
+        const int j = tx + B16_TX * c;
+        if (j < n) m[a][c] = (j >= k0 && j < k0 + bs) ? Pk[i - k0][j - k0] : Rk[i - k0][j];
       }
     }
     __syncthreads();   // the next step overwrites Cb, Rk and Pk

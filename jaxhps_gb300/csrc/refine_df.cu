@@ -546,40 +546,75 @@ cudaError_t accumulate_pair_max(long long n, const float* x, float* hi, float* l
 }
 
 // u_full[l][k] = (P g)[k] on the Chebyshev boundary and hi + lo on the
-// interior (FP64), exterior-first leaf order
-__global__ void assemble_u_pair_2d_kernel(int n_leaves, int p, int q, int nsrc, const double* __restrict__ Pside,
-                                          const float* __restrict__ u_hi, const float* __restrict__ u_lo,
-                                          const double* __restrict__ g, double* u_full) {
+// interior (FP64), exterior-first leaf order.  One CTA per leaf.  The
+// interior is the exact FP64 sum of the pair (contiguous, no index
+// arithmetic).  The boundary interpolation (q terms per side and point, two
+// sides at the corners) runs in double-float on the FP32 pipe: P's pairs are
+// staged once per CTA and the leaf's boundary data once per chunk of sc
+// right-hand sides, so each FP64 input is split once instead of once per
+// product (relative error about 2^-46 of sum |P||g|, against the FP64 pipe's
+// 1/64 rate for q multiply-adds per point).
+__global__ void assemble_u_pair_2d_kernel(int n_leaves, int p, int q, int nsrc, int sc,
+                                          const double* __restrict__ Pside, const float* __restrict__ u_hi,
+                                          const float* __restrict__ u_lo, const double* __restrict__ g,
+                                          double* u_full) {
+  extern __shared__ df32 au_smem[];
+  df32* Pp = au_smem;            // [p][q]
+  df32* gp = au_smem + p * q;    // [4q][sc]
   const int pp = p * p, ncb = 4 * (p - 1), ni = pp - ncb, nq = 4 * q;
   const long long l = blockIdx.x;
-  for (int e = threadIdx.x; e < pp * nsrc; e += blockDim.x) {
-    const int k = e / nsrc, s = e % nsrc;
-    double v;
-    if (k >= ncb) {
-      const long long o = (l * ni + (k - ncb)) * nsrc + s;
-      v = (double)u_hi[o] + (double)u_lo[o];
-    } else {
-      double acc = 0.0;
+  for (int e = threadIdx.x; e < p * q; e += blockDim.x) Pp[e] = df_split(Pside[e]);
+  {
+    const float* hl = u_hi + l * ni * (long long)nsrc;
+    const float* ll = u_lo + l * ni * (long long)nsrc;
+    double* out = u_full + (l * pp + ncb) * (long long)nsrc;
+    for (int e = threadIdx.x; e < ni * nsrc; e += blockDim.x) out[e] = (double)hl[e] + (double)ll[e];
+  }
+  for (int s0 = 0; s0 < nsrc; s0 += sc) {
+    const int ns = min(sc, nsrc - s0);
+    __syncthreads();   // P staged; the previous chunk's readers are done with gp
+    for (int e = threadIdx.x; e < nq * ns; e += blockDim.x) {
+      const int b = e / ns, s = e - b * ns;
+      gp[b * sc + s] = df_split(g[(l * nq + b) * nsrc + s0 + s]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ncb * ns; e += blockDim.x) {
+      const int k = e / ns, s = e - k * ns;
+      float sh = 0.f, se = 0.f;
       int cnt = 0;
       for (int side = 0; side < 4; ++side) {
         int t = k - side * (p - 1);
         if (side == 3 && k == 0) t = p - 1;
         if (t < 0 || t > p - 1) continue;
         if (side == 3 && t == p - 1 && k != 0) continue;
-        for (int j = 0; j < q; ++j) acc = fma(Pside[t * q + j], g[(l * nq + side * q + j) * nsrc + s], acc);
+        const df32* pr = Pp + t * q;
+        const df32* gc = gp + side * q * sc + s;
+        for (int j = 0; j < q; ++j) df_mac(sh, se, pr[j], gc[j * sc]);
         ++cnt;
       }
-      v = (cnt == 2) ? 0.5 * acc : acc;
+      const double v = df_join(sh, se);
+      u_full[(l * pp + k) * (long long)nsrc + s0 + s] = (cnt == 2) ? 0.5 * v : v;
     }
-    u_full[(l * pp + k) * nsrc + s] = v;
   }
 }
 
 cudaError_t assemble_u_pair_2d(int n_leaves, int p, int q, int nsrc, const double* Pside, const float* u_hi,
                                const float* u_lo, const double* g, double* u_full, cudaStream_t st) {
+  // right-hand sides per chunk: up to 32, fewer when P and the chunk's
+  // boundary data would not fit 160 KB of shared memory
+  const size_t budget = 160 * 1024, pbytes = sizeof(df32) * (size_t)p * q;
+  if (pbytes + sizeof(df32) * 4 * (size_t)q > budget) return cudaErrorNotSupported;
+  int sc = nsrc < 32 ? nsrc : 32;
+  while (sc > 1 && pbytes + sizeof(df32) * 4 * (size_t)q * sc > budget) sc >>= 1;
+  const size_t smem = pbytes + sizeof(df32) * 4 * (size_t)q * sc;
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(assemble_u_pair_2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   ProfScope ps(KC_MOVE, st, 8.0 * n_leaves * (double)p * p * nsrc * 2.0);
   note_launch();
-  assemble_u_pair_2d_kernel<<<n_leaves, 256, 0, st>>>(n_leaves, p, q, nsrc, Pside, u_hi, u_lo, g, u_full);
+  assemble_u_pair_2d_kernel<<<n_leaves, 256, smem, st>>>(n_leaves, p, q, nsrc, sc, Pside, u_hi, u_lo, g, u_full);
   return cudaGetLastError();
 }
 

@@ -214,3 +214,42 @@ def test_pair_accumulator_matches_fp64(cuda):
         assert abs(my - np.abs(ref).max()) <= 1e-6 * np.abs(ref).max()
     got = hi.double().cpu().numpy() + lo.double().cpu().numpy()
     assert np.abs(got - ref).max() <= 1e-14 * np.abs(ref).max()
+
+
+def _boundary_interp_ref(Pside, g, p, q):
+    """FP64 Chebyshev-boundary values of every leaf from its Gauss boundary
+    data: point k of the exterior-first order lies on one side (two at the
+    corners, averaged), side s holding points s(p-1) .. s(p-1)+p-1 (mod ncb)."""
+    ncb = 4 * (p - 1)
+    out = np.zeros((g.shape[0], ncb, g.shape[2]))
+    cnt = np.zeros(ncb)
+    for side in range(4):
+        for t in range(p):
+            k = (side * (p - 1) + t) % ncb
+            out[:, k] += np.einsum("j,ljs->ls", Pside[t], g[:, side * q:(side + 1) * q])
+            cnt[k] += 1
+    return out / cnt[None, :, None]
+
+
+@pytest.mark.parametrize("p,q,ns", [(16, 14, 64), (12, 10, 3), (7, 5, 40)])
+def test_pair_assembly_matches_fp64(cuda, p, q, ns):
+    """hps_assemble_u_2d_df: the interior is hi + lo exactly, the boundary the
+    FP64 interpolation of g to double-float accuracy (<= 1e-13 relative)."""
+    from jaxhps_gb300 import _native as nat
+
+    rng = np.random.default_rng(p * 100 + ns)
+    nl, ncb = 37, 4 * (p - 1)
+    ni = p * p - ncb
+    Pside = rng.standard_normal((p, q))
+    hi = rng.standard_normal((nl, ni, ns)).astype(np.float32)
+    lo = (rng.standard_normal((nl, ni, ns)) * 1e-8).astype(np.float32)
+    g = rng.standard_normal((nl, 4 * q, ns))
+    out = torch.full((nl, p * p, ns), float("nan"), dtype=torch.float64, device=cuda)
+    t = [torch.as_tensor(a, device=cuda) for a in (Pside, hi, lo, g)]
+    nat.check(nat.lib().hps_assemble_u_2d_df(nl, p, q, ns, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr(),
+                                             t[3].data_ptr(), out.data_ptr(), nat.stream_ptr()),
+              "hps_assemble_u_2d_df")
+    u = out.cpu().numpy()
+    assert np.array_equal(u[:, ncb:], hi.astype(np.float64) + lo.astype(np.float64))
+    ref = _boundary_interp_ref(Pside, g, p, q)
+    assert np.abs(u[:, :ncb] - ref).max() <= 1e-13 * np.abs(ref).max()
