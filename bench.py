@@ -685,7 +685,7 @@ BYTES_CLASSES = (3, 5, 6)
 # scaled by the number of leaves to L = 7 (the leaf kernels' traffic grows in
 # proportion), for the classes with one launch shape per step:
 # (workload, L, class) -> bytes
-NCU_TRAFFIC = {("poisson", 7, 4): 16 * 355.4e6, ("poisson", 7, 6): 16 * 453.6e6, ("poisson", 7, 7): 16 * 255.0e6}
+NCU_TRAFFIC = {("poisson", 7, 4): 16 * 281.2e6, ("poisson", 7, 6): 16 * 268.2e6, ("poisson", 7, 7): 16 * 254.9e6}
 
 
 def class_roofline(nat, c, v, step_ms, peaks, mhz, res_bytes, workload, L):
