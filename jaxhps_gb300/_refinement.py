@@ -214,6 +214,9 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     if cplx:
         raise NotImplementedError("mixed precision with complex coefficients is not implemented")
     names = [n for n in COEFF_NAMES_2D if getattr(pde_problem, f"{n}_coefficients") is not None]
+    # the interior columns of Q, on the device before the source upload starts
+    Q32 = st._device_copy(pde_problem, "Q_int", lambda: np.ascontiguousarray(pde_problem.Q[:, n_cb:]),
+                          torch.float32, dev)
     upload = st._SourceUpload(pde_problem.source, n_leaves, p * p, torch.float64, dev)
     Y, T, _, _, Aii = st._local_solve_dtn(pde_problem, pde_problem.P, pde_problem.Q, dev, leaf_dtype,
                                           keep_inverse=True, want_source=False,
@@ -221,9 +224,7 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
     Y, Aii = Y.float(), Aii.float()
     consts = _domain_constants(dom, dev)
     if leaf_refine and leaf_dtype == torch.float32:
-        T = _refine_leaf_operators(dom, coeffs, [OP_KIND_2D[n] for n in names], consts, Y, Aii,
-                                   torch.as_tensor(np.ascontiguousarray(pde_problem.Q[:, n_cb:]), device=dev,
-                                                   dtype=torch.float32))
+        T = _refine_leaf_operators(dom, coeffs, [OP_KIND_2D[n] for n in names], consts, Y, Aii, Q32)
     S_lst, Dinv_lst, B_lst, infos = [], [], [], []
     Tc = T.to(merge_dtype)
     n_levels = max(dom.L, 1)
@@ -242,7 +243,6 @@ def build_mixed(pde_problem, return_top_T=False, device=None, tol: float = 1e-12
 
     f, multi = upload.result()
 
-    Q32 = torch.as_tensor(np.ascontiguousarray(pde_problem.Q[:, n_cb:]), device=dev, dtype=torch.float32)
     state = MixedState(
         mixed=True, n_leaves=n_leaves, p=p, q=q, Y_int=Y[:, n_cb:, :], Aii_inv=Aii, Q_int=Q32, S_lst=S_lst,
         Dinv_lst=Dinv_lst, B_lst=B_lst, coeffs=coeffs, op_kind=[OP_KIND_2D[n] for n in names], f=f, multi=multi,

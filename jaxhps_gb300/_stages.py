@@ -19,6 +19,7 @@ import torch
 from . import _native as nat
 from . import _phases as phases
 from ._index_maps import colour_perm, merge_rects, quad_merge_maps_dtn
+from ._pdeproblem import COEFF_NAMES_2D, COEFF_NAMES_3D
 
 # Block-structured merge products (merge_rects); HPS_MERGE_RECTS=0 selects the
 # dense products.  ItI merges invert D through its two-colour structure
@@ -55,6 +56,22 @@ def _as_tensor(a, dtype, device) -> torch.Tensor:
         return a.to(device=device, dtype=dtype).contiguous()
     arr = np.asarray(a)
     return torch.as_tensor(np.ascontiguousarray(arr)).to(device=device, dtype=dtype)
+
+
+def _device_copy(owner, key: str, make, dtype, dev) -> torch.Tensor:
+    """Device copy of a small host operator that stays fixed over the life of
+    ``owner`` (a PDEProblem's P, Q, G, QH and differential operators), made
+    once per (key, dtype, device) and kept on the owner.  A build that reuses
+    them issues no pageable host-to-device copy: such a copy blocks the host
+    and queues behind an asynchronous source upload on the copy engine, so
+    the GPU would idle until that upload ends."""
+    cache = owner.__dict__.setdefault("_device_copies", {})
+    k = (key, str(dtype), str(dev))
+    t = cache.get(k)
+    if t is None:
+        t = _as_tensor(make(), dtype, dev)
+        cache[k] = t
+    return t
 
 
 def _is_complex(a) -> bool:
@@ -147,7 +164,9 @@ def _coefficients(pde_problem, dev):
     cplx = any(_is_complex(c) for c in cs)
     ctype = torch.complex128 if cplx else torch.float64
     coeffs = torch.stack([_as_tensor(c, ctype, dev) for c in cs]).contiguous()
-    ops_t = torch.as_tensor(np.stack(ops)).to(device=dev, dtype=torch.float64).contiguous()
+    names = tuple(n for n in (COEFF_NAMES_2D if pde_problem.domain.bool_2D else COEFF_NAMES_3D)
+                  if getattr(pde_problem, f"{n}_coefficients") is not None)
+    ops_t = _device_copy(pde_problem, "ops:" + ",".join(names), lambda: np.stack(ops), torch.float64, dev)
     phases.mark("coefficients_h2d")
     return ops_t, coeffs, cplx
 
@@ -183,8 +202,10 @@ def _local_solve_dtn(pde_problem, P_np, Q_np, device, dtype, keep_inverse, sourc
     ops_t, coeffs, cplx = _coefficients(pde_problem, dev) if coefficients is None else coefficients
     if cplx or _is_complex(pde_problem.source if source is None else source):
         dtype = REAL_TO_COMPLEX.get(dtype, dtype)
-    P = _as_tensor(P_np, dtype, dev)
-    Q = _as_tensor(Q_np, dtype, dev)
+    P = _device_copy(pde_problem, "P", lambda: P_np, dtype, dev) if P_np is pde_problem.P else \
+        _as_tensor(P_np, dtype, dev)
+    Q = _device_copy(pde_problem, "Q", lambda: Q_np, dtype, dev) if Q_np is pde_problem.Q else \
+        _as_tensor(Q_np, dtype, dev)
     src = pde_problem.source if source is None else source
     multi = False
     if want_source and src is not None:
@@ -263,9 +284,9 @@ def local_solve_stage_uniform_2D_ItI(pde_problem, host_device=None, device=None,
     n_cb, ng = P_np.shape
     ops_t, coeffs, cplx = _coefficients(pde_problem, dev)
     dtype = REAL_TO_COMPLEX.get(dtype, dtype)
-    P = _as_tensor(P_np, dtype, dev)
-    G = _as_tensor(pde_problem.G, dtype, dev)
-    QH = _as_tensor(pde_problem.QH, dtype, dev)
+    P = _device_copy(pde_problem, "P", lambda: P_np, dtype, dev)
+    G = _device_copy(pde_problem, "G", lambda: pde_problem.G, dtype, dev)
+    QH = _device_copy(pde_problem, "QH", lambda: pde_problem.QH, dtype, dev)
     multi = False
     if pde_problem.source is not None:
         f, multi = _src3(pde_problem.source, n_leaves, n_pts, dtype, dev)
