@@ -1294,40 +1294,59 @@ inv_block16_kernel(int n, const float* __restrict__ A, long long lda, long long 
         else t[r] = (lane - B16_B == r) ? 1.f : 0.f;
       }
       unsigned used = 0;
+      unsigned long long rows = 0;   // pivot row of step k in bits 4k .. 4k+3
+      int first_zero = -1;
 #pragma unroll 1
       for (int k = 0; k < B16_B; ++k) {
-        float best = -1.f;
-        int who = 0;
+        // largest unused |t| of the column, the lowest row on ties, as a
+        // tree (each merge keeps its lower half unless the upper is larger)
+        float bv[B16_B];
+        int bi[B16_B];
 #pragma unroll
         for (int r = 0; r < B16_B; ++r) {
           float v = ((used >> r) & 1u) ? -1.f : fabsf(t[r]);
           if (v != v) v = INFINITY;   // a NaN pivot is taken (and poisons the result) rather than skipped
-          if (v > best) {
-            best = v;
-            who = r;
-          }
+          bv[r] = v;
+          bi[r] = r;
         }
-        best = __shfl_sync(0xffffffffu, best, k);
-        who = __shfl_sync(0xffffffffu, who, k);
+#pragma unroll
+        for (int w = 1; w < B16_B; w <<= 1)
+#pragma unroll
+          for (int r = 0; r < B16_B; r += 2 * w)
+            if (bv[r + w] > bv[r]) {
+              bv[r] = bv[r + w];
+              bi[r] = bi[r + w];
+            }
+        const float best = __shfl_sync(0xffffffffu, bv[0], k);
+        const int who = __shfl_sync(0xffffffffu, bi[0], k);
         float f[B16_B];
 #pragma unroll
         for (int r = 0; r < B16_B; ++r) f[r] = __shfl_sync(0xffffffffu, t[r], k);
-        float prow = 0.f, fk = 0.f;   // this column's entry in the pivot row; column k's
+        // t[who] and f[who] by a multiplexer tree on the bits of who
+        float mt[B16_B / 2], mf[B16_B / 2];
 #pragma unroll
-        for (int r = 0; r < B16_B; ++r) {
-          prow = (r == who) ? t[r] : prow;
-          fk = (r == who) ? f[r] : fk;
+        for (int r = 0; r < B16_B / 2; ++r) {
+          mt[r] = (who & 1) ? t[2 * r + 1] : t[2 * r];
+          mf[r] = (who & 1) ? f[2 * r + 1] : f[2 * r];
         }
-        const float pinv = (best > 0.f) ? 1.f / fk : 0.f;
+#pragma unroll
+        for (int w = 2, bit = 2; w <= B16_B / 2; w <<= 1, bit <<= 1)
+#pragma unroll
+          for (int r = 0; r < B16_B / 2; r += w) {
+            mt[r] = (who & bit) ? mt[r + w / 2] : mt[r];
+            mf[r] = (who & bit) ? mf[r + w / 2] : mf[r];
+          }
+        const float prow = mt[0], fk = mf[0];   // this column's entry in the pivot row; column k's
+        const float pinv = (best > 0.f) ? __frcp_rn(fk) : 0.f;
         const float pv = prow * pinv;
 #pragma unroll
         for (int r = 0; r < B16_B; ++r) t[r] = (r == who) ? pv : fmaf(-f[r], pv, t[r]);
         used |= 1u << who;
-        if (lane == 0) {
-          if (!(best > 0.f) && k < bs && s_info == 0) s_info = k0 + k + 1;
-          rowof_s[k] = who;
-        }
+        rows |= (unsigned long long)who << (4 * k);
+        if (first_zero < 0 && !(best > 0.f) && k < bs) first_zero = k;
       }
+      if (lane < B16_B) rowof_s[lane] = (int)((rows >> (4 * lane)) & 15ull);
+      if (lane == 0 && first_zero >= 0 && s_info == 0) s_info = k0 + first_zero + 1;
 #pragma unroll
       for (int r = 0; r < B16_B; ++r) Ag[0][r][lane] = t[r];
     }
