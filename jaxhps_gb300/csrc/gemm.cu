@@ -667,12 +667,29 @@ cudaError_t gemm_batched(int M, int N, int K, T alpha, const T* A, long long lda
   }
   const int pol = gemm_policy();
   if constexpr (std::is_same<T, float>::value) {
-    // many small products with few right-hand-side columns (the leaf
-    // solves): the streaming TMA kernel, one persistent CTA per SM
-    if (pol == 1 && N > 8 && N <= 64 && (long long)((M + 127) / 128) * batch >= 4 * 152) {
+    // products with few right-hand-side columns (the leaf solves, the
+    // refinement's corrections at every level): the streaming TMA kernel, one
+    // persistent CTA per SM.  Measured against the autotuner's timings of the
+    // 2D workloads: it wins from M, K >= 128 and about 48 row tiles on; with
+    // K <= 64 or M < 128 (half-empty 128-row tiles) the SIMT tiles are faster,
+    // and with fewer row tiles K split over a cluster (below)
+    if (pol == 1 && N > 8 && N <= 64 && M >= 128 && K >= 128 && (long long)((M + 127) / 128) * batch >= 48) {
       const cudaError_t e = gemm_tma_f32(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd, sD, batch,
                                          st);
       if (e != cudaErrorNotSupported) return e;
+    }
+    // a wide product with fewer 64 x 64 output tiles than SMs (the top merge
+    // levels and the recursive inversion's blocks, one to four matrices):
+    // K split over the CTAs of a cluster fills the GPU where the tensor-core
+    // kernel's 128 x 128 tiles would leave most SMs idle (measured 2-3x)
+    if (pol == 1 && N > 64 && K >= 128) {
+      const long long t64 = (long long)((M + 63) / 64) * ((N + 63) / 64) * batch;
+      if (t64 < 152) {
+        int S = 8;
+        while (S > 2 && (t64 * S > 4 * 152 || K / S < 16)) S >>= 1;
+        return launch_gemm_f32_v4_split<64, 64>(M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, D, ldd,
+                                                sD, batch, S, st);
+      }
     }
     // measured: the tensor-core kernel wins once tiles are wide (N >= 128)
     // and have enough K-steps to amortise its pipeline prologue and epilogue;
