@@ -8,7 +8,9 @@ and index tables) as one file of raw tensors plus a manifest of the domain
 it was built on.  ``load_solver(pde_problem, path)`` puts that set back on
 a problem over the same domain, on the given device, after which ``solve``
 runs without a build.  A manifest that does not match the problem's domain
-(dimension, p, q, L, root bounds, ItI and eta) raises ValueError.
+(dimension, p, q, L, root bounds, ItI and eta) raises ValueError.  The file
+is a torch pickle (the refinement state is a dataclass): load only files
+written by a process you trust.
 
 The reference keeps its solver state on the ``PDEProblem`` object only
 (src/jaxhps/_pdeproblem.py:219-234) and has no save/load; its examples save
