@@ -311,3 +311,29 @@ def test_result_copy_into_caller_buffer():
         st._to_host(t, None, out=torch.zeros(2, 3, 5, dtype=torch.float64))
     with pytest.raises(ValueError):
         st._to_host(t, None, out=torch.zeros(2, 3, 4, dtype=torch.float32))
+
+
+def test_device_copies_of_fixed_operators_are_made_once():
+    """The build's copies of a problem's fixed host operators (P, Q, the
+    differential operators) are made once per (key, dtype, device) and
+    reused, so a rebuild issues no pageable host-to-device copy."""
+    import torch
+
+    from jaxhps_gb300 import _stages as st
+
+    dom = hps.Domain(p=6, q=4, root=hps.DiscretizationNode2D(-1.0, 1.0, -1.0, 1.0), L=1)
+    ones = np.ones(dom.interior_points.shape[:2])
+    pde = hps.PDEProblem(dom, source=ones, D_xx_coefficients=ones, D_yy_coefficients=ones)
+    calls = []
+
+    def make():
+        calls.append(1)
+        return pde.P
+
+    a = st._device_copy(pde, "P", make, torch.float64, torch.device("cpu"))
+    b = st._device_copy(pde, "P", make, torch.float64, torch.device("cpu"))
+    c = st._device_copy(pde, "P", make, torch.float32, torch.device("cpu"))
+    assert a is b and c is not a and len(calls) == 2
+    assert np.array_equal(a.numpy(), pde.P) and c.dtype == torch.float32
+    pde.reset()   # dropping the solver state keeps the copies
+    assert st._device_copy(pde, "P", make, torch.float64, torch.device("cpu")) is a and len(calls) == 2
