@@ -337,3 +337,24 @@ def test_device_copies_of_fixed_operators_are_made_once():
     assert np.array_equal(a.numpy(), pde.P) and c.dtype == torch.float32
     pde.reset()   # dropping the solver state keeps the copies
     assert st._device_copy(pde, "P", make, torch.float64, torch.device("cpu")) is a and len(calls) == 2
+
+
+def test_pair_kernels_support_table_and_argument_checks_without_a_gpu():
+    """Host-only parts of the C ABI: which (p, q) the double-float residual
+    kernels are compiled for, and the argument checks of the pair entries,
+    which return HPS_ERR_ARG with a message before any device call."""
+    import ctypes as C
+
+    from jaxhps_gb300 import _native as nat
+
+    lib = nat.load_library()
+    for p in range(4, 20):
+        for q in range(2, p):
+            want = q == p - 2 and p in (8, 10, 12, 14, 16)
+            assert bool(lib.hps_residual_df_supported(p, q)) == want, (p, q)
+    null = None
+    assert lib.hps_assemble_u_2d_df(0, 16, 14, 1, null, null, null, null, null, null) == 1
+    buf = C.create_string_buffer(256)
+    lib.hps_last_error(buf, 256)
+    assert b"hps_assemble_u_2d_df" in buf.value
+    assert lib.hps_mapped_pointer(null, null) == 1
